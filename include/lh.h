@@ -1,0 +1,142 @@
+/*
+ * lh.h — C ABI of the GB300 RK3 substep of the "littleharsh" channel DNS.
+ *
+ * The reference (Fortran 90 + MPI) has no plugin API: its boundary is the set of
+ * Fortran subroutines `program littleharsh` calls once per RK3 substep
+ * (littleharsh.f90:174-217), with all shared data in `module declaration`
+ * (declaration.f90). This header replaces that boundary with plain C entry points
+ * that a Fortran host binds through ISO_C_BINDING and that
+ * the Python package binds through ctypes.
+ *
+ * Conventions
+ *  - A "level" j is a reference y-index. u/w live on levels N(4,0)..N(4,3)+1
+ *    (ghosts included), v on N(3,0)..N(3,3)+1 (walls included), p/psi/div on
+ *    N(4,0)+1..N(4,3). N(3,0) = N(4,0) = -dny (dny > 0 only with posts).
+ *  - Spectral state arrays on the host use the reference's `type(cfield)` layout
+ *    of the midband (long-column) band: f(level, column), complex(8),
+ *    column-major with the level fastest, one column per (kx, kz) mode in the
+ *    order of proc_lims_columns with one process (start.f90:1610-1631):
+ *    column = ikz * (N1/2+1) + ikx, ikz = 0..N2-1 in k1F_z order.
+ *  - All entry points return LH_OK or a negative error code; lh_last_error()
+ *    returns a message for the last failure on that handle.
+ *  - One handle per host thread. No internal threads.
+ */
+#ifndef LH_H
+#define LH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LH_ABI_VERSION 1
+
+enum {
+  LH_OK = 0,
+  LH_EINVAL = -1,      /* bad argument or unsupported configuration */
+  LH_ENONFINITE = -2,  /* a NaN/Inf appeared in the state (blow-up guard) */
+  LH_ETIMEOUT = -3,    /* a bounded device wait gave up */
+  LH_ECUDA = -4,       /* a CUDA runtime call failed */
+  LH_ENOMEM = -5
+};
+
+enum {
+  LH_PREC_FP64 = 0,    /* plain form: every kernel in FP64 */
+  LH_PREC_MIXED = 1    /* precision form: FP32 transforms/products, FP64 state, solves and (0,0) mode */
+};
+
+/* Everything the substep reads from `module declaration`, for one channel whose
+ * three bands share one x/z resolution (start.f90:36-691 computes these). */
+typedef struct lh_config {
+  int32_t abi_version;            /* LH_ABI_VERSION */
+  int32_t precision;              /* LH_PREC_* */
+  int32_t N1, N2;                 /* retained Fourier modes N(1,b), N(2,b) */
+  int32_t Ngal1, Ngal2;           /* physical points Ngal(1,b), Ngal(2,b) */
+  int32_t dny;                    /* depth of the immersed region: N(3,0) = N(4,0) = -dny */
+  int32_t nn;                     /* N(3,nband) before the immersed region is added (= ny-2) */
+  int32_t N3[4], N4[4];           /* band limits N(3,0:3), N(4,0:3) */
+  int32_t nyu, nyv;               /* number of u levels and v levels */
+  const double *yu, *yv;          /* [nyu], [nyv] : yu(j), yv(j) at index j+dny */
+  const double *dthdyu, *dthdyv;  /* [nyu], [nyv] */
+  const double *dyu2i, *dyv2i;    /* [3][nyu], [3][nyv] : dyu2i(c, j) at [c-1][j+dny] */
+  const double *k1x, *k2x;        /* [N1/2+1] : Im k1F_x(i), k2F_x(i) */
+  const double *k1z, *k2z;        /* [N2]     : Im k1F_z(k), k2F_z(k) */
+  double Re, CFL, dtv, ddthetavi, dthetavi, alp, bet, Kib;
+  double aRK[3], bRK[3], cRK[3], dRK[3], gRK[3];
+  double gw[3][2];                /* gridweighting(band, 1:2) */
+  double gw_interp[3][2];         /* gridweighting_interp(band, 1:2) */
+  double gw_bc_u1, gw_bc_u3;      /* gridweighting_bc_u1/u3 */
+  int32_t flag_ctpress;           /* 0 constant flow rate, 1 constant pressure gradient */
+  int32_t ib_enable;              /* apply the immersed-boundary forcing */
+  int32_t nib_u, nib_v;           /* number of listed solid points, u/w grid and v grid */
+  const int32_t *list_ib_u;       /* [nib_u][6] : i, k, j, i1, k1, j1 (i,k 1-based physical) */
+  const int32_t *list_ib_v;       /* [nib_v][6] */
+  const double *A_ib_u, *A_ib_v;  /* [nib_u], [nib_v] */
+} lh_config;
+
+/* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter). */
+typedef struct lh_scalars {
+  double t, dt, dti, dtc, err, mpgx, QxT, Qx;
+  int64_t iter;
+} lh_scalars;
+
+typedef struct lh_handle lh_handle;
+
+/* Replaces `start` + the allocations of littleharsh.f90:110-152 and the pressure
+ * factorisation LU_buildP/LU_decP (start.f90:656-658, tridLU_3D.f90:333-518).
+ * The config's arrays are copied; the caller may free them afterwards. */
+int lh_create(const lh_config *cfg, lh_handle **out);
+int lh_destroy(lh_handle *h);
+const char *lh_last_error(lh_handle *h);
+
+/* Upload / download the state (u1, u2, u3, p) in the host cfield layout
+ * (replaces getini's planes_to_modes_UVP, start.f90:2226-2229, and the
+ * modes_to_planes_UVP feeding record_out, littleharsh.f90:398-402).
+ * u1, u3: complex(8) [ncols][nyu]; u2: [ncols][nyv]; p: [ncols][nyu-2]
+ * (interleaved re/im doubles, level fastest). Any pointer may be NULL to skip
+ * that field. Blocking. */
+int lh_upload_state(lh_handle *h, const double *u1, const double *u2,
+                    const double *u3, const double *p);
+int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p);
+
+/* Scalars: lh_set_scalars also (re)computes Qx, and QxT when flag_ctpress == 0,
+ * as getini does (start.f90:2170-2176), and the initial divergence. */
+int lh_set_scalars(lh_handle *h, const lh_scalars *s);
+int lh_get_scalars(lh_handle *h, lh_scalars *s);
+
+/* One RK3 substep kRK = 1..3: RHS0_u1/u2/u3, nonlinear, solveU_W, solveV,
+ * [meanflow_ctU], solveP, v_corr (littleharsh.f90:176-215). Asynchronous on the
+ * handle's stream; dt and err stay on the device. */
+int lh_substep(lh_handle *h, int kRK);
+
+/* One full step: three substeps, then meanflow_ctP when flag_ctpress == 1,
+ * then iter += 1 (littleharsh.f90:174-226). Replayed from a CUDA graph after
+ * the first call. Asynchronous. */
+int lh_step(lh_handle *h);
+
+/* Block until the handle's work is done; returns LH_ENONFINITE if the blow-up
+ * guard fired (max|div| or a velocity became non-finite). */
+int lh_synchronize(lh_handle *h);
+
+/* Device-resident views for callers that keep the state on the GPU (e.g. a
+ * PyTorch host). Plane-major layout [level][kz][kx] complex128. */
+int lh_device_state(lh_handle *h, void **u1, void **u2, void **u3, void **p);
+/* The CUDA stream the handle runs on (cudaStream_t as void*). */
+void *lh_stream(lh_handle *h);
+
+/* ---- leaves, for per-kernel parity checks (device pointers, handle's stream) ----
+ * Batched x/z transforms of `nplanes` spectral planes [N2][N1/2+1] complex to
+ * physical planes [Ngal2][Ngal1] real and back: four_to_phys_du / phys_to_four_du
+ * (FOU3D.f90:766-781, 2253-2272) over cft/rft (cft_buff.f:1-65, rft_buff.f:24-86). */
+int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int nplanes);
+int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes);
+
+/* Number of CUDA kernel launches issued by the handle since creation. */
+int64_t lh_kernel_launches(lh_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LH_H */

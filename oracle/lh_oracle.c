@@ -1,0 +1,862 @@
+/*
+ * lh_oracle.c — CPU FP64 restatement of the reference's RK3 substep.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle the tests, smoke() and the
+ * CPU-baseline leg of bench.py check the CUDA library against. It is never linked
+ * into, loaded by, or called from the product path.
+ *
+ * It follows, loop by loop and in the same floating-point evaluation order:
+ *   littleharsh.f90:174-217  substep sequence
+ *   littleharsh.f90:237-272  divergence
+ *   littleharsh.f90:274-340  laplacian_U / laplacian_V
+ *   littleharsh.f90:435-509  flowrateIm / flowrateRe / flowrate_corr
+ *   littleharsh.f90:529-562  meanflow_ctP / meanflow_ctU
+ *   littleharsh.f90:581-633  solveP
+ *   littleharsh.f90:635-788  RHS0_u1 / RHS0_u2 / RHS0_u3
+ *   littleharsh.f90:791-907  solveU_W / solveV
+ *   littleharsh.f90:956-1052 v_corr
+ *   FOU3D.f90:41-425         nonlinear (plain pseudo-spectral products, ops_in_planes2
+ *                            FOU3D.f90:2090-2251, in place of the triad-list ops_in_planes)
+ *   FOU3D.f90:427-474        interp_u / interp_v
+ *   FOU3D.f90:476-593        der_x / der_z
+ *   FOU3D.f90:636-676        der_yu_h / der_yv_h
+ *   FOU3D.f90:699-736        dtc_calc (dthetavi is never assigned in the reference, so the
+ *                            wall-normal term is 1/(u2m*0) = +inf; reproduced)
+ *   FOU3D.f90:738-764, 2253-2272 four_to_phys_u / phys_to_four_du
+ *   FOU3D.f90:806-998        imm_bounds_u / imm_bounds_v (disabled in the reference: the call
+ *                            is commented out at FOU3D.f90:413-423; restated here, switchable)
+ *   tridLU_3D.f90:55-537     LUsolU_W, LUsolV, LUsolP, LUsol0, LU_build*, LU_dec*
+ * The x/z transforms follow the mathematics of rft_buff.f:24-86 and cft_buff.f:1-65
+ * (forward scaled by 1/n, Im of x-modes 0 and n/2 zeroed, inverse unscaled); the FFT
+ * itself is written here from the DFT definition (mixed radix 2/3/4 Cooley-Tukey),
+ * not taken from FFTPACK.
+ *
+ * Layout: every spectral field is plane-major, complex [level][kz][kx].
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "lh_oracle.h"
+
+typedef double complex cplx;
+
+/* ------------------------------------------------------------------------- */
+/* FFT: recursive mixed-radix decimation in time, twiddles exp(-2 pi i e/n).  */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int n;
+  int nfac;
+  int fac[32];
+  cplx *tw; /* [n] exp(-2 pi i e / n) */
+} fftplan;
+
+static int plan_init(fftplan *P, int n) {
+  P->n = n;
+  P->nfac = 0;
+  int m = n;
+  while (m > 1) {
+    int f;
+    if (m % 4 == 0) f = 4;
+    else if (m % 2 == 0) f = 2;
+    else if (m % 3 == 0) f = 3;
+    else if (m % 5 == 0) f = 5;
+    else f = m; /* generic prime */
+    P->fac[P->nfac++] = f;
+    m /= f;
+  }
+  P->tw = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  if (!P->tw) return -1;
+  for (int e = 0; e < n; ++e) {
+    double a = -2.0 * M_PI * (double)e / (double)n;
+    P->tw[e] = cos(a) + I * sin(a);
+  }
+  return 0;
+}
+
+static void plan_free(fftplan *P) { free(P->tw); P->tw = NULL; }
+
+/* out[0..m*p) from in[] with stride `st`; `ts` = twiddle stride (n / current length). */
+static void fft_rec(const fftplan *P, const cplx *in, cplx *out, int len, int st, int fi,
+                    int sgn, cplx *scr) {
+  if (len == 1) { out[0] = in[0]; return; }
+  int p = P->fac[fi];
+  int m = len / p;
+  for (int r = 0; r < p; ++r) fft_rec(P, in + (size_t)r * st, out + (size_t)r * m, m, st * p, fi + 1, sgn, scr);
+  int ts = P->n / len; /* W_len^e = tw[e*ts] */
+  const cplx *tw = P->tw;
+  for (int k = 0; k < m; ++k) {
+    cplx t[64];
+    for (int r = 0; r < p; ++r) {
+      cplx w = tw[(size_t)r * k * ts % P->n];
+      if (sgn > 0) w = conj(w);
+      t[r] = (r == 0) ? out[k] : w * out[r * m + k];
+    }
+    if (p == 2) {
+      out[k] = t[0] + t[1];
+      out[k + m] = t[0] - t[1];
+    } else if (p == 4) {
+      cplx a0 = t[0] + t[2], a1 = t[0] - t[2], a2 = t[1] + t[3], a3 = t[1] - t[3];
+      cplx rot = (sgn > 0) ? I * a3 : -I * a3; /* W_4^1 = -i (forward), +i (backward) */
+      out[k] = a0 + a2;
+      out[k + m] = a1 + rot;
+      out[k + 2 * m] = a0 - a2;
+      out[k + 3 * m] = a1 - rot;
+    } else {
+      for (int q = 0; q < p; ++q) {
+        cplx s = 0;
+        for (int r = 0; r < p; ++r) {
+          cplx w = tw[(size_t)((r * q) % p) * (P->n / p)];
+          if (sgn > 0) w = conj(w);
+          s += w * t[r];
+        }
+        scr[q] = s;
+      }
+      for (int q = 0; q < p; ++q) out[k + q * m] = scr[q];
+    }
+  }
+}
+
+/* in-place complex transform of x[0..n) with element stride 1 */
+static void fft_inplace(const fftplan *P, cplx *x, int sgn, cplx *tmp) {
+  cplx scr[64];
+  memcpy(tmp, x, sizeof(cplx) * (size_t)P->n);
+  fft_rec(P, tmp, x, P->n, 1, 0, sgn, scr);
+}
+
+/* ------------------------------------------------------------------------- */
+struct orc {
+  lh_config c;
+  /* owned copies of the config arrays */
+  double *yu, *yv, *thu, *thv, *d2u, *d2v, *k1x, *k2x, *k1z, *k2z, *Au, *Av;
+  int32_t *lu, *lv;
+  int N1, N2, N1h, G1, G2, dny, nu, nv, np, ncol, nn;
+  fftplan px, pz; /* complex plans of length G1 and G2 */
+  cplx *u1, *u2, *u3, *p;
+  cplx *Nu1, *Nu2, *Nu3, *du1, *du2, *du3, *psi, *div;
+  cplx *u1i, *u2i, *u3i; /* u1,u3 at v levels; u2 at u levels */
+  cplx *uvf, *wvf, *vvc, *N1xz, *N2xz, *N3xz;
+  double *DG; /* [np][ncol][3] factorised pressure matrices */
+  double *phys_u1, *phys_u3, *phys_u2; /* physical planes, all levels (for IB) */
+  double t, dt, dti, dtc, err, mpgx, QxT, Qx;
+  int64_t iter;
+};
+
+#define UIDX(j) ((j) + O->dny)          /* u or v level j -> array index */
+#define PIDX(j) ((j) + O->dny - 1)      /* p level j -> array index */
+#define PL(F, idx) ((F) + (size_t)(idx) * O->ncol)
+
+static double *dupd(const double *s, size_t n) {
+  double *d = (double *)malloc(sizeof(double) * (n ? n : 1));
+  if (n) memcpy(d, s, sizeof(double) * n);
+  return d;
+}
+
+static cplx *zalloc(size_t n) { return (cplx *)calloc(n ? n : 1, sizeof(cplx)); }
+
+/* pressure matrix, LU_buildP + LU_decP (tridLU_3D.f90:333-407, 477-518) */
+static void build_DG(orc *O) {
+  const double dd = O->c.ddthetavi;
+  int ns = O->c.N4[0] + 1, ne = O->c.N4[3];
+  int n = ne - ns + 1;
+  double *Db = (double *)malloc(sizeof(double) * (n + 2)); /* index m - (ns-1) */
+  double *Gb = (double *)malloc(sizeof(double) * (n + 2));
+  double *Dt = (double *)malloc(sizeof(double) * (n + 2));
+  double *Gt = (double *)malloc(sizeof(double) * (n + 2));
+#define X(m) ((m) - (ns - 1))
+  for (int j = ns; j <= ne; ++j) {
+    Db[X(j - 1)] = -dd * O->thu[UIDX(j)];
+    Gb[X(j)] = -dd * O->thv[UIDX(j)];
+    Dt[X(j)] = dd * O->thu[UIDX(j)];
+    Gt[X(j + 1)] = dd * O->thv[UIDX(j)];
+  }
+  for (int kz = 0; kz < O->N2; ++kz)
+    for (int kx = 0; kx < O->N1h; ++kx) {
+      int col = kz * O->N1h + kx;
+      double k2x = O->k2x[kx], k2z = O->k2z[kz];
+#define A(c, j) O->DG[((size_t)((j) - ns) * O->ncol + col) * 3 + (c) - 1]
+      A(1, ns) = 0.0;
+      A(2, ns) = (Dt[X(ns)] * Gb[X(ns)]) + k2x + k2z;
+      A(3, ns) = (Dt[X(ns)] * Gt[X(ns + 1)]);
+      A(2, ne) = (Db[X(ne - 1)] * Gt[X(ne)]) + k2x + k2z;
+      A(1, ne) = (Db[X(ne - 1)] * Gb[X(ne - 1)]);
+      A(3, ne) = 0.0;
+      for (int j = ns + 1; j <= ne - 1; ++j) {
+        A(2, j) = (Db[X(j - 1)] * Gt[X(j)]) + (Dt[X(j)] * Gb[X(j)]) + k2x + k2z;
+        A(1, j) = (Db[X(j - 1)] * Gb[X(j - 1)]);
+        A(3, j) = (Dt[X(j)] * Gt[X(j + 1)]);
+      }
+      if (col == 0) { /* gauge of mode (0,0), tridLU_3D.f90:384-390 */
+        double h = O->yu[UIDX(1 + 1)] - O->yu[UIDX(1)];
+        A(1, ns) = 0.0;
+        A(2, ns) = 1.0 / (h * h);
+        A(3, ns) = 0.0;
+      }
+      A(2, ns) = 1.0 / A(2, ns);
+      for (int j = ns + 1; j <= ne; ++j) {
+        A(3, j - 1) = A(3, j - 1) * A(2, j - 1);
+        A(2, j) = 1.0 / (A(2, j) - A(1, j) * A(3, j - 1));
+      }
+#undef A
+    }
+#undef X
+  free(Db); free(Gb); free(Dt); free(Gt);
+}
+
+orc *orc_create(const lh_config *cfg) {
+  orc *O = (orc *)calloc(1, sizeof(orc));
+  if (!O) return NULL;
+  O->c = *cfg;
+  O->N1 = cfg->N1; O->N2 = cfg->N2; O->N1h = cfg->N1 / 2 + 1;
+  O->G1 = cfg->Ngal1; O->G2 = cfg->Ngal2; O->dny = cfg->dny;
+  O->nu = cfg->nyu; O->nv = cfg->nyv; O->np = cfg->nyu - 2; O->nn = cfg->nn;
+  O->ncol = O->N1h * O->N2;
+  O->yu = dupd(cfg->yu, O->nu); O->yv = dupd(cfg->yv, O->nv);
+  O->thu = dupd(cfg->dthdyu, O->nu); O->thv = dupd(cfg->dthdyv, O->nv);
+  O->d2u = dupd(cfg->dyu2i, 3 * (size_t)O->nu); O->d2v = dupd(cfg->dyv2i, 3 * (size_t)O->nv);
+  O->k1x = dupd(cfg->k1x, O->N1h); O->k2x = dupd(cfg->k2x, O->N1h);
+  O->k1z = dupd(cfg->k1z, O->N2); O->k2z = dupd(cfg->k2z, O->N2);
+  O->lu = (int32_t *)malloc(sizeof(int32_t) * (6 * (size_t)cfg->nib_u + 1));
+  O->lv = (int32_t *)malloc(sizeof(int32_t) * (6 * (size_t)cfg->nib_v + 1));
+  if (cfg->nib_u) memcpy(O->lu, cfg->list_ib_u, sizeof(int32_t) * 6 * (size_t)cfg->nib_u);
+  if (cfg->nib_v) memcpy(O->lv, cfg->list_ib_v, sizeof(int32_t) * 6 * (size_t)cfg->nib_v);
+  O->Au = dupd(cfg->A_ib_u, cfg->nib_u); O->Av = dupd(cfg->A_ib_v, cfg->nib_v);
+  O->c.yu = O->yu; O->c.yv = O->yv; O->c.dthdyu = O->thu; O->c.dthdyv = O->thv;
+  O->c.dyu2i = O->d2u; O->c.dyv2i = O->d2v; O->c.k1x = O->k1x; O->c.k2x = O->k2x;
+  O->c.k1z = O->k1z; O->c.k2z = O->k2z; O->c.list_ib_u = O->lu; O->c.list_ib_v = O->lv;
+  O->c.A_ib_u = O->Au; O->c.A_ib_v = O->Av;
+  if (plan_init(&O->px, O->G1) || plan_init(&O->pz, O->G2)) return NULL;
+  size_t nc = (size_t)O->ncol;
+  O->u1 = zalloc(nc * O->nu); O->u3 = zalloc(nc * O->nu); O->u2 = zalloc(nc * O->nv);
+  O->p = zalloc(nc * O->np);
+  O->Nu1 = zalloc(nc * O->nu); O->Nu3 = zalloc(nc * O->nu); O->Nu2 = zalloc(nc * O->nv);
+  O->du1 = zalloc(nc * O->nu); O->du3 = zalloc(nc * O->nu); O->du2 = zalloc(nc * O->nv);
+  O->psi = zalloc(nc * O->np); O->div = zalloc(nc * O->np);
+  O->u1i = zalloc(nc * O->nv); O->u3i = zalloc(nc * O->nv); O->u2i = zalloc(nc * O->nu);
+  O->uvf = zalloc(nc * O->nv); O->wvf = zalloc(nc * O->nv); O->vvc = zalloc(nc * O->nu);
+  O->N1xz = zalloc(nc * O->nu); O->N3xz = zalloc(nc * O->nu); O->N2xz = zalloc(nc * O->nv);
+  O->DG = (double *)calloc(3 * nc * O->np, sizeof(double));
+  size_t pp = (size_t)O->G1 * O->G2;
+  O->phys_u1 = (double *)calloc(pp * O->nu, sizeof(double));
+  O->phys_u3 = (double *)calloc(pp * O->nu, sizeof(double));
+  O->phys_u2 = (double *)calloc(pp * O->nv, sizeof(double));
+  build_DG(O);
+  O->dt = 0; O->t = 0; O->mpgx = cfg->Re * 0; O->iter = 0;
+  return O;
+}
+
+void orc_destroy(orc *O) {
+  if (!O) return;
+  void *ptrs[] = {O->yu, O->yv, O->thu, O->thv, O->d2u, O->d2v, O->k1x, O->k2x, O->k1z, O->k2z,
+                  O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
+                  O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
+                  O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2};
+  for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
+  plan_free(&O->px); plan_free(&O->pz);
+  free(O);
+}
+
+/* ------------------------------------------------------------------------- */
+/* transforms of one plane                                                     */
+/* ------------------------------------------------------------------------- */
+/* plane row (0-based, physical z index) of column kz-index r (0-based) */
+static inline int prow(const orc *O, int r) { return r < O->N2 / 2 ? r : r - O->N2 + O->G2; }
+
+/* work buffers for one thread */
+typedef struct { cplx *A; cplx *line; cplx *tmp; } pwork;
+
+static void pwork_init(const orc *O, pwork *w) {
+  int n = O->G1 > O->G2 ? O->G1 : O->G2;
+  w->A = zalloc((size_t)O->G2 * (O->G1 / 2 + 1));
+  w->line = zalloc((size_t)n);
+  w->tmp = zalloc((size_t)n);
+}
+static void pwork_free(pwork *w) { free(w->A); free(w->line); free(w->tmp); }
+
+/* four_to_phys (FOU3D.f90:738-781): spectral plane S[kz][kx] -> phys[l][m] (G2 x G1).
+ * z: backward complex transform of the N1/2+1 retained x-modes; x: backward real
+ * transform of every row, Im of x-modes 0 and G1/2 ignored. */
+static void four_to_phys_plane(const orc *O, const cplx *S, double *phys, pwork *w) {
+  const int G1 = O->G1, G2 = O->G2, Gh = G1 / 2 + 1, N1h = O->N1h;
+  memset(w->A, 0, sizeof(cplx) * (size_t)G2 * Gh);
+  for (int kx = 0; kx < N1h; ++kx) {
+    for (int l = 0; l < G2; ++l) w->line[l] = 0;
+    for (int r = 0; r < O->N2; ++r) w->line[prow(O, r)] = S[(size_t)r * N1h + kx];
+    w->line[G2 / 2] = 0; /* zeroed z 'oddball' row */
+    fft_inplace(&O->pz, w->line, +1, w->tmp);
+    for (int l = 0; l < G2; ++l) w->A[(size_t)l * Gh + kx] = w->line[l];
+  }
+  /* x: pair rows (a, b) into one complex backward transform */
+  for (int l = 0; l < G2; l += 2) {
+    const cplx *a = w->A + (size_t)l * Gh;
+    const cplx *b = (l + 1 < G2) ? w->A + (size_t)(l + 1) * Gh : NULL;
+    for (int k = 0; k < G1; ++k) w->line[k] = 0;
+    for (int k = 0; k <= G1 / 2; ++k) {
+      cplx ak = a[k], bk = b ? b[k] : 0;
+      if (k == 0 || k == G1 / 2) { ak = creal(ak); bk = creal(bk); }
+      w->line[k] = ak + I * bk;
+      if (k > 0 && k < G1 / 2) w->line[G1 - k] = conj(ak) + I * conj(bk);
+    }
+    fft_inplace(&O->px, w->line, +1, w->tmp);
+    for (int m = 0; m < G1; ++m) {
+      phys[(size_t)l * G1 + m] = creal(w->line[m]);
+      if (b) phys[(size_t)(l + 1) * G1 + m] = cimag(w->line[m]);
+    }
+  }
+}
+
+/* phys_to_four (FOU3D.f90:2253-2272) restricted to the retained modes: returns
+ * C[kz-index r][kx] for all N2 column rows (the zeroed row G2/2 is never retained). */
+static void phys_to_four_plane(const orc *O, const double *phys, cplx *C, pwork *w) {
+  const int G1 = O->G1, G2 = O->G2, Gh = G1 / 2 + 1, N1h = O->N1h;
+  const double s1 = 1.0 / G1, s2 = 1.0 / G2;
+  for (int l = 0; l < G2; l += 2) {
+    int hasb = (l + 1 < G2);
+    for (int m = 0; m < G1; ++m)
+      w->line[m] = phys[(size_t)l * G1 + m] + I * (hasb ? phys[(size_t)(l + 1) * G1 + m] : 0.0);
+    fft_inplace(&O->px, w->line, -1, w->tmp);
+    for (int k = 0; k <= G1 / 2; ++k) {
+      cplx z = w->line[k], zc = conj(w->line[(G1 - k) % G1]);
+      cplx A = 0.5 * (z + zc), B = -0.5 * I * (z - zc);
+      A *= s1; B *= s1;
+      if (k == 0 || k == G1 / 2) { A = creal(A); B = creal(B); }
+      w->A[(size_t)l * Gh + k] = A;
+      if (hasb) w->A[(size_t)(l + 1) * Gh + k] = B;
+    }
+  }
+  for (int kx = 0; kx < N1h; ++kx) {
+    for (int l = 0; l < G2; ++l) w->line[l] = w->A[(size_t)l * Gh + kx];
+    fft_inplace(&O->pz, w->line, -1, w->tmp);
+    for (int r = 0; r < O->N2; ++r) C[(size_t)r * N1h + kx] = w->line[prow(O, r)] * s2;
+  }
+}
+
+/* der_x / der_z (FOU3D.f90:476-593) of retained-mode planes, summed:
+ * out = i kx * X + i kz * Z, with the row kz = -N2/2 (column r = N2/2) zeroed. */
+static void derxz(const orc *O, const cplx *X, const cplx *Z, cplx *out) {
+  for (int r = 0; r < O->N2; ++r)
+    for (int kx = 0; kx < O->N1h; ++kx) {
+      size_t c = (size_t)r * O->N1h + kx;
+      if (r == O->N2 / 2) { out[c] = 0; continue; }
+      cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[r];
+      out[c] = kxF * X[c] + kzF * Z[c];
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* nonlinear (FOU3D.f90:41-425 with ops_in_planes2)                          */
+/* ------------------------------------------------------------------------- */
+static void nonlinear(orc *O, int kRK) {
+  const int nc = O->ncol;
+  const double dd = O->c.ddthetavi;
+  /* interp_u (u1,u3 -> v levels) and interp_v (u2 -> u levels), FOU3D.f90:427-474 */
+  for (int jv = O->c.N3[0]; jv <= O->c.N3[3] + 1; ++jv) {
+    double yv = O->yv[UIDX(jv)], yuj = O->yu[UIDX(jv)], yu1 = O->yu[UIDX(jv + 1)];
+    for (int c = 0; c < nc; ++c) {
+      cplx a = PL(O->u1, UIDX(jv + 1))[c], b = PL(O->u1, UIDX(jv))[c];
+      PL(O->u1i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * b) / (yu1 - yuj);
+      a = PL(O->u3, UIDX(jv + 1))[c]; b = PL(O->u3, UIDX(jv))[c];
+      PL(O->u3i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * b) / (yu1 - yuj);
+    }
+  }
+  for (int ju = O->c.N4[0] + 1; ju <= O->c.N4[3]; ++ju) {
+    double yuj = O->yu[UIDX(ju)], yvm = O->yv[UIDX(ju - 1)], yvj = O->yv[UIDX(ju)];
+    for (int c = 0; c < nc; ++c)
+      PL(O->u2i, UIDX(ju))[c] = ((yuj - yvm) * PL(O->u2, UIDX(ju))[c]
+                                 + (yvj - yuj) * PL(O->u2, UIDX(ju - 1))[c]) / (yvj - yvm);
+  }
+  {
+    int lo = O->c.N4[0], hi = O->c.N4[3] + 1, vlo = O->c.N3[0], vhi = O->c.N3[3] + 1;
+    for (int c = 0; c < nc; ++c) {
+      cplx i1 = PL(O->u2i, UIDX(lo + 1))[c], i2 = PL(O->u2i, UIDX(hi - 1))[c];
+      PL(O->u2i, UIDX(lo))[c] = O->c.gw_interp[1][0] * (PL(O->u2, UIDX(vlo))[c] - i1) + i1;
+      PL(O->u2i, UIDX(hi))[c] = O->c.gw_interp[1][1] * (PL(O->u2, UIDX(vhi))[c] - i2) + i2;
+    }
+  }
+
+  const int G1 = O->G1, G2 = O->G2;
+  const size_t pp = (size_t)G1 * G2;
+  double u1m = 0.0, u3m = 0.0, u2m = 1e-6;
+  int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3];
+  int vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
+
+#pragma omp parallel reduction(max : u1m, u3m, u2m)
+  {
+    pwork w; pwork_init(O, &w);
+    double *f1 = (double *)malloc(sizeof(double) * pp), *f2 = (double *)malloc(sizeof(double) * pp);
+    double *f3 = (double *)malloc(sizeof(double) * pp);
+    double *q1 = (double *)malloc(sizeof(double) * pp), *q2 = (double *)malloc(sizeof(double) * pp);
+    double *q3 = (double *)malloc(sizeof(double) * pp), *q4 = (double *)malloc(sizeof(double) * pp);
+    cplx *c1 = zalloc(nc), *c2 = zalloc(nc), *c3 = zalloc(nc), *c4 = zalloc(nc);
+#pragma omp for schedule(dynamic)
+    for (int ju = ulo; ju <= uhi; ++ju) {
+      four_to_phys_plane(O, PL(O->u1, UIDX(ju)), f1, &w);
+      four_to_phys_plane(O, PL(O->u2i, UIDX(ju)), f2, &w);
+      four_to_phys_plane(O, PL(O->u3, UIDX(ju)), f3, &w);
+      for (size_t e = 0; e < pp; ++e) {
+        q1[e] = f1[e] * f1[e];
+        q2[e] = f1[e] * f3[e];
+        q3[e] = f2[e] * f2[e];
+        q4[e] = f3[e] * f3[e];
+        if (fabs(f1[e]) > u1m) u1m = fabs(f1[e]);
+        if (fabs(f3[e]) > u3m) u3m = fabs(f3[e]);
+      }
+      memcpy(O->phys_u1 + pp * UIDX(ju), f1, sizeof(double) * pp);
+      memcpy(O->phys_u3 + pp * UIDX(ju), f3, sizeof(double) * pp);
+      phys_to_four_plane(O, q1, c1, &w);
+      phys_to_four_plane(O, q2, c2, &w);
+      phys_to_four_plane(O, q3, PL(O->vvc, UIDX(ju)), &w);
+      phys_to_four_plane(O, q4, c4, &w);
+      derxz(O, c1, c2, PL(O->N1xz, UIDX(ju)));
+      derxz(O, c2, c4, PL(O->N3xz, UIDX(ju)));
+    }
+#pragma omp for schedule(dynamic)
+    for (int jv = vlo; jv <= vhi; ++jv) {
+      four_to_phys_plane(O, PL(O->u1i, UIDX(jv)), f1, &w);
+      four_to_phys_plane(O, PL(O->u2, UIDX(jv)), f2, &w);
+      four_to_phys_plane(O, PL(O->u3i, UIDX(jv)), f3, &w);
+      double th = O->thv[UIDX(jv)];
+      for (size_t e = 0; e < pp; ++e) {
+        q1[e] = f1[e] * f2[e];
+        q2[e] = f3[e] * f2[e];
+        double a = fabs(f2[e]) * th;
+        if (a > u2m) u2m = a;
+      }
+      memcpy(O->phys_u2 + pp * UIDX(jv), f2, sizeof(double) * pp);
+      phys_to_four_plane(O, q1, PL(O->uvf, UIDX(jv)), &w);
+      phys_to_four_plane(O, q2, PL(O->wvf, UIDX(jv)), &w);
+      derxz(O, PL(O->uvf, UIDX(jv)), PL(O->wvf, UIDX(jv)), PL(O->N2xz, UIDX(jv)));
+    }
+    free(f1); free(f2); free(f3); free(q1); free(q2); free(q3); free(q4);
+    free(c1); free(c2); free(c3); free(c4);
+    pwork_free(&w);
+  }
+  /* product wall planes are never computed: zero (v = 0 at the walls) */
+  memset(PL(O->uvf, UIDX(O->c.N3[0])), 0, sizeof(cplx) * nc);
+  memset(PL(O->wvf, UIDX(O->c.N3[0])), 0, sizeof(cplx) * nc);
+  memset(PL(O->uvf, UIDX(O->c.N3[3] + 1)), 0, sizeof(cplx) * nc);
+  memset(PL(O->wvf, UIDX(O->c.N3[3] + 1)), 0, sizeof(cplx) * nc);
+
+  /* y-derivatives and assembly (FOU3D.f90:262-283, 636-676) */
+  for (int ju = ulo; ju <= uhi; ++ju) {
+    double th = O->thu[UIDX(ju)];
+    for (int c = 0; c < nc; ++c) {
+      cplx d1 = (PL(O->uvf, UIDX(ju))[c] - PL(O->uvf, UIDX(ju - 1))[c]) * th * dd;
+      cplx d3 = (PL(O->wvf, UIDX(ju))[c] - PL(O->wvf, UIDX(ju - 1))[c]) * th * dd;
+      PL(O->Nu1, UIDX(ju))[c] = PL(O->N1xz, UIDX(ju))[c] + d1;
+      PL(O->Nu3, UIDX(ju))[c] = PL(O->N3xz, UIDX(ju))[c] + d3;
+    }
+  }
+  for (int jv = vlo; jv <= vhi; ++jv) {
+    double th = O->thv[UIDX(jv)];
+    for (int c = 0; c < nc; ++c) {
+      cplx d2 = (PL(O->vvc, UIDX(jv + 1))[c] - PL(O->vvc, UIDX(jv))[c]) * th * dd;
+      PL(O->Nu2, UIDX(jv))[c] = PL(O->N2xz, UIDX(jv))[c] + d2;
+    }
+  }
+
+  if (kRK == 1) {
+    double a = 1.0 / (O->c.alp * (double)(O->N1 / 2) * u1m);
+    double b = 1.0 / (O->c.bet * (double)(O->N2 / 2) * u3m);
+    double cv = 1.0 / (u2m * O->c.dthetavi);
+    double d = a < b ? a : b;
+    O->dtc = d < cv ? d : cv;
+    double lim = 2.5 * O->c.dtv, cfl = O->c.CFL * O->dtc;
+    O->dt = lim < cfl ? lim : cfl;
+    O->dti = 1.0 / O->dt;
+    O->t = O->t + O->dt;
+  }
+}
+
+/* immersed-boundary forcing (FOU3D.f90:806-998), one grid */
+static void imm_bounds(orc *O, cplx *du, const double *uphys, int nlist, const int32_t *list,
+                       const double *A, int lo0, int hi0, int lo1, int hi1) {
+  const int G1 = O->G1, G2 = O->G2;
+  const size_t pp = (size_t)G1 * G2;
+  const double Kibdt = O->c.Kib / O->dt;
+  int ranges[2][2] = {{lo0, hi0}, {lo1, hi1}};
+  for (int rg = 0; rg < 2; ++rg) {
+#pragma omp parallel
+    {
+      pwork w; pwork_init(O, &w);
+      double *ph = (double *)malloc(sizeof(double) * pp);
+#pragma omp for schedule(dynamic)
+      for (int j = ranges[rg][0]; j <= ranges[rg][1]; ++j) {
+        four_to_phys_plane(O, PL(du, UIDX(j)), ph, &w);
+        for (int e = 0; e < nlist; ++e) {
+          const int32_t *L = list + 6 * (size_t)e;
+          if (L[2] != j) continue;
+          double V = A[e] * uphys[pp * UIDX(L[5]) + (size_t)(L[4] - 1) * G1 + (L[3] - 1)];
+          double u = uphys[pp * UIDX(j) + (size_t)(L[1] - 1) * G1 + (L[0] - 1)];
+          ph[(size_t)(L[1] - 1) * G1 + (L[0] - 1)] = Kibdt * (V - u);
+        }
+        phys_to_four_plane(O, ph, PL(du, UIDX(j)), &w);
+      }
+      free(ph);
+      pwork_free(&w);
+    }
+  }
+}
+
+/* tridiagonal LU of one column (LU_dec, tridLU_3D.f90:437-474) and both sweeps */
+static void lu_dec(double *a1, double *a2, double *a3, int n) {
+  a2[0] = 1.0 / a2[0];
+  for (int j = 1; j < n; ++j) {
+    a3[j - 1] = a3[j - 1] * a2[j - 1];
+    a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+  }
+}
+static void lu_sol(const double *a1, const double *a2, const double *a3, cplx *x, int n,
+                   size_t stride) {
+  x[0] = x[0] * a2[0];
+  for (int j = 1; j < n; ++j) x[j * stride] = (x[j * stride] - a1[j] * x[(j - 1) * stride]) * a2[j];
+  for (int j = n - 2; j >= 0; --j) x[j * stride] = x[j * stride] - a3[j] * x[(j + 1) * stride];
+}
+
+static void flowrate_corr(orc *O, int kRK) {
+  int nn = O->nn;
+  int n = nn + 3; /* levels 0..nn+2 */
+  double *u11 = (double *)calloc(n, sizeof(double));
+  double *a1 = (double *)calloc(n, sizeof(double)), *a2 = (double *)calloc(n, sizeof(double));
+  double *a3 = (double *)calloc(n, sizeof(double));
+  double bdt = -O->c.dRK[kRK - 1] * O->dt;
+  u11[0] = 0.0;
+  for (int j = 1; j <= nn + 1; ++j) u11[j] = bdt;
+  u11[nn + 2] = 0.0;
+  double beta = O->c.bRK[kRK - 1] * O->dt / O->c.Re;
+  a1[0] = 0.0; a2[0] = 1.0; a3[0] = O->c.gw[1][0];
+  for (int j = 1; j <= nn + 1; ++j) {
+    a1[j] = -beta * O->d2u[0 * O->nu + UIDX(j)];
+    a2[j] = 1.0 - beta * O->d2u[1 * O->nu + UIDX(j)];
+    a3[j] = -beta * O->d2u[2 * O->nu + UIDX(j)];
+  }
+  a1[nn + 2] = O->c.gw[1][1]; a2[nn + 2] = 1.0; a3[nn + 2] = 0.0;
+  lu_dec(a1, a2, a3, n);
+  u11[0] = u11[0] * a2[0];
+  for (int j = 1; j < n; ++j) u11[j] = (u11[j] - a1[j] * u11[j - 1]) * a2[j];
+  for (int j = n - 2; j >= 0; --j) u11[j] = u11[j] - a3[j] * u11[j + 1];
+  double Qx1 = 0.0, Qx0 = 0.0;
+  for (int j = 1; j <= nn + 1; ++j) Qx1 = Qx1 + (O->yv[UIDX(j)] - O->yv[UIDX(j - 1)]) * u11[j];
+  for (int j = 1; j <= nn + 1; ++j)
+    Qx0 = Qx0 + (O->yv[UIDX(j)] - O->yv[UIDX(j - 1)]) * creal(PL(O->u1, UIDX(j))[0]);
+  double g = (O->QxT - Qx0) / Qx1;
+  O->mpgx = O->mpgx + g;
+  for (int j = 0; j <= nn + 2; ++j) PL(O->u1, UIDX(j))[0] = PL(O->u1, UIDX(j))[0] + g * u11[j];
+  free(u11); free(a1); free(a2); free(a3);
+}
+
+static double flowrateIm(const orc *O) {
+  double Q = 0.0;
+  for (int j = 1; j <= O->nn + 1; ++j)
+    Q = Q + (O->yv[UIDX(j)] - O->yv[UIDX(j - 1)]) * creal(PL(O->u1, UIDX(j))[0]);
+  return Q;
+}
+
+static void divergence(orc *O) {
+  const int nc = O->ncol;
+  const double dd = O->c.ddthetavi;
+  for (int j = O->c.N4[0] + 1; j <= O->c.N4[3]; ++j) {
+    double th = dd * O->thu[UIDX(j)];
+    for (int r = 0; r < O->N2; ++r)
+      for (int kx = 0; kx < O->N1h; ++kx) {
+        int c = r * O->N1h + kx;
+        cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[r];
+        PL(O->div, PIDX(j))[c] = kxF * PL(O->u1, UIDX(j))[c] + kzF * PL(O->u3, UIDX(j))[c]
+                                 + th * (PL(O->u2, UIDX(j))[c] - PL(O->u2, UIDX(j - 1))[c]);
+      }
+  }
+}
+
+static double max_abs_div(const orc *O) {
+  double m = 0.0;
+  size_t n = (size_t)O->ncol * O->np;
+  for (size_t e = 0; e < n; ++e) { double a = cabs(O->div[e]); if (a > m) m = a; }
+  return m;
+}
+
+int orc_substep(orc *O, int kRK) {
+  if (kRK < 1 || kRK > 3) return -1;
+  const int nc = O->ncol, N1h = O->N1h;
+  const double C1 = O->c.aRK[kRK - 1] / O->c.Re, C2 = -O->c.cRK[kRK - 1];
+  const double dR = O->c.dRK[kRK - 1];
+  const int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3], vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
+
+  /* RHS0_u1 / RHS0_u3 (littleharsh.f90:635-679, 739-788) */
+#pragma omp parallel for schedule(static)
+  for (int j = ulo; j <= uhi; ++j) {
+    const double a = O->d2u[0 * O->nu + UIDX(j)], b = O->d2u[1 * O->nu + UIDX(j)];
+    const double cc = O->d2u[2 * O->nu + UIDX(j)];
+    for (int r = 0; r < O->N2; ++r)
+      for (int kx = 0; kx < N1h; ++kx) {
+        int c = r * N1h + kx;
+        double dg = O->k2x[kx] + O->k2z[r] + b;
+        cplx L1 = a * PL(O->u1, UIDX(j - 1))[c] + dg * PL(O->u1, UIDX(j))[c] + cc * PL(O->u1, UIDX(j + 1))[c];
+        cplx L3 = a * PL(O->u3, UIDX(j - 1))[c] + dg * PL(O->u3, UIDX(j))[c] + cc * PL(O->u3, UIDX(j + 1))[c];
+        cplx C3x = -dR * (I * O->k1x[kx]);
+        cplx C3z = -dR * (I * O->k1z[r]);
+        cplx pj = PL(O->p, PIDX(j))[c];
+        PL(O->du1, UIDX(j))[c] = C1 * L1 + C2 * PL(O->Nu1, UIDX(j))[c] + C3x * pj;
+        PL(O->du3, UIDX(j))[c] = C1 * L3 + C2 * PL(O->Nu3, UIDX(j))[c] + C3z * pj;
+      }
+    PL(O->du1, UIDX(j))[0] = PL(O->du1, UIDX(j))[0] + (-dR * O->mpgx);
+  }
+  /* RHS0_u2 (littleharsh.f90:681-737) */
+#pragma omp parallel for schedule(static)
+  for (int j = vlo; j <= vhi; ++j) {
+    const double a = O->d2v[0 * O->nv + UIDX(j)], b = O->d2v[1 * O->nv + UIDX(j)];
+    const double cc = O->d2v[2 * O->nv + UIDX(j)];
+    const double C3 = -dR * O->c.ddthetavi * O->thv[UIDX(j)];
+    for (int r = 0; r < O->N2; ++r)
+      for (int kx = 0; kx < N1h; ++kx) {
+        int c = r * N1h + kx;
+        double dg = O->k2x[kx] + O->k2z[r] + b;
+        cplx L2 = a * PL(O->u2, UIDX(j - 1))[c] + dg * PL(O->u2, UIDX(j))[c] + cc * PL(O->u2, UIDX(j + 1))[c];
+        PL(O->du2, UIDX(j))[c] = C1 * L2 + C2 * PL(O->Nu2, UIDX(j))[c]
+                                 + C3 * (PL(O->p, PIDX(j + 1))[c] - PL(O->p, PIDX(j))[c]);
+      }
+  }
+
+  nonlinear(O, kRK);
+
+  /* du += -gRK * Nu (FOU3D.f90:399-410) */
+  const double G = -O->c.gRK[kRK - 1];
+#pragma omp parallel for schedule(static)
+  for (int j = ulo; j <= uhi; ++j)
+    for (int c = 0; c < nc; ++c) {
+      PL(O->du1, UIDX(j))[c] = PL(O->du1, UIDX(j))[c] + G * PL(O->Nu1, UIDX(j))[c];
+      PL(O->du3, UIDX(j))[c] = PL(O->du3, UIDX(j))[c] + G * PL(O->Nu3, UIDX(j))[c];
+    }
+#pragma omp parallel for schedule(static)
+  for (int j = vlo; j <= vhi; ++j)
+    for (int c = 0; c < nc; ++c) PL(O->du2, UIDX(j))[c] = PL(O->du2, UIDX(j))[c] + G * PL(O->Nu2, UIDX(j))[c];
+
+  if (O->c.ib_enable && O->dny > 0) {
+    int d = O->dny, nn = O->nn;
+    imm_bounds(O, O->du1, O->phys_u1, O->c.nib_u, O->lu, O->Au, -d + 1, 0, nn + 2, nn + 1 + d);
+    imm_bounds(O, O->du2, O->phys_u2, O->c.nib_v, O->lv, O->Av, -d + 1, 0, nn + 1, nn + d);
+    imm_bounds(O, O->du3, O->phys_u3, O->c.nib_u, O->lu, O->Au, -d + 1, 0, nn + 2, nn + 1 + d);
+  }
+
+  /* solveU_W (littleharsh.f90:791-828, tridLU_3D.f90:55-132, 257-291) */
+  const double dt = O->dt;
+  const double beta = O->c.bRK[kRK - 1] * dt / O->c.Re;
+  const int lo = O->c.N4[0], hi = O->c.N4[3] + 1, n = hi - lo + 1;
+#pragma omp parallel
+  {
+    double *a1 = (double *)malloc(sizeof(double) * n), *a2 = (double *)malloc(sizeof(double) * n);
+    double *a3 = (double *)malloc(sizeof(double) * n);
+#pragma omp for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+      int r = c / N1h, kx = c % N1h;
+      PL(O->du1, UIDX(lo))[c] = 0; PL(O->du3, UIDX(lo))[c] = 0;
+      for (int j = lo + 1; j <= hi - 1; ++j) {
+        PL(O->du1, UIDX(j))[c] = PL(O->u1, UIDX(j))[c] + dt * PL(O->du1, UIDX(j))[c];
+        PL(O->du3, UIDX(j))[c] = PL(O->u3, UIDX(j))[c] + dt * PL(O->du3, UIDX(j))[c];
+      }
+      PL(O->du1, UIDX(hi))[c] = 0; PL(O->du3, UIDX(hi))[c] = 0;
+      double k2x = O->k2x[kx], k2z = O->k2z[r];
+      a1[0] = 0.0; a2[0] = 1.0; a3[0] = O->c.gw[1][0];
+      for (int j = lo + 1; j <= hi - 1; ++j) {
+        int q = j - lo;
+        a1[q] = -beta * O->d2u[0 * O->nu + UIDX(j)];
+        a2[q] = 1.0 - beta * (O->d2u[1 * O->nu + UIDX(j)] + k2x + k2z);
+        a3[q] = -beta * O->d2u[2 * O->nu + UIDX(j)];
+      }
+      a1[n - 1] = O->c.gw[1][1]; a2[n - 1] = 1.0; a3[n - 1] = 0.0;
+      lu_dec(a1, a2, a3, n);
+      for (int j = 0; j < n; ++j) {
+        PL(O->u1, UIDX(lo + j))[c] = PL(O->du1, UIDX(lo + j))[c];
+        PL(O->u3, UIDX(lo + j))[c] = PL(O->du3, UIDX(lo + j))[c];
+      }
+      lu_sol(a1, a2, a3, PL(O->u1, UIDX(lo)) + c, n, (size_t)nc);
+      lu_sol(a1, a2, a3, PL(O->u3, UIDX(lo)) + c, n, (size_t)nc);
+    }
+    free(a1); free(a2); free(a3);
+  }
+  /* solveV (littleharsh.f90:877-907, tridLU_3D.f90:135-189, 294-329) */
+  const int vlo0 = O->c.N3[0], vhi0 = O->c.N3[3] + 1, nvv = vhi0 - vlo0 + 1;
+#pragma omp parallel
+  {
+    double *a1 = (double *)malloc(sizeof(double) * nvv), *a2 = (double *)malloc(sizeof(double) * nvv);
+    double *a3 = (double *)malloc(sizeof(double) * nvv);
+#pragma omp for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+      int r = c / N1h, kx = c % N1h;
+      PL(O->du2, UIDX(vlo0))[c] = 0;
+      for (int j = vlo0 + 1; j <= vhi0 - 1; ++j)
+        PL(O->du2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] + dt * PL(O->du2, UIDX(j))[c];
+      PL(O->du2, UIDX(vhi0))[c] = 0;
+      double k2x = O->k2x[kx], k2z = O->k2z[r];
+      a1[0] = 0.0; a2[0] = 1.0; a3[0] = 0.0;
+      for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
+        int q = j - vlo0;
+        a1[q] = -beta * O->d2v[0 * O->nv + UIDX(j)];
+        a2[q] = 1.0 - beta * (O->d2v[1 * O->nv + UIDX(j)] + k2x + k2z);
+        a3[q] = -beta * O->d2v[2 * O->nv + UIDX(j)];
+      }
+      a1[nvv - 1] = 0.0; a2[nvv - 1] = 1.0; a3[nvv - 1] = 0.0;
+      lu_dec(a1, a2, a3, nvv);
+      for (int j = 0; j < nvv; ++j) PL(O->u2, UIDX(vlo0 + j))[c] = PL(O->du2, UIDX(vlo0 + j))[c];
+      lu_sol(a1, a2, a3, PL(O->u2, UIDX(vlo0)) + c, nvv, (size_t)nc);
+    }
+    free(a1); free(a2); free(a3);
+  }
+
+  if (O->c.flag_ctpress == 0) flowrate_corr(O, kRK);
+
+  /* solveP (littleharsh.f90:581-633) */
+  divergence(O);
+  const double dtirk = O->dti / (O->c.aRK[kRK - 1] + O->c.bRK[kRK - 1]);
+  const int pns = O->c.N4[0] + 1, pne = O->c.N4[3], npn = pne - pns + 1;
+  for (size_t e = 0; e < (size_t)nc * O->np; ++e) O->psi[e] = dtirk * O->div[e];
+  PL(O->psi, PIDX(pns))[0] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nc; ++c) {
+    cplx *x = PL(O->psi, PIDX(pns)) + c;
+    const double *D = O->DG;
+#define DGA(cc, q) D[((size_t)(q) * nc + c) * 3 + (cc) - 1]
+    x[0] = x[0] * DGA(2, 0);
+    for (int q = 1; q < npn; ++q) x[(size_t)q * nc] = (x[(size_t)q * nc] - DGA(1, q) * x[(size_t)(q - 1) * nc]) * DGA(2, q);
+    for (int q = npn - 2; q >= 0; --q) x[(size_t)q * nc] = x[(size_t)q * nc] - DGA(3, q) * x[(size_t)(q + 1) * nc];
+#undef DGA
+  }
+  for (size_t e = 0; e < (size_t)nc * O->np; ++e) O->p[e] = O->p[e] + O->psi[e];
+
+  /* v_corr (littleharsh.f90:956-1052) */
+  const double dtrk = dt * (O->c.aRK[kRK - 1] + O->c.bRK[kRK - 1]);
+#pragma omp parallel for schedule(static)
+  for (int j = lo + 1; j <= hi - 1; ++j)
+    for (int r = 0; r < O->N2; ++r)
+      for (int kx = 0; kx < N1h; ++kx) {
+        int c = r * N1h + kx;
+        cplx kxc = (cplx)dtrk * (I * O->k1x[kx]);
+        cplx kzc = (cplx)dtrk * (I * O->k1z[r]);
+        PL(O->u1, UIDX(j))[c] = PL(O->u1, UIDX(j))[c] - kxc * PL(O->psi, PIDX(j))[c];
+        PL(O->u3, UIDX(j))[c] = PL(O->u3, UIDX(j))[c] - kzc * PL(O->psi, PIDX(j))[c];
+      }
+  for (int c = 0; c < nc; ++c) {
+    PL(O->u1, UIDX(lo))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(lo + 1))[c];
+    PL(O->u1, UIDX(hi))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(hi - 1))[c];
+    PL(O->u3, UIDX(lo))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(lo + 1))[c];
+    PL(O->u3, UIDX(hi))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(hi - 1))[c];
+  }
+  const double dtrk_u2 = dtrk * O->c.ddthetavi;
+#pragma omp parallel for schedule(static)
+  for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
+    double f = dtrk_u2 * O->thv[UIDX(j)];
+    for (int c = 0; c < nc; ++c)
+      PL(O->u2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] - f * (PL(O->psi, PIDX(j + 1))[c] - PL(O->psi, PIDX(j))[c]);
+  }
+  for (int c = 0; c < nc; ++c) { PL(O->u2, UIDX(vlo0))[c] = 0; PL(O->u2, UIDX(vhi0))[c] = 0; }
+  divergence(O);
+  return 0;
+}
+
+int orc_step(orc *O) {
+  for (int k = 1; k <= 3; ++k)
+    if (orc_substep(O, k)) return -1;
+  if (O->c.flag_ctpress == 1) O->Qx = flowrateIm(O);
+  O->iter += 1;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* state access: host cfield layout f(level, column), level fastest           */
+/* ------------------------------------------------------------------------- */
+static void put_field(orc *O, cplx *F, int nlev, const double *src) {
+  const int nc = O->ncol;
+  for (int c = 0; c < nc; ++c)
+    for (int l = 0; l < nlev; ++l) {
+      const double *s = src + 2 * ((size_t)c * nlev + l);
+      F[(size_t)l * nc + c] = s[0] + I * s[1];
+    }
+}
+static void get_field(const orc *O, const cplx *F, int nlev, double *dst) {
+  const int nc = O->ncol;
+  for (int c = 0; c < nc; ++c)
+    for (int l = 0; l < nlev; ++l) {
+      double *d = dst + 2 * ((size_t)c * nlev + l);
+      cplx v = F[(size_t)l * nc + c];
+      d[0] = creal(v); d[1] = cimag(v);
+    }
+}
+
+int orc_set_state(orc *O, const double *u1, const double *u2, const double *u3, const double *p) {
+  if (u1) put_field(O, O->u1, O->nu, u1);
+  if (u2) put_field(O, O->u2, O->nv, u2);
+  if (u3) put_field(O, O->u3, O->nu, u3);
+  if (p) put_field(O, O->p, O->np, p);
+  return 0;
+}
+int orc_get_state(orc *O, double *u1, double *u2, double *u3, double *p) {
+  if (u1) get_field(O, O->u1, O->nu, u1);
+  if (u2) get_field(O, O->u2, O->nv, u2);
+  if (u3) get_field(O, O->u3, O->nu, u3);
+  if (p) get_field(O, O->p, O->np, p);
+  return 0;
+}
+/* Nu1/Nu2/Nu3 of the last substep, same layout (levels of u, v, u) */
+int orc_get_nonlinear(orc *O, double *n1, double *n2, double *n3) {
+  if (n1) get_field(O, O->Nu1, O->nu, n1);
+  if (n2) get_field(O, O->Nu2, O->nv, n2);
+  if (n3) get_field(O, O->Nu3, O->nu, n3);
+  return 0;
+}
+
+int orc_set_scalars(orc *O, const lh_scalars *s) {
+  O->t = s->t; O->dt = s->dt; O->dti = s->dti; O->dtc = s->dtc; O->mpgx = s->mpgx;
+  O->iter = s->iter;
+  /* getini: Qx from the (0,0) mode, QxT = Qx for constant flow rate, initial divergence */
+  O->Qx = flowrateIm(O);
+  O->QxT = (O->c.flag_ctpress != 1) ? O->Qx : s->QxT;
+  divergence(O);
+  O->err = max_abs_div(O);
+  return 0;
+}
+int orc_get_scalars(orc *O, lh_scalars *s) {
+  O->err = max_abs_div(O);
+  s->t = O->t; s->dt = O->dt; s->dti = O->dti; s->dtc = O->dtc; s->err = O->err;
+  s->mpgx = O->mpgx; s->QxT = O->QxT; s->Qx = O->Qx; s->iter = O->iter;
+  return 0;
+}
+
+/* leaves: batched plane transforms, spectral [N2][N1/2+1] <-> physical [G2][G1] */
+int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes) {
+  const size_t ns = (size_t)O->ncol, pp = (size_t)O->G1 * O->G2;
+#pragma omp parallel
+  {
+    pwork w; pwork_init(O, &w);
+#pragma omp for
+    for (int q = 0; q < nplanes; ++q)
+      four_to_phys_plane(O, (const cplx *)spec + ns * q, phys + pp * q, &w);
+    pwork_free(&w);
+  }
+  return 0;
+}
+int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes) {
+  const size_t ns = (size_t)O->ncol, pp = (size_t)O->G1 * O->G2;
+#pragma omp parallel
+  {
+    pwork w; pwork_init(O, &w);
+#pragma omp for
+    for (int q = 0; q < nplanes; ++q)
+      phys_to_four_plane(O, phys + pp * q, (cplx *)spec + ns * q, &w);
+    pwork_free(&w);
+  }
+  return 0;
+}
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}

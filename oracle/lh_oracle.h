@@ -1,0 +1,20 @@
+/* lh_oracle.h — CPU FP64 restatement of the reference RK3 substep.
+ * TEST INFRASTRUCTURE ONLY: used by tests/, smoke() and bench.py's CPU-baseline leg
+ * as the checker; never by the product path. */
+#ifndef LH_ORACLE_H
+#define LH_ORACLE_H
+#include "../include/lh.h"
+typedef struct orc orc;
+orc *orc_create(const lh_config *cfg);
+void orc_destroy(orc *O);
+int orc_set_state(orc *O, const double *u1, const double *u2, const double *u3, const double *p);
+int orc_get_state(orc *O, double *u1, double *u2, double *u3, double *p);
+int orc_get_nonlinear(orc *O, double *n1, double *n2, double *n3);
+int orc_set_scalars(orc *O, const lh_scalars *s);
+int orc_get_scalars(orc *O, lh_scalars *s);
+int orc_substep(orc *O, int kRK);
+int orc_step(orc *O);
+int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes);
+int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes);
+int orc_set_threads(int n);
+#endif

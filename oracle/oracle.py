@@ -1,0 +1,129 @@
+"""ctypes wrapper of the CPU oracle (liblh_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from rnl_multiblock_nofft_gb300.abi import LhScalars, cfield_shape, make_config
+from rnl_multiblock_nofft_gb300.setup_grid import ChannelSetup
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "liblh_oracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(_HERE, "lh_oracle.c")
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "liblh_oracle.so"],
+                       check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB)
+        vp, dp = C.c_void_p, C.POINTER(C.c_double)
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [vp]
+        L.orc_destroy.argtypes = [vp]
+        for f in ("orc_set_state", "orc_get_state", "orc_get_nonlinear"):
+            getattr(L, f).argtypes = [vp] + [dp] * (4 if f != "orc_get_nonlinear" else 3)
+        L.orc_set_scalars.argtypes = [vp, vp]
+        L.orc_get_scalars.argtypes = [vp, vp]
+        L.orc_substep.argtypes = [vp, C.c_int]
+        L.orc_step.argtypes = [vp]
+        L.orc_four_to_phys.argtypes = [vp, dp, dp, C.c_int]
+        L.orc_phys_to_four.argtypes = [vp, dp, dp, C.c_int]
+        L.orc_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+class Oracle:
+    """One channel on the CPU oracle. State arrays use the host cfield layout
+    (complex128 [ncols, nlevels])."""
+
+    def __init__(self, setup: ChannelSetup, threads: int = 0):
+        self.s = setup
+        L = lib()
+        if threads:
+            L.orc_set_threads(threads)
+        cfg, self._keep = make_config(setup)
+        self._cfg = cfg
+        self.h = L.orc_create(C.byref(cfg))
+        if not self.h:
+            raise RuntimeError("orc_create failed")
+        self.shapes = cfield_shape(setup)
+
+    def close(self):
+        if self.h:
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_state(self, u1, u2, u3, p):
+        arrs = [np.ascontiguousarray(a, np.complex128) if a is not None else None for a in (u1, u2, u3, p)]
+        for a, sh in zip(arrs, self.shapes):
+            if a is not None and a.shape != sh:
+                raise ValueError(f"shape {a.shape} != {sh}")
+        lib().orc_set_state(self.h, *[_dptr(a) for a in arrs])
+
+    def get_state(self):
+        out = [np.zeros(sh, np.complex128) for sh in self.shapes]
+        lib().orc_get_state(self.h, *[_dptr(a) for a in out])
+        return out
+
+    def get_nonlinear(self):
+        sh = (self.shapes[0], self.shapes[1], self.shapes[2])
+        out = [np.zeros(x, np.complex128) for x in sh]
+        lib().orc_get_nonlinear(self.h, *[_dptr(a) for a in out])
+        return out
+
+    def set_scalars(self, **kw):
+        s = LhScalars()
+        for k, v in kw.items():
+            setattr(s, k, v)
+        lib().orc_set_scalars(self.h, C.byref(s))
+
+    def scalars(self) -> dict:
+        s = LhScalars()
+        lib().orc_get_scalars(self.h, C.byref(s))
+        return s.as_dict()
+
+    def substep(self, kRK: int):
+        if lib().orc_substep(self.h, kRK) != 0:
+            raise RuntimeError("orc_substep failed")
+
+    def step(self, n: int = 1):
+        for _ in range(n):
+            if lib().orc_step(self.h) != 0:
+                raise RuntimeError("orc_step failed")
+
+    def four_to_phys(self, spec: np.ndarray) -> np.ndarray:
+        spec = np.ascontiguousarray(spec, np.complex128)
+        npl = spec.shape[0]
+        phys = np.zeros((npl, self.s.G2, self.s.G1))
+        lib().orc_four_to_phys(self.h, _dptr(spec.view(np.float64)), _dptr(phys), npl)
+        return phys
+
+    def phys_to_four(self, phys: np.ndarray) -> np.ndarray:
+        phys = np.ascontiguousarray(phys, np.float64)
+        npl = phys.shape[0]
+        spec = np.zeros((npl, self.s.N2, self.s.N1 // 2 + 1), np.complex128)
+        lib().orc_phys_to_four(self.h, _dptr(phys), _dptr(spec.view(np.float64)), npl)
+        return spec

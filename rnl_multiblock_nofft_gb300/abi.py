@@ -1,0 +1,108 @@
+"""ctypes mirror of include/lh.h (`lh_config`, `lh_scalars`) and the packing of a
+ChannelSetup into an `lh_config`."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .setup_grid import UGRID, VGRID, ChannelSetup
+
+LH_ABI_VERSION = 1
+LH_OK, LH_EINVAL, LH_ENONFINITE, LH_ETIMEOUT, LH_ECUDA, LH_ENOMEM = 0, -1, -2, -3, -4, -5
+LH_PREC_FP64, LH_PREC_MIXED = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class LhConfig(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32), ("precision", C.c_int32),
+        ("N1", C.c_int32), ("N2", C.c_int32), ("Ngal1", C.c_int32), ("Ngal2", C.c_int32),
+        ("dny", C.c_int32), ("nn", C.c_int32),
+        ("N3", C.c_int32 * 4), ("N4", C.c_int32 * 4),
+        ("nyu", C.c_int32), ("nyv", C.c_int32),
+        ("yu", _dp), ("yv", _dp), ("dthdyu", _dp), ("dthdyv", _dp),
+        ("dyu2i", _dp), ("dyv2i", _dp), ("k1x", _dp), ("k2x", _dp), ("k1z", _dp), ("k2z", _dp),
+        ("Re", C.c_double), ("CFL", C.c_double), ("dtv", C.c_double), ("ddthetavi", C.c_double),
+        ("dthetavi", C.c_double), ("alp", C.c_double), ("bet", C.c_double), ("Kib", C.c_double),
+        ("aRK", C.c_double * 3), ("bRK", C.c_double * 3), ("cRK", C.c_double * 3),
+        ("dRK", C.c_double * 3), ("gRK", C.c_double * 3),
+        ("gw", (C.c_double * 2) * 3), ("gw_interp", (C.c_double * 2) * 3),
+        ("gw_bc_u1", C.c_double), ("gw_bc_u3", C.c_double),
+        ("flag_ctpress", C.c_int32), ("ib_enable", C.c_int32),
+        ("nib_u", C.c_int32), ("nib_v", C.c_int32),
+        ("list_ib_u", _ip), ("list_ib_v", _ip), ("A_ib_u", _dp), ("A_ib_v", _dp),
+    ]
+
+
+class LhScalars(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("dti", C.c_double), ("dtc", C.c_double),
+                ("err", C.c_double), ("mpgx", C.c_double), ("QxT", C.c_double), ("Qx", C.c_double),
+                ("iter", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def _ptr(a: np.ndarray, typ):
+    return a.ctypes.data_as(typ)
+
+
+def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64):
+    """Returns (LhConfig, keepalive) for a single-resolution channel."""
+    if s.multiblock:
+        raise ValueError("bands with different x/z resolution are not supported by this build")
+    keep = []
+
+    def d(a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        return _ptr(a, _dp)
+
+    def i32(a):
+        a = np.ascontiguousarray(a, dtype=np.int32)
+        keep.append(a)
+        return _ptr(a, _ip)
+
+    c = LhConfig()
+    c.abi_version = LH_ABI_VERSION
+    c.precision = precision
+    c.N1, c.N2 = s.N1, s.N2
+    c.Ngal1, c.Ngal2 = s.G1, s.G2
+    c.dny, c.nn = s.dny, s.nn
+    for b in range(4):
+        c.N3[b] = int(s.N[2, b])
+        c.N4[b] = int(s.N[3, b])
+    c.nyu, c.nyv = s.nyu, s.nyv
+    c.yu, c.yv, c.dthdyu, c.dthdyv = d(s.yu), d(s.yv), d(s.dthdyu), d(s.dthdyv)
+    c.dyu2i, c.dyv2i = d(s.dyu2i), d(s.dyv2i)
+    c.k1x, c.k2x, c.k1z, c.k2z = d(s.k1x), d(s.k2x), d(s.k1z), d(s.k2z)
+    p = s.p
+    c.Re, c.CFL, c.dtv = p.Re, p.CFL, s.dtv
+    c.ddthetavi = s.ddthetavi
+    c.dthetavi = 0.0   # never assigned in the reference (declaration.f90:76); see dtc_calc
+    c.alp, c.bet, c.Kib = p.alp, p.bet, p.Kib
+    for k in range(3):
+        c.aRK[k], c.bRK[k], c.cRK[k] = s.aRK[k], s.bRK[k], s.cRK[k]
+        c.dRK[k], c.gRK[k] = s.dRK[k], s.gRK[k]
+    for b in range(3):
+        for e in range(2):
+            c.gw[b][e] = s.gw[b, e]
+            c.gw_interp[b][e] = s.gw_interp[b, e]
+    c.gw_bc_u1, c.gw_bc_u3 = s.gw_bc_u1, s.gw_bc_u3
+    c.flag_ctpress = p.flpress
+    c.ib_enable = int(bool(p.ib_enable) and p.geometry_type == 2 and s.dny > 0)
+    lu, lv = s.list_ib[UGRID], s.list_ib[VGRID]
+    c.nib_u, c.nib_v = len(lu), len(lv)
+    c.list_ib_u = i32(lu.reshape(-1) if len(lu) else np.zeros(6, np.int32))
+    c.list_ib_v = i32(lv.reshape(-1) if len(lv) else np.zeros(6, np.int32))
+    c.A_ib_u = d(s.A_ib[UGRID] if len(lu) else np.zeros(1))
+    c.A_ib_v = d(s.A_ib[VGRID] if len(lv) else np.zeros(1))
+    return c, keep
+
+
+def cfield_shape(s: ChannelSetup):
+    """Host cfield shapes (ncols, nlevels) of u1, u2, u3, p."""
+    return ((s.ncols, s.nyu), (s.ncols, s.nyv), (s.ncols, s.nyu), (s.ncols, s.nyu - 2))

@@ -1,0 +1,589 @@
+// lh_capi.cu — the C ABI of include/lh.h: one handle = one channel on one GPU.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "lh_internal.cuh"
+
+#include "lh_kernels.cuh"
+
+namespace {
+const int NTHR_H = 256;
+const size_t SMEM_BUDGET = 98304;  // two blocks per SM
+}
+
+struct lh_handle {
+  lh_config cfg;
+  std::vector<double> h_yu, h_yv, h_thu, h_thv, h_d2u, h_d2v, h_k1x, h_k2x, h_k1z, h_k2z;
+  std::vector<int> h_lu, h_lv;
+  std::vector<double> h_Au, h_Av;
+  Geo g;
+  int prec;  // LH_PREC_*
+  size_t vsz;  // bytes of one complex value in the transforms
+  RadixPlan px, pz;
+  int KBz, PBx, KBf, KBs, PBs;
+  cudaStream_t st;
+  // device buffers
+  double2 *u1, *u2, *u3, *p, *Nu1, *Nu2, *Nu3, *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf, *psi;
+  double *a3s, *mfw;
+  void *A, *B, *twx, *twz, *twx64, *twz64;
+  size_t Abytes, Bbytes;
+  long long graph_nodes_per_step;
+  double *geo_pool;
+  DevScalars *sc;
+  double2 *stage;  // staging for transposes
+  // immersed boundaries
+  int ib, nib, ncap;
+  int *d_lu, *d_lv, *d_capslot, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
+  double *d_Au, *d_Av, *cap, *duphys;
+  double2 *duib;
+  cudaGraph_t graph;
+  cudaGraphExec_t gexec;
+  bool graph_ready;
+  long long launches;
+  std::string err;
+};
+
+static int fail(lh_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                            \
+  do {                                                                                      \
+    cudaError_t e__ = (call);                                                               \
+    if (e__ != cudaSuccess)                                                                 \
+      return fail(h, LH_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e__));        \
+  } while (0)
+
+static bool make_plan(int n, RadixPlan &P) {
+  P.n = n;
+  P.nst = 0;
+  int m = n;
+  while (m % 4 == 0) { P.rad[P.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { P.rad[P.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { P.rad[P.nst++] = 3; m /= 3; }
+  return m == 1 && P.nst <= LH_MAX_STAGES;
+}
+
+template <typename T>
+static void twiddles(int n, std::vector<T> &out) {
+  out.resize(2 * (size_t)n);
+  for (int e = 0; e < n; ++e) {
+    long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)e / (long double)n;
+    out[2 * e] = (T)cosl(a);
+    out[2 * e + 1] = (T)sinl(a);
+  }
+}
+
+template <typename T>
+static void *upload_vec(const std::vector<T> &v, cudaError_t &err) {
+  void *d = nullptr;
+  err = cudaMalloc(&d, sizeof(T) * (v.size() ? v.size() : 1));
+  if (err == cudaSuccess && v.size()) err = cudaMemcpy(d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
+  return d;
+}
+
+static int count_launch(lh_handle *h) {
+  h->launches++;
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return LH_OK;
+}
+#define LAUNCHED()                    \
+  do {                                \
+    int rc__ = count_launch(h);       \
+    if (rc__ != LH_OK) return rc__;   \
+  } while (0)
+
+template <typename T>
+static int set_smem_attrs(lh_handle *h) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  int lim = optin > 0 ? optin : 49152;
+  CK(cudaFuncSetAttribute((const void *)k_zinv_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  CK(cudaFuncSetAttribute((const void *)k_xpass_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  CK(cudaFuncSetAttribute((const void *)k_zfwd_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  return LH_OK;
+}
+static int set_smem_attrs_generic(lh_handle *h) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  int lim = optin > 0 ? optin : 49152;
+  CK(cudaFuncSetAttribute((const void *)k_spec_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  CK(cudaFuncSetAttribute((const void *)k_xinv_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  CK(cudaFuncSetAttribute((const void *)k_xfwd_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  CK(cudaFuncSetAttribute((const void *)k_zfwd_spec<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+  return LH_OK;
+}
+
+static int clampi(long v, int lo, int hi) { return (int)(v < lo ? lo : (v > hi ? hi : v)); }
+
+extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
+  lh_handle *h = nullptr;
+  if (!cfg || !out) return LH_EINVAL;
+  *out = nullptr;
+  if (cfg->abi_version != LH_ABI_VERSION) return LH_EINVAL;
+  if (cfg->precision != LH_PREC_FP64 && cfg->precision != LH_PREC_MIXED) return LH_EINVAL;
+  if (cfg->N1 <= 0 || cfg->N2 <= 0 || (cfg->N1 & 1) || (cfg->N2 & 1) || cfg->Ngal1 <= cfg->N1 ||
+      cfg->Ngal2 <= cfg->N2 || (cfg->Ngal1 & 1) || (cfg->Ngal2 & 1) || cfg->dny < 0)
+    return LH_EINVAL;
+  if (cfg->nyu != cfg->N4[3] + 1 - cfg->N4[0] + 1 || cfg->nyv != cfg->N3[3] + 1 - cfg->N3[0] + 1 ||
+      cfg->nyv != cfg->nyu - 1 || cfg->N4[0] != -cfg->dny || cfg->N3[0] != -cfg->dny || cfg->nyu < 5)
+    return LH_EINVAL;
+  h = new lh_handle();
+  memset(&h->g, 0, sizeof(Geo));
+  h->cfg = *cfg;
+  h->prec = cfg->precision;
+  h->vsz = (h->prec == LH_PREC_FP64) ? sizeof(double2) : sizeof(float2);
+  h->graph_ready = false;
+  h->launches = 0;
+  RadixPlan px, pz;
+  if (!make_plan(cfg->Ngal1, px) || !make_plan(cfg->Ngal2, pz)) {
+    int rc = fail(h, LH_EINVAL, "Ngal must factor into 2, 3 and 4");
+    delete h;
+    return rc;
+  }
+  h->px = px;
+  h->pz = pz;
+  Geo &g = h->g;
+  g.N1 = cfg->N1; g.N2 = cfg->N2; g.N1h = cfg->N1 / 2 + 1; g.G1 = cfg->Ngal1; g.G2 = cfg->Ngal2;
+  g.dny = cfg->dny; g.nu = cfg->nyu; g.nv = cfg->nyv; g.np = cfg->nyu - 2; g.ncol = g.N1h * g.N2;
+  g.nuI = g.nu - 2; g.nvI = g.nv - 2; g.nn = cfg->nn;
+  for (int b = 0; b < 4; ++b) { g.N3[b] = cfg->N3[b]; g.N4[b] = cfg->N4[b]; }
+  g.Re = cfg->Re; g.CFL = cfg->CFL; g.dtv = cfg->dtv; g.dd = cfg->ddthetavi; g.dthetavi = cfg->dthetavi;
+  g.alp = cfg->alp; g.bet = cfg->bet; g.Kib = cfg->Kib;
+  for (int k = 0; k < 3; ++k) {
+    g.aRK[k] = cfg->aRK[k]; g.bRK[k] = cfg->bRK[k]; g.cRK[k] = cfg->cRK[k]; g.dRK[k] = cfg->dRK[k]; g.gRK[k] = cfg->gRK[k];
+  }
+  for (int b = 0; b < 3; ++b) { g.gw[b][0] = cfg->gw[b][0]; g.gw[b][1] = cfg->gw[b][1]; }
+  g.gwbc1 = cfg->gw_bc_u1; g.gwbc3 = cfg->gw_bc_u3;
+  g.flag_ctpress = cfg->flag_ctpress;
+  const int nu = g.nu, nv = g.nv;
+  // geometry pool: yu yv thu thv d2u(3nu) d2v(3nv) k1x k2x k1z k2z iua iub iud iva ivb ivd
+  std::vector<double> pool;
+  auto put = [&](const double *src, size_t n) { size_t o = pool.size(); pool.insert(pool.end(), src, src + n); return o; };
+  std::vector<double> iua(nu, 1.0), iub(nu, 0.0), iud(nu, 1.0), iva(nv, 1.0), ivb(nv, 0.0), ivd(nv, 1.0);
+  for (int q = 1; q <= nu - 2; ++q) {
+    iua[q] = cfg->yu[q] - cfg->yv[q - 1];
+    iub[q] = cfg->yv[q] - cfg->yu[q];
+    iud[q] = cfg->yv[q] - cfg->yv[q - 1];
+  }
+  for (int q = 0; q <= nv - 1; ++q) {
+    iva[q] = cfg->yv[q] - cfg->yu[q];
+    ivb[q] = cfg->yu[q + 1] - cfg->yv[q];
+    ivd[q] = cfg->yu[q + 1] - cfg->yu[q];
+  }
+  size_t o_yu = put(cfg->yu, nu), o_yv = put(cfg->yv, nv), o_thu = put(cfg->dthdyu, nu), o_thv = put(cfg->dthdyv, nv);
+  size_t o_d2u = put(cfg->dyu2i, 3 * (size_t)nu), o_d2v = put(cfg->dyv2i, 3 * (size_t)nv);
+  size_t o_k1x = put(cfg->k1x, g.N1h), o_k2x = put(cfg->k2x, g.N1h), o_k1z = put(cfg->k1z, g.N2), o_k2z = put(cfg->k2z, g.N2);
+  size_t o_iua = put(iua.data(), nu), o_iub = put(iub.data(), nu), o_iud = put(iud.data(), nu);
+  size_t o_iva = put(iva.data(), nv), o_ivb = put(ivb.data(), nv), o_ivd = put(ivd.data(), nv);
+  cudaError_t ce;
+  h->geo_pool = (double *)upload_vec(pool, ce);
+  if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+  double *P = h->geo_pool;
+  g.yu = P + o_yu; g.yv = P + o_yv; g.thu = P + o_thu; g.thv = P + o_thv; g.d2u = P + o_d2u; g.d2v = P + o_d2v;
+  g.k1x = P + o_k1x; g.k2x = P + o_k2x; g.k1z = P + o_k1z; g.k2z = P + o_k2z;
+  g.iua = P + o_iua; g.iub = P + o_iub; g.iud = P + o_iud; g.iva = P + o_iva; g.ivb = P + o_ivb; g.ivd = P + o_ivd;
+
+  // transform tiling from the shared-memory budget
+  const size_t vs = h->vsz;
+  h->KBz = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * vs)), 1, g.N1h < 16 ? g.N1h : 16);
+  h->PBx = clampi((long)(SMEM_BUDGET / (8 * (size_t)g.G1 * vs)), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
+  h->KBf = clampi((long)(SMEM_BUDGET / (8 * (size_t)g.G2 * vs)), 1, g.N1h < 8 ? g.N1h : 8);
+  h->KBs = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * sizeof(double2))), 1, g.N1h < 16 ? g.N1h : 16);
+  h->PBs = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G1 * sizeof(double2))), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
+
+  size_t nc = g.ncol;
+  auto zalloc = [&](void **ptr, size_t bytes) -> cudaError_t {
+    cudaError_t e = cudaMalloc(ptr, bytes ? bytes : 16);
+    if (e == cudaSuccess) e = cudaMemset(*ptr, 0, bytes ? bytes : 16);
+    return e;
+  };
+#define ZA(ptr, bytes)                                                                       \
+  do {                                                                                       \
+    cudaError_t e__ = zalloc((void **)&(ptr), (bytes));                                      \
+    if (e__ != cudaSuccess) {                                                                \
+      int rc__ = fail(h, e__ == cudaErrorMemoryAllocation ? LH_ENOMEM : LH_ECUDA,            \
+                      std::string("cudaMalloc: ") + cudaGetErrorString(e__));                \
+      lh_destroy(h);                                                                         \
+      return rc__;                                                                           \
+    }                                                                                        \
+  } while (0)
+  const size_t cz = sizeof(double2);
+  ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
+  ZA(h->Nu1, cz * nu * nc); ZA(h->Nu3, cz * nu * nc); ZA(h->Nu2, cz * nv * nc);
+  ZA(h->N1xz, cz * nu * nc); ZA(h->N3xz, cz * nu * nc); ZA(h->vvc, cz * nu * nc);
+  ZA(h->N2xz, cz * nv * nc); ZA(h->uvf, cz * nv * nc); ZA(h->wvf, cz * nv * nc);
+  ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
+  ZA(h->mfw, sizeof(double) * 4 * (size_t)(g.nn + 3));
+  h->Abytes = vs * (size_t)(g.nuI + g.nvI) * 3 * g.G2 * g.N1h;
+  h->Bbytes = vs * (size_t)(4 * g.nuI + 2 * g.nvI) * g.N1h * g.G2;
+  ZA(h->A, h->Abytes);
+  ZA(h->B, h->Bbytes);
+  ZA(h->sc, sizeof(DevScalars));
+  ZA(h->stage, cz * nu * nc);
+  {
+    if (h->prec == LH_PREC_FP64) {
+      std::vector<double> tx, tz;
+      twiddles(g.G1, tx); twiddles(g.G2, tz);
+      h->twx = upload_vec(tx, ce); if (ce == cudaSuccess) h->twz = upload_vec(tz, ce);
+    } else {
+      std::vector<float> tx, tz;
+      twiddles(g.G1, tx); twiddles(g.G2, tz);
+      h->twx = upload_vec(tx, ce); if (ce == cudaSuccess) h->twz = upload_vec(tz, ce);
+    }
+    if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+  }
+  {  // FP64 twiddles for the leaves and the immersed-boundary round trip
+    std::vector<double> tx, tz;
+    twiddles(g.G1, tx); twiddles(g.G2, tz);
+    h->twx64 = upload_vec(tx, ce); if (ce == cudaSuccess) h->twz64 = upload_vec(tz, ce);
+    if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+  }
+  // immersed boundaries
+  h->ib = (cfg->ib_enable && cfg->dny > 0) ? 1 : 0;
+  h->nib = 0; h->ncap = 0;
+  h->d_lu = h->d_lv = h->d_capslot = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
+  h->d_Au = h->d_Av = h->cap = h->duphys = nullptr;
+  h->duib = nullptr;
+  if (h->ib) {
+    const int d = cfg->dny;
+    h->nib = 2 * d;
+    std::vector<int> iblev(2 * h->nib), ibslot_u(nu, -1), ibslot_v(nv, -1);
+    for (int s = 0; s < h->nib; ++s) {
+      int qu = (s < d) ? 1 + s : nu - 1 - d + (s - d);
+      int qv = (s < d) ? 1 + s : nv - 1 - d + (s - d);
+      iblev[2 * s] = qu; iblev[2 * s + 1] = qv;
+      ibslot_u[qu] = s; ibslot_v[qv] = s;
+    }
+    // captured levels: u ib levels + the two tip reference levels; v ib levels
+    std::vector<int> capslot(g.nuI + g.nvI, -1), lev2cap_u(nu, -1), lev2cap_v(nv, -1);
+    int nc2 = 0;
+    for (int q = 1; q <= nu - 2; ++q) {
+      bool need = ibslot_u[q] >= 0 || q == d + 1 || q == cfg->nn + 1 + d;
+      if (need) { capslot[q - 1] = nc2; lev2cap_u[q] = nc2; ++nc2; }
+    }
+    for (int q = 1; q <= nv - 2; ++q)
+      if (ibslot_v[q] >= 0) { capslot[g.nuI + q - 1] = nc2; lev2cap_v[q] = nc2; ++nc2; }
+    h->ncap = nc2;
+    std::vector<int> lu(cfg->list_ib_u, cfg->list_ib_u + 6 * (size_t)cfg->nib_u);
+    std::vector<int> lv(cfg->list_ib_v, cfg->list_ib_v + 6 * (size_t)cfg->nib_v);
+    // validate list indices against the plane and the level ranges
+    for (size_t e = 0; e < lu.size() / 6; ++e) {
+      const int *L = &lu[6 * e];
+      if (L[0] < 1 || L[0] > g.G1 || L[1] < 1 || L[1] > g.G2 || L[3] < 1 || L[3] > g.G1 || L[4] < 1 || L[4] > g.G2 ||
+          L[2] + d < 0 || L[2] + d >= nu || L[5] + d < 0 || L[5] + d >= nu) {
+        int rc = fail(h, LH_EINVAL, "immersed-boundary u list index out of range"); lh_destroy(h); return rc;
+      }
+    }
+    for (size_t e = 0; e < lv.size() / 6; ++e) {
+      const int *L = &lv[6 * e];
+      if (L[0] < 1 || L[0] > g.G1 || L[1] < 1 || L[1] > g.G2 || L[3] < 1 || L[3] > g.G1 || L[4] < 1 || L[4] > g.G2 ||
+          L[2] + d < 0 || L[2] + d >= nv || L[5] + d < 0 || L[5] + d >= nv) {
+        int rc = fail(h, LH_EINVAL, "immersed-boundary v list index out of range"); lh_destroy(h); return rc;
+      }
+    }
+    std::vector<double> Au(cfg->A_ib_u, cfg->A_ib_u + cfg->nib_u), Av(cfg->A_ib_v, cfg->A_ib_v + cfg->nib_v);
+    h->d_lu = (int *)upload_vec(lu, ce); h->d_lv = (int *)upload_vec(lv, ce);
+    h->d_Au = (double *)upload_vec(Au, ce); h->d_Av = (double *)upload_vec(Av, ce);
+    h->d_capslot = (int *)upload_vec(capslot, ce);
+    h->d_ibslot_u = (int *)upload_vec(ibslot_u, ce); h->d_ibslot_v = (int *)upload_vec(ibslot_v, ce);
+    h->d_iblev = (int *)upload_vec(iblev, ce);
+    h->d_lev2cap_u = (int *)upload_vec(lev2cap_u, ce); h->d_lev2cap_v = (int *)upload_vec(lev2cap_v, ce);
+    if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+    const size_t pp = (size_t)g.G1 * g.G2;
+    ZA(h->cap, sizeof(double) * (size_t)h->ncap * 3 * pp);
+    ZA(h->duphys, sizeof(double) * (size_t)h->nib * 3 * pp);
+    ZA(h->duib, cz * (size_t)h->nib * 3 * nc);
+  }
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+    int rc = fail(h, LH_ECUDA, "cudaStreamCreate"); lh_destroy(h); return rc;
+  }
+  int rc = (h->prec == LH_PREC_FP64) ? set_smem_attrs<double>(h) : set_smem_attrs<float>(h);
+  if (rc == LH_OK) rc = set_smem_attrs_generic(h);
+  if (rc != LH_OK) { lh_destroy(h); return rc; }
+  // keep host copies of the arrays
+  h->h_yu.assign(cfg->yu, cfg->yu + nu);
+  h->h_yv.assign(cfg->yv, cfg->yv + nv);
+  h->cfg.yu = h->h_yu.data(); h->cfg.yv = h->h_yv.data();
+  h->cfg.dthdyu = h->cfg.dthdyv = h->cfg.dyu2i = h->cfg.dyv2i = nullptr;
+  h->cfg.k1x = h->cfg.k2x = h->cfg.k1z = h->cfg.k2z = nullptr;
+  h->cfg.list_ib_u = h->cfg.list_ib_v = nullptr;
+  h->cfg.A_ib_u = h->cfg.A_ib_v = nullptr;
+  *out = h;
+  return LH_OK;
+}
+
+extern "C" int lh_destroy(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
+  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
+                  h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->sc, h->stage,
+                  h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
+                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return LH_OK;
+}
+
+extern "C" const char *lh_last_error(lh_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" void *lh_stream(lh_handle *h) { return h ? (void *)h->st : nullptr; }
+
+extern "C" int64_t lh_kernel_launches(lh_handle *h) { return h ? h->launches : -1; }
+
+extern "C" int lh_device_state(lh_handle *h, void **u1, void **u2, void **u3, void **p) {
+  if (!h) return LH_EINVAL;
+  if (u1) *u1 = h->u1;
+  if (u2) *u2 = h->u2;
+  if (u3) *u3 = h->u3;
+  if (p) *p = h->p;
+  return LH_OK;
+}
+
+// host [col][lev] -> device [lev][col]
+static int put_field(lh_handle *h, double2 *dst, int nlev, const double *src) {
+  const int nc = h->g.ncol;
+  CK(cudaMemcpyAsync(h->stage, src, sizeof(double2) * (size_t)nc * nlev, cudaMemcpyHostToDevice, h->st));
+  dim3 grid((nlev + 31) / 32, (nc + 31) / 32), blk(32, 8);
+  k_transpose<<<grid, blk, 0, h->st>>>(h->stage, dst, nc, nlev);
+  LAUNCHED();
+  return LH_OK;
+}
+static int get_field(lh_handle *h, const double2 *srcd, int nlev, double *dst) {
+  const int nc = h->g.ncol;
+  dim3 grid((nc + 31) / 32, (nlev + 31) / 32), blk(32, 8);
+  k_transpose<<<grid, blk, 0, h->st>>>(srcd, h->stage, nlev, nc);
+  LAUNCHED();
+  CK(cudaMemcpyAsync(dst, h->stage, sizeof(double2) * (size_t)nc * nlev, cudaMemcpyDeviceToHost, h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_upload_state(lh_handle *h, const double *u1, const double *u2, const double *u3, const double *p) {
+  if (!h) return LH_EINVAL;
+  int rc;
+  if (u1 && (rc = put_field(h, h->u1, h->g.nu, u1))) return rc;
+  if (u2 && (rc = put_field(h, h->u2, h->g.nv, u2))) return rc;
+  if (u3 && (rc = put_field(h, h->u3, h->g.nu, u3))) return rc;
+  if (p && (rc = put_field(h, h->p, h->g.np, p))) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p) {
+  if (!h) return LH_EINVAL;
+  int rc;
+  if (u1) { if ((rc = get_field(h, h->u1, h->g.nu, u1))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  if (u2) { if ((rc = get_field(h, h->u2, h->g.nv, u2))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  if (u3) { if ((rc = get_field(h, h->u3, h->g.nu, u3))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  if (p) { if ((rc = get_field(h, h->p, h->g.np, p))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  return LH_OK;
+}
+
+extern "C" int lh_set_scalars(lh_handle *h, const lh_scalars *s) {
+  if (!h || !s) return LH_EINVAL;
+  DevScalars d;
+  memset(&d, 0, sizeof(d));
+  d.t = s->t; d.dt = s->dt; d.dti = s->dti; d.dtc = s->dtc; d.err = s->err; d.mpgx = s->mpgx;
+  d.QxT = s->QxT; d.Qx = s->Qx; d.iter = s->iter;
+  CK(cudaMemcpyAsync(h->sc, &d, sizeof(d), cudaMemcpyHostToDevice, h->st));
+  k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, h->g.flag_ctpress != 1 ? 1 : 0);
+  LAUNCHED();
+  const int nb = (h->g.ncol + NTHR_H - 1) / NTHR_H;
+  k_reset_err<<<1, 32, 0, h->st>>>(h->sc);
+  LAUNCHED();
+  k_divmax<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->g, h->sc);
+  LAUNCHED();
+  k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc);
+  LAUNCHED();
+  CK(cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_get_scalars(lh_handle *h, lh_scalars *s) {
+  if (!h || !s) return LH_EINVAL;
+  DevScalars d;
+  CK(cudaMemcpyAsync(&d, h->sc, sizeof(d), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  s->t = d.t; s->dt = d.dt; s->dti = d.dti; s->dtc = d.dtc; s->err = d.err; s->mpgx = d.mpgx;
+  s->QxT = d.QxT; s->Qx = d.Qx; s->iter = d.iter;
+  return LH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one substep
+// ---------------------------------------------------------------------------
+template <typename T>
+static int nonlinear_transforms(lh_handle *h, int kRK) {
+  typedef typename C2<T>::t V;
+  const Geo &g = h->g;
+  const size_t vs = sizeof(V);
+  const int nslots = g.nuI + g.nvI;
+  if (kRK == 1) { k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc); LAUNCHED(); }
+  {
+    dim3 grid((g.N1h + h->KBz - 1) / h->KBz, nslots, 3);
+    size_t sm = 2 * (size_t)h->KBz * g.G2 * vs;
+    k_zinv_nl<T><<<grid, NTHR_H, sm, h->st>>>(h->u1, h->u2, h->u3, (V *)h->A, g, h->pz, (const V *)h->twz, h->KBz);
+    LAUNCHED();
+  }
+  {
+    dim3 grid((g.G2 / 2 + h->PBx - 1) / h->PBx, nslots);
+    size_t sm = 8 * (size_t)h->PBx * g.G1 * vs;
+    k_xpass_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->A, (V *)h->B, g, h->px, (const V *)h->twx, h->PBx,
+                                                kRK == 1 ? 1 : 0, h->sc, h->ib ? h->d_capslot : nullptr, h->cap);
+    LAUNCHED();
+  }
+  {
+    dim3 grid((g.N1h + h->KBf - 1) / h->KBf, nslots);
+    size_t sm = 8 * (size_t)h->KBf * g.G2 * vs;
+    k_zfwd_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->B, g, h->pz, (const V *)h->twz, h->KBf, h->N1xz, h->N2xz,
+                                               h->N3xz, h->uvf, h->vvc, h->wvf);
+    LAUNCHED();
+  }
+  return LH_OK;
+}
+
+// FP64 plane transforms through the scratch buffers (leaves and immersed boundaries)
+static int spec_to_phys(lh_handle *h, const double2 *spec, double *phys, int npl, double2 *Ascr, const double2 *twx,
+                        const double2 *twz) {
+  const Geo &g = h->g;
+  dim3 g1((g.N1h + h->KBs - 1) / h->KBs, npl);
+  k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(spec, Ascr, g, h->pz, twz, h->KBs);
+  LAUNCHED();
+  dim3 g2((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
+  k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(Ascr, phys, g, h->px, twx, h->PBs);
+  LAUNCHED();
+  return LH_OK;
+}
+static int phys_to_spec(lh_handle *h, const double *phys, double2 *spec, int npl, double2 *Bscr, const double2 *twx,
+                        const double2 *twz) {
+  const Geo &g = h->g;
+  dim3 g1((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
+  k_xfwd_phys<double><<<g1, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(phys, Bscr, g, h->px, twx, h->PBs);
+  LAUNCHED();
+  dim3 g2((g.N1h + h->KBs - 1) / h->KBs, npl);
+  k_zfwd_spec<double><<<g2, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(Bscr, spec, g, h->pz, twz, h->KBs, nullptr);
+  LAUNCHED();
+  return LH_OK;
+}
+
+static const double2 *fp64_tw(lh_handle *h, bool x) { return (const double2 *)(x ? h->twx64 : h->twz64); }
+
+static int substep_launches(lh_handle *h, int kRK) {
+  const Geo &g = h->g;
+  int rc = (h->prec == LH_PREC_FP64) ? nonlinear_transforms<double>(h, kRK) : nonlinear_transforms<float>(h, kRK);
+  if (rc) return rc;
+  if (kRK == 1) { k_dt<<<1, 32, 0, h->st>>>(g, h->sc); LAUNCHED(); }
+  const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
+  if (h->ib) {
+    dim3 gd(nb, h->nib);
+    k_ib_du<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf,
+                                       h->vvc, h->wvf, h->p, h->duib, h->d_iblev, h->nib, g, h->sc, kRK);
+    LAUNCHED();
+    const double2 *twx = fp64_tw(h, true), *twz = fp64_tw(h, false);
+    if ((rc = spec_to_phys(h, h->duib, h->duphys, 3 * h->nib, (double2 *)h->A, twx, twz))) return rc;
+    int ibu = (h->cfg.nib_u + 255) / 256, ibv = (h->cfg.nib_v + 255) / 256;
+    if (h->cfg.nib_u > 0) {
+      k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1, h->d_ibslot_u,
+                                         h->d_lev2cap_u, g, h->sc);
+      LAUNCHED();
+    }
+    if (h->cfg.nib_v > 0) {
+      k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0, h->d_ibslot_v,
+                                         h->d_lev2cap_v, g, h->sc);
+      LAUNCHED();
+    }
+    if ((rc = phys_to_spec(h, h->duphys, h->duib, 3 * h->nib, (double2 *)h->B, twx, twz))) return rc;
+  }
+  k_helm_uw<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, h->N1xz, h->N3xz, h->uvf, h->wvf, h->p, h->a3s, g,
+                                      h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib);
+  LAUNCHED();
+  k_helm_v<<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, h->N2xz, h->vvc, h->p, h->a3s, g, h->sc, kRK,
+                                     h->ib ? h->d_ibslot_v : nullptr, h->duib);
+  LAUNCHED();
+  if (g.flag_ctpress == 0) { k_meanflow<<<1, 32, 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw); LAUNCHED(); }
+  k_reset_err<<<1, 32, 0, h->st>>>(h->sc);
+  LAUNCHED();
+  k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->a3s, g, h->sc, kRK);
+  LAUNCHED();
+  k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc);
+  LAUNCHED();
+  return LH_OK;
+}
+
+
+extern "C" int lh_substep(lh_handle *h, int kRK) {
+  if (!h) return LH_EINVAL;
+  if (kRK < 1 || kRK > 3) return fail(h, LH_EINVAL, "kRK must be 1, 2 or 3");
+  return substep_launches(h, kRK);
+}
+
+static int step_launches(lh_handle *h) {
+  int rc;
+  for (int k = 1; k <= 3; ++k)
+    if ((rc = substep_launches(h, k))) return rc;
+  if (h->g.flag_ctpress == 1) { k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, 0); LAUNCHED(); }
+  k_step_end<<<1, 32, 0, h->st>>>(h->sc);
+  LAUNCHED();
+  return LH_OK;
+}
+
+extern "C" int lh_step(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  if (!h->graph_ready) {
+    // capture once; every later step replays the graph
+    long long before = h->launches;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = step_launches(h);
+    cudaGraph_t gr;
+    cudaError_t e = cudaStreamEndCapture(h->st, &gr);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->gexec, gr, 0);
+    if (e != cudaSuccess) { cudaGraphDestroy(gr); return fail(h, LH_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+    h->graph = gr;
+    h->graph_ready = true;
+    h->launches = before;  // the captured launches run below
+    h->graph_nodes_per_step = 0;
+    size_t n = 0;
+    if (cudaGraphGetNodes(gr, nullptr, &n) == cudaSuccess) h->graph_nodes_per_step = (long long)n;
+  }
+  CK(cudaGraphLaunch(h->gexec, h->st));
+  h->launches += h->graph_nodes_per_step;
+  return LH_OK;
+}
+
+extern "C" int lh_synchronize(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  CK(cudaStreamSynchronize(h->st));
+  int status = 0;
+  CK(cudaMemcpy(&status, &h->sc->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status == LH_ENONFINITE) return fail(h, LH_ENONFINITE, "non-finite state (divergence or dt)");
+  return LH_OK;
+}
+
+extern "C" int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int nplanes) {
+  if (!h || !spec || !phys || nplanes <= 0) return LH_EINVAL;
+  const size_t need = sizeof(double2) * (size_t)nplanes * h->g.G2 * h->g.N1h;
+  if (need > h->Abytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
+  return spec_to_phys(h, (const double2 *)spec, (double *)phys, nplanes, (double2 *)h->A, fp64_tw(h, true), fp64_tw(h, false));
+}
+
+extern "C" int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes) {
+  if (!h || !spec || !phys || nplanes <= 0) return LH_EINVAL;
+  const size_t need = sizeof(double2) * (size_t)nplanes * h->g.G2 * h->g.N1h;
+  if (need > h->Bbytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
+  return phys_to_spec(h, (const double *)phys, (double2 *)spec, nplanes, (double2 *)h->B, fp64_tw(h, true), fp64_tw(h, false));
+}

@@ -1,0 +1,150 @@
+// lh_internal.cuh — device-side data model of one channel and the shared-memory FFT.
+//
+// Layout in HBM: every spectral field is plane-major, complex [level][col] with
+// col = ikz * (N1/2+1) + ikx. A y-level of a field is therefore one spectral x/z
+// plane (what the reference builds with modes_to_planes_*, FOU3D.f90:1000-1098),
+// and for a fixed level consecutive columns are consecutive in memory, so the
+// per-column tridiagonal solves (one thread per column) load coalesced.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lh.h"
+
+#define LH_MAX_STAGES 16
+
+struct RadixPlan {
+  int n;
+  int nst;
+  int rad[LH_MAX_STAGES];
+};
+
+// Geometry and coefficients, passed to kernels by value.
+struct Geo {
+  int N1, N2, N1h, G1, G2, dny, nu, nv, np, ncol, nuI, nvI, nn;
+  int N3[4], N4[4];
+  const double *yu, *yv, *thu, *thv, *d2u, *d2v, *k1x, *k2x, *k1z, *k2z;
+  // stagger interpolation: u-level q (v -> centre): (iua*v[q] + iub*v[q-1]) / iud
+  const double *iua, *iub, *iud;
+  // v-level q (centre -> face): (iva*u[q+1] + ivb*u[q]) / ivd
+  const double *iva, *ivb, *ivd;
+  double Re, CFL, dtv, dd, dthetavi, alp, bet, Kib;
+  double aRK[3], bRK[3], cRK[3], dRK[3], gRK[3];
+  double gw[3][2];
+  double gwbc1, gwbc3;
+  int flag_ctpress;
+};
+
+// Scalars kept on the device (no host round trip inside a step).
+struct DevScalars {
+  double t, dt, dti, dtc, err, mpgx, QxT, Qx;
+  long long iter;
+  unsigned long long u1m, u2m, u3m;  // bit patterns of non-negative doubles (atomicMax)
+  unsigned long long errbits;
+  int status;
+  int pad;
+};
+
+// ---------------------------------------------------------------------------
+// complex helpers (double2 / float2)
+// ---------------------------------------------------------------------------
+template <typename T> struct C2;
+template <> struct C2<double> { typedef double2 t; };
+template <> struct C2<float> { typedef float2 t; };
+
+template <typename V> __device__ __forceinline__ V cadd(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename V> __device__ __forceinline__ V csub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+  V r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename V, typename S> __device__ __forceinline__ V cscale(V a, S s) { V r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename V> __device__ __forceinline__ V cconj(V a) { a.y = -a.y; return a; }
+template <typename V> __device__ __forceinline__ V czero() { V r; r.x = 0; r.y = 0; return r; }
+// i*k*a for a real k: (-k*a.y, k*a.x)
+template <typename V, typename S> __device__ __forceinline__ V cimul(S k, V a) { V r; r.x = -k * a.y; r.y = k * a.x; return r; }
+
+// ---------------------------------------------------------------------------
+// Stockham mixed-radix (2, 3, 4) FFT of `nl` lines of length n held in shared
+// memory, ping-ponging between two buffers. tw[e] = exp(-2 pi i e / n).
+// INV = true: backward (exp(+i)), unscaled. Returns the buffer holding the result.
+// ---------------------------------------------------------------------------
+template <int R, bool INV, typename V>
+__device__ __forceinline__ void dftR(V *v) {
+  if (R == 2) {
+    V a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if (R == 4) {
+    V a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    V a2 = cadd(v[1], v[3]), a3 = csub(v[1], v[3]);
+    V rot;  // forward: -i*a3 = (a3.y, -a3.x); backward: +i*a3 = (-a3.y, a3.x)
+    if (INV) { rot.x = -a3.y; rot.y = a3.x; } else { rot.x = a3.y; rot.y = -a3.x; }
+    v[0] = cadd(a0, a2);
+    v[2] = csub(a0, a2);
+    v[1] = cadd(a1, rot);
+    v[3] = csub(a1, rot);
+  } else if (R == 3) {
+    typedef decltype(v[0].x) S;
+    const S c = (S)-0.5;
+    const S s = (S)0.86602540378443864676372317075294;  // sin(2 pi / 3)
+    V t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    V m = v[0];
+    v[0] = cadd(m, t1);
+    V b; b.x = m.x + c * t1.x; b.y = m.y + c * t1.y;
+    V st;  // forward: -i*s*t2 = (s*t2.y, -s*t2.x)
+    if (INV) { st.x = -s * t2.y; st.y = s * t2.x; } else { st.x = s * t2.y; st.y = -s * t2.x; }
+    v[1] = cadd(b, st);
+    v[2] = csub(b, st);
+  }
+}
+
+template <int R, bool INV, typename V>
+__device__ __forceinline__ void fft_stage(const V *__restrict__ src, V *__restrict__ dst, int n, int nl,
+                                          int Ns, const V *__restrict__ tw) {
+  const int nb = n / R;
+  const int total = nb * nl;
+  const int step = n / (Ns * R);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int line = idx / nb;
+    const int j = idx - line * nb;
+    const V *in = src + line * n;
+    V *out = dst + line * n;
+    const int k = j % Ns;
+    V v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = in[j + t * nb];
+#pragma unroll
+    for (int t = 1; t < R; ++t) {
+      V w = tw[k * step * t];
+      if (INV) w.y = -w.y;
+      v[t] = cmul(v[t], w);
+    }
+    dftR<R, INV>(v);
+    const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int t = 0; t < R; ++t) out[base + t * Ns] = v[t];
+  }
+}
+
+template <bool INV, typename V>
+__device__ V *smem_fft(V *a, V *b, int nl, const RadixPlan &P, const V *__restrict__ tw) {
+  int Ns = 1;
+  for (int s = 0; s < P.nst; ++s) {
+    const int R = P.rad[s];
+    if (R == 4) fft_stage<4, INV>(a, b, P.n, nl, Ns, tw);
+    else if (R == 2) fft_stage<2, INV>(a, b, P.n, nl, Ns, tw);
+    else fft_stage<3, INV>(a, b, P.n, nl, Ns, tw);
+    __syncthreads();
+    V *t = a; a = b; b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+// plane row (physical z index, 0-based) of spectral kz-row r
+__device__ __forceinline__ int prow(const Geo &g, int r) { return r < g.N2 / 2 ? r : r - g.N2 + g.G2; }
+
+// ---------------------------------------------------------------------------
+// kernel launch wrappers (lh_kernels.cu)
+// ---------------------------------------------------------------------------
+struct Work;  // defined in lh_kernels.cu users

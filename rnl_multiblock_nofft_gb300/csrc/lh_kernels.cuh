@@ -1,0 +1,985 @@
+// lh_kernels.cuh — CUDA kernels of the RK3 substep (FP64 plain form; transforms
+// templated on the transform precision).
+//
+// Per substep (littleharsh.f90:174-217):
+//   k_zinv_nl   : stagger interpolation (FOU3D.f90:427-474) fused into the inverse z
+//                 transforms of the six velocity planes of every level (cft, iopt>=0)
+//   k_xpass_nl  : inverse x transforms (rft, iopt>=0), physical products
+//                 (ops_in_planes2, FOU3D.f90:2090-2251), CFL maxima (dtc_calc), forward x
+//                 transforms (rft, iopt<0) of the products
+//   k_zfwd_nl   : forward z transforms (cft, iopt<0) + der_x/der_z (FOU3D.f90:476-593):
+//                 N_xz of u, v, w and the y-flux products uv, vv, wv
+//   k_dt        : dt = min(2.5 dtv, CFL dtc) on the device (FOU3D.f90:291-297)
+//   k_helm_uw   : RHS0_u1/u3 + der_yu_h + du += -gRK N + solveU_W, one thread per column
+//   k_helm_v    : RHS0_u2 + der_yv_h + du += -gRK N + solveV
+//   k_meanflow  : flowrate_corr on mode (0,0) (constant flow rate)
+//   k_press     : divergence + solveP (LUsolP with the factor rebuilt on the fly) + v_corr
+//                 + divergence of the corrected field (max |div| -> err)
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "lh_internal.cuh"
+
+#define NTHR 256
+
+__device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double v) {
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v || isnan((double)w)) ? w : v;
+  }
+  return v;
+}
+
+// ============================================================================
+// T1: inverse z transforms of the velocity planes (with stagger interpolation)
+// grid: x = kx group of KB lines, y = level slot (u-levels then v-levels), z = field
+// A layout: [(slot*3 + f)][l][kx], l = 0..G2-1, kx = 0..N1h-1
+// ============================================================================
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                  const double2 *__restrict__ u3, typename C2<T>::t *__restrict__ A,
+                                                  Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
+                                                  int KB) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + KB * g.G2;
+  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
+  const bool isU = slot < g.nuI;
+  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int nc = g.ncol;
+  for (int i = threadIdx.x; i < KB * g.G2; i += blockDim.x) b0[i] = czero<V>();
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < g.N2 * KB; idx += blockDim.x) {
+    const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
+    if (kx >= g.N1h) continue;
+    const int c = r * g.N1h + kx;
+    double2 val;
+    if (isU) {
+      if (f == 0) val = u1[(size_t)q * nc + c];
+      else if (f == 2) val = u3[(size_t)q * nc + c];
+      else {  // interp_v: v faces -> centre q
+        const double a = g.iua[q], b = g.iub[q], d = g.iud[q];
+        const double2 v0 = u2[(size_t)q * nc + c], vm = u2[(size_t)(q - 1) * nc + c];
+        val.x = (a * v0.x + b * vm.x) / d;
+        val.y = (a * v0.y + b * vm.y) / d;
+      }
+    } else {
+      if (f == 1) val = u2[(size_t)q * nc + c];
+      else {  // interp_u: centres -> face q
+        const double2 *src = (f == 0) ? u1 : u3;
+        const double a = g.iva[q], b = g.ivb[q], d = g.ivd[q];
+        const double2 up = src[(size_t)(q + 1) * nc + c], u0 = src[(size_t)q * nc + c];
+        val.x = (a * up.x + b * u0.x) / d;
+        val.y = (a * up.y + b * u0.y) / d;
+      }
+    }
+    V v;
+    v.x = (T)val.x;
+    v.y = (T)val.y;
+    b0[kk * g.G2 + prow(g, r)] = v;
+  }
+  __syncthreads();
+  V *res = smem_fft<true>(b0, b1, KB, pz, twz);
+  V *dst = A + (size_t)(slot * 3 + f) * g.G2 * g.N1h;
+  for (int idx = threadIdx.x; idx < g.G2 * KB; idx += blockDim.x) {
+    const int l = idx / KB, kk = idx - l * KB, kx = kx0 + kk;
+    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[kk * g.G2 + l];
+  }
+}
+
+// ============================================================================
+// T2: x pass. PB row pairs per block; each pair of rows (l, l+1) of a field is
+// carried by one complex line (row l in .x, row l+1 in .y after the transform).
+// B layout: [pslot][kx][l]; pslot = slot*4 + p (u levels), nuI*4 + (slot-nuI)*2 + p (v).
+// capture (optional): physical velocities of selected levels, [cap][l][m].
+// ============================================================================
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__restrict__ A,
+                                                   typename C2<T>::t *__restrict__ B, Geo g, RadixPlan px,
+                                                   const typename C2<T>::t *__restrict__ twx, int PB, int doCFL,
+                                                   DevScalars *sc, const int *__restrict__ capslot,
+                                                   double *__restrict__ cap) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h, H = G1 / 2;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + 4 * PB * G1;
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const size_t fstride = (size_t)G2 * N1h;
+  const V *Af = A + (size_t)slot * 3 * fstride;
+  // gather Hermitian-completed lines of the 3 fields: line f*PB + pb
+  for (int idx = threadIdx.x; idx < 3 * PB * G1; idx += blockDim.x) {
+    const int line = idx / G1, m = idx - line * G1;
+    const int f = line / PB, pb = line - f * PB;
+    V z = czero<V>();
+    if (pb < npairs) {
+      const int l = l0 + 2 * pb;
+      int k = m;
+      bool conjpart = false;
+      if (m > H) { k = G1 - m; conjpart = true; }
+      if (k < N1h) {
+        V a = Af[f * fstride + (size_t)l * N1h + k];
+        V b = Af[f * fstride + (size_t)(l + 1) * N1h + k];
+        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
+        if (!conjpart) { z.x = a.x - b.y; z.y = a.y + b.x; }      // a + i b
+        else { z.x = a.x + b.y; z.y = -a.y + b.x; }              // conj(a) + i conj(b)
+      }
+    }
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = smem_fft<true>(b0, b1, 3 * PB, px, twx);
+  V *oth = (res == b0) ? b1 : b0;
+  // optional capture of physical velocities (immersed-boundary levels)
+  if (capslot) {
+    const int cs = capslot[slot];
+    if (cs >= 0) {
+      for (int idx = threadIdx.x; idx < 3 * PB * G1; idx += blockDim.x) {
+        const int line = idx / G1, m = idx - line * G1;
+        const int f = line / PB, pb = line - f * PB;
+        if (pb >= npairs) continue;
+        const int l = l0 + 2 * pb;
+        double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * G1;
+        V z = res[idx];
+        cp[(size_t)l * G1 + m] = (double)z.x;
+        cp[(size_t)(l + 1) * G1 + m] = (double)z.y;
+      }
+    }
+  }
+  // products, written into `oth` lines p*PB + pb
+  T m1 = 0, m2 = 0, m3 = 0;
+  const T thv = isU ? (T)0 : (T)g.thv[q];
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    const V u = res[(0 * PB + pb) * G1 + m], v = res[(1 * PB + pb) * G1 + m], w = res[(2 * PB + pb) * G1 + m];
+    const bool valid = pb < npairs;
+    if (isU) {
+      V p0, p1, p2, p3;
+      p0.x = u.x * u.x; p0.y = u.y * u.y;
+      p1.x = u.x * w.x; p1.y = u.y * w.y;
+      p2.x = v.x * v.x; p2.y = v.y * v.y;
+      p3.x = w.x * w.x; p3.y = w.y * w.y;
+      oth[(0 * PB + pb) * G1 + m] = p0;
+      oth[(1 * PB + pb) * G1 + m] = p1;
+      oth[(2 * PB + pb) * G1 + m] = p2;
+      oth[(3 * PB + pb) * G1 + m] = p3;
+      if (valid) {
+        m1 = fmax(m1, fmax(fabs(u.x), fabs(u.y)));
+        m3 = fmax(m3, fmax(fabs(w.x), fabs(w.y)));
+      }
+    } else {
+      V p0, p1;
+      p0.x = u.x * v.x; p0.y = u.y * v.y;
+      p1.x = w.x * v.x; p1.y = w.y * v.y;
+      oth[(0 * PB + pb) * G1 + m] = p0;
+      oth[(1 * PB + pb) * G1 + m] = p1;
+      if (valid) m2 = fmax(m2, fmax(fabs(v.x), fabs(v.y)) * thv);
+    }
+  }
+  if (doCFL) {
+    m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
+    if ((threadIdx.x & 31) == 0) {
+      if (isU) { atomic_max_pos(&sc->u1m, (double)m1); atomic_max_pos(&sc->u3m, (double)m3); }
+      else atomic_max_pos(&sc->u2m, (double)m2);
+    }
+  }
+  __syncthreads();
+  const int nprod = isU ? 4 : 2;
+  V *pres = smem_fft<false>(oth, res, nprod * PB, px, twx);
+  const T s1 = (T)1 / (T)G1;
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  // separate the two rows of each pair, keep kx = 0..N1h-1; pb fastest for coalesced writes
+  for (int idx = threadIdx.x; idx < nprod * N1h * PB; idx += blockDim.x) {
+    const int pb = idx % PB;
+    const int rest = idx / PB;
+    const int k = rest % N1h, p = rest / N1h;
+    if (pb >= npairs) continue;
+    const V *L = pres + (p * PB + pb) * G1;
+    const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
+    V a, b;
+    a.x = (T)0.5 * (z.x + zc.x) * s1; a.y = (T)0.5 * (z.y + zc.y) * s1;
+    // -0.5 i (z - zc)
+    b.x = (T)0.5 * (z.y - zc.y) * s1; b.y = (T)-0.5 * (z.x - zc.x) * s1;
+    if (k == 0) { a.y = 0; b.y = 0; }
+    V *dst = B + ((size_t)(pbase + p) * N1h + k) * G2 + l0 + 2 * pb;
+    dst[0] = a;
+    dst[1] = b;
+  }
+}
+
+// ============================================================================
+// T3: forward z transforms + der_x/der_z. grid: x = kx group (KB), y = level slot.
+// u level: products uu, uw, vv, ww -> N1xz, N3xz, vvc.   v level: uv, wv -> N2xz, uvf, wvf.
+// ============================================================================
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_zfwd_nl(const typename C2<T>::t *__restrict__ B, Geo g, RadixPlan pz,
+                                                  const typename C2<T>::t *__restrict__ twz, int KB,
+                                                  double2 *__restrict__ N1xz, double2 *__restrict__ N2xz,
+                                                  double2 *__restrict__ N3xz, double2 *__restrict__ uvf,
+                                                  double2 *__restrict__ vvc, double2 *__restrict__ wvf) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G2 = g.G2, N1h = g.N1h, N2 = g.N2;
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int nprod = isU ? 4 : 2;
+  const int kx0 = blockIdx.x * KB;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + 4 * KB * G2;
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  for (int idx = threadIdx.x; idx < nprod * KB * G2; idx += blockDim.x) {
+    const int line = idx / G2, l = idx - line * G2;
+    const int p = line / KB, kk = line - p * KB, kx = kx0 + kk;
+    V z = czero<V>();
+    if (kx < N1h) z = B[((size_t)(pbase + p) * N1h + kx) * G2 + l];
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = smem_fft<false>(b0, b1, nprod * KB, pz, twz);
+  const double s2 = 1.0 / (double)G2;
+  const size_t off = (size_t)q * g.ncol;
+  for (int idx = threadIdx.x; idx < N2 * KB; idx += blockDim.x) {
+    const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
+    if (kx >= N1h) continue;
+    const int row = prow(g, r);
+    const int c = r * N1h + kx;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    const bool zr = (r == N2 / 2);  // der_x/der_z zero the kz = -N2/2 row
+    if (isU) {
+      V t;
+      double2 uu, uw, vv, ww;
+      t = res[(0 * KB + kk) * G2 + row]; uu.x = (double)t.x * s2; uu.y = (double)t.y * s2;
+      t = res[(1 * KB + kk) * G2 + row]; uw.x = (double)t.x * s2; uw.y = (double)t.y * s2;
+      t = res[(2 * KB + kk) * G2 + row]; vv.x = (double)t.x * s2; vv.y = (double)t.y * s2;
+      t = res[(3 * KB + kk) * G2 + row]; ww.x = (double)t.x * s2; ww.y = (double)t.y * s2;
+      double2 n1 = czero<double2>(), n3 = czero<double2>();
+      if (!zr) {
+        n1 = cadd(cimul(kxv, uu), cimul(kzv, uw));
+        n3 = cadd(cimul(kxv, uw), cimul(kzv, ww));
+      }
+      N1xz[off + c] = n1;
+      N3xz[off + c] = n3;
+      vvc[off + c] = vv;
+    } else {
+      V t;
+      double2 uv, wv;
+      t = res[(0 * KB + kk) * G2 + row]; uv.x = (double)t.x * s2; uv.y = (double)t.y * s2;
+      t = res[(1 * KB + kk) * G2 + row]; wv.x = (double)t.x * s2; wv.y = (double)t.y * s2;
+      double2 n2 = czero<double2>();
+      if (!zr) n2 = cadd(cimul(kxv, uv), cimul(kzv, wv));
+      N2xz[off + c] = n2;
+      uvf[off + c] = uv;
+      wvf[off + c] = wv;
+    }
+  }
+}
+
+// ============================================================================
+// dt (kRK = 1): dtc_calc + MPI_ALLREDUCE(MIN) + dt = min(2.5 dtv, CFL dtc)
+// ============================================================================
+__global__ void k_dt(Geo g, DevScalars *sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double u1m = __longlong_as_double((long long)sc->u1m);
+  const double u3m = __longlong_as_double((long long)sc->u3m);
+  double u2m = __longlong_as_double((long long)sc->u2m);
+  if (!(u2m > 1e-6)) u2m = (u2m != u2m) ? u2m : 1e-6;
+  const double a = 1.0 / (g.alp * (double)(g.N1 / 2) * u1m);
+  const double b = 1.0 / (g.bet * (double)(g.N2 / 2) * u3m);
+  const double cv = 1.0 / (u2m * g.dthetavi);
+  double d = fmin(a, b);
+  d = fmin(d, cv);
+  if (a != a || b != b) d = a + b;  // propagate a NaN
+  sc->dtc = d;
+  const double lim = 2.5 * g.dtv, cfl = g.CFL * d;
+  const double dt = (cfl != cfl) ? cfl : fmin(lim, cfl);
+  sc->dt = dt;
+  sc->dti = 1.0 / dt;
+  sc->t = sc->t + dt;
+}
+
+__global__ void k_reset_cfl(DevScalars *sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) { sc->u1m = 0ull; sc->u2m = 0ull; sc->u3m = 0ull; }
+}
+
+// ============================================================================
+// Helmholtz u and w (shared matrix), one thread per column.
+// Levels q = 0 .. nu-1 (ghosts at 0 and nu-1). For interior q the right-hand side
+// is u + dt * du with du = RHS0 (laplacian, -cRK Nu_old, -dRK grad p, -dRK mpgx on
+// (0,0)) - gRK Nu_new, Nu_new = N_xz + d/dy(uv or wv); Nu_new replaces Nu.
+// The forward sweep stores y in u and the upper factor in `a3s`; the backward
+// sweep writes the solution in place. At immersed-boundary levels du is read from
+// `duib` (assembled and forced beforehand) instead of being formed here.
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, double2 *__restrict__ u3,
+                                                  double2 *__restrict__ Nu1, double2 *__restrict__ Nu3,
+                                                  const double2 *__restrict__ N1xz, const double2 *__restrict__ N3xz,
+                                                  const double2 *__restrict__ uvf, const double2 *__restrict__ wvf,
+                                                  const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
+                                                  const DevScalars *__restrict__ sc, int kRK,
+                                                  const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  if (c >= nc) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const double k2x = g.k2x[kx], k2z = g.k2z[r];
+  const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1];
+  const double G = -g.gRK[kRK - 1];
+  const double dt = sc->dt;
+  const double beta = g.bRK[kRK - 1] * dt / g.Re;
+  const double C3x = -dR * g.k1x[kx], C3z = -dR * g.k1z[r];  // imaginary parts of -dRK*k1F
+  const double mp = (c == 0) ? -dR * sc->mpgx : 0.0;
+  const int nu = g.nu;
+  const double *d0 = g.d2u, *d1 = g.d2u + nu, *d2 = g.d2u + 2 * nu;
+  // row 0: [1, gw(2,1)], rhs 0
+  double a3raw = g.gw[1][0];
+  double a2p = 1.0;  // 1/a2(0)
+  double2 y1 = czero<double2>(), y3 = czero<double2>();
+  double2 um1 = u1[c], u0 = u1[(size_t)nc + c];
+  double2 wm1 = u3[c], w0 = u3[(size_t)nc + c];
+  u1[c] = y1;
+  u3[c] = y3;
+  double2 uvm = uvf[c], wvm = wvf[c];
+  for (int q = 1; q <= nu - 2; ++q) {
+    const size_t o = (size_t)q * nc + c;
+    const double2 up1 = u1[o + nc], wp1 = u3[o + nc];
+    const double2 uvq = uvf[o], wvq = wvf[o];
+    double2 du1, du3;
+    const int ibs = ibslot_u ? ibslot_u[q] : -1;
+    if (ibs < 0) {
+      const double a = d0[q], dg = (k2x + k2z) + d1[q], cc = d2[q];
+      double2 L1, L3;
+      L1.x = (a * um1.x + dg * u0.x) + cc * up1.x; L1.y = (a * um1.y + dg * u0.y) + cc * up1.y;
+      L3.x = (a * wm1.x + dg * w0.x) + cc * wp1.x; L3.y = (a * wm1.y + dg * w0.y) + cc * wp1.y;
+      const double2 pj = p[(size_t)(q - 1) * nc + c];
+      const double2 no1 = Nu1[o], no3 = Nu3[o];
+      du1.x = (C1 * L1.x + C2 * no1.x) + (-C3x * pj.y);
+      du1.y = (C1 * L1.y + C2 * no1.y) + (C3x * pj.x);
+      du3.x = (C1 * L3.x + C2 * no3.x) + (-C3z * pj.y);
+      du3.y = (C1 * L3.y + C2 * no3.y) + (C3z * pj.x);
+      du1.x += mp;
+      const double th = g.thu[q];
+      const double2 x1 = N1xz[o], x3 = N3xz[o];
+      double2 n1, n3;
+      n1.x = x1.x + (uvq.x - uvm.x) * th * g.dd; n1.y = x1.y + (uvq.y - uvm.y) * th * g.dd;
+      n3.x = x3.x + (wvq.x - wvm.x) * th * g.dd; n3.y = x3.y + (wvq.y - wvm.y) * th * g.dd;
+      Nu1[o] = n1;
+      Nu3[o] = n3;
+      du1.x = du1.x + G * n1.x; du1.y = du1.y + G * n1.y;
+      du3.x = du3.x + G * n3.x; du3.y = du3.y + G * n3.y;
+    } else {
+      du1 = duib[((size_t)ibs * 3 + 0) * nc + c];
+      du3 = duib[((size_t)ibs * 3 + 2) * nc + c];
+    }
+    double2 rhs1, rhs3;
+    rhs1.x = u0.x + dt * du1.x; rhs1.y = u0.y + dt * du1.y;
+    rhs3.x = w0.x + dt * du3.x; rhs3.y = w0.y + dt * du3.y;
+    const double a1 = -beta * d0[q];
+    const double a2 = 1.0 - beta * ((d1[q] + k2x) + k2z);
+    const double a3p = a3raw * a2p;  // a3'(q-1)
+    a3s[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.0 / (a2 - a1 * a3p);
+    y1.x = (rhs1.x - a1 * y1.x) * a2p; y1.y = (rhs1.y - a1 * y1.y) * a2p;
+    y3.x = (rhs3.x - a1 * y3.x) * a2p; y3.y = (rhs3.y - a1 * y3.y) * a2p;
+    u1[o] = y1;
+    u3[o] = y3;
+    a3raw = -beta * d2[q];
+    um1 = u0; u0 = up1; wm1 = w0; w0 = wp1;
+    uvm = uvq; wvm = wvq;
+  }
+  {  // last row: [gw(2,2), 1], rhs 0
+    const int q = nu - 1;
+    const double a1 = g.gw[1][1];
+    const double a3p = a3raw * a2p;
+    a3s[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.0 / (1.0 - a1 * a3p);
+    y1.x = (0.0 - a1 * y1.x) * a2p; y1.y = (0.0 - a1 * y1.y) * a2p;
+    y3.x = (0.0 - a1 * y3.x) * a2p; y3.y = (0.0 - a1 * y3.y) * a2p;
+    u1[(size_t)q * nc + c] = y1;
+    u3[(size_t)q * nc + c] = y3;
+  }
+  double2 x1 = y1, x3 = y3;
+  for (int q = nu - 2; q >= 0; --q) {
+    const size_t o = (size_t)q * nc + c;
+    const double a3p = a3s[o];
+    const double2 yy1 = u1[o], yy3 = u3[o];
+    x1.x = yy1.x - a3p * x1.x; x1.y = yy1.y - a3p * x1.y;
+    x3.x = yy3.x - a3p * x3.x; x3.y = yy3.y - a3p * x3.y;
+    u1[o] = x1;
+    u3[o] = x3;
+  }
+}
+
+// ============================================================================
+// Helmholtz v, one thread per column. Levels q = 0 .. nv-1 (walls at both ends).
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, double2 *__restrict__ Nu2,
+                                                 const double2 *__restrict__ N2xz, const double2 *__restrict__ vvc,
+                                                 const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
+                                                 const DevScalars *__restrict__ sc, int kRK,
+                                                 const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  if (c >= nc) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const double k2x = g.k2x[kx], k2z = g.k2z[r];
+  const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1];
+  const double G = -g.gRK[kRK - 1];
+  const double dt = sc->dt;
+  const double beta = g.bRK[kRK - 1] * dt / g.Re;
+  const int nv = g.nv;
+  const double *d0 = g.d2v, *d1 = g.d2v + nv, *d2 = g.d2v + 2 * nv;
+  double a3raw = 0.0, a2p = 1.0;
+  double2 y = czero<double2>();
+  double2 vm1 = u2[c], v0 = u2[(size_t)nc + c];
+  u2[c] = y;
+  double2 vvq = vvc[(size_t)1 * nc + c];  // vv at u level q (interior starts at 1)
+  for (int q = 1; q <= nv - 2; ++q) {
+    const size_t o = (size_t)q * nc + c;
+    const double2 vp1 = u2[o + nc];
+    const double2 vvp = vvc[o + nc];  // vv at u level q+1
+    double2 du;
+    const int ibs = ibslot_v ? ibslot_v[q] : -1;
+    if (ibs < 0) {
+      const double a = d0[q], dg = (k2x + k2z) + d1[q], cc = d2[q];
+      double2 L;
+      L.x = (a * vm1.x + dg * v0.x) + cc * vp1.x; L.y = (a * vm1.y + dg * v0.y) + cc * vp1.y;
+      const double C3 = -dR * g.dd * g.thv[q];
+      const double2 pp = p[(size_t)q * nc + c], pm = p[(size_t)(q - 1) * nc + c];
+      const double2 no = Nu2[o];
+      du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
+      du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
+      const double th = g.thv[q];
+      const double2 x2 = N2xz[o];
+      double2 n2;
+      n2.x = x2.x + (vvp.x - vvq.x) * th * g.dd; n2.y = x2.y + (vvp.y - vvq.y) * th * g.dd;
+      Nu2[o] = n2;
+      du.x = du.x + G * n2.x; du.y = du.y + G * n2.y;
+    } else {
+      du = duib[((size_t)ibs * 3 + 1) * nc + c];
+    }
+    double2 rhs;
+    rhs.x = v0.x + dt * du.x; rhs.y = v0.y + dt * du.y;
+    const double a1 = -beta * d0[q];
+    const double a2 = 1.0 - beta * ((d1[q] + k2x) + k2z);
+    const double a3p = a3raw * a2p;
+    a3s[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.0 / (a2 - a1 * a3p);
+    y.x = (rhs.x - a1 * y.x) * a2p; y.y = (rhs.y - a1 * y.y) * a2p;
+    u2[o] = y;
+    a3raw = -beta * d2[q];
+    vm1 = v0; v0 = vp1; vvq = vvp;
+  }
+  {
+    const int q = nv - 1;
+    const double a3p = a3raw * a2p;
+    a3s[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.0 / (1.0 - 0.0 * a3p);
+    y.x = (0.0 - 0.0 * y.x) * a2p; y.y = (0.0 - 0.0 * y.y) * a2p;
+    u2[(size_t)q * nc + c] = y;
+  }
+  double2 x = y;
+  for (int q = nv - 2; q >= 0; --q) {
+    const size_t o = (size_t)q * nc + c;
+    const double a3p = a3s[o];
+    const double2 yy = u2[o];
+    x.x = yy.x - a3p * x.x; x.y = yy.y - a3p * x.y;
+    u2[o] = x;
+  }
+}
+
+// ============================================================================
+// flowrate_corr (littleharsh.f90:476-509) on mode (0,0) of u1, serial (one thread)
+// u11 levels 0..nn+2 (reference levels), scratch of 4*(nn+3) doubles.
+// ============================================================================
+__global__ void k_meanflow(double2 *__restrict__ u1, Geo g, DevScalars *sc, int kRK, double *__restrict__ w) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int nn = g.nn, n = nn + 3, dny = g.dny, nc = g.ncol;
+  double *u11 = w, *a1 = w + n, *a2 = w + 2 * n, *a3 = w + 3 * n;
+  const double dt = sc->dt;
+  const double bdt = -g.dRK[kRK - 1] * dt;
+  const double beta = g.bRK[kRK - 1] * dt / g.Re;
+  const int nu = g.nu;
+  u11[0] = 0.0;
+  for (int j = 1; j <= nn + 1; ++j) u11[j] = bdt;
+  u11[nn + 2] = 0.0;
+  a1[0] = 0.0; a2[0] = 1.0; a3[0] = g.gw[1][0];
+  for (int j = 1; j <= nn + 1; ++j) {
+    a1[j] = -beta * g.d2u[j + dny];
+    a2[j] = 1.0 - beta * g.d2u[nu + j + dny];
+    a3[j] = -beta * g.d2u[2 * nu + j + dny];
+  }
+  a1[nn + 2] = g.gw[1][1]; a2[nn + 2] = 1.0; a3[nn + 2] = 0.0;
+  a2[0] = 1.0 / a2[0];
+  for (int j = 1; j < n; ++j) {
+    a3[j - 1] = a3[j - 1] * a2[j - 1];
+    a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+  }
+  u11[0] = u11[0] * a2[0];
+  for (int j = 1; j < n; ++j) u11[j] = (u11[j] - a1[j] * u11[j - 1]) * a2[j];
+  for (int j = n - 2; j >= 0; --j) u11[j] = u11[j] - a3[j] * u11[j + 1];
+  double Qx1 = 0.0, Qx0 = 0.0;
+  for (int j = 1; j <= nn + 1; ++j) Qx1 = Qx1 + (g.yv[j + dny] - g.yv[j - 1 + dny]) * u11[j];
+  for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + (g.yv[j + dny] - g.yv[j - 1 + dny]) * u1[(size_t)(j + dny) * nc].x;
+  const double gg = (sc->QxT - Qx0) / Qx1;
+  sc->mpgx = sc->mpgx + gg;
+  for (int j = 0; j <= nn + 2; ++j) u1[(size_t)(j + dny) * nc].x = u1[(size_t)(j + dny) * nc].x + gg * u11[j];
+}
+
+// flowrateIm of u1 (0,0): Qx (meanflow_ctP, littleharsh.f90:529-545; getini)
+__global__ void k_flowrate(const double2 *__restrict__ u1, Geo g, DevScalars *sc, int setQxT) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double Q = 0.0;
+  for (int j = 1; j <= g.nn + 1; ++j) Q = Q + (g.yv[j + g.dny] - g.yv[j - 1 + g.dny]) * u1[(size_t)(j + g.dny) * g.ncol].x;
+  sc->Qx = Q;
+  if (setQxT) sc->QxT = Q;
+}
+
+__global__ void k_step_end(DevScalars *sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  sc->iter += 1;
+  const double e = __longlong_as_double((long long)sc->errbits);
+  sc->err = e;
+  if (!(e == e) || isinf(e) || !(sc->dt == sc->dt)) sc->status = LH_ENONFINITE;
+}
+
+// ============================================================================
+// Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
+// factor of LU_buildP/LU_decP recomputed in the same operation order, p += psi,
+// v_corr, and the divergence of the corrected field (max |div| -> errbits).
+// One thread per column. p levels qp = 0..np-1 <-> u/v index q = qp + 1.
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double2 *__restrict__ u2,
+                                                double2 *__restrict__ u3, double2 *__restrict__ p,
+                                                double2 *__restrict__ psi, double *__restrict__ a3s, Geo g,
+                                                DevScalars *sc, int kRK) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  double dmax = 0.0;
+  if (c < nc) {
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    const double k2x = g.k2x[kx], k2z = g.k2z[r];
+    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dtirk = sc->dti / aRb;
+    const double dt = sc->dt;
+    const int np = g.np;
+    const double dd = g.dd;
+    // forward sweep
+    double a3raw = 0.0, a2p = 0.0;
+    double2 y = czero<double2>();
+    double2 vm = u2[c];
+    for (int qp = 0; qp < np; ++qp) {
+      const int q = qp + 1;
+      const size_t o = (size_t)q * nc + c;
+      const double2 a = u1[o], w = u3[o], v = u2[o];
+      const double th = dd * g.thu[q];
+      double2 dv;
+      dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
+      dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
+      vm = v;
+      double2 rhs;
+      rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
+      // matrix row qp (D/G vectors of LU_buildP)
+      const double Dt = dd * g.thu[q];
+      const double Gb = -dd * g.thv[q];
+      double A1, A2, A3;
+      if (qp == 0) {
+        A1 = 0.0;
+        A2 = (Dt * Gb) + k2x + k2z;
+        A3 = (Dt * (dd * g.thv[q]));
+        if (c == 0) {
+          const double h = g.yu[2 + g.dny] - g.yu[1 + g.dny];
+          A1 = 0.0; A2 = 1.0 / (h * h); A3 = 0.0;
+          rhs.x = 0.0; rhs.y = 0.0;
+        }
+      } else {
+        const double Db = -dd * g.thu[q];     // D_vec_b(j-1)
+        const double Gt = dd * g.thv[q - 1];  // G_vec_t(j)
+        const double Gbm = -dd * g.thv[q - 1];  // G_vec_b(j-1)
+        if (qp == np - 1) {
+          A2 = (Db * Gt) + k2x + k2z;
+          A1 = (Db * Gbm);
+          A3 = 0.0;
+        } else {
+          A2 = (Db * Gt) + (Dt * Gb) + k2x + k2z;
+          A1 = (Db * Gbm);
+          A3 = (Dt * (dd * g.thv[q]));
+        }
+      }
+      if (qp == 0) {
+        a2p = 1.0 / A2;
+      } else {
+        const double a3p = a3raw * a2p;
+        a3s[(size_t)(qp - 1) * nc + c] = a3p;
+        a2p = 1.0 / (A2 - A1 * a3p);
+      }
+      if (qp == 0) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
+      else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
+      psi[(size_t)qp * nc + c] = y;
+      a3raw = A3;
+    }
+    // backward sweep + p update + v_corr
+    const double dtrk = dt * aRb;
+    const double dtrk2 = dtrk * dd;
+    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
+    double2 xn = y;  // psi(np-1)
+    double2 vup = u2[(size_t)(np) * nc + c];  // v at index np+... (updated value of the level above)
+    // level above the top p level is the top v wall (index nv-1 = np): v = 0 there
+    double2 a_up = czero<double2>(), w_up = czero<double2>();
+    for (int qp = np - 1; qp >= 0; --qp) {
+      const int q = qp + 1;
+      const size_t o = (size_t)q * nc + c;
+      double2 x;
+      if (qp == np - 1) x = xn;
+      else {
+        const double a3p = a3s[(size_t)qp * nc + c];
+        const double2 yy = psi[(size_t)qp * nc + c];
+        x.x = yy.x - a3p * xn.x; x.y = yy.y - a3p * xn.y;
+      }
+      psi[(size_t)qp * nc + c] = x;
+      double2 pp = p[(size_t)qp * nc + c];
+      pp.x = pp.x + x.x; pp.y = pp.y + x.y;
+      p[(size_t)qp * nc + c] = pp;
+      double2 a = u1[o], w = u3[o];
+      // u -= (dtrk * i kx) psi
+      a.x = a.x - (-kxd * x.y); a.y = a.y - (kxd * x.x);
+      w.x = w.x - (-kzd * x.y); w.y = w.y - (kzd * x.x);
+      u1[o] = a;
+      u3[o] = w;
+      double2 v = u2[o];
+      if (q <= g.nv - 2) {
+        const double f = dtrk2 * g.thv[q];
+        v.x = v.x - f * (xn.x - x.x);
+        v.y = v.y - f * (xn.y - x.y);
+        u2[o] = v;
+      }
+      // divergence of the level above (q+1), now that v(q) is final
+      if (qp < np - 1) {
+        const double th = dd * g.thu[q + 1];
+        double2 dv;
+        dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
+        dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - v.y);
+        dmax = fmax(dmax, hypot(dv.x, dv.y));
+      }
+      a_up = a; w_up = w; vup = v;
+      xn = x;
+    }
+    {  // divergence of the lowest level (v below is the wall, 0)
+      const double th = dd * g.thu[1];
+      const double2 vb = u2[c];
+      double2 dv;
+      dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
+      dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
+      dmax = fmax(dmax, hypot(dv.x, dv.y));
+    }
+    // ghost extrapolation of u and w, walls of v
+    const int nu = g.nu;
+    double2 t1 = u1[(size_t)nc + c], t3 = u3[(size_t)nc + c];
+    u1[c] = cscale(t1, g.gwbc1);
+    u3[c] = cscale(t3, g.gwbc3);
+    t1 = u1[(size_t)(nu - 2) * nc + c]; t3 = u3[(size_t)(nu - 2) * nc + c];
+    u1[(size_t)(nu - 1) * nc + c] = cscale(t1, g.gwbc1);
+    u3[(size_t)(nu - 1) * nc + c] = cscale(t3, g.gwbc3);
+    u2[c] = czero<double2>();
+    u2[(size_t)(g.nv - 1) * nc + c] = czero<double2>();
+  }
+  dmax = warp_max(dmax);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
+}
+
+__global__ void k_reset_err(DevScalars *sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) sc->errbits = 0ull;
+}
+
+// max |div| of the current state (getini's divergence + error())
+__global__ void __launch_bounds__(NTHR) k_divmax(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                 const double2 *__restrict__ u3, Geo g, DevScalars *sc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  double dmax = 0.0;
+  if (c < g.ncol) {
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    for (int q = 1; q <= g.nu - 2; ++q) {
+      const size_t o = (size_t)q * g.ncol + c;
+      const double2 a = u1[o], w = u3[o], v = u2[o], vm = u2[o - g.ncol];
+      const double th = g.dd * g.thu[q];
+      double2 dv;
+      dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
+      dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
+      dmax = fmax(dmax, hypot(dv.x, dv.y));
+    }
+  }
+  dmax = warp_max(dmax);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
+}
+
+__global__ void k_err_from_bits(DevScalars *sc) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) sc->err = __longlong_as_double((long long)sc->errbits);
+}
+
+// host cfield [col][lev] <-> device [lev][col] (complex), tiled transpose
+__global__ void k_transpose(const double2 *__restrict__ src, double2 *__restrict__ dst, int rows, int cols) {
+  __shared__ double2 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int rr = by + i, cc = bx + threadIdx.x;
+    if (rr < rows && cc < cols) tile[i][threadIdx.x] = src[(size_t)rr * cols + cc];
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int rr = bx + i, cc = by + threadIdx.x;  // dst is cols x rows
+    if (rr < cols && cc < rows) dst[(size_t)rr * rows + cc] = tile[threadIdx.x][i];
+  }
+}
+
+// ============================================================================
+// Generic plane transforms (leaves lh_four_to_phys / lh_phys_to_four and the
+// immersed-boundary round trip of du). spec [plane][N2][N1h] complex, phys
+// [plane][G2][G1] real.
+// ============================================================================
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_spec_zinv(const double2 *__restrict__ spec, typename C2<T>::t *__restrict__ A,
+                                                    Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
+                                                    int KB) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + KB * g.G2;
+  const int pl = blockIdx.y, kx0 = blockIdx.x * KB;
+  for (int i = threadIdx.x; i < KB * g.G2; i += blockDim.x) b0[i] = czero<V>();
+  __syncthreads();
+  const double2 *S = spec + (size_t)pl * g.ncol;
+  for (int idx = threadIdx.x; idx < g.N2 * KB; idx += blockDim.x) {
+    const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
+    if (kx >= g.N1h) continue;
+    const double2 val = S[r * g.N1h + kx];
+    V v; v.x = (T)val.x; v.y = (T)val.y;
+    b0[kk * g.G2 + prow(g, r)] = v;
+  }
+  __syncthreads();
+  V *res = smem_fft<true>(b0, b1, KB, pz, twz);
+  V *dst = A + (size_t)pl * g.G2 * g.N1h;
+  for (int idx = threadIdx.x; idx < g.G2 * KB; idx += blockDim.x) {
+    const int l = idx / KB, kk = idx - l * KB, kx = kx0 + kk;
+    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[kk * g.G2 + l];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_xinv_phys(const typename C2<T>::t *__restrict__ A, double *__restrict__ phys,
+                                                    Geo g, RadixPlan px, const typename C2<T>::t *__restrict__ twx,
+                                                    int PB) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h, H = G1 / 2;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + PB * G1;
+  const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const V *Ap = A + (size_t)pl * G2 * N1h;
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    V z = czero<V>();
+    if (pb < npairs) {
+      const int l = l0 + 2 * pb;
+      int k = m; bool cj = false;
+      if (m > H) { k = G1 - m; cj = true; }
+      if (k < N1h) {
+        V a = Ap[(size_t)l * N1h + k], b = Ap[(size_t)(l + 1) * N1h + k];
+        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
+        if (!cj) { z.x = a.x - b.y; z.y = a.y + b.x; } else { z.x = a.x + b.y; z.y = -a.y + b.x; }
+      }
+    }
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = smem_fft<true>(b0, b1, PB, px, twx);
+  double *P = phys + (size_t)pl * G2 * G1;
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    if (pb >= npairs) continue;
+    const int l = l0 + 2 * pb;
+    P[(size_t)l * G1 + m] = (double)res[idx].x;
+    P[(size_t)(l + 1) * G1 + m] = (double)res[idx].y;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_xfwd_phys(const double *__restrict__ phys, typename C2<T>::t *__restrict__ B,
+                                                    Geo g, RadixPlan px, const typename C2<T>::t *__restrict__ twx,
+                                                    int PB) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + PB * G1;
+  const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const double *P = phys + (size_t)pl * G2 * G1;
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    V z = czero<V>();
+    if (pb < npairs) {
+      const int l = l0 + 2 * pb;
+      z.x = (T)P[(size_t)l * G1 + m];
+      z.y = (T)P[(size_t)(l + 1) * G1 + m];
+    }
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = smem_fft<false>(b0, b1, PB, px, twx);
+  const T s1 = (T)1 / (T)G1;
+  for (int idx = threadIdx.x; idx < N1h * PB; idx += blockDim.x) {
+    const int pb = idx % PB, k = idx / PB;
+    if (pb >= npairs) continue;
+    const V *L = res + pb * G1;
+    const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
+    V a, b;
+    a.x = (T)0.5 * (z.x + zc.x) * s1; a.y = (T)0.5 * (z.y + zc.y) * s1;
+    b.x = (T)0.5 * (z.y - zc.y) * s1; b.y = (T)-0.5 * (z.x - zc.x) * s1;
+    if (k == 0) { a.y = 0; b.y = 0; }
+    V *dst = B + ((size_t)pl * N1h + k) * G2 + l0 + 2 * pb;
+    dst[0] = a;
+    dst[1] = b;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__restrict__ B, double2 *__restrict__ spec,
+                                                    Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
+                                                    int KB, const int *__restrict__ plmap) {
+  typedef typename C2<T>::t V;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G2 = g.G2, N1h = g.N1h, N2 = g.N2;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + KB * G2;
+  const int pl = blockIdx.y, kx0 = blockIdx.x * KB;
+  for (int idx = threadIdx.x; idx < KB * G2; idx += blockDim.x) {
+    const int kk = idx / G2, l = idx - kk * G2, kx = kx0 + kk;
+    V z = czero<V>();
+    if (kx < N1h) z = B[((size_t)pl * N1h + kx) * G2 + l];
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = smem_fft<false>(b0, b1, KB, pz, twz);
+  const double s2 = 1.0 / (double)G2;
+  double2 *S = spec + (size_t)(plmap ? plmap[pl] : pl) * g.ncol;
+  for (int idx = threadIdx.x; idx < N2 * KB; idx += blockDim.x) {
+    const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
+    if (kx >= N1h) continue;
+    const V t = res[kk * G2 + prow(g, r)];
+    double2 o; o.x = (double)t.x * s2; o.y = (double)t.y * s2;
+    S[r * N1h + kx] = o;
+  }
+}
+
+// ============================================================================
+// Immersed boundaries (FOU3D.f90:806-998): assemble du at the listed levels,
+// then (after the inverse transform) the forcing at the solid points.
+// duib layout: [ibslot][field 0..2][col]; ib levels of u (fields 0, 2) and v (1).
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                const double2 *__restrict__ u3, const double2 *__restrict__ Nu1o,
+                                                const double2 *__restrict__ Nu2o, const double2 *__restrict__ Nu3o,
+                                                const double2 *__restrict__ N1xz, const double2 *__restrict__ N2xz,
+                                                const double2 *__restrict__ N3xz, const double2 *__restrict__ uvf,
+                                                const double2 *__restrict__ vvc, const double2 *__restrict__ wvf,
+                                                const double2 *__restrict__ p, double2 *__restrict__ duib,
+                                                const int *__restrict__ iblev, int nib, Geo g,
+                                                const DevScalars *__restrict__ sc, int kRK) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;  // ib slot
+  const int nc = g.ncol;
+  if (c >= nc || s >= nib) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const double k2x = g.k2x[kx], k2z = g.k2z[r];
+  const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1];
+  const double G = -g.gRK[kRK - 1];
+  const int qu = iblev[2 * s], qv = iblev[2 * s + 1];
+  if (qu > 0) {  // u and w at u-level qu
+    const double *d0 = g.d2u, *d1 = g.d2u + g.nu, *d2 = g.d2u + 2 * g.nu;
+    const size_t o = (size_t)qu * nc + c;
+    const double a = d0[qu], dg = (k2x + k2z) + d1[qu], cc = d2[qu];
+    const double2 pj = p[(size_t)(qu - 1) * nc + c];
+    const double C3x = -dR * g.k1x[kx], C3z = -dR * g.k1z[r];
+    const double th = g.thu[qu];
+    for (int f = 0; f < 2; ++f) {
+      const double2 *U = f ? u3 : u1;
+      const double2 *No = f ? Nu3o : Nu1o;
+      const double2 *X = f ? N3xz : N1xz;
+      const double2 *F = f ? wvf : uvf;
+      const double C3 = f ? C3z : C3x;
+      const double2 um = U[o - nc], u0 = U[o], up = U[o + nc];
+      double2 L;
+      L.x = (a * um.x + dg * u0.x) + cc * up.x; L.y = (a * um.y + dg * u0.y) + cc * up.y;
+      const double2 no = No[o];
+      double2 du;
+      du.x = (C1 * L.x + C2 * no.x) + (-C3 * pj.y);
+      du.y = (C1 * L.y + C2 * no.y) + (C3 * pj.x);
+      if (f == 0 && c == 0) du.x += -dR * sc->mpgx;
+      const double2 x = X[o], fq = F[o], fm = F[o - nc];
+      double2 n;
+      n.x = x.x + (fq.x - fm.x) * th * g.dd; n.y = x.y + (fq.y - fm.y) * th * g.dd;
+      du.x = du.x + G * n.x; du.y = du.y + G * n.y;
+      duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = du;
+    }
+  }
+  if (qv > 0) {
+    const double *d0 = g.d2v, *d1 = g.d2v + g.nv, *d2 = g.d2v + 2 * g.nv;
+    const size_t o = (size_t)qv * nc + c;
+    const double a = d0[qv], dg = (k2x + k2z) + d1[qv], cc = d2[qv];
+    const double2 vm = u2[o - nc], v0 = u2[o], vp = u2[o + nc];
+    double2 L;
+    L.x = (a * vm.x + dg * v0.x) + cc * vp.x; L.y = (a * vm.y + dg * v0.y) + cc * vp.y;
+    const double C3 = -dR * g.dd * g.thv[qv];
+    const double2 pp = p[(size_t)qv * nc + c], pm = p[(size_t)(qv - 1) * nc + c];
+    const double2 no = Nu2o[o];
+    double2 du;
+    du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
+    du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
+    const double th = g.thv[qv];
+    const double2 x = N2xz[o], vp1 = vvc[o + nc], vq = vvc[o];
+    double2 n;
+    n.x = x.x + (vp1.x - vq.x) * th * g.dd; n.y = x.y + (vp1.y - vq.y) * th * g.dd;
+    du.x = du.x + G * n.x; du.y = du.y + G * n.y;
+    duib[((size_t)s * 3 + 1) * nc + c] = du;
+  }
+}
+
+// forcing at listed solid points: list entries (i,k,j,i1,k1,j1), 1-based i,k
+// duphys [ibslot][field][G2][G1]; cap [capslot][field][G2][G1] (physical u,v,w)
+__global__ void k_ib_force(double *__restrict__ duphys, const double *__restrict__ cap,
+                           const int *__restrict__ list, const double *__restrict__ A, int n, int grid_is_u,
+                           const int *__restrict__ lev2ib, const int *__restrict__ lev2cap, Geo g,
+                           const DevScalars *__restrict__ sc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int *L = list + 6 * (size_t)e;
+  const int i = L[0] - 1, k = L[1] - 1, q = L[2] + g.dny, i1 = L[3] - 1, k1 = L[4] - 1, q1 = L[5] + g.dny;
+  const double Kibdt = g.Kib / sc->dt;
+  const size_t pp = (size_t)g.G1 * g.G2;
+  const int s = lev2ib[q];
+  const int cs = lev2cap[q], cs1 = lev2cap[q1];
+  if (s < 0 || cs < 0 || cs1 < 0) return;
+  const int nf = grid_is_u ? 2 : 1;
+  for (int t = 0; t < nf; ++t) {
+    const int f = grid_is_u ? (t ? 2 : 0) : 1;
+    const double V = A[e] * cap[((size_t)cs1 * 3 + f) * pp + (size_t)k1 * g.G1 + i1];
+    const double u = cap[((size_t)cs * 3 + f) * pp + (size_t)k * g.G1 + i];
+    duphys[((size_t)s * 3 + f) * pp + (size_t)k * g.G1 + i] = Kibdt * (V - u);
+  }
+}
+

@@ -1,0 +1,151 @@
+"""ctypes binding of the CUDA library (liblh.so, include/lh.h).
+
+There is no CPU fallback: constructing a GpuChannel without the built library or
+without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import LH_OK, LH_PREC_FP64, LH_PREC_MIXED, LhConfig, LhScalars, cfield_shape, make_config
+from .setup_grid import ChannelSetup
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
+_lib = None
+
+EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
+           "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
+           "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches")
+
+
+class LhError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lh error {code}: {msg}")
+        self.code = code
+
+
+def load(path: str = _LIB_PATH):
+    """Load liblh.so and declare the signatures. Raises if the library is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"native library not built: {path} (run __graft_entry__.build())")
+    L = C.CDLL(path)
+    vp, dp, i = C.c_void_p, C.POINTER(C.c_double), C.c_int
+    L.lh_create.argtypes = [C.POINTER(LhConfig), C.POINTER(vp)]
+    L.lh_destroy.argtypes = [vp]
+    L.lh_last_error.argtypes = [vp]
+    L.lh_last_error.restype = C.c_char_p
+    L.lh_upload_state.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_download_state.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_set_scalars.argtypes = [vp, C.POINTER(LhScalars)]
+    L.lh_get_scalars.argtypes = [vp, C.POINTER(LhScalars)]
+    L.lh_substep.argtypes = [vp, i]
+    L.lh_step.argtypes = [vp]
+    L.lh_synchronize.argtypes = [vp]
+    L.lh_device_state.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+    L.lh_stream.argtypes = [vp]
+    L.lh_stream.restype = vp
+    L.lh_four_to_phys.argtypes = [vp, vp, vp, i]
+    L.lh_phys_to_four.argtypes = [vp, vp, vp, i]
+    L.lh_kernel_launches.argtypes = [vp]
+    L.lh_kernel_launches.restype = C.c_int64
+    _lib = L
+    return L
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+class GpuChannel:
+    """One channel whose RK3 substep runs on the GPU through the C ABI.
+
+    State arrays on the host use the reference's cfield layout: complex128
+    [ncols, nlevels] (level fastest), one column per (kx, kz) mode."""
+
+    def __init__(self, setup: ChannelSetup, precision: str = "fp64"):
+        self.s = setup
+        self.L = load()
+        prec = {"fp64": LH_PREC_FP64, "mixed": LH_PREC_MIXED}[precision]
+        self.precision = precision
+        cfg, self._keep = make_config(setup, prec)
+        self._cfg = cfg
+        h = C.c_void_p()
+        rc = self.L.lh_create(C.byref(cfg), C.byref(h))
+        if rc != LH_OK:
+            raise LhError(rc, "lh_create failed (is a CUDA device present?)")
+        self.h = h
+        self.shapes = cfield_shape(setup)
+
+    def _check(self, rc: int):
+        if rc != LH_OK:
+            raise LhError(rc, self.L.lh_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state ----
+    def upload_state(self, u1, u2, u3, p):
+        arrs = [np.ascontiguousarray(a, np.complex128) if a is not None else None for a in (u1, u2, u3, p)]
+        for a, sh in zip(arrs, self.shapes):
+            if a is not None and a.shape != sh:
+                raise ValueError(f"shape {a.shape} != {sh}")
+        self._check(self.L.lh_upload_state(self.h, *[_dptr(a) for a in arrs]))
+
+    def download_state(self):
+        out = [np.zeros(sh, np.complex128) for sh in self.shapes]
+        self._check(self.L.lh_download_state(self.h, *[_dptr(a) for a in out]))
+        return out
+
+    def set_scalars(self, **kw):
+        s = LhScalars()
+        for k, v in kw.items():
+            setattr(s, k, v)
+        self._check(self.L.lh_set_scalars(self.h, C.byref(s)))
+
+    def scalars(self) -> dict:
+        s = LhScalars()
+        self._check(self.L.lh_get_scalars(self.h, C.byref(s)))
+        return s.as_dict()
+
+    # ---- time stepping ----
+    def substep(self, kRK: int):
+        self._check(self.L.lh_substep(self.h, kRK))
+
+    def step(self, n: int = 1):
+        for _ in range(n):
+            self._check(self.L.lh_step(self.h))
+
+    def synchronize(self):
+        self._check(self.L.lh_synchronize(self.h))
+
+    def kernel_launches(self) -> int:
+        return int(self.L.lh_kernel_launches(self.h))
+
+    def stream(self) -> int:
+        return int(self.L.lh_stream(self.h) or 0)
+
+    def device_state(self):
+        ptrs = [C.c_void_p() for _ in range(4)]
+        self._check(self.L.lh_device_state(self.h, *[C.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]
+
+    # ---- leaves (device pointers, e.g. torch tensors' data_ptr()) ----
+    def four_to_phys(self, spec_ptr: int, phys_ptr: int, nplanes: int):
+        self._check(self.L.lh_four_to_phys(self.h, C.c_void_p(spec_ptr), C.c_void_p(phys_ptr), nplanes))
+
+    def phys_to_four(self, phys_ptr: int, spec_ptr: int, nplanes: int):
+        self._check(self.L.lh_phys_to_four(self.h, C.c_void_p(phys_ptr), C.c_void_p(spec_ptr), nplanes))
