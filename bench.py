@@ -1,0 +1,360 @@
+"""Throughput of the RK3 substep on one GB300 (or N replicas, one per GPU).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload C1] [--form both|fp64|mixed]
+
+Metric: Mpts*substeps/s = N1*N2*ny mode-points per RK3 substep, 3 substeps per step.
+`value` is the headline form (mixed when its velocity error against the FP64 form
+stays within 1e-5, else FP64) with the state resident in HBM; `e2e` is the same
+metric through the C ABI with the state copied from pinned host memory and back
+every step. The path does not shard (replicas only): with N > 1 every rank runs its
+own channel and `value` sums the replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpts·RK3-substeps/s on 1 GB300, mixed vs FP64 at ≤1e-5 rel err; CPU ref beside"
+UNIT = "Mpts*substeps/s"
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def reduce_max(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() and pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [l.strip().split(",") for l in self.f.read().splitlines() if l.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary
+    (profiles/ncu_traffic_C1.txt: `kernel form bytes_per_launch` lines)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic_C1.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            f = line.split()
+            if len(f) >= 3 and not line.startswith("#"):
+                try:
+                    out[(f[0], f[1])] = float(f[2])
+                except ValueError:
+                    pass
+    return out
+
+
+def algorithmic_bytes(s, kernel: str, form: str) -> float:
+    """Compulsory HBM bytes of one launch: every input and output element once.
+    Spectral fields are complex128; the transform intermediates are complex128 in
+    the FP64 form and complex64 in the mixed form."""
+    nc = s.ncols
+    nuI, nvI = s.nyu - 2, s.nyv - 2
+    G1, G2, N1h = s.G1, s.G2, s.N1 // 2 + 1
+    vs = 16 if form == "fp64" else 8
+    A = (nuI + nvI) * 3 * G2 * N1h * vs
+    B = (4 * nuI + 2 * nvI) * N1h * G2 * vs
+    z = 16
+    if kernel == "k_zinv_nl":
+        return (nuI + nvI) * 3 * nc * z + A
+    if kernel == "k_xpass_nl":
+        return A + B
+    if kernel == "k_zfwd_nl":
+        return B + (nuI + nvI) * 3 * nc * z
+    if kernel == "k_helm_uw":
+        return s.nyu * nc * z * 13
+    if kernel == "k_helm_v":
+        return s.nyv * nc * z * 7
+    if kernel == "k_press":
+        return s.nyu * nc * z * 8
+    return float("nan")
+
+
+def run_reference(args, ws, rank):
+    """The reference's CPU path on the host cores: the Fortran/MPI reference cannot
+    be built here (no Fortran compiler), so its restatement (the oracle) runs on
+    every host thread; each timed step is one RK3 substep of the workload."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars, workload_setup
+    s = workload_setup(args.workload)
+    cores = os.cpu_count() or 1
+    o = Oracle(s, threads=cores)
+    o.set_state(*initial_field(s, 1000))
+    o.set_scalars(**initial_scalars(s))
+    k = 0
+    for _ in range(args.warmup):
+        o.substep(k % 3 + 1)
+        k += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.substep(k % 3 + 1)
+        k += 1
+    dt = time.perf_counter() - t0
+    pts = s.mode_points()
+    val = pts * args.steps / dt / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded perturbed laminar channel)",
+            "config": {"workload": f"{args.workload}: {workload_desc(args.workload)}", "form": "fp64",
+                       "step": "one RK3 substep"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} RK3 substeps of {args.workload} on the CPU oracle "
+                                       f"(the Fortran reference cannot be compiled on this image)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_desc(name):
+    from rnl_multiblock_nofft_gb300.workloads import WORKLOADS
+    return WORKLOADS[name]["desc"]
+
+
+def cpu_baseline(s, budget_s: float = 20.0):
+    """Oracle on the host cores, bounded: RK3 substeps of the same workload until
+    ~budget_s of CPU work (at least one)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars
+    cores = os.cpu_count() or 1
+    o = Oracle(s, threads=cores)
+    o.set_state(*initial_field(s, 1000))
+    o.set_scalars(**initial_scalars(s))
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.substep(n % 3 + 1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 6 or (n >= 1 and el * (n + 1) / n > 2 * budget_s):
+            break
+    return {"value": s.mode_points() * n / el / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} RK3 substeps of the same workload on the CPU oracle, {cores} OpenMP threads, {el:.1f} s"}
+
+
+def time_steps(g, steps, torch):
+    stream = torch.cuda.ExternalStream(g.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = g.kernel_launches()
+    e0.record(stream)
+    g.step(steps)
+    e1.record(stream)
+    g.synchronize()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), g.kernel_launches() - l0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="C1")
+    ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local, pg = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        barrier(pg)
+        return
+
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    from rnl_multiblock_nofft_gb300.native import GpuChannel
+    from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars, workload_setup
+
+    s = workload_setup(args.workload)
+    ic = initial_field(s, 1000 + rank)
+    sc0 = initial_scalars(s)
+    pts = s.mode_points()
+    forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
+    res, states = {}, {}
+    for form in forms:
+        g = GpuChannel(s, form)
+        g.upload_state(*ic)
+        g.set_scalars(**sc0)
+        g.step(args.warmup)
+        g.synchronize()
+        barrier(pg)
+        clk = ClockSampler(local)
+        ms, launches = time_steps(g, args.steps, torch)
+        clocks = clk.stop()
+        barrier(pg)
+        ms = reduce_max(pg, ms)
+        res[form] = {"ms": ms, "launches": launches, "clocks": clocks,
+                     "value": ws * pts * 3 * args.steps / (ms * 1e-3) / 1e6}
+        states[form] = g.download_state()
+        sc = g.scalars()
+        res[form]["scalars"] = {k: sc[k] for k in ("t", "dt", "err", "Qx", "iter")}
+        # per-kernel times (eager, events around each launch) for the roofline
+        prof = g.profile_steps(1)
+        res[form]["kernels"] = prof
+        g.close()
+        del g
+        torch.cuda.empty_cache()
+
+    # accuracy of the mixed form against the FP64 form after the same steps
+    relerr = None
+    if "fp64" in states and "mixed" in states:
+        relerr = {}
+        for f, a, b in zip(("u1", "u2", "u3", "p"), states["fp64"], states["mixed"]):
+            relerr[f] = float(np.linalg.norm(b - a) / np.linalg.norm(a))
+    vel_err = max(relerr[f] for f in ("u1", "u2", "u3")) if relerr else None
+    head = "mixed" if ("mixed" in res and (relerr is None or vel_err <= 1e-5)) else "fp64"
+    if "fp64" not in res:
+        head = forms[0]
+    R = res[head]
+
+    # e2e through the C ABI: pinned host state in, step, state out, every step
+    g = GpuChannel(s, head)
+    shapes = g.shapes
+    pinned = [torch.empty(sh + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+              for sh in shapes]
+    for dst, src in zip(pinned, ic):
+        dst[...] = src
+    g.upload_state(*pinned)
+    g.set_scalars(**sc0)
+    g.step(1)
+    g.synchronize()
+    barrier(pg)
+    pinned_out = [torch.empty(sh + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+                  for sh in shapes]
+    nb = sum(a.nbytes for a in pinned)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.upload_state(*pinned)
+        g.step(1)
+        g.download_state(out=pinned_out)   # the step's result read back to the host
+    g.synchronize()
+    e2e_s = reduce_max(pg, time.perf_counter() - t0)
+    g.close()
+    e2e = {"value": ws * pts * 3 * args.steps / e2e_s / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
+    del pinned_out
+
+    # roofline of the dominant kernel (largest share of the step)
+    kern = R["kernels"]
+    dom = max(kern.items(), key=lambda kv: kv[1][1])
+    dname, (dlaunch, dms) = dom
+    avg_ms = dms / dlaunch
+    alg = algorithmic_bytes(s, dname, head)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (avg_ms * 1e-3) / 1e9
+    tt = traffic_table().get((dname, head))
+    step_total = sum(v[1] for v in kern.values())
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": tt, "kernel": dname,
+                "kernel_share": dms / step_total, "avg_launch_ms": avg_ms,
+                "algorithmic_bytes_per_launch": alg, "peak_source": peak_kind}
+    line = {"metric": METRIC, "value": R["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": R["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head == "fp64" else "f32 transforms/products, f64 state and solves",
+            "data": "synthetic (seeded perturbed laminar channel, see rnl_multiblock_nofft_gb300/workloads.py)",
+            "config": {"workload": f"{args.workload}: {workload_desc(args.workload)}", "form": head,
+                       "mode_points_per_substep": pts, "N1": s.N1, "N2": s.N2, "ny": s.p.ny,
+                       "ny_with_immersed_region": s.nyv, "Ngal": [s.G1, s.G2],
+                       "l2": "inputs larger than L2 (state ~%.0f MB)" % (sum(a.nbytes for a in ic) / 1e6),
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roofline, "gpu_launches": R["launches"], "clocks": R["clocks"], "e2e": e2e,
+            "forms": {f: {"value": r["value"], "ms_per_step": r["ms"] / args.steps, "scalars": r["scalars"],
+                          "kernel_ms_per_step": {k: v[1] for k, v in r["kernels"].items()}}
+                      for f, r in res.items()},
+            "mixed_rel_err_vs_fp64": relerr}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    barrier(pg)
+
+
+if __name__ == "__main__":
+    main()

@@ -133,8 +133,19 @@ void *lh_stream(lh_handle *h);
 int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int nplanes);
 int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes);
 
-/* Number of CUDA kernel launches issued by the handle since creation. */
+/* Number of CUDA kernel launches issued by the handle since creation (graph
+ * replays count every kernel node). */
 int64_t lh_kernel_launches(lh_handle *h);
+
+/* Diagnostic, no counterpart in the reference: run `nsteps` steps eagerly (not
+ * from the graph) with CUDA events around every launch on the handle's stream and
+ * return the time per kernel name. Advances the state like lh_step. */
+typedef struct lh_kernel_time {
+  char name[32];
+  int32_t launches;
+  double total_ms;
+} lh_kernel_time;
+int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, int nmax, int *nout);
 
 #ifdef __cplusplus
 }

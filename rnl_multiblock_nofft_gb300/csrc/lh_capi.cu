@@ -46,6 +46,10 @@ struct lh_handle {
   bool graph_ready;
   long long launches;
   std::string err;
+  // per-kernel timing (lh_profile_steps): events around each launch
+  bool prof;
+  std::vector<std::pair<const char *, std::pair<cudaEvent_t, cudaEvent_t>>> prof_ev;
+  const char *cur_name;
 };
 
 static int fail(lh_handle *h, int code, const std::string &msg) {
@@ -88,14 +92,27 @@ static void *upload_vec(const std::vector<T> &v, cudaError_t &err) {
   return d;
 }
 
+static void prof_begin(lh_handle *h, const char *name) {
+  if (!h->prof) return;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, h->st);
+  h->prof_ev.push_back({name, {a, b}});
+}
 static int count_launch(lh_handle *h) {
   h->launches++;
+  if (h->prof && !h->prof_ev.empty()) cudaEventRecord(h->prof_ev.back().second.second, h->st);
   cudaError_t e = cudaPeekAtLastError();
   if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   return LH_OK;
 }
-#define LAUNCHED()                    \
+// KL(name, kernel<<<...>>>(...)): launch on the handle's stream, counted and (when
+// profiling) bracketed by CUDA events
+#define KL(name, ...)                 \
   do {                                \
+    prof_begin(h, name);              \
+    __VA_ARGS__;                      \
     int rc__ = count_launch(h);       \
     if (rc__ != LH_OK) return rc__;   \
   } while (0)
@@ -358,15 +375,13 @@ static int put_field(lh_handle *h, double2 *dst, int nlev, const double *src) {
   const int nc = h->g.ncol;
   CK(cudaMemcpyAsync(h->stage, src, sizeof(double2) * (size_t)nc * nlev, cudaMemcpyHostToDevice, h->st));
   dim3 grid((nlev + 31) / 32, (nc + 31) / 32), blk(32, 8);
-  k_transpose<<<grid, blk, 0, h->st>>>(h->stage, dst, nc, nlev);
-  LAUNCHED();
+  KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(h->stage, dst, nc, nlev));
   return LH_OK;
 }
 static int get_field(lh_handle *h, const double2 *srcd, int nlev, double *dst) {
   const int nc = h->g.ncol;
   dim3 grid((nc + 31) / 32, (nlev + 31) / 32), blk(32, 8);
-  k_transpose<<<grid, blk, 0, h->st>>>(srcd, h->stage, nlev, nc);
-  LAUNCHED();
+  KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(srcd, h->stage, nlev, nc));
   CK(cudaMemcpyAsync(dst, h->stage, sizeof(double2) * (size_t)nc * nlev, cudaMemcpyDeviceToHost, h->st));
   return LH_OK;
 }
@@ -399,15 +414,11 @@ extern "C" int lh_set_scalars(lh_handle *h, const lh_scalars *s) {
   d.t = s->t; d.dt = s->dt; d.dti = s->dti; d.dtc = s->dtc; d.err = s->err; d.mpgx = s->mpgx;
   d.QxT = s->QxT; d.Qx = s->Qx; d.iter = s->iter;
   CK(cudaMemcpyAsync(h->sc, &d, sizeof(d), cudaMemcpyHostToDevice, h->st));
-  k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, h->g.flag_ctpress != 1 ? 1 : 0);
-  LAUNCHED();
+  KL("k_flowrate", k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, h->g.flag_ctpress != 1 ? 1 : 0));
   const int nb = (h->g.ncol + NTHR_H - 1) / NTHR_H;
-  k_reset_err<<<1, 32, 0, h->st>>>(h->sc);
-  LAUNCHED();
-  k_divmax<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->g, h->sc);
-  LAUNCHED();
-  k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc);
-  LAUNCHED();
+  KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
+  KL("k_divmax", k_divmax<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->g, h->sc));
+  KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   CK(cudaStreamSynchronize(h->st));
   return LH_OK;
 }
@@ -431,26 +442,23 @@ static int nonlinear_transforms(lh_handle *h, int kRK) {
   const Geo &g = h->g;
   const size_t vs = sizeof(V);
   const int nslots = g.nuI + g.nvI;
-  if (kRK == 1) { k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc); LAUNCHED(); }
+  if (kRK == 1) { KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc)); }
   {
     dim3 grid((g.N1h + h->KBz - 1) / h->KBz, nslots, 3);
     size_t sm = 2 * (size_t)h->KBz * g.G2 * vs;
-    k_zinv_nl<T><<<grid, NTHR_H, sm, h->st>>>(h->u1, h->u2, h->u3, (V *)h->A, g, h->pz, (const V *)h->twz, h->KBz);
-    LAUNCHED();
+    KL("k_zinv_nl", k_zinv_nl<T><<<grid, NTHR_H, sm, h->st>>>(h->u1, h->u2, h->u3, (V *)h->A, g, h->pz, (const V *)h->twz, h->KBz));
   }
   {
     dim3 grid((g.G2 / 2 + h->PBx - 1) / h->PBx, nslots);
     size_t sm = 8 * (size_t)h->PBx * g.G1 * vs;
-    k_xpass_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->A, (V *)h->B, g, h->px, (const V *)h->twx, h->PBx,
-                                                kRK == 1 ? 1 : 0, h->sc, h->ib ? h->d_capslot : nullptr, h->cap);
-    LAUNCHED();
+    KL("k_xpass_nl", k_xpass_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->A, (V *)h->B, g, h->px, (const V *)h->twx, h->PBx,
+                                                kRK == 1 ? 1 : 0, h->sc, h->ib ? h->d_capslot : nullptr, h->cap));
   }
   {
     dim3 grid((g.N1h + h->KBf - 1) / h->KBf, nslots);
     size_t sm = 8 * (size_t)h->KBf * g.G2 * vs;
-    k_zfwd_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->B, g, h->pz, (const V *)h->twz, h->KBf, h->N1xz, h->N2xz,
-                                               h->N3xz, h->uvf, h->vvc, h->wvf);
-    LAUNCHED();
+    KL("k_zfwd_nl", k_zfwd_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->B, g, h->pz, (const V *)h->twz, h->KBf, h->N1xz, h->N2xz,
+                                               h->N3xz, h->uvf, h->vvc, h->wvf));
   }
   return LH_OK;
 }
@@ -460,22 +468,18 @@ static int spec_to_phys(lh_handle *h, const double2 *spec, double *phys, int npl
                         const double2 *twz) {
   const Geo &g = h->g;
   dim3 g1((g.N1h + h->KBs - 1) / h->KBs, npl);
-  k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(spec, Ascr, g, h->pz, twz, h->KBs);
-  LAUNCHED();
+  KL("k_spec_zinv", k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(spec, Ascr, g, h->pz, twz, h->KBs));
   dim3 g2((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
-  k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(Ascr, phys, g, h->px, twx, h->PBs);
-  LAUNCHED();
+  KL("k_xinv_phys", k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(Ascr, phys, g, h->px, twx, h->PBs));
   return LH_OK;
 }
 static int phys_to_spec(lh_handle *h, const double *phys, double2 *spec, int npl, double2 *Bscr, const double2 *twx,
                         const double2 *twz) {
   const Geo &g = h->g;
   dim3 g1((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
-  k_xfwd_phys<double><<<g1, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(phys, Bscr, g, h->px, twx, h->PBs);
-  LAUNCHED();
+  KL("k_xfwd_phys", k_xfwd_phys<double><<<g1, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(phys, Bscr, g, h->px, twx, h->PBs));
   dim3 g2((g.N1h + h->KBs - 1) / h->KBs, npl);
-  k_zfwd_spec<double><<<g2, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(Bscr, spec, g, h->pz, twz, h->KBs, nullptr);
-  LAUNCHED();
+  KL("k_zfwd_spec", k_zfwd_spec<double><<<g2, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(Bscr, spec, g, h->pz, twz, h->KBs, nullptr));
   return LH_OK;
 }
 
@@ -485,41 +489,33 @@ static int substep_launches(lh_handle *h, int kRK) {
   const Geo &g = h->g;
   int rc = (h->prec == LH_PREC_FP64) ? nonlinear_transforms<double>(h, kRK) : nonlinear_transforms<float>(h, kRK);
   if (rc) return rc;
-  if (kRK == 1) { k_dt<<<1, 32, 0, h->st>>>(g, h->sc); LAUNCHED(); }
+  if (kRK == 1) { KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc)); }
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
   if (h->ib) {
     dim3 gd(nb, h->nib);
-    k_ib_du<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf,
-                                       h->vvc, h->wvf, h->p, h->duib, h->d_iblev, h->nib, g, h->sc, kRK);
-    LAUNCHED();
+    KL("k_ib_du", k_ib_du<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf,
+                                       h->vvc, h->wvf, h->p, h->duib, h->d_iblev, h->nib, g, h->sc, kRK));
     const double2 *twx = fp64_tw(h, true), *twz = fp64_tw(h, false);
     if ((rc = spec_to_phys(h, h->duib, h->duphys, 3 * h->nib, (double2 *)h->A, twx, twz))) return rc;
     int ibu = (h->cfg.nib_u + 255) / 256, ibv = (h->cfg.nib_v + 255) / 256;
     if (h->cfg.nib_u > 0) {
-      k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1, h->d_ibslot_u,
-                                         h->d_lev2cap_u, g, h->sc);
-      LAUNCHED();
+      KL("k_ib_force", k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1, h->d_ibslot_u,
+                                         h->d_lev2cap_u, g, h->sc));
     }
     if (h->cfg.nib_v > 0) {
-      k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0, h->d_ibslot_v,
-                                         h->d_lev2cap_v, g, h->sc);
-      LAUNCHED();
+      KL("k_ib_force", k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0, h->d_ibslot_v,
+                                         h->d_lev2cap_v, g, h->sc));
     }
     if ((rc = phys_to_spec(h, h->duphys, h->duib, 3 * h->nib, (double2 *)h->B, twx, twz))) return rc;
   }
-  k_helm_uw<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, h->N1xz, h->N3xz, h->uvf, h->wvf, h->p, h->a3s, g,
-                                      h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib);
-  LAUNCHED();
-  k_helm_v<<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, h->N2xz, h->vvc, h->p, h->a3s, g, h->sc, kRK,
-                                     h->ib ? h->d_ibslot_v : nullptr, h->duib);
-  LAUNCHED();
-  if (g.flag_ctpress == 0) { k_meanflow<<<1, 32, 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw); LAUNCHED(); }
-  k_reset_err<<<1, 32, 0, h->st>>>(h->sc);
-  LAUNCHED();
-  k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->a3s, g, h->sc, kRK);
-  LAUNCHED();
-  k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc);
-  LAUNCHED();
+  KL("k_helm_uw", k_helm_uw<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, h->N1xz, h->N3xz, h->uvf, h->wvf, h->p, h->a3s, g,
+                                      h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
+  KL("k_helm_v", k_helm_v<<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, h->N2xz, h->vvc, h->p, h->a3s, g, h->sc, kRK,
+                                     h->ib ? h->d_ibslot_v : nullptr, h->duib));
+  if (g.flag_ctpress == 0) { KL("k_meanflow", k_meanflow<<<1, 32, 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw)); }
+  KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
+  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->a3s, g, h->sc, kRK));
+  KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }
 
@@ -534,9 +530,8 @@ static int step_launches(lh_handle *h) {
   int rc;
   for (int k = 1; k <= 3; ++k)
     if ((rc = substep_launches(h, k))) return rc;
-  if (h->g.flag_ctpress == 1) { k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, 0); LAUNCHED(); }
-  k_step_end<<<1, 32, 0, h->st>>>(h->sc);
-  LAUNCHED();
+  if (h->g.flag_ctpress == 1) { KL("k_flowrate", k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, 0)); }
+  KL("k_step_end", k_step_end<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }
 
@@ -562,6 +557,40 @@ extern "C" int lh_step(lh_handle *h) {
   }
   CK(cudaGraphLaunch(h->gexec, h->st));
   h->launches += h->graph_nodes_per_step;
+  return LH_OK;
+}
+
+extern "C" int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, int nmax, int *nout) {
+  if (!h || nsteps <= 0 || !out || nmax <= 0 || !nout) return LH_EINVAL;
+  CK(cudaStreamSynchronize(h->st));
+  h->prof = true;
+  h->prof_ev.clear();
+  int rc = LH_OK;
+  for (int k = 0; k < nsteps && rc == LH_OK; ++k) rc = step_launches(h);
+  h->prof = false;
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  int n = 0;
+  for (auto &pe : h->prof_ev) {
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, pe.second.first, pe.second.second);
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+    int i = 0;
+    for (; i < n; ++i)
+      if (strncmp(out[i].name, pe.first, sizeof(out[i].name)) == 0) break;
+    if (i == n) {
+      if (n >= nmax) continue;
+      memset(&out[n], 0, sizeof(out[n]));
+      strncpy(out[n].name, pe.first, sizeof(out[n].name) - 1);
+      ++n;
+    }
+    out[i].launches += 1;
+    out[i].total_ms += ms;
+  }
+  h->prof_ev.clear();
+  *nout = n;
+  if (rc != LH_OK) return rc;
+  if (e != cudaSuccess) return fail(h, LH_ECUDA, cudaGetErrorString(e));
   return LH_OK;
 }
 

@@ -892,8 +892,8 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__r
 // duib layout: [ibslot][field 0..2][col]; ib levels of u (fields 0, 2) and v (1).
 // ============================================================================
 __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
-                                                const double2 *__restrict__ u3, const double2 *__restrict__ Nu1o,
-                                                const double2 *__restrict__ Nu2o, const double2 *__restrict__ Nu3o,
+                                                const double2 *__restrict__ u3, double2 *__restrict__ Nu1o,
+                                                double2 *__restrict__ Nu2o, double2 *__restrict__ Nu3o,
                                                 const double2 *__restrict__ N1xz, const double2 *__restrict__ N2xz,
                                                 const double2 *__restrict__ N3xz, const double2 *__restrict__ uvf,
                                                 const double2 *__restrict__ vvc, const double2 *__restrict__ wvf,
@@ -918,7 +918,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     const double th = g.thu[qu];
     for (int f = 0; f < 2; ++f) {
       const double2 *U = f ? u3 : u1;
-      const double2 *No = f ? Nu3o : Nu1o;
+      double2 *No = f ? Nu3o : Nu1o;
       const double2 *X = f ? N3xz : N1xz;
       const double2 *F = f ? wvf : uvf;
       const double C3 = f ? C3z : C3x;
@@ -933,6 +933,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
       const double2 x = X[o], fq = F[o], fm = F[o - nc];
       double2 n;
       n.x = x.x + (fq.x - fm.x) * th * g.dd; n.y = x.y + (fq.y - fm.y) * th * g.dd;
+      No[o] = n;  // N of this substep (the next substep's -cRK term)
       du.x = du.x + G * n.x; du.y = du.y + G * n.y;
       duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = du;
     }
@@ -954,6 +955,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     const double2 x = N2xz[o], vp1 = vvc[o + nc], vq = vvc[o];
     double2 n;
     n.x = x.x + (vp1.x - vq.x) * th * g.dd; n.y = x.y + (vp1.y - vq.y) * th * g.dd;
+    Nu2o[o] = n;
     du.x = du.x + G * n.x; du.y = du.y + G * n.y;
     duib[((size_t)s * 3 + 1) * nc + c] = du;
   }

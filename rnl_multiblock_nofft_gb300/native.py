@@ -18,7 +18,12 @@ _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
-           "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches")
+           "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
+           "lh_profile_steps")
+
+
+class LhKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int32), ("total_ms", C.c_double)]
 
 
 class LhError(RuntimeError):
@@ -54,6 +59,7 @@ def load(path: str = _LIB_PATH):
     L.lh_phys_to_four.argtypes = [vp, vp, vp, i]
     L.lh_kernel_launches.argtypes = [vp]
     L.lh_kernel_launches.restype = C.c_int64
+    L.lh_profile_steps.argtypes = [vp, i, C.POINTER(LhKernelTime), i, C.POINTER(i)]
     _lib = L
     return L
 
@@ -105,8 +111,14 @@ class GpuChannel:
                 raise ValueError(f"shape {a.shape} != {sh}")
         self._check(self.L.lh_upload_state(self.h, *[_dptr(a) for a in arrs]))
 
-    def download_state(self):
-        out = [np.zeros(sh, np.complex128) for sh in self.shapes]
+    def download_state(self, out=None):
+        """Returns (u1, u2, u3, p); `out` may supply C-contiguous complex128 arrays
+        (e.g. views of pinned host memory) to receive them."""
+        if out is None:
+            out = [np.zeros(sh, np.complex128) for sh in self.shapes]
+        for a, sh in zip(out, self.shapes):
+            if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                raise ValueError("download buffers must be C-contiguous complex128 of the state shapes")
         self._check(self.L.lh_download_state(self.h, *[_dptr(a) for a in out]))
         return out
 
@@ -134,6 +146,13 @@ class GpuChannel:
 
     def kernel_launches(self) -> int:
         return int(self.L.lh_kernel_launches(self.h))
+
+    def profile_steps(self, nsteps: int) -> dict:
+        """{kernel name: (launches, total ms)} over `nsteps` eager steps."""
+        buf = (LhKernelTime * 64)()
+        n = C.c_int(0)
+        self._check(self.L.lh_profile_steps(self.h, nsteps, buf, 64, C.byref(n)))
+        return {buf[k].name.decode(): (buf[k].launches, buf[k].total_ms) for k in range(n.value)}
 
     def stream(self) -> int:
         return int(self.L.lh_stream(self.h) or 0)
