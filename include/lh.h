@@ -147,6 +147,28 @@ typedef struct lh_kernel_time {
 } lh_kernel_time;
 int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, int nmax, int *nout);
 
+/* ---- four_to_phys without a handle and without allocating ----
+ * No counterpart in the reference. For callers that cannot call cudaMalloc: hosts
+ * that own every byte of device memory themselves (a solver that sizes HBM once at
+ * start-up and forbids later allocation, or one running at the edge of the
+ * device's capacity) and therefore cannot create a handle, since lh_create
+ * allocates the whole channel state. Same transform as lh_four_to_phys on
+ * `nplanes` spectral planes [N2][N1/2+1] complex128 -> physical [Ngal2][Ngal1]
+ * double, caller-owned device buffers, on `stream` (cudaStream_t as void*,
+ * NULL = default stream). Its working memory is a fixed device array of
+ * LH_NOALLOC_SCRATCH_BYTES inside the library, which every GPU that loads the
+ * library holds until exit. It must hold the two twiddle tables and the
+ * intermediate planes: 16*Ngal1 and 16*Ngal2 bytes (each rounded up to 256) plus
+ * nplanes * Ngal2 * (N1/2+1) * 16 bytes; larger requests are rejected with
+ * LH_EINVAL and *err (if not NULL) points to a static message. The first call on a device
+ * does a one-time set-up for that device (looks up the array's device address and
+ * sets the kernels' shared-memory limit); make that first call before any stream
+ * capture. Every call shares the one array and overwrites what it needs, so calls
+ * that overlap on the GPU (other streams, other host threads) race: serialise them. */
+#define LH_NOALLOC_SCRATCH_BYTES (32u << 20)
+int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, const void *spec, void *phys,
+                            int nplanes, void *stream, const char **err);
+
 #ifdef __cplusplus
 }
 #endif

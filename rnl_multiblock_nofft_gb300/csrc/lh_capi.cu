@@ -616,3 +616,103 @@ extern "C" int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int n
   if (need > h->Bbytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
   return phys_to_spec(h, (const double *)phys, (double2 *)spec, nplanes, (double2 *)h->B, fp64_tw(h, true), fp64_tw(h, false));
 }
+
+// ===========================================================================
+// lh_four_to_phys_noalloc: the four_to_phys transform without a handle and
+// without any device allocation.
+//
+// Who needs it: hosts that own every byte of device memory themselves (a
+// Fortran solver that sizes HBM once at start-up and forbids later allocation,
+// or an application running at the edge of the device's capacity) cannot call
+// cudaMalloc, and so cannot create a handle (lh_create allocates the whole
+// channel state). This entry point takes only the caller's input and output
+// buffers; its working memory is the fixed array below, which every GPU that
+// loads the library holds until the process exits.
+// ===========================================================================
+static __device__ __align__(256) unsigned char lh_noalloc_scratch[LH_NOALLOC_SCRATCH_BYTES];
+
+// exp(-2 pi i e / n) for the two transform lengths, written by every call
+__global__ void k_noalloc_twiddles(double2 *twx, int n1, double2 *twz, int n2) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n1) { double s, c; sincospi(-2.0 * (double)e / (double)n1, &s, &c); twx[e] = make_double2(c, s); }
+  if (e < n2) { double s, c; sincospi(-2.0 * (double)e / (double)n2, &s, &c); twz[e] = make_double2(c, s); }
+}
+
+namespace {
+const int LH_NOALLOC_MAX_DEVICES = 256;
+unsigned char *g_noalloc_ptr[LH_NOALLOC_MAX_DEVICES];
+bool g_noalloc_ready[LH_NOALLOC_MAX_DEVICES];
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Set-up, once per device, with that device current: the device address of the
+// scratch array (a host-side name of a __device__ array is not a device address)
+// and the shared-memory limit of the two kernels.
+int noalloc_setup(int dev, unsigned char **ptr, const char **err) {
+  if (dev < 0 || dev >= LH_NOALLOC_MAX_DEVICES) { if (err) *err = "device index out of range"; return LH_EINVAL; }
+  if (!g_noalloc_ready[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, lh_noalloc_scratch) != cudaSuccess || !p) {
+      if (err) *err = "cudaGetSymbolAddress of the scratch array failed";
+      return LH_ECUDA;
+    }
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 49152;
+    if (cudaFuncSetAttribute((const void *)k_spec_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_xinv_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+      if (err) *err = "cudaFuncSetAttribute failed";
+      return LH_ECUDA;
+    }
+    g_noalloc_ptr[dev] = (unsigned char *)p;
+    g_noalloc_ready[dev] = true;
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return LH_OK;
+}
+}  // namespace
+
+static size_t noalloc_max_planes(int N1, int N2, int Ngal1, int Ngal2) {
+  if (N1 <= 0 || N2 <= 0 || Ngal1 <= 0 || Ngal2 <= 0) return 0;
+  const size_t tw = align256(sizeof(double2) * (size_t)Ngal1) + align256(sizeof(double2) * (size_t)Ngal2);
+  const size_t plane = sizeof(double2) * (size_t)Ngal2 * (size_t)(N1 / 2 + 1);
+  if (tw >= LH_NOALLOC_SCRATCH_BYTES || plane == 0) return 0;
+  return (LH_NOALLOC_SCRATCH_BYTES - tw) / plane;
+}
+
+extern "C" int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, const void *spec, void *phys,
+                                       int nplanes, void *stream, const char **err) {
+  if (err) *err = "";
+  RadixPlan px, pz;
+  if (N1 <= 0 || N2 <= 0 || (N1 & 1) || (N2 & 1) || Ngal1 <= N1 || Ngal2 <= N2 || (Ngal1 & 1) || (Ngal2 & 1) ||
+      !make_plan(Ngal1, px) || !make_plan(Ngal2, pz) || !spec || !phys || nplanes <= 0) {
+    if (err) *err = "invalid sizes or pointers (Ngal > N, even, factors 2/3/4 only)";
+    return LH_EINVAL;
+  }
+  if ((size_t)nplanes > noalloc_max_planes(N1, N2, Ngal1, Ngal2)) {
+    if (err) *err = "too many planes for the fixed scratch of LH_NOALLOC_SCRATCH_BYTES; split the call";
+    return LH_EINVAL;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { if (err) *err = "cudaGetDevice failed"; return LH_ECUDA; }
+  unsigned char *base = nullptr;
+  int rc = noalloc_setup(dev, &base, err);
+  if (rc != LH_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  double2 *twx = (double2 *)base;
+  double2 *twz = (double2 *)(base + align256(sizeof(double2) * (size_t)Ngal1));
+  double2 *Ascr = (double2 *)(base + align256(sizeof(double2) * (size_t)Ngal1) + align256(sizeof(double2) * (size_t)Ngal2));
+  Geo g;
+  memset(&g, 0, sizeof(g));
+  g.N1 = N1; g.N2 = N2; g.N1h = N1 / 2 + 1; g.G1 = Ngal1; g.G2 = Ngal2; g.ncol = g.N1h * N2;
+  const int KB = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * sizeof(double2))), 1, g.N1h < 16 ? g.N1h : 16);
+  const int PB = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G1 * sizeof(double2))), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
+  const int nt = Ngal1 > Ngal2 ? Ngal1 : Ngal2;
+  k_noalloc_twiddles<<<(nt + 255) / 256, 256, 0, st>>>(twx, Ngal1, twz, Ngal2);
+  dim3 g1((g.N1h + KB - 1) / KB, nplanes);
+  k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)KB * g.G2 * sizeof(double2), st>>>((const double2 *)spec, Ascr, g, pz, twz, KB);
+  dim3 g2((g.G2 / 2 + PB - 1) / PB, nplanes);
+  k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)PB * g.G1 * sizeof(double2), st>>>(Ascr, (double *)phys, g, px, twx, PB);
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) { if (err) *err = "kernel launch failed"; return LH_ECUDA; }
+  return LH_OK;
+}

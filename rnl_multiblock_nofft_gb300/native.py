@@ -19,7 +19,7 @@ _lib = None
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
-           "lh_profile_steps")
+           "lh_profile_steps", "lh_four_to_phys_noalloc")
 
 
 class LhKernelTime(C.Structure):
@@ -60,6 +60,7 @@ def load(path: str = _LIB_PATH):
     L.lh_kernel_launches.argtypes = [vp]
     L.lh_kernel_launches.restype = C.c_int64
     L.lh_profile_steps.argtypes = [vp, i, C.POINTER(LhKernelTime), i, C.POINTER(i)]
+    L.lh_four_to_phys_noalloc.argtypes = [i, i, i, i, vp, vp, i, vp, C.POINTER(C.c_char_p)]
     _lib = L
     return L
 
