@@ -13,7 +13,6 @@
 
 namespace {
 const int NTHR_H = 256;
-const size_t SMEM_BUDGET = 98304;  // two blocks per SM
 }
 
 struct lh_handle {
@@ -24,11 +23,10 @@ struct lh_handle {
   Geo g;
   int prec;  // LH_PREC_*
   size_t vsz;  // bytes of one complex value in the transforms
-  RadixPlan px, pz;
-  int KBz, PBx, KBf, KBs, PBs;
   cudaStream_t st;
   // device buffers
-  double2 *u1, *u2, *u3, *p, *Nu1, *Nu2, *Nu3, *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf, *psi;
+  double2 *u1, *u2, *u3, *p, *Nu1, *Nu2, *Nu3, *psi;
+  void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
   double *a3s, *mfw;
   void *A, *B, *twx, *twz, *twx64, *twz64;
   size_t Abytes, Bbytes;
@@ -63,16 +61,6 @@ static int fail(lh_handle *h, int code, const std::string &msg) {
     if (e__ != cudaSuccess)                                                                 \
       return fail(h, LH_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e__));        \
   } while (0)
-
-static bool make_plan(int n, RadixPlan &P) {
-  P.n = n;
-  P.nst = 0;
-  int m = n;
-  while (m % 4 == 0) { P.rad[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0) { P.rad[P.nst++] = 2; m /= 2; }
-  while (m % 3 == 0) { P.rad[P.nst++] = 3; m /= 3; }
-  return m == 1 && P.nst <= LH_MAX_STAGES;
-}
 
 template <typename T>
 static void twiddles(int n, std::vector<T> &out) {
@@ -117,32 +105,66 @@ static int count_launch(lh_handle *h) {
     if (rc__ != LH_OK) return rc__;   \
   } while (0)
 
-template <typename T>
-static int set_smem_attrs(lh_handle *h) {
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  int optin = 0;
-  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  int lim = optin > 0 ? optin : 49152;
-  CK(cudaFuncSetAttribute((const void *)k_zinv_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  CK(cudaFuncSetAttribute((const void *)k_xpass_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  CK(cudaFuncSetAttribute((const void *)k_zfwd_nl<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  return LH_OK;
+// FFT lengths compiled into the library (Ngal values of every workload)
+#define LH_FOR_SIZES(X) X(24) X(48) X(72) X(96) X(144) X(192) X(288) X(384) X(576) X(768) X(1152)
+static bool size_supported(int n) {
+  switch (n) {
+#define LH_CASE_TRUE(n_) case n_: return true;
+    LH_FOR_SIZES(LH_CASE_TRUE)
+#undef LH_CASE_TRUE
+    default: return false;
+  }
 }
-static int set_smem_attrs_generic(lh_handle *h) {
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  int optin = 0;
-  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  int lim = optin > 0 ? optin : 49152;
-  CK(cudaFuncSetAttribute((const void *)k_spec_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  CK(cudaFuncSetAttribute((const void *)k_xinv_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  CK(cudaFuncSetAttribute((const void *)k_xfwd_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-  CK(cudaFuncSetAttribute((const void *)k_zfwd_spec<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+// run CALL with the compile-time constant N equal to n
+#define LH_DISPATCH(n, ...)                               \
+  switch (n) {                                            \
+    case 24: { constexpr int N = 24; __VA_ARGS__; } break;       \
+    case 48: { constexpr int N = 48; __VA_ARGS__; } break;       \
+    case 72: { constexpr int N = 72; __VA_ARGS__; } break;       \
+    case 96: { constexpr int N = 96; __VA_ARGS__; } break;       \
+    case 144: { constexpr int N = 144; __VA_ARGS__; } break;     \
+    case 192: { constexpr int N = 192; __VA_ARGS__; } break;     \
+    case 288: { constexpr int N = 288; __VA_ARGS__; } break;     \
+    case 384: { constexpr int N = 384; __VA_ARGS__; } break;     \
+    case 576: { constexpr int N = 576; __VA_ARGS__; } break;     \
+    case 768: { constexpr int N = 768; __VA_ARGS__; } break;     \
+    case 1152: { constexpr int N = 1152; __VA_ARGS__; } break;   \
+    default: break;                                       \
+  }
+
+template <typename T, int N>
+static cudaError_t set_attrs_sized(int lim) {
+  cudaError_t e = cudaSuccess;
+  const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv_nl<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass_nl<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_nl<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xfwd_phys<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec<T, N>, A, lim);
+  return e;
+}
+
+static int smem_optin(int *lim) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return -1;
+  *lim = optin > 0 ? optin : 49152;
+  return 0;
+}
+
+static int set_smem_attrs_all(lh_handle *h) {
+  int lim = 0;
+  if (smem_optin(&lim)) return fail(h, LH_ECUDA, "cudaDeviceGetAttribute");
+  cudaError_t e = cudaSuccess;
+  for (int n : {h->g.G1, h->g.G2}) {
+    LH_DISPATCH(n, e = set_attrs_sized<double, N>(lim); if (e == cudaSuccess) e = set_attrs_sized<float, N>(lim));
+    if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  }
   return LH_OK;
 }
 
-static int clampi(long v, int lo, int hi) { return (int)(v < lo ? lo : (v > hi ? hi : v)); }
 
 extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   lh_handle *h = nullptr;
@@ -163,14 +185,11 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->vsz = (h->prec == LH_PREC_FP64) ? sizeof(double2) : sizeof(float2);
   h->graph_ready = false;
   h->launches = 0;
-  RadixPlan px, pz;
-  if (!make_plan(cfg->Ngal1, px) || !make_plan(cfg->Ngal2, pz)) {
-    int rc = fail(h, LH_EINVAL, "Ngal must factor into 2, 3 and 4");
+  if (!size_supported(cfg->Ngal1) || !size_supported(cfg->Ngal2)) {
+    int rc = fail(h, LH_EINVAL, "Ngal must be one of 24 48 72 96 144 192 288 384 576 768 1152");
     delete h;
     return rc;
   }
-  h->px = px;
-  h->pz = pz;
   Geo &g = h->g;
   g.N1 = cfg->N1; g.N2 = cfg->N2; g.N1h = cfg->N1 / 2 + 1; g.G1 = cfg->Ngal1; g.G2 = cfg->Ngal2;
   g.dny = cfg->dny; g.nu = cfg->nyu; g.nv = cfg->nyv; g.np = cfg->nyu - 2; g.ncol = g.N1h * g.N2;
@@ -189,15 +208,16 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   std::vector<double> pool;
   auto put = [&](const double *src, size_t n) { size_t o = pool.size(); pool.insert(pool.end(), src, src + n); return o; };
   std::vector<double> iua(nu, 1.0), iub(nu, 0.0), iud(nu, 1.0), iva(nv, 1.0), ivb(nv, 0.0), ivd(nv, 1.0);
+  // interp_v / interp_u weights (FOU3D.f90:427-474) as ratios: one multiply-add per value
   for (int q = 1; q <= nu - 2; ++q) {
-    iua[q] = cfg->yu[q] - cfg->yv[q - 1];
-    iub[q] = cfg->yv[q] - cfg->yu[q];
     iud[q] = cfg->yv[q] - cfg->yv[q - 1];
+    iua[q] = (cfg->yu[q] - cfg->yv[q - 1]) / iud[q];
+    iub[q] = (cfg->yv[q] - cfg->yu[q]) / iud[q];
   }
   for (int q = 0; q <= nv - 1; ++q) {
-    iva[q] = cfg->yv[q] - cfg->yu[q];
-    ivb[q] = cfg->yu[q + 1] - cfg->yv[q];
     ivd[q] = cfg->yu[q + 1] - cfg->yu[q];
+    iva[q] = (cfg->yv[q] - cfg->yu[q]) / ivd[q];
+    ivb[q] = (cfg->yu[q + 1] - cfg->yv[q]) / ivd[q];
   }
   size_t o_yu = put(cfg->yu, nu), o_yv = put(cfg->yv, nv), o_thu = put(cfg->dthdyu, nu), o_thv = put(cfg->dthdyv, nv);
   size_t o_d2u = put(cfg->dyu2i, 3 * (size_t)nu), o_d2v = put(cfg->dyv2i, 3 * (size_t)nv);
@@ -212,13 +232,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   g.k1x = P + o_k1x; g.k2x = P + o_k2x; g.k1z = P + o_k1z; g.k2z = P + o_k2z;
   g.iua = P + o_iua; g.iub = P + o_iub; g.iud = P + o_iud; g.iva = P + o_iva; g.ivb = P + o_ivb; g.ivd = P + o_ivd;
 
-  // transform tiling from the shared-memory budget
   const size_t vs = h->vsz;
-  h->KBz = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * vs)), 1, g.N1h < 16 ? g.N1h : 16);
-  h->PBx = clampi((long)(SMEM_BUDGET / (8 * (size_t)g.G1 * vs)), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
-  h->KBf = clampi((long)(SMEM_BUDGET / (8 * (size_t)g.G2 * vs)), 1, g.N1h < 8 ? g.N1h : 8);
-  h->KBs = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * sizeof(double2))), 1, g.N1h < 16 ? g.N1h : 16);
-  h->PBs = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G1 * sizeof(double2))), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
 
   size_t nc = g.ncol;
   auto zalloc = [&](void **ptr, size_t bytes) -> cudaError_t {
@@ -239,10 +253,10 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   const size_t cz = sizeof(double2);
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
   ZA(h->Nu1, cz * nu * nc); ZA(h->Nu3, cz * nu * nc); ZA(h->Nu2, cz * nv * nc);
-  ZA(h->N1xz, cz * nu * nc); ZA(h->N3xz, cz * nu * nc); ZA(h->vvc, cz * nu * nc);
-  ZA(h->N2xz, cz * nv * nc); ZA(h->uvf, cz * nv * nc); ZA(h->wvf, cz * nv * nc);
+  ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
+  ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
   ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
-  ZA(h->mfw, sizeof(double) * 4 * (size_t)(g.nn + 3));
+  ZA(h->mfw, sizeof(double) * 6 * (size_t)(g.nn + 3));
   h->Abytes = vs * (size_t)(g.nuI + g.nvI) * 3 * g.G2 * g.N1h;
   h->Bbytes = vs * (size_t)(4 * g.nuI + 2 * g.nvI) * g.N1h * g.G2;
   ZA(h->A, h->Abytes);
@@ -326,8 +340,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
     int rc = fail(h, LH_ECUDA, "cudaStreamCreate"); lh_destroy(h); return rc;
   }
-  int rc = (h->prec == LH_PREC_FP64) ? set_smem_attrs<double>(h) : set_smem_attrs<float>(h);
-  if (rc == LH_OK) rc = set_smem_attrs_generic(h);
+  int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
   // keep host copies of the arrays
   h->h_yu.assign(cfg->yu, cfg->yu + nu);
@@ -436,89 +449,158 @@ extern "C" int lh_get_scalars(lh_handle *h, lh_scalars *s) {
 // ---------------------------------------------------------------------------
 // one substep
 // ---------------------------------------------------------------------------
+template <typename T, int N>
+static int launch_zinv(lh_handle *h, int nslots) {
+  typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
+  const Geo &g = h->g;
+  dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
+  KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
+                      h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)h->twz));
+  return LH_OK;
+}
+template <typename T, int N>
+static int launch_xpass(lh_handle *h, int nslots, int doCFL) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = pb_xpass<V>(N);
+  const Geo &g = h->g;
+  dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
+  KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, NTHR_H, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
+                       (const V *)h->A, (V *)h->B, g, (const V *)h->twx, doCFL, h->sc,
+                       h->ib ? h->d_capslot : nullptr, h->cap));
+  return LH_OK;
+}
+template <typename T, int N>
+static int launch_zfwd(lh_handle *h, int nslots) {
+  typedef typename C2<T>::t V;
+  constexpr int KB = kb_zfwd<V>(N);
+  const Geo &g = h->g;
+  dim3 grid((g.N1h + KB - 1) / KB, nslots);
+  KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, NTHR_H, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
+                      (const V *)h->B, g, (const V *)h->twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
+                      (V *)h->vvc, (V *)h->wvf));
+  return LH_OK;
+}
+
 template <typename T>
 static int nonlinear_transforms(lh_handle *h, int kRK) {
+  const Geo &g = h->g;
+  const int nslots = g.nuI + g.nvI;
+  int rc = LH_EINVAL;
+  if (kRK == 1) KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc));
+  LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, nslots));
+  if (rc) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(g.G1, rc = launch_xpass<T, N>(h, nslots, kRK == 1 ? 1 : 0));
+  if (rc) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(g.G2, rc = launch_zfwd<T, N>(h, nslots));
+  return rc;
+}
+
+// plane transforms through scratch buffers in precision T (leaves: FP64; immersed
+// boundaries: the form's transform precision)
+template <typename T, int N>
+static int launch_spec_zinv(lh_handle *h, const double2 *spec, void *Ascr, int npl, const void *twz) {
+  typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
+  dim3 g1((h->g.N1h + KB - 1) / KB, npl);
+  KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(spec, (V *)Ascr, h->g, (const V *)twz));
+  return LH_OK;
+}
+template <typename T, int N>
+static int launch_xinv_phys(lh_handle *h, const void *Ascr, double *phys, int npl, const void *twx) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  dim3 g2((h->g.G2 / 2 + PB - 1) / PB, npl);
+  KL("k_xinv_phys", k_xinv_phys<T, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>((const V *)Ascr, phys, h->g, (const V *)twx));
+  return LH_OK;
+}
+template <typename T, int N>
+static int launch_xfwd_phys(lh_handle *h, const double *phys, void *Bscr, int npl, const void *twx) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  dim3 g1((h->g.G2 / 2 + PB - 1) / PB, npl);
+  KL("k_xfwd_phys", k_xfwd_phys<T, N><<<g1, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>(phys, (V *)Bscr, h->g, (const V *)twx));
+  return LH_OK;
+}
+template <typename T, int N>
+static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int npl, const void *twz) {
+  typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
+  dim3 g2((h->g.N1h + KB - 1) / KB, npl);
+  KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, spec, h->g, (const V *)twz));
+  return LH_OK;
+}
+
+template <typename T>
+static int spec_to_phys(lh_handle *h, const double2 *spec, double *phys, int npl, void *Ascr, const void *twx,
+                        const void *twz) {
+  int rc = LH_EINVAL;
+  LH_DISPATCH(h->g.G2, rc = launch_spec_zinv<T, N>(h, spec, Ascr, npl, twz));
+  if (rc) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(h->g.G1, rc = launch_xinv_phys<T, N>(h, Ascr, phys, npl, twx));
+  return rc;
+}
+template <typename T>
+static int phys_to_spec(lh_handle *h, const double *phys, double2 *spec, int npl, void *Bscr, const void *twx,
+                        const void *twz) {
+  int rc = LH_EINVAL;
+  LH_DISPATCH(h->g.G1, rc = launch_xfwd_phys<T, N>(h, phys, Bscr, npl, twx));
+  if (rc) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(h->g.G2, rc = launch_zfwd_spec<T, N>(h, Bscr, spec, npl, twz));
+  return rc;
+}
+
+static const void *fp64_tw(lh_handle *h, bool x) { return x ? h->twx64 : h->twz64; }
+
+template <typename T>
+static int substep_launches_t(lh_handle *h, int kRK) {
   typedef typename C2<T>::t V;
   const Geo &g = h->g;
-  const size_t vs = sizeof(V);
-  const int nslots = g.nuI + g.nvI;
-  if (kRK == 1) { KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc)); }
-  {
-    dim3 grid((g.N1h + h->KBz - 1) / h->KBz, nslots, 3);
-    size_t sm = 2 * (size_t)h->KBz * g.G2 * vs;
-    KL("k_zinv_nl", k_zinv_nl<T><<<grid, NTHR_H, sm, h->st>>>(h->u1, h->u2, h->u3, (V *)h->A, g, h->pz, (const V *)h->twz, h->KBz));
-  }
-  {
-    dim3 grid((g.G2 / 2 + h->PBx - 1) / h->PBx, nslots);
-    size_t sm = 8 * (size_t)h->PBx * g.G1 * vs;
-    KL("k_xpass_nl", k_xpass_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->A, (V *)h->B, g, h->px, (const V *)h->twx, h->PBx,
-                                                kRK == 1 ? 1 : 0, h->sc, h->ib ? h->d_capslot : nullptr, h->cap));
-  }
-  {
-    dim3 grid((g.N1h + h->KBf - 1) / h->KBf, nslots);
-    size_t sm = 8 * (size_t)h->KBf * g.G2 * vs;
-    KL("k_zfwd_nl", k_zfwd_nl<T><<<grid, NTHR_H, sm, h->st>>>((const V *)h->B, g, h->pz, (const V *)h->twz, h->KBf, h->N1xz, h->N2xz,
-                                               h->N3xz, h->uvf, h->vvc, h->wvf));
-  }
-  return LH_OK;
-}
-
-// FP64 plane transforms through the scratch buffers (leaves and immersed boundaries)
-static int spec_to_phys(lh_handle *h, const double2 *spec, double *phys, int npl, double2 *Ascr, const double2 *twx,
-                        const double2 *twz) {
-  const Geo &g = h->g;
-  dim3 g1((g.N1h + h->KBs - 1) / h->KBs, npl);
-  KL("k_spec_zinv", k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(spec, Ascr, g, h->pz, twz, h->KBs));
-  dim3 g2((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
-  KL("k_xinv_phys", k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(Ascr, phys, g, h->px, twx, h->PBs));
-  return LH_OK;
-}
-static int phys_to_spec(lh_handle *h, const double *phys, double2 *spec, int npl, double2 *Bscr, const double2 *twx,
-                        const double2 *twz) {
-  const Geo &g = h->g;
-  dim3 g1((g.G2 / 2 + h->PBs - 1) / h->PBs, npl);
-  KL("k_xfwd_phys", k_xfwd_phys<double><<<g1, NTHR_H, 2 * (size_t)h->PBs * g.G1 * sizeof(double2), h->st>>>(phys, Bscr, g, h->px, twx, h->PBs));
-  dim3 g2((g.N1h + h->KBs - 1) / h->KBs, npl);
-  KL("k_zfwd_spec", k_zfwd_spec<double><<<g2, NTHR_H, 2 * (size_t)h->KBs * g.G2 * sizeof(double2), h->st>>>(Bscr, spec, g, h->pz, twz, h->KBs, nullptr));
-  return LH_OK;
-}
-
-static const double2 *fp64_tw(lh_handle *h, bool x) { return (const double2 *)(x ? h->twx64 : h->twz64); }
-
-static int substep_launches(lh_handle *h, int kRK) {
-  const Geo &g = h->g;
-  int rc = (h->prec == LH_PREC_FP64) ? nonlinear_transforms<double>(h, kRK) : nonlinear_transforms<float>(h, kRK);
+  int rc = nonlinear_transforms<T>(h, kRK);
   if (rc) return rc;
-  if (kRK == 1) { KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc)); }
+  if (kRK == 1) KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc));
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
   if (h->ib) {
     dim3 gd(nb, h->nib);
-    KL("k_ib_du", k_ib_du<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf,
-                                       h->vvc, h->wvf, h->p, h->duib, h->d_iblev, h->nib, g, h->sc, kRK));
-    const double2 *twx = fp64_tw(h, true), *twz = fp64_tw(h, false);
-    if ((rc = spec_to_phys(h, h->duib, h->duphys, 3 * h->nib, (double2 *)h->A, twx, twz))) return rc;
+    KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, (const V *)h->N1xz,
+                                                       (const V *)h->N2xz, (const V *)h->N3xz, (const V *)h->uvf,
+                                                       (const V *)h->vvc, (const V *)h->wvf, h->p, h->duib, h->d_iblev,
+                                                       h->nib, g, h->sc, kRK));
+    if ((rc = spec_to_phys<T>(h, h->duib, h->duphys, 3 * h->nib, h->A, h->twx, h->twz))) return rc;
     int ibu = (h->cfg.nib_u + 255) / 256, ibv = (h->cfg.nib_v + 255) / 256;
-    if (h->cfg.nib_u > 0) {
-      KL("k_ib_force", k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1, h->d_ibslot_u,
-                                         h->d_lev2cap_u, g, h->sc));
-    }
-    if (h->cfg.nib_v > 0) {
-      KL("k_ib_force", k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0, h->d_ibslot_v,
-                                         h->d_lev2cap_v, g, h->sc));
-    }
-    if ((rc = phys_to_spec(h, h->duphys, h->duib, 3 * h->nib, (double2 *)h->B, twx, twz))) return rc;
+    if (h->cfg.nib_u > 0)
+      KL("k_ib_force", k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1,
+                                                          h->d_ibslot_u, h->d_lev2cap_u, g, h->sc));
+    if (h->cfg.nib_v > 0)
+      KL("k_ib_force", k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0,
+                                                          h->d_ibslot_v, h->d_lev2cap_v, g, h->sc));
+    if ((rc = phys_to_spec<T>(h, h->duphys, h->duib, 3 * h->nib, h->B, h->twx, h->twz))) return rc;
   }
-  KL("k_helm_uw", k_helm_uw<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, h->N1xz, h->N3xz, h->uvf, h->wvf, h->p, h->a3s, g,
-                                      h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
-  KL("k_helm_v", k_helm_v<<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, h->N2xz, h->vvc, h->p, h->a3s, g, h->sc, kRK,
-                                     h->ib ? h->d_ibslot_v : nullptr, h->duib));
-  if (g.flag_ctpress == 0) { KL("k_meanflow", k_meanflow<<<1, 32, 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw)); }
+  KL("k_helm_uw", k_helm_uw<T><<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, (const V *)h->N1xz,
+                                                         (const V *)h->N3xz, (const V *)h->uvf, (const V *)h->wvf, h->p,
+                                                         h->a3s, g, h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr,
+                                                         h->duib));
+  KL("k_helm_v", k_helm_v<T><<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, (const V *)h->N2xz, (const V *)h->vvc, h->p,
+                                                       h->a3s, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr,
+                                                       h->duib));
+  if (g.flag_ctpress == 0) {
+    const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
+    const int sm = mb <= 48 * 1024 ? 1 : 0;
+    KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
+  }
   KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->a3s, g, h->sc, kRK));
   KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }
 
+static int substep_launches(lh_handle *h, int kRK) {
+  return (h->prec == LH_PREC_FP64) ? substep_launches_t<double>(h, kRK) : substep_launches_t<float>(h, kRK);
+}
 
 extern "C" int lh_substep(lh_handle *h, int kRK) {
   if (!h) return LH_EINVAL;
@@ -607,14 +689,14 @@ extern "C" int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int n
   if (!h || !spec || !phys || nplanes <= 0) return LH_EINVAL;
   const size_t need = sizeof(double2) * (size_t)nplanes * h->g.G2 * h->g.N1h;
   if (need > h->Abytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
-  return spec_to_phys(h, (const double2 *)spec, (double *)phys, nplanes, (double2 *)h->A, fp64_tw(h, true), fp64_tw(h, false));
+  return spec_to_phys<double>(h, (const double2 *)spec, (double *)phys, nplanes, h->A, fp64_tw(h, true), fp64_tw(h, false));
 }
 
 extern "C" int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes) {
   if (!h || !spec || !phys || nplanes <= 0) return LH_EINVAL;
   const size_t need = sizeof(double2) * (size_t)nplanes * h->g.G2 * h->g.N1h;
   if (need > h->Bbytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
-  return phys_to_spec(h, (const double *)phys, (double2 *)spec, nplanes, (double2 *)h->B, fp64_tw(h, true), fp64_tw(h, false));
+  return phys_to_spec<double>(h, (const double *)phys, (double2 *)spec, nplanes, h->B, fp64_tw(h, true), fp64_tw(h, false));
 }
 
 // ===========================================================================
@@ -658,8 +740,15 @@ int noalloc_setup(int dev, unsigned char **ptr, const char **err) {
     }
     int optin = 0;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 49152;
-    if (cudaFuncSetAttribute((const void *)k_spec_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess ||
-        cudaFuncSetAttribute((const void *)k_xinv_phys<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+    cudaError_t e = cudaSuccess;
+#define LH_NOALLOC_ATTR(n_)                                                                                   \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<double, n_>,                    \
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);    \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<double, n_>,                    \
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    LH_FOR_SIZES(LH_NOALLOC_ATTR)
+#undef LH_NOALLOC_ATTR
+    if (e != cudaSuccess) {
       if (err) *err = "cudaFuncSetAttribute failed";
       return LH_ECUDA;
     }
@@ -682,10 +771,9 @@ static size_t noalloc_max_planes(int N1, int N2, int Ngal1, int Ngal2) {
 extern "C" int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, const void *spec, void *phys,
                                        int nplanes, void *stream, const char **err) {
   if (err) *err = "";
-  RadixPlan px, pz;
-  if (N1 <= 0 || N2 <= 0 || (N1 & 1) || (N2 & 1) || Ngal1 <= N1 || Ngal2 <= N2 || (Ngal1 & 1) || (Ngal2 & 1) ||
-      !make_plan(Ngal1, px) || !make_plan(Ngal2, pz) || !spec || !phys || nplanes <= 0) {
-    if (err) *err = "invalid sizes or pointers (Ngal > N, even, factors 2/3/4 only)";
+  if (N1 <= 0 || N2 <= 0 || (N1 & 1) || (N2 & 1) || Ngal1 <= N1 || Ngal2 <= N2 || !size_supported(Ngal1) ||
+      !size_supported(Ngal2) || !spec || !phys || nplanes <= 0) {
+    if (err) *err = "invalid sizes or pointers (N even, Ngal > N and one of 24 48 72 96 144 192 288 384 576 768 1152)";
     return LH_EINVAL;
   }
   if ((size_t)nplanes > noalloc_max_planes(N1, N2, Ngal1, Ngal2)) {
@@ -704,14 +792,20 @@ extern "C" int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, con
   Geo g;
   memset(&g, 0, sizeof(g));
   g.N1 = N1; g.N2 = N2; g.N1h = N1 / 2 + 1; g.G1 = Ngal1; g.G2 = Ngal2; g.ncol = g.N1h * N2;
-  const int KB = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G2 * sizeof(double2))), 1, g.N1h < 16 ? g.N1h : 16);
-  const int PB = clampi((long)(SMEM_BUDGET / (2 * (size_t)g.G1 * sizeof(double2))), 1, g.G2 / 2 < 8 ? g.G2 / 2 : 8);
   const int nt = Ngal1 > Ngal2 ? Ngal1 : Ngal2;
   k_noalloc_twiddles<<<(nt + 255) / 256, 256, 0, st>>>(twx, Ngal1, twz, Ngal2);
-  dim3 g1((g.N1h + KB - 1) / KB, nplanes);
-  k_spec_zinv<double><<<g1, NTHR_H, 2 * (size_t)KB * g.G2 * sizeof(double2), st>>>((const double2 *)spec, Ascr, g, pz, twz, KB);
-  dim3 g2((g.G2 / 2 + PB - 1) / PB, nplanes);
-  k_xinv_phys<double><<<g2, NTHR_H, 2 * (size_t)PB * g.G1 * sizeof(double2), st>>>(Ascr, (double *)phys, g, px, twx, PB);
+  {
+    LH_DISPATCH(Ngal2, {
+      constexpr int KB = kb_zinv<double2>(N);
+      dim3 g1((g.N1h + KB - 1) / KB, nplanes);
+      k_spec_zinv<double, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(double2), st>>>((const double2 *)spec, Ascr, g, twz);
+    });
+    LH_DISPATCH(Ngal1, {
+      constexpr int PB = 4 * pb_xpass<double2>(N);
+      dim3 g2((g.G2 / 2 + PB - 1) / PB, nplanes);
+      k_xinv_phys<double, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(double2), st>>>(Ascr, (double *)phys, g, twx);
+    });
+  }
   cudaError_t e = cudaPeekAtLastError();
   if (e != cudaSuccess) { if (err) *err = "kernel launch failed"; return LH_ECUDA; }
   return LH_OK;

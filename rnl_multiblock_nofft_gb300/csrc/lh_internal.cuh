@@ -11,14 +11,6 @@
 
 #include "../../include/lh.h"
 
-#define LH_MAX_STAGES 16
-
-struct RadixPlan {
-  int n;
-  int nst;
-  int rad[LH_MAX_STAGES];
-};
-
 // Geometry and coefficients, passed to kernels by value.
 struct Geo {
   int N1, N2, N1h, G1, G2, dny, nu, nv, np, ncol, nuI, nvI, nn;
@@ -64,8 +56,8 @@ template <typename V> __device__ __forceinline__ V czero() { V r; r.x = 0; r.y =
 template <typename V, typename S> __device__ __forceinline__ V cimul(S k, V a) { V r; r.x = -k * a.y; r.y = k * a.x; return r; }
 
 // ---------------------------------------------------------------------------
-// Stockham mixed-radix (2, 3, 4) FFT of `nl` lines of length n held in shared
-// memory, ping-ponging between two buffers. tw[e] = exp(-2 pi i e / n).
+// Stockham mixed-radix (2, 3, 4) FFT of NL lines of length N held in shared
+// memory, ping-ponging between two buffers. tw[e] = exp(-2 pi i e / N).
 // INV = true: backward (exp(+i)), unscaled. Returns the buffer holding the result.
 // ---------------------------------------------------------------------------
 template <int R, bool INV, typename V>
@@ -98,21 +90,27 @@ __device__ __forceinline__ void dftR(V *v) {
   }
 }
 
-template <int R, bool INV, typename V>
-__device__ __forceinline__ void fft_stage(const V *__restrict__ src, V *__restrict__ dst, int n, int nl,
-                                          int Ns, const V *__restrict__ tw) {
-  const int nb = n / R;
-  const int total = nb * nl;
-  const int step = n / (Ns * R);
+// ---------------------------------------------------------------------------
+// N and NL are compile-time (index arithmetic becomes shifts and multiplies); the
+// radices run 4, ..., 4, [2], 3, ..., 3. IL selects the layout
+// of the lines in shared memory: IL = false, line-contiguous (element e of line
+// l at l*N + e, threads over e); IL = true, interleaved (at e*NL + l, threads
+// over l first), which makes every stage's loads and stores bank-conflict free.
+// ---------------------------------------------------------------------------
+template <int R, bool INV, int N, int Ns, int NL, bool IL, typename V>
+__device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__restrict__ dst,
+                                            const V *__restrict__ tw) {
+  constexpr int nb = N / R;
+  constexpr int total = nb * NL;
+  constexpr int step = N / (Ns * R);
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int line = idx / nb;
-    const int j = idx - line * nb;
-    const V *in = src + line * n;
-    V *out = dst + line * n;
+    int line, j;
+    if (IL) { j = idx / NL; line = idx - j * NL; }
+    else { line = idx / nb; j = idx - line * nb; }
     const int k = j % Ns;
     V v[R];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = in[j + t * nb];
+    for (int t = 0; t < R; ++t) v[t] = IL ? src[(j + t * nb) * NL + line] : src[line * N + j + t * nb];
 #pragma unroll
     for (int t = 1; t < R; ++t) {
       V w = tw[k * step * t];
@@ -122,29 +120,31 @@ __device__ __forceinline__ void fft_stage(const V *__restrict__ src, V *__restri
     dftR<R, INV>(v);
     const int base = (j / Ns) * Ns * R + k;
 #pragma unroll
-    for (int t = 0; t < R; ++t) out[base + t * Ns] = v[t];
+    for (int t = 0; t < R; ++t) {
+      if (IL) dst[(base + t * Ns) * NL + line] = v[t];
+      else dst[line * N + base + t * Ns] = v[t];
+    }
   }
 }
 
-template <bool INV, typename V>
-__device__ V *smem_fft(V *a, V *b, int nl, const RadixPlan &P, const V *__restrict__ tw) {
-  int Ns = 1;
-  for (int s = 0; s < P.nst; ++s) {
-    const int R = P.rad[s];
-    if (R == 4) fft_stage<4, INV>(a, b, P.n, nl, Ns, tw);
-    else if (R == 2) fft_stage<2, INV>(a, b, P.n, nl, Ns, tw);
-    else fft_stage<3, INV>(a, b, P.n, nl, Ns, tw);
+template <bool INV, int N, int Ns, int NL, bool IL, typename V>
+__device__ __forceinline__ V *fft_rec_c(V *a, V *b, const V *__restrict__ tw) {
+  if constexpr (Ns >= N) {
+    return a;
+  } else {
+    constexpr int rem = N / Ns;
+    constexpr int R = (rem % 4 == 0) ? 4 : ((rem % 2 == 0) ? 2 : 3);
+    fft_stage_c<R, INV, N, Ns, NL, IL>(a, b, tw);
     __syncthreads();
-    V *t = a; a = b; b = t;
-    Ns *= R;
+    return fft_rec_c<INV, N, Ns * R, NL, IL>(b, a, tw);
   }
-  return a;
+}
+
+template <bool INV, int N, int NL, bool IL, typename V>
+__device__ __forceinline__ V *line_fft(V *a, V *b, const V *__restrict__ tw) {
+  return fft_rec_c<INV, N, 1, NL, IL>(a, b, tw);
 }
 
 // plane row (physical z index, 0-based) of spectral kz-row r
 __device__ __forceinline__ int prow(const Geo &g, int r) { return r < g.N2 / 2 ? r : r - g.N2 + g.G2; }
 
-// ---------------------------------------------------------------------------
-// kernel launch wrappers (lh_kernels.cu)
-// ---------------------------------------------------------------------------
-struct Work;  // defined in lh_kernels.cu users

@@ -37,79 +37,92 @@ __device__ __forceinline__ T warp_max(T v) {
   return v;
 }
 
+// Lines per block of the transform kernels, from a shared-memory budget of two
+// blocks per SM (same values on the host and the device).
+#define LH_SMEM_BUDGET 98304
+template <typename V> __host__ __device__ constexpr int kb_zinv(int n) {
+  return (LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))) > 16 ? 16 : (LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))));
+}
+template <typename V> __host__ __device__ constexpr int pb_xpass(int n) {
+  return (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) > 8 ? 8 : (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))));
+}
+template <typename V> __host__ __device__ constexpr int kb_zfwd(int n) {
+  return (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) > 8 ? 8 : (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))));
+}
+
 // ============================================================================
-// T1: inverse z transforms of the velocity planes (with stagger interpolation)
-// grid: x = kx group of KB lines, y = level slot (u-levels then v-levels), z = field
-// A layout: [(slot*3 + f)][l][kx], l = 0..G2-1, kx = 0..N1h-1
+// T1: inverse z transforms of the velocity planes (with stagger interpolation).
+// grid: x = kx group of KB lines, y = level slot (u-levels then v-levels), z = field.
+// A layout: [(slot*3 + f)][l][kx], l = 0..G2-1, kx = 0..N1h-1.
+// Lines are interleaved in shared memory (element l of line kk at l*KB + kk).
 // ============================================================================
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                   const double2 *__restrict__ u3, typename C2<T>::t *__restrict__ A,
-                                                  Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
-                                                  int KB) {
+                                                  Geo g, const typename C2<T>::t *__restrict__ twz) {
   typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *b0 = reinterpret_cast<V *>(smem_raw);
-  V *b1 = b0 + KB * g.G2;
+  V *b1 = b0 + KB * N;
   const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
   const bool isU = slot < g.nuI;
   const int q = isU ? slot + 1 : slot - g.nuI + 1;
   const int nc = g.ncol;
-  for (int i = threadIdx.x; i < KB * g.G2; i += blockDim.x) b0[i] = czero<V>();
+  for (int i = threadIdx.x; i < KB * N; i += blockDim.x) b0[i] = czero<V>();
   __syncthreads();
   for (int idx = threadIdx.x; idx < g.N2 * KB; idx += blockDim.x) {
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= g.N1h) continue;
     const int c = r * g.N1h + kx;
-    double2 val;
+    V v;
     if (isU) {
-      if (f == 0) val = u1[(size_t)q * nc + c];
-      else if (f == 2) val = u3[(size_t)q * nc + c];
+      if (f == 0) { const double2 x = u1[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
+      else if (f == 2) { const double2 x = u3[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
       else {  // interp_v: v faces -> centre q
-        const double a = g.iua[q], b = g.iub[q], d = g.iud[q];
+        const T a = (T)g.iua[q], b = (T)g.iub[q];
         const double2 v0 = u2[(size_t)q * nc + c], vm = u2[(size_t)(q - 1) * nc + c];
-        val.x = (a * v0.x + b * vm.x) / d;
-        val.y = (a * v0.y + b * vm.y) / d;
+        v.x = a * (T)v0.x + b * (T)vm.x;
+        v.y = a * (T)v0.y + b * (T)vm.y;
       }
     } else {
-      if (f == 1) val = u2[(size_t)q * nc + c];
+      if (f == 1) { const double2 x = u2[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
       else {  // interp_u: centres -> face q
         const double2 *src = (f == 0) ? u1 : u3;
-        const double a = g.iva[q], b = g.ivb[q], d = g.ivd[q];
+        const T a = (T)g.iva[q], b = (T)g.ivb[q];
         const double2 up = src[(size_t)(q + 1) * nc + c], u0 = src[(size_t)q * nc + c];
-        val.x = (a * up.x + b * u0.x) / d;
-        val.y = (a * up.y + b * u0.y) / d;
+        v.x = a * (T)up.x + b * (T)u0.x;
+        v.y = a * (T)up.y + b * (T)u0.y;
       }
     }
-    V v;
-    v.x = (T)val.x;
-    v.y = (T)val.y;
-    b0[kk * g.G2 + prow(g, r)] = v;
+    b0[prow(g, r) * KB + kk] = v;
   }
   __syncthreads();
-  V *res = smem_fft<true>(b0, b1, KB, pz, twz);
-  V *dst = A + (size_t)(slot * 3 + f) * g.G2 * g.N1h;
-  for (int idx = threadIdx.x; idx < g.G2 * KB; idx += blockDim.x) {
+  V *res = line_fft<true, N, KB, true>(b0, b1, twz);
+  V *dst = A + (size_t)(slot * 3 + f) * N * g.N1h;
+  for (int idx = threadIdx.x; idx < N * KB; idx += blockDim.x) {
     const int l = idx / KB, kk = idx - l * KB, kx = kx0 + kk;
-    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[kk * g.G2 + l];
+    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[l * KB + kk];
   }
 }
 
 // ============================================================================
 // T2: x pass. PB row pairs per block; each pair of rows (l, l+1) of a field is
 // carried by one complex line (row l in .x, row l+1 in .y after the transform).
-// B layout: [pslot][kx][l]; pslot = slot*4 + p (u levels), nuI*4 + (slot-nuI)*2 + p (v).
-// capture (optional): physical velocities of selected levels, [cap][l][m].
+// B layout: [pslot][l][kx]; pslot = slot*4 + p (u levels), nuI*4 + (slot-nuI)*2 + p (v).
+// capture (optional): physical velocities of selected levels, [cap][f][l][m].
 // ============================================================================
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__restrict__ A,
-                                                   typename C2<T>::t *__restrict__ B, Geo g, RadixPlan px,
-                                                   const typename C2<T>::t *__restrict__ twx, int PB, int doCFL,
+                                                   typename C2<T>::t *__restrict__ B, Geo g,
+                                                   const typename C2<T>::t *__restrict__ twx, int doCFL,
                                                    DevScalars *sc, const int *__restrict__ capslot,
                                                    double *__restrict__ cap) {
   typedef typename C2<T>::t V;
+  constexpr int PB = pb_xpass<V>(N);
+  constexpr int G1 = N, H = N / 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h, H = G1 / 2;
+  const int G2 = g.G2, N1h = g.N1h;
   V *b0 = reinterpret_cast<V *>(smem_raw);
   V *b1 = b0 + 4 * PB * G1;
   const int slot = blockIdx.y;
@@ -140,9 +153,8 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
     b0[idx] = z;
   }
   __syncthreads();
-  V *res = smem_fft<true>(b0, b1, 3 * PB, px, twx);
+  V *res = line_fft<true, N, 3 * PB, false>(b0, b1, twx);
   V *oth = (res == b0) ? b1 : b0;
-  // optional capture of physical velocities (immersed-boundary levels)
   if (capslot) {
     const int cs = capslot[slot];
     if (cs >= 0) {
@@ -152,13 +164,12 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
         if (pb >= npairs) continue;
         const int l = l0 + 2 * pb;
         double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * G1;
-        V z = res[idx];
+        const V z = res[idx];
         cp[(size_t)l * G1 + m] = (double)z.x;
         cp[(size_t)(l + 1) * G1 + m] = (double)z.y;
       }
     }
   }
-  // products, written into `oth` lines p*PB + pb
   T m1 = 0, m2 = 0, m3 = 0;
   const T thv = isU ? (T)0 : (T)g.thv[q];
   for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
@@ -196,95 +207,98 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
     }
   }
   __syncthreads();
+  V *pres = isU ? line_fft<false, N, 4 * PB, false>(oth, res, twx) : line_fft<false, N, 2 * PB, false>(oth, res, twx);
   const int nprod = isU ? 4 : 2;
-  V *pres = smem_fft<false>(oth, res, nprod * PB, px, twx);
   const T s1 = (T)1 / (T)G1;
   const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
-  // separate the two rows of each pair, keep kx = 0..N1h-1; pb fastest for coalesced writes
-  for (int idx = threadIdx.x; idx < nprod * N1h * PB; idx += blockDim.x) {
-    const int pb = idx % PB;
-    const int rest = idx / PB;
-    const int k = rest % N1h, p = rest / N1h;
+  // separate the two rows of each pair, keep kx = 0..N1h-1; kx fastest (coalesced rows)
+  for (int idx = threadIdx.x; idx < nprod * PB * 2 * N1h; idx += blockDim.x) {
+    const int k = idx % N1h;
+    const int rest = idx / N1h;
+    const int half = rest & 1;
+    const int pb = (rest >> 1) % PB, p = (rest >> 1) / PB;
     if (pb >= npairs) continue;
     const V *L = pres + (p * PB + pb) * G1;
     const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
-    V a, b;
-    a.x = (T)0.5 * (z.x + zc.x) * s1; a.y = (T)0.5 * (z.y + zc.y) * s1;
-    // -0.5 i (z - zc)
-    b.x = (T)0.5 * (z.y - zc.y) * s1; b.y = (T)-0.5 * (z.x - zc.x) * s1;
-    if (k == 0) { a.y = 0; b.y = 0; }
-    V *dst = B + ((size_t)(pbase + p) * N1h + k) * G2 + l0 + 2 * pb;
-    dst[0] = a;
-    dst[1] = b;
+    V o;
+    if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
+    else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }  // -0.5 i (z - zc)
+    if (k == 0) o.y = 0;
+    B[((size_t)(pbase + p) * G2 + l0 + 2 * pb + half) * N1h + k] = o;
   }
 }
 
 // ============================================================================
 // T3: forward z transforms + der_x/der_z. grid: x = kx group (KB), y = level slot.
 // u level: products uu, uw, vv, ww -> N1xz, N3xz, vvc.   v level: uv, wv -> N2xz, uvf, wvf.
+// Outputs are complex in the transform precision (TO = T).
 // ============================================================================
-template <typename T>
-__global__ void __launch_bounds__(NTHR) k_zfwd_nl(const typename C2<T>::t *__restrict__ B, Geo g, RadixPlan pz,
-                                                  const typename C2<T>::t *__restrict__ twz, int KB,
-                                                  double2 *__restrict__ N1xz, double2 *__restrict__ N2xz,
-                                                  double2 *__restrict__ N3xz, double2 *__restrict__ uvf,
-                                                  double2 *__restrict__ vvc, double2 *__restrict__ wvf) {
+template <typename T, int N, int NP>
+__device__ __forceinline__ void zfwd_body(const typename C2<T>::t *__restrict__ B, const Geo &g,
+                                          const typename C2<T>::t *__restrict__ twz, int slot, int q, int pbase,
+                                          typename C2<T>::t *o0, typename C2<T>::t *o1, typename C2<T>::t *o2,
+                                          typename C2<T>::t *o3, typename C2<T>::t *o4, typename C2<T>::t *o5) {
   typedef typename C2<T>::t V;
+  constexpr int KB = kb_zfwd<V>(N);
+  constexpr int NL = NP * KB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int G2 = g.G2, N1h = g.N1h, N2 = g.N2;
-  const int slot = blockIdx.y;
-  const bool isU = slot < g.nuI;
-  const int q = isU ? slot + 1 : slot - g.nuI + 1;
-  const int nprod = isU ? 4 : 2;
+  const int N1h = g.N1h, N2 = g.N2;
   const int kx0 = blockIdx.x * KB;
   V *b0 = reinterpret_cast<V *>(smem_raw);
-  V *b1 = b0 + 4 * KB * G2;
-  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
-  for (int idx = threadIdx.x; idx < nprod * KB * G2; idx += blockDim.x) {
-    const int line = idx / G2, l = idx - line * G2;
+  V *b1 = b0 + 4 * KB * N;
+  // line = p*KB + kk; element l at l*NL + line
+  for (int idx = threadIdx.x; idx < N * NL; idx += blockDim.x) {
+    const int l = idx / NL, line = idx - l * NL;
     const int p = line / KB, kk = line - p * KB, kx = kx0 + kk;
     V z = czero<V>();
-    if (kx < N1h) z = B[((size_t)(pbase + p) * N1h + kx) * G2 + l];
+    if (kx < N1h) z = B[((size_t)(pbase + p) * N + l) * N1h + kx];
     b0[idx] = z;
   }
   __syncthreads();
-  V *res = smem_fft<false>(b0, b1, nprod * KB, pz, twz);
-  const double s2 = 1.0 / (double)G2;
+  V *res = line_fft<false, N, NL, true>(b0, b1, twz);
+  const T s2 = (T)1 / (T)N;
   const size_t off = (size_t)q * g.ncol;
   for (int idx = threadIdx.x; idx < N2 * KB; idx += blockDim.x) {
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= N1h) continue;
     const int row = prow(g, r);
     const int c = r * N1h + kx;
-    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    const T kxv = (T)g.k1x[kx], kzv = (T)g.k1z[r];
     const bool zr = (r == N2 / 2);  // der_x/der_z zero the kz = -N2/2 row
-    if (isU) {
-      V t;
-      double2 uu, uw, vv, ww;
-      t = res[(0 * KB + kk) * G2 + row]; uu.x = (double)t.x * s2; uu.y = (double)t.y * s2;
-      t = res[(1 * KB + kk) * G2 + row]; uw.x = (double)t.x * s2; uw.y = (double)t.y * s2;
-      t = res[(2 * KB + kk) * G2 + row]; vv.x = (double)t.x * s2; vv.y = (double)t.y * s2;
-      t = res[(3 * KB + kk) * G2 + row]; ww.x = (double)t.x * s2; ww.y = (double)t.y * s2;
-      double2 n1 = czero<double2>(), n3 = czero<double2>();
+    if (NP == 4) {
+      const V uu = cscale(res[row * NL + 0 * KB + kk], s2), uw = cscale(res[row * NL + 1 * KB + kk], s2);
+      const V vv = cscale(res[row * NL + 2 * KB + kk], s2), ww = cscale(res[row * NL + 3 * KB + kk], s2);
+      V n1 = czero<V>(), n3 = czero<V>();
       if (!zr) {
         n1 = cadd(cimul(kxv, uu), cimul(kzv, uw));
         n3 = cadd(cimul(kxv, uw), cimul(kzv, ww));
       }
-      N1xz[off + c] = n1;
-      N3xz[off + c] = n3;
-      vvc[off + c] = vv;
+      o0[off + c] = n1;  // N1xz
+      o2[off + c] = n3;  // N3xz
+      o4[off + c] = vv;  // vvc
     } else {
-      V t;
-      double2 uv, wv;
-      t = res[(0 * KB + kk) * G2 + row]; uv.x = (double)t.x * s2; uv.y = (double)t.y * s2;
-      t = res[(1 * KB + kk) * G2 + row]; wv.x = (double)t.x * s2; wv.y = (double)t.y * s2;
-      double2 n2 = czero<double2>();
+      const V uv = cscale(res[row * NL + 0 * KB + kk], s2), wv = cscale(res[row * NL + 1 * KB + kk], s2);
+      V n2 = czero<V>();
       if (!zr) n2 = cadd(cimul(kxv, uv), cimul(kzv, wv));
-      N2xz[off + c] = n2;
-      uvf[off + c] = uv;
-      wvf[off + c] = wv;
+      o1[off + c] = n2;  // N2xz
+      o3[off + c] = uv;  // uvf
+      o5[off + c] = wv;  // wvf
     }
   }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(NTHR) k_zfwd_nl(const typename C2<T>::t *__restrict__ B, Geo g,
+                                                  const typename C2<T>::t *__restrict__ twz,
+                                                  typename C2<T>::t *__restrict__ N1xz, typename C2<T>::t *__restrict__ N2xz,
+                                                  typename C2<T>::t *__restrict__ N3xz, typename C2<T>::t *__restrict__ uvf,
+                                                  typename C2<T>::t *__restrict__ vvc, typename C2<T>::t *__restrict__ wvf) {
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  if (isU) zfwd_body<T, N, 4>(B, g, twz, slot, q, pbase, N1xz, N2xz, N3xz, uvf, vvc, wvf);
+  else zfwd_body<T, N, 2>(B, g, twz, slot, q, pbase, N1xz, N2xz, N3xz, uvf, vvc, wvf);
 }
 
 // ============================================================================
@@ -323,10 +337,14 @@ __global__ void k_reset_cfl(DevScalars *sc) {
 // sweep writes the solution in place. At immersed-boundary levels du is read from
 // `duib` (assembled and forced beforehand) instead of being formed here.
 // ============================================================================
+template <typename VN>
+__device__ __forceinline__ double2 ld2(const VN &v) { return make_double2((double)v.x, (double)v.y); }
+
+template <typename TN>
 __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, double2 *__restrict__ u3,
                                                   double2 *__restrict__ Nu1, double2 *__restrict__ Nu3,
-                                                  const double2 *__restrict__ N1xz, const double2 *__restrict__ N3xz,
-                                                  const double2 *__restrict__ uvf, const double2 *__restrict__ wvf,
+                                                  const typename C2<TN>::t *__restrict__ N1xz, const typename C2<TN>::t *__restrict__ N3xz,
+                                                  const typename C2<TN>::t *__restrict__ uvf, const typename C2<TN>::t *__restrict__ wvf,
                                                   const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
                                                   const DevScalars *__restrict__ sc, int kRK,
                                                   const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
@@ -351,11 +369,11 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
   double2 wm1 = u3[c], w0 = u3[(size_t)nc + c];
   u1[c] = y1;
   u3[c] = y3;
-  double2 uvm = uvf[c], wvm = wvf[c];
+  double2 uvm = ld2(uvf[c]), wvm = ld2(wvf[c]);
   for (int q = 1; q <= nu - 2; ++q) {
     const size_t o = (size_t)q * nc + c;
     const double2 up1 = u1[o + nc], wp1 = u3[o + nc];
-    const double2 uvq = uvf[o], wvq = wvf[o];
+    const double2 uvq = ld2(uvf[o]), wvq = ld2(wvf[o]);
     double2 du1, du3;
     const int ibs = ibslot_u ? ibslot_u[q] : -1;
     if (ibs < 0) {
@@ -371,7 +389,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
       du3.y = (C1 * L3.y + C2 * no3.y) + (C3z * pj.x);
       du1.x += mp;
       const double th = g.thu[q];
-      const double2 x1 = N1xz[o], x3 = N3xz[o];
+      const double2 x1 = ld2(N1xz[o]), x3 = ld2(N3xz[o]);
       double2 n1, n3;
       n1.x = x1.x + (uvq.x - uvm.x) * th * g.dd; n1.y = x1.y + (uvq.y - uvm.y) * th * g.dd;
       n3.x = x3.x + (wvq.x - wvm.x) * th * g.dd; n3.y = x3.y + (wvq.y - wvm.y) * th * g.dd;
@@ -425,8 +443,9 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
 // ============================================================================
 // Helmholtz v, one thread per column. Levels q = 0 .. nv-1 (walls at both ends).
 // ============================================================================
+template <typename TN>
 __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, double2 *__restrict__ Nu2,
-                                                 const double2 *__restrict__ N2xz, const double2 *__restrict__ vvc,
+                                                 const typename C2<TN>::t *__restrict__ N2xz, const typename C2<TN>::t *__restrict__ vvc,
                                                  const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
                                                  const DevScalars *__restrict__ sc, int kRK,
                                                  const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
@@ -445,11 +464,11 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
   double2 y = czero<double2>();
   double2 vm1 = u2[c], v0 = u2[(size_t)nc + c];
   u2[c] = y;
-  double2 vvq = vvc[(size_t)1 * nc + c];  // vv at u level q (interior starts at 1)
+  double2 vvq = ld2(vvc[(size_t)1 * nc + c]);  // vv at u level q (interior starts at 1)
   for (int q = 1; q <= nv - 2; ++q) {
     const size_t o = (size_t)q * nc + c;
     const double2 vp1 = u2[o + nc];
-    const double2 vvp = vvc[o + nc];  // vv at u level q+1
+    const double2 vvp = ld2(vvc[o + nc]);  // vv at u level q+1
     double2 du;
     const int ibs = ibslot_v ? ibslot_v[q] : -1;
     if (ibs < 0) {
@@ -462,7 +481,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
       du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
       du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
       const double th = g.thv[q];
-      const double2 x2 = N2xz[o];
+      const double2 x2 = ld2(N2xz[o]);
       double2 n2;
       n2.x = x2.x + (vvp.x - vvq.x) * th * g.dd; n2.y = x2.y + (vvp.y - vvq.y) * th * g.dd;
       Nu2[o] = n2;
@@ -501,41 +520,54 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
 }
 
 // ============================================================================
-// flowrate_corr (littleharsh.f90:476-509) on mode (0,0) of u1, serial (one thread)
-// u11 levels 0..nn+2 (reference levels), scratch of 4*(nn+3) doubles.
+// flowrate_corr (littleharsh.f90:476-509) on mode (0,0) of u1. The block stages the
+// coefficients, the level widths and u(0,0) in `w` (shared memory when it fits,
+// else global scratch); thread 0 runs the recurrence and the sums in the
+// reference's order; the block applies the correction.
+// w: 6*(nn+3) doubles: u11, a1, a2, a3, dy, ur
 // ============================================================================
-__global__ void k_meanflow(double2 *__restrict__ u1, Geo g, DevScalars *sc, int kRK, double *__restrict__ w) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int nn = g.nn, n = nn + 3, dny = g.dny, nc = g.ncol;
-  double *u11 = w, *a1 = w + n, *a2 = w + 2 * n, *a3 = w + 3 * n;
+__global__ void k_meanflow(double2 *__restrict__ u1, Geo g, DevScalars *sc, int kRK, double *__restrict__ wg,
+                           int use_smem) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nn = g.nn, n = nn + 3, dny = g.dny, nc = g.ncol, nu = g.nu;
+  double *w = use_smem ? reinterpret_cast<double *>(smem_raw) : wg;
+  double *u11 = w, *a1 = w + n, *a2 = w + 2 * n, *a3 = w + 3 * n, *dy = w + 4 * n, *ur = w + 5 * n;
+  __shared__ double gg_sh;
   const double dt = sc->dt;
   const double bdt = -g.dRK[kRK - 1] * dt;
   const double beta = g.bRK[kRK - 1] * dt / g.Re;
-  const int nu = g.nu;
-  u11[0] = 0.0;
-  for (int j = 1; j <= nn + 1; ++j) u11[j] = bdt;
-  u11[nn + 2] = 0.0;
-  a1[0] = 0.0; a2[0] = 1.0; a3[0] = g.gw[1][0];
-  for (int j = 1; j <= nn + 1; ++j) {
-    a1[j] = -beta * g.d2u[j + dny];
-    a2[j] = 1.0 - beta * g.d2u[nu + j + dny];
-    a3[j] = -beta * g.d2u[2 * nu + j + dny];
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (j == 0) { a1[j] = 0.0; a2[j] = 1.0; a3[j] = g.gw[1][0]; u11[j] = 0.0; }
+    else if (j == nn + 2) { a1[j] = g.gw[1][1]; a2[j] = 1.0; a3[j] = 0.0; u11[j] = 0.0; }
+    else {
+      a1[j] = -beta * g.d2u[j + dny];
+      a2[j] = 1.0 - beta * g.d2u[nu + j + dny];
+      a3[j] = -beta * g.d2u[2 * nu + j + dny];
+      u11[j] = bdt;
+    }
+    dy[j] = (j >= 1 && j <= nn + 1) ? (g.yv[j + dny] - g.yv[j - 1 + dny]) : 0.0;
+    ur[j] = u1[(size_t)(j + dny) * nc].x;
   }
-  a1[nn + 2] = g.gw[1][1]; a2[nn + 2] = 1.0; a3[nn + 2] = 0.0;
-  a2[0] = 1.0 / a2[0];
-  for (int j = 1; j < n; ++j) {
-    a3[j - 1] = a3[j - 1] * a2[j - 1];
-    a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a2[0] = 1.0 / a2[0];
+    for (int j = 1; j < n; ++j) {
+      a3[j - 1] = a3[j - 1] * a2[j - 1];
+      a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+    }
+    u11[0] = u11[0] * a2[0];
+    for (int j = 1; j < n; ++j) u11[j] = (u11[j] - a1[j] * u11[j - 1]) * a2[j];
+    for (int j = n - 2; j >= 0; --j) u11[j] = u11[j] - a3[j] * u11[j + 1];
+    double Qx1 = 0.0, Qx0 = 0.0;
+    for (int j = 1; j <= nn + 1; ++j) Qx1 = Qx1 + dy[j] * u11[j];
+    for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + dy[j] * ur[j];
+    const double gg = (sc->QxT - Qx0) / Qx1;
+    sc->mpgx = sc->mpgx + gg;
+    gg_sh = gg;
   }
-  u11[0] = u11[0] * a2[0];
-  for (int j = 1; j < n; ++j) u11[j] = (u11[j] - a1[j] * u11[j - 1]) * a2[j];
-  for (int j = n - 2; j >= 0; --j) u11[j] = u11[j] - a3[j] * u11[j + 1];
-  double Qx1 = 0.0, Qx0 = 0.0;
-  for (int j = 1; j <= nn + 1; ++j) Qx1 = Qx1 + (g.yv[j + dny] - g.yv[j - 1 + dny]) * u11[j];
-  for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + (g.yv[j + dny] - g.yv[j - 1 + dny]) * u1[(size_t)(j + dny) * nc].x;
-  const double gg = (sc->QxT - Qx0) / Qx1;
-  sc->mpgx = sc->mpgx + gg;
-  for (int j = 0; j <= nn + 2; ++j) u1[(size_t)(j + dny) * nc].x = u1[(size_t)(j + dny) * nc].x + gg * u11[j];
+  __syncthreads();
+  const double gg = gg_sh;
+  for (int j = threadIdx.x; j <= nn + 2; j += blockDim.x) u1[(size_t)(j + dny) * nc].x = ur[j] + gg * u11[j];
 }
 
 // flowrateIm of u1 (0,0): Qx (meanflow_ctP, littleharsh.f90:529-545; getini)
@@ -747,19 +779,19 @@ __global__ void k_transpose(const double2 *__restrict__ src, double2 *__restrict
 
 // ============================================================================
 // Generic plane transforms (leaves lh_four_to_phys / lh_phys_to_four and the
-// immersed-boundary round trip of du). spec [plane][N2][N1h] complex, phys
-// [plane][G2][G1] real.
+// immersed-boundary round trip of du). spec [plane][N2][N1h] complex128, phys
+// [plane][G2][G1] double, scratch A/B [plane][l][kx] in the transform precision.
 // ============================================================================
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_spec_zinv(const double2 *__restrict__ spec, typename C2<T>::t *__restrict__ A,
-                                                    Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
-                                                    int KB) {
+                                                    Geo g, const typename C2<T>::t *__restrict__ twz) {
   typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *b0 = reinterpret_cast<V *>(smem_raw);
-  V *b1 = b0 + KB * g.G2;
+  V *b1 = b0 + KB * N;
   const int pl = blockIdx.y, kx0 = blockIdx.x * KB;
-  for (int i = threadIdx.x; i < KB * g.G2; i += blockDim.x) b0[i] = czero<V>();
+  for (int i = threadIdx.x; i < KB * N; i += blockDim.x) b0[i] = czero<V>();
   __syncthreads();
   const double2 *S = spec + (size_t)pl * g.ncol;
   for (int idx = threadIdx.x; idx < g.N2 * KB; idx += blockDim.x) {
@@ -767,24 +799,25 @@ __global__ void __launch_bounds__(NTHR) k_spec_zinv(const double2 *__restrict__ 
     if (kx >= g.N1h) continue;
     const double2 val = S[r * g.N1h + kx];
     V v; v.x = (T)val.x; v.y = (T)val.y;
-    b0[kk * g.G2 + prow(g, r)] = v;
+    b0[prow(g, r) * KB + kk] = v;
   }
   __syncthreads();
-  V *res = smem_fft<true>(b0, b1, KB, pz, twz);
-  V *dst = A + (size_t)pl * g.G2 * g.N1h;
-  for (int idx = threadIdx.x; idx < g.G2 * KB; idx += blockDim.x) {
+  V *res = line_fft<true, N, KB, true>(b0, b1, twz);
+  V *dst = A + (size_t)pl * N * g.N1h;
+  for (int idx = threadIdx.x; idx < N * KB; idx += blockDim.x) {
     const int l = idx / KB, kk = idx - l * KB, kx = kx0 + kk;
-    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[kk * g.G2 + l];
+    if (kx < g.N1h) dst[(size_t)l * g.N1h + kx] = res[l * KB + kk];
   }
 }
 
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_xinv_phys(const typename C2<T>::t *__restrict__ A, double *__restrict__ phys,
-                                                    Geo g, RadixPlan px, const typename C2<T>::t *__restrict__ twx,
-                                                    int PB) {
+                                                    Geo g, const typename C2<T>::t *__restrict__ twx) {
   typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  constexpr int G1 = N, H = N / 2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h, H = G1 / 2;
+  const int G2 = g.G2, N1h = g.N1h;
   V *b0 = reinterpret_cast<V *>(smem_raw);
   V *b1 = b0 + PB * G1;
   const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
@@ -806,7 +839,7 @@ __global__ void __launch_bounds__(NTHR) k_xinv_phys(const typename C2<T>::t *__r
     b0[idx] = z;
   }
   __syncthreads();
-  V *res = smem_fft<true>(b0, b1, PB, px, twx);
+  V *res = line_fft<true, N, PB, false>(b0, b1, twx);
   double *P = phys + (size_t)pl * G2 * G1;
   for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
     const int pb = idx / G1, m = idx - pb * G1;
@@ -817,13 +850,14 @@ __global__ void __launch_bounds__(NTHR) k_xinv_phys(const typename C2<T>::t *__r
   }
 }
 
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_xfwd_phys(const double *__restrict__ phys, typename C2<T>::t *__restrict__ B,
-                                                    Geo g, RadixPlan px, const typename C2<T>::t *__restrict__ twx,
-                                                    int PB) {
+                                                    Geo g, const typename C2<T>::t *__restrict__ twx) {
   typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  constexpr int G1 = N;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int G1 = g.G1, G2 = g.G2, N1h = g.N1h;
+  const int G2 = g.G2, N1h = g.N1h;
   V *b0 = reinterpret_cast<V *>(smem_raw);
   V *b1 = b0 + PB * G1;
   const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
@@ -840,47 +874,46 @@ __global__ void __launch_bounds__(NTHR) k_xfwd_phys(const double *__restrict__ p
     b0[idx] = z;
   }
   __syncthreads();
-  V *res = smem_fft<false>(b0, b1, PB, px, twx);
+  V *res = line_fft<false, N, PB, false>(b0, b1, twx);
   const T s1 = (T)1 / (T)G1;
-  for (int idx = threadIdx.x; idx < N1h * PB; idx += blockDim.x) {
-    const int pb = idx % PB, k = idx / PB;
+  for (int idx = threadIdx.x; idx < PB * 2 * N1h; idx += blockDim.x) {
+    const int k = idx % N1h, rest = idx / N1h;
+    const int half = rest & 1, pb = rest >> 1;
     if (pb >= npairs) continue;
     const V *L = res + pb * G1;
     const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
-    V a, b;
-    a.x = (T)0.5 * (z.x + zc.x) * s1; a.y = (T)0.5 * (z.y + zc.y) * s1;
-    b.x = (T)0.5 * (z.y - zc.y) * s1; b.y = (T)-0.5 * (z.x - zc.x) * s1;
-    if (k == 0) { a.y = 0; b.y = 0; }
-    V *dst = B + ((size_t)pl * N1h + k) * G2 + l0 + 2 * pb;
-    dst[0] = a;
-    dst[1] = b;
+    V o;
+    if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
+    else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }
+    if (k == 0) o.y = 0;
+    B[((size_t)pl * G2 + l0 + 2 * pb + half) * N1h + k] = o;
   }
 }
 
-template <typename T>
+template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__restrict__ B, double2 *__restrict__ spec,
-                                                    Geo g, RadixPlan pz, const typename C2<T>::t *__restrict__ twz,
-                                                    int KB, const int *__restrict__ plmap) {
+                                                    Geo g, const typename C2<T>::t *__restrict__ twz) {
   typedef typename C2<T>::t V;
+  constexpr int KB = kb_zinv<V>(N);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int G2 = g.G2, N1h = g.N1h, N2 = g.N2;
+  const int N1h = g.N1h, N2 = g.N2;
   V *b0 = reinterpret_cast<V *>(smem_raw);
-  V *b1 = b0 + KB * G2;
+  V *b1 = b0 + KB * N;
   const int pl = blockIdx.y, kx0 = blockIdx.x * KB;
-  for (int idx = threadIdx.x; idx < KB * G2; idx += blockDim.x) {
-    const int kk = idx / G2, l = idx - kk * G2, kx = kx0 + kk;
+  for (int idx = threadIdx.x; idx < N * KB; idx += blockDim.x) {
+    const int l = idx / KB, kk = idx - l * KB, kx = kx0 + kk;
     V z = czero<V>();
-    if (kx < N1h) z = B[((size_t)pl * N1h + kx) * G2 + l];
+    if (kx < N1h) z = B[((size_t)pl * N + l) * N1h + kx];
     b0[idx] = z;
   }
   __syncthreads();
-  V *res = smem_fft<false>(b0, b1, KB, pz, twz);
-  const double s2 = 1.0 / (double)G2;
-  double2 *S = spec + (size_t)(plmap ? plmap[pl] : pl) * g.ncol;
+  V *res = line_fft<false, N, KB, true>(b0, b1, twz);
+  const double s2 = 1.0 / (double)N;
+  double2 *S = spec + (size_t)pl * g.ncol;
   for (int idx = threadIdx.x; idx < N2 * KB; idx += blockDim.x) {
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= N1h) continue;
-    const V t = res[kk * G2 + prow(g, r)];
+    const V t = res[prow(g, r) * KB + kk];
     double2 o; o.x = (double)t.x * s2; o.y = (double)t.y * s2;
     S[r * N1h + kx] = o;
   }
@@ -891,12 +924,13 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__r
 // then (after the inverse transform) the forcing at the solid points.
 // duib layout: [ibslot][field 0..2][col]; ib levels of u (fields 0, 2) and v (1).
 // ============================================================================
+template <typename TN>
 __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                 const double2 *__restrict__ u3, double2 *__restrict__ Nu1o,
                                                 double2 *__restrict__ Nu2o, double2 *__restrict__ Nu3o,
-                                                const double2 *__restrict__ N1xz, const double2 *__restrict__ N2xz,
-                                                const double2 *__restrict__ N3xz, const double2 *__restrict__ uvf,
-                                                const double2 *__restrict__ vvc, const double2 *__restrict__ wvf,
+                                                const typename C2<TN>::t *__restrict__ N1xz, const typename C2<TN>::t *__restrict__ N2xz,
+                                                const typename C2<TN>::t *__restrict__ N3xz, const typename C2<TN>::t *__restrict__ uvf,
+                                                const typename C2<TN>::t *__restrict__ vvc, const typename C2<TN>::t *__restrict__ wvf,
                                                 const double2 *__restrict__ p, double2 *__restrict__ duib,
                                                 const int *__restrict__ iblev, int nib, Geo g,
                                                 const DevScalars *__restrict__ sc, int kRK) {
@@ -919,8 +953,8 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     for (int f = 0; f < 2; ++f) {
       const double2 *U = f ? u3 : u1;
       double2 *No = f ? Nu3o : Nu1o;
-      const double2 *X = f ? N3xz : N1xz;
-      const double2 *F = f ? wvf : uvf;
+      const typename ::C2<TN>::t *X = f ? N3xz : N1xz;
+      const typename ::C2<TN>::t *F = f ? wvf : uvf;
       const double C3 = f ? C3z : C3x;
       const double2 um = U[o - nc], u0 = U[o], up = U[o + nc];
       double2 L;
@@ -930,7 +964,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
       du.x = (C1 * L.x + C2 * no.x) + (-C3 * pj.y);
       du.y = (C1 * L.y + C2 * no.y) + (C3 * pj.x);
       if (f == 0 && c == 0) du.x += -dR * sc->mpgx;
-      const double2 x = X[o], fq = F[o], fm = F[o - nc];
+      const double2 x = ld2(X[o]), fq = ld2(F[o]), fm = ld2(F[o - nc]);
       double2 n;
       n.x = x.x + (fq.x - fm.x) * th * g.dd; n.y = x.y + (fq.y - fm.y) * th * g.dd;
       No[o] = n;  // N of this substep (the next substep's -cRK term)
@@ -952,7 +986,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
     du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
     const double th = g.thv[qv];
-    const double2 x = N2xz[o], vp1 = vvc[o + nc], vq = vvc[o];
+    const double2 x = ld2(N2xz[o]), vp1 = ld2(vvc[o + nc]), vq = ld2(vvc[o]);
     double2 n;
     n.x = x.x + (vp1.x - vq.x) * th * g.dd; n.y = x.y + (vp1.y - vq.y) * th * g.dd;
     Nu2o[o] = n;
