@@ -25,7 +25,11 @@ struct lh_handle {
   size_t vsz;  // bytes of one complex value in the transforms
   cudaStream_t st;
   // device buffers
-  double2 *u1, *u2, *u3, *p, *Nu1, *Nu2, *Nu3, *psi;
+  double2 *u1, *u2, *u3, *p, *psi;
+  void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
+  double *dg1, *dg2, *dg3;  // factorised pressure matrices (constant)
+  float *a3f;  // FP32 scratch of the mixed-form solves
+  void *ysf;
   void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
   double *a3s, *mfw;
   void *A, *B, *twx, *twz, *twx64, *twz64;
@@ -252,7 +256,9 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   } while (0)
   const size_t cz = sizeof(double2);
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
-  ZA(h->Nu1, cz * nu * nc); ZA(h->Nu3, cz * nu * nc); ZA(h->Nu2, cz * nv * nc);
+  ZA(h->Nu1, vs * nu * nc); ZA(h->Nu3, vs * nu * nc); ZA(h->Nu2, vs * nv * nc);
+  ZA(h->dg1, sizeof(double) * g.np * nc); ZA(h->dg2, sizeof(double) * g.np * nc); ZA(h->dg3, sizeof(double) * g.np * nc);
+  if (h->prec == LH_PREC_MIXED) { ZA(h->a3f, sizeof(float) * nu * nc); ZA(h->ysf, sizeof(float4) * nu * nc); }
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
   ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
@@ -342,6 +348,13 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
+  {  // pressure factors, once (start.f90:656-658)
+    const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
+    k_build_dg<<<nb, NTHR_H, 0, h->st>>>(h->dg1, h->dg2, h->dg3, g);
+    cudaError_t e = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("k_build_dg: ") + cudaGetErrorString(e)); lh_destroy(h); return rc; }
+  }
   // keep host copies of the arrays
   h->h_yu.assign(cfg->yu, cfg->yu + nu);
   h->h_yv.assign(cfg->yv, cfg->yv + nv);
@@ -357,7 +370,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
 extern "C" int lh_destroy(lh_handle *h) {
   if (!h) return LH_EINVAL;
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
-  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
+  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->a3f, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
@@ -566,7 +579,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
   if (h->ib) {
     dim3 gd(nb, h->nib);
-    KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->Nu1, h->Nu2, h->Nu3, (const V *)h->N1xz,
+    KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (V *)h->Nu1, (V *)h->Nu2, (V *)h->Nu3, (const V *)h->N1xz,
                                                        (const V *)h->N2xz, (const V *)h->N3xz, (const V *)h->uvf,
                                                        (const V *)h->vvc, (const V *)h->wvf, h->p, h->duib, h->d_iblev,
                                                        h->nib, g, h->sc, kRK));
@@ -580,20 +593,32 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                           h->d_ibslot_v, h->d_lev2cap_v, g, h->sc));
     if ((rc = phys_to_spec<T>(h, h->duphys, h->duib, 3 * h->nib, h->B, h->twx, h->twz))) return rc;
   }
-  KL("k_helm_uw", k_helm_uw<T><<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, h->Nu1, h->Nu3, (const V *)h->N1xz,
-                                                         (const V *)h->N3xz, (const V *)h->uvf, (const V *)h->wvf, h->p,
-                                                         h->a3s, g, h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr,
-                                                         h->duib));
-  KL("k_helm_v", k_helm_v<T><<<nb, NTHR_H, 0, h->st>>>(h->u2, h->Nu2, (const V *)h->N2xz, (const V *)h->vvc, h->p,
-                                                       h->a3s, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr,
-                                                       h->duib));
+  if (h->prec == LH_PREC_FP64) {
+    KL("k_helm_uw", k_helm_uw<T><<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
+                                                           (const V *)h->N1xz, (const V *)h->N3xz, (const V *)h->uvf,
+                                                           (const V *)h->wvf, h->p, h->a3s, g, h->sc, kRK,
+                                                           h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    KL("k_helm_v", k_helm_v<T><<<nb, NTHR_H, 0, h->st>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz,
+                                                         (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
+                                                         h->ib ? h->d_ibslot_v : nullptr, h->duib));
+  } else {
+    KL("k_helm_uw", k_helm_uw_mx<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, (float2 *)h->Nu1, (float2 *)h->Nu3,
+                                                           (const float2 *)h->N1xz, (const float2 *)h->N3xz,
+                                                           (const float2 *)h->uvf, (const float2 *)h->wvf, h->p, h->a3f,
+                                                           (float4 *)h->ysf, g, h->sc, kRK,
+                                                           h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    KL("k_helm_v", k_helm_v_mx<<<nb, NTHR_H, 0, h->st>>>(h->u2, (float2 *)h->Nu2, (const float2 *)h->N2xz,
+                                                         (const float2 *)h->vvc, h->p, h->a3f, (float2 *)h->ysf, g,
+                                                         h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
+  }
   if (g.flag_ctpress == 0) {
     const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
     const int sm = mb <= 48 * 1024 ? 1 : 0;
     KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
   }
   KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
-  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->a3s, g, h->sc, kRK));
+  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
+                                                  h->sc, kRK));
   KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }

@@ -520,6 +520,211 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
 }
 
 // ============================================================================
+// Mixed form of the Helmholtz solves: the same equations written for the
+// increment d = u_new - u, (I - beta L) d = dt du + beta L(u), with the BC rows
+// d(0) + gw1 d(1) = -(u(0) + gw1 u(1)) (and the top row alike). d is small, so
+// the right-hand side, the factorisation and both sweeps run in FP32; L(u) is
+// formed from FP64 neighbour differences (u(j+-1) - u(j)); u_new = u + d in FP64.
+// Scratch: ys [q][col] float4 (y of u and w), a3f [q][col] float.
+// ============================================================================
+__device__ __forceinline__ float2 f2d(double2 a) { return make_float2((float)a.x, (float)a.y); }
+__device__ __forceinline__ float2 f2sub(double2 a, double2 b) { return make_float2((float)(a.x - b.x), (float)(a.y - b.y)); }
+
+__global__ void __launch_bounds__(NTHR) k_helm_uw_mx(double2 *__restrict__ u1, double2 *__restrict__ u3,
+                                                     float2 *__restrict__ Nu1, float2 *__restrict__ Nu3,
+                                                     const float2 *__restrict__ N1xz, const float2 *__restrict__ N3xz,
+                                                     const float2 *__restrict__ uvf, const float2 *__restrict__ wvf,
+                                                     const double2 *__restrict__ p, float *__restrict__ a3f,
+                                                     float4 *__restrict__ ys, Geo g, const DevScalars *__restrict__ sc,
+                                                     int kRK, const int *__restrict__ ibslot_u,
+                                                     const double2 *__restrict__ duib) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  if (c >= nc) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
+  const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
+  const double dR = g.dRK[kRK - 1];
+  const float G = (float)(-g.gRK[kRK - 1]);
+  const double dt = sc->dt;
+  const float dtf = (float)dt;
+  const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
+  const float C3x = (float)(-dR * g.k1x[kx]), C3z = (float)(-dR * g.k1z[r]);
+  const float mp = (c == 0) ? (float)(-dR * sc->mpgx) : 0.f;
+  const float dd = (float)g.dd;
+  const int nu = g.nu;
+  const double *d0 = g.d2u, *d1 = g.d2u + nu, *d2 = g.d2u + 2 * nu;
+  const double gw1 = g.gw[1][0], gw2 = g.gw[1][1];
+  double2 um = u1[c], u0 = u1[(size_t)nc + c];
+  double2 wm = u3[c], w0 = u3[(size_t)nc + c];
+  // row 0
+  float2 yu = make_float2((float)(-(um.x + gw1 * u0.x)), (float)(-(um.y + gw1 * u0.y)));
+  float2 yw = make_float2((float)(-(wm.x + gw1 * w0.x)), (float)(-(wm.y + gw1 * w0.y)));
+  ys[c] = make_float4(yu.x, yu.y, yw.x, yw.y);
+  float a3raw = (float)gw1, a2p = 1.f;
+  float2 uvm = uvf[c], wvm = wvf[c];
+  for (int q = 1; q <= nu - 2; ++q) {
+    const size_t o = (size_t)q * nc + c;
+    const double2 up1 = u1[o + nc], wp1 = u3[o + nc];
+    const float2 uvq = uvf[o], wvq = wvf[o];
+    const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
+    const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
+    const float2 dmu = f2sub(um, u0), dpu = f2sub(up1, u0), uq = f2d(u0);
+    const float2 dmw = f2sub(wm, w0), dpw = f2sub(wp1, w0), wq = f2d(w0);
+    float2 L1, L3;
+    L1.x = a * dmu.x + cc * dpu.x + sdg * uq.x; L1.y = a * dmu.y + cc * dpu.y + sdg * uq.y;
+    L3.x = a * dmw.x + cc * dpw.x + sdg * wq.x; L3.y = a * dmw.y + cc * dpw.y + sdg * wq.y;
+    float2 du1, du3;
+    const int ibs = ibslot_u ? ibslot_u[q] : -1;
+    if (ibs < 0) {
+      const float2 pj = f2d(p[(size_t)(q - 1) * nc + c]);
+      const float2 no1 = Nu1[o], no3 = Nu3[o];
+      du1.x = (C1 * L1.x + C2 * no1.x) + (-C3x * pj.y) + mp;
+      du1.y = (C1 * L1.y + C2 * no1.y) + (C3x * pj.x);
+      du3.x = (C1 * L3.x + C2 * no3.x) + (-C3z * pj.y);
+      du3.y = (C1 * L3.y + C2 * no3.y) + (C3z * pj.x);
+      const float th = (float)g.thu[q];
+      const float2 x1 = N1xz[o], x3 = N3xz[o];
+      float2 n1, n3;
+      n1.x = x1.x + (uvq.x - uvm.x) * th * dd; n1.y = x1.y + (uvq.y - uvm.y) * th * dd;
+      n3.x = x3.x + (wvq.x - wvm.x) * th * dd; n3.y = x3.y + (wvq.y - wvm.y) * th * dd;
+      Nu1[o] = n1;
+      Nu3[o] = n3;
+      du1.x += G * n1.x; du1.y += G * n1.y;
+      du3.x += G * n3.x; du3.y += G * n3.y;
+    } else {
+      du1 = f2d(duib[((size_t)ibs * 3 + 0) * nc + c]);
+      du3 = f2d(duib[((size_t)ibs * 3 + 2) * nc + c]);
+    }
+    float2 r1, r3;
+    r1.x = dtf * du1.x + beta * L1.x; r1.y = dtf * du1.y + beta * L1.y;
+    r3.x = dtf * du3.x + beta * L3.x; r3.y = dtf * du3.y + beta * L3.y;
+    const float a1 = -beta * a;
+    const float a2 = 1.f - beta * (b + k2f);
+    const float a3p = a3raw * a2p;
+    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.f / (a2 - a1 * a3p);
+    yu.x = (r1.x - a1 * yu.x) * a2p; yu.y = (r1.y - a1 * yu.y) * a2p;
+    yw.x = (r3.x - a1 * yw.x) * a2p; yw.y = (r3.y - a1 * yw.y) * a2p;
+    ys[o] = make_float4(yu.x, yu.y, yw.x, yw.y);
+    a3raw = -beta * cc;
+    um = u0; u0 = up1; wm = w0; w0 = wp1;
+    uvm = uvq; wvm = wvq;
+  }
+  {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1)); here um = u(n-2), u0 = u(n-1)
+    const int q = nu - 1;
+    const float a1 = (float)gw2;
+    const float2 rl = make_float2((float)(-(gw2 * um.x + u0.x)), (float)(-(gw2 * um.y + u0.y)));
+    const float2 rw = make_float2((float)(-(gw2 * wm.x + w0.x)), (float)(-(gw2 * wm.y + w0.y)));
+    const float a3p = a3raw * a2p;
+    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.f / (1.f - a1 * a3p);
+    yu.x = (rl.x - a1 * yu.x) * a2p; yu.y = (rl.y - a1 * yu.y) * a2p;
+    yw.x = (rw.x - a1 * yw.x) * a2p; yw.y = (rw.y - a1 * yw.y) * a2p;
+    double2 t = u1[(size_t)q * nc + c], s3 = u3[(size_t)q * nc + c];
+    t.x += (double)yu.x; t.y += (double)yu.y; s3.x += (double)yw.x; s3.y += (double)yw.y;
+    u1[(size_t)q * nc + c] = t;
+    u3[(size_t)q * nc + c] = s3;
+  }
+  float2 xu = yu, xw = yw;
+  for (int q = nu - 2; q >= 0; --q) {
+    const size_t o = (size_t)q * nc + c;
+    const float a3p = a3f[o];
+    const float4 yy = ys[o];
+    xu.x = yy.x - a3p * xu.x; xu.y = yy.y - a3p * xu.y;
+    xw.x = yy.z - a3p * xw.x; xw.y = yy.w - a3p * xw.y;
+    double2 t = u1[o], s3 = u3[o];
+    t.x += (double)xu.x; t.y += (double)xu.y; s3.x += (double)xw.x; s3.y += (double)xw.y;
+    u1[o] = t;
+    u3[o] = s3;
+  }
+}
+
+__global__ void __launch_bounds__(NTHR) k_helm_v_mx(double2 *__restrict__ u2, float2 *__restrict__ Nu2,
+                                                    const float2 *__restrict__ N2xz, const float2 *__restrict__ vvc,
+                                                    const double2 *__restrict__ p, float *__restrict__ a3f,
+                                                    float2 *__restrict__ ys, Geo g, const DevScalars *__restrict__ sc,
+                                                    int kRK, const int *__restrict__ ibslot_v,
+                                                    const double2 *__restrict__ duib) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  if (c >= nc) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
+  const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
+  const double dR = g.dRK[kRK - 1];
+  const float G = (float)(-g.gRK[kRK - 1]);
+  const double dt = sc->dt;
+  const float dtf = (float)dt;
+  const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
+  const float dd = (float)g.dd;
+  const int nv = g.nv;
+  const double *d0 = g.d2v, *d1 = g.d2v + nv, *d2 = g.d2v + 2 * nv;
+  double2 vm = u2[c], v0 = u2[(size_t)nc + c];
+  float2 y = make_float2((float)(-vm.x), (float)(-vm.y));  // row 0: d(0) = -v(0)
+  ys[c] = y;
+  float a3raw = 0.f, a2p = 1.f;
+  float2 vvq = vvc[(size_t)1 * nc + c];
+  for (int q = 1; q <= nv - 2; ++q) {
+    const size_t o = (size_t)q * nc + c;
+    const double2 vp1 = u2[o + nc];
+    const float2 vvp = vvc[o + nc];
+    const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
+    const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
+    const float2 dm = f2sub(vm, v0), dp = f2sub(vp1, v0), vq = f2d(v0);
+    float2 L;
+    L.x = a * dm.x + cc * dp.x + sdg * vq.x; L.y = a * dm.y + cc * dp.y + sdg * vq.y;
+    float2 du;
+    const int ibs = ibslot_v ? ibslot_v[q] : -1;
+    if (ibs < 0) {
+      const float C3 = (float)(-dR * g.dd * g.thv[q]);
+      const float2 pp = f2d(p[(size_t)q * nc + c]), pm = f2d(p[(size_t)(q - 1) * nc + c]);
+      const float2 no = Nu2[o];
+      du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
+      du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
+      const float th = (float)g.thv[q];
+      const float2 x2 = N2xz[o];
+      float2 n2;
+      n2.x = x2.x + (vvp.x - vvq.x) * th * dd; n2.y = x2.y + (vvp.y - vvq.y) * th * dd;
+      Nu2[o] = n2;
+      du.x += G * n2.x; du.y += G * n2.y;
+    } else {
+      du = f2d(duib[((size_t)ibs * 3 + 1) * nc + c]);
+    }
+    float2 rr;
+    rr.x = dtf * du.x + beta * L.x; rr.y = dtf * du.y + beta * L.y;
+    const float a1 = -beta * a;
+    const float a2 = 1.f - beta * (b + k2f);
+    const float a3p = a3raw * a2p;
+    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    a2p = 1.f / (a2 - a1 * a3p);
+    y.x = (rr.x - a1 * y.x) * a2p; y.y = (rr.y - a1 * y.y) * a2p;
+    ys[o] = y;
+    a3raw = -beta * cc;
+    vm = v0; v0 = vp1; vvq = vvp;
+  }
+  {  // last row: d(n-1) = -v(n-1)
+    const int q = nv - 1;
+    const float a3p = a3raw * a2p;
+    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    y = make_float2((float)(-v0.x), (float)(-v0.y));
+    double2 t = u2[(size_t)q * nc + c];
+    t.x += (double)y.x; t.y += (double)y.y;
+    u2[(size_t)q * nc + c] = t;
+  }
+  float2 x = y;
+  for (int q = nv - 2; q >= 0; --q) {
+    const size_t o = (size_t)q * nc + c;
+    const float a3p = a3f[o];
+    const float2 yy = ys[o];
+    x.x = yy.x - a3p * x.x; x.y = yy.y - a3p * x.y;
+    double2 t = u2[o];
+    t.x += (double)x.x; t.y += (double)x.y;
+    u2[o] = t;
+  }
+}
+
+// ============================================================================
 // flowrate_corr (littleharsh.f90:476-509) on mode (0,0) of u1. The block stages the
 // coefficients, the level widths and u(0,0) in `w` (shared memory when it fits,
 // else global scratch); thread 0 runs the recurrence and the sums in the
@@ -582,20 +787,69 @@ __global__ void k_flowrate(const double2 *__restrict__ u1, Geo g, DevScalars *sc
 __global__ void k_step_end(DevScalars *sc) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   sc->iter += 1;
-  const double e = __longlong_as_double((long long)sc->errbits);
+  const double e = sqrt(__longlong_as_double((long long)sc->errbits));
   sc->err = e;
   if (!(e == e) || isinf(e) || !(sc->dt == sc->dt)) sc->status = LH_ENONFINITE;
 }
 
 // ============================================================================
+// LU_buildP + LU_decP (tridLU_3D.f90:333-407, 477-518), once per channel: the
+// pressure matrix does not depend on time. dg1 = a1 (lower), dg2 = 1/pivot,
+// dg3 = upper factor; [qp][col], qp = 0..np-1 <-> p level N(4,0)+1+qp.
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, double *__restrict__ dg2,
+                                                   double *__restrict__ dg3, Geo g) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  if (c >= nc) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const double k2x = g.k2x[kx], k2z = g.k2z[r];
+  const double dd = g.dd;
+  const int np = g.np;
+  double a3raw = 0.0, a2p = 0.0;
+  for (int qp = 0; qp < np; ++qp) {
+    const int q = qp + 1;
+    const double Dt = dd * g.thu[q];
+    const double Gb = -dd * g.thv[q];
+    double A1, A2, A3;
+    if (qp == 0) {
+      A1 = 0.0;
+      A2 = (Dt * Gb) + k2x + k2z;
+      A3 = (Dt * (dd * g.thv[q]));
+      if (c == 0) {  // gauge of mode (0,0)
+        const double h = g.yu[2 + g.dny] - g.yu[1 + g.dny];
+        A1 = 0.0; A2 = 1.0 / (h * h); A3 = 0.0;
+      }
+    } else {
+      const double Db = -dd * g.thu[q];
+      const double Gt = dd * g.thv[q - 1];
+      const double Gbm = -dd * g.thv[q - 1];
+      if (qp == np - 1) { A2 = (Db * Gt) + k2x + k2z; A1 = (Db * Gbm); A3 = 0.0; }
+      else { A2 = (Db * Gt) + (Dt * Gb) + k2x + k2z; A1 = (Db * Gbm); A3 = (Dt * (dd * g.thv[q])); }
+    }
+    if (qp == 0) a2p = 1.0 / A2;
+    else {
+      const double a3p = a3raw * a2p;
+      dg3[(size_t)(qp - 1) * nc + c] = a3p;
+      a2p = 1.0 / (A2 - A1 * a3p);
+    }
+    dg1[(size_t)qp * nc + c] = A1;
+    dg2[(size_t)qp * nc + c] = a2p;
+    a3raw = A3;
+  }
+  dg3[(size_t)(np - 1) * nc + c] = 0.0;
+}
+
+// ============================================================================
 // Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
-// factor of LU_buildP/LU_decP recomputed in the same operation order, p += psi,
-// v_corr, and the divergence of the corrected field (max |div| -> errbits).
-// One thread per column. p levels qp = 0..np-1 <-> u/v index q = qp + 1.
+// stored factors, p += psi, v_corr, and the divergence of the corrected field
+// (max |div|^2 -> errbits). One thread per column. p levels qp = 0..np-1 <->
+// u/v index q = qp + 1. `psi` holds the forward-sweep values, then psi.
 // ============================================================================
 __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double2 *__restrict__ u2,
                                                 double2 *__restrict__ u3, double2 *__restrict__ p,
-                                                double2 *__restrict__ psi, double *__restrict__ a3s, Geo g,
+                                                double2 *__restrict__ psi, const double *__restrict__ dg1,
+                                                const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
                                                 DevScalars *sc, int kRK) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = g.ncol;
@@ -603,14 +857,11 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
   if (c < nc) {
     const int r = c / g.N1h, kx = c - r * g.N1h;
     const double kxv = g.k1x[kx], kzv = g.k1z[r];
-    const double k2x = g.k2x[kx], k2z = g.k2z[r];
     const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
     const double dtirk = sc->dti / aRb;
     const double dt = sc->dt;
     const int np = g.np;
     const double dd = g.dd;
-    // forward sweep
-    double a3raw = 0.0, a2p = 0.0;
     double2 y = czero<double2>();
     double2 vm = u2[c];
     for (int qp = 0; qp < np; ++qp) {
@@ -624,60 +875,24 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
       vm = v;
       double2 rhs;
       rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
-      // matrix row qp (D/G vectors of LU_buildP)
-      const double Dt = dd * g.thu[q];
-      const double Gb = -dd * g.thv[q];
-      double A1, A2, A3;
-      if (qp == 0) {
-        A1 = 0.0;
-        A2 = (Dt * Gb) + k2x + k2z;
-        A3 = (Dt * (dd * g.thv[q]));
-        if (c == 0) {
-          const double h = g.yu[2 + g.dny] - g.yu[1 + g.dny];
-          A1 = 0.0; A2 = 1.0 / (h * h); A3 = 0.0;
-          rhs.x = 0.0; rhs.y = 0.0;
-        }
-      } else {
-        const double Db = -dd * g.thu[q];     // D_vec_b(j-1)
-        const double Gt = dd * g.thv[q - 1];  // G_vec_t(j)
-        const double Gbm = -dd * g.thv[q - 1];  // G_vec_b(j-1)
-        if (qp == np - 1) {
-          A2 = (Db * Gt) + k2x + k2z;
-          A1 = (Db * Gbm);
-          A3 = 0.0;
-        } else {
-          A2 = (Db * Gt) + (Dt * Gb) + k2x + k2z;
-          A1 = (Db * Gbm);
-          A3 = (Dt * (dd * g.thv[q]));
-        }
-      }
-      if (qp == 0) {
-        a2p = 1.0 / A2;
-      } else {
-        const double a3p = a3raw * a2p;
-        a3s[(size_t)(qp - 1) * nc + c] = a3p;
-        a2p = 1.0 / (A2 - A1 * a3p);
-      }
+      if (qp == 0 && c == 0) { rhs.x = 0.0; rhs.y = 0.0; }
+      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
       if (qp == 0) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
       else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
       psi[(size_t)qp * nc + c] = y;
-      a3raw = A3;
     }
-    // backward sweep + p update + v_corr
     const double dtrk = dt * aRb;
     const double dtrk2 = dtrk * dd;
     const double kxd = dtrk * kxv, kzd = dtrk * kzv;
-    double2 xn = y;  // psi(np-1)
-    double2 vup = u2[(size_t)(np) * nc + c];  // v at index np+... (updated value of the level above)
-    // level above the top p level is the top v wall (index nv-1 = np): v = 0 there
-    double2 a_up = czero<double2>(), w_up = czero<double2>();
+    double2 xn = y;
+    double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
     for (int qp = np - 1; qp >= 0; --qp) {
       const int q = qp + 1;
       const size_t o = (size_t)q * nc + c;
       double2 x;
       if (qp == np - 1) x = xn;
       else {
-        const double a3p = a3s[(size_t)qp * nc + c];
+        const double a3p = dg3[(size_t)qp * nc + c];
         const double2 yy = psi[(size_t)qp * nc + c];
         x.x = yy.x - a3p * xn.x; x.y = yy.y - a3p * xn.y;
       }
@@ -686,7 +901,6 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
       pp.x = pp.x + x.x; pp.y = pp.y + x.y;
       p[(size_t)qp * nc + c] = pp;
       double2 a = u1[o], w = u3[o];
-      // u -= (dtrk * i kx) psi
       a.x = a.x - (-kxd * x.y); a.y = a.y - (kxd * x.x);
       w.x = w.x - (-kzd * x.y); w.y = w.y - (kzd * x.x);
       u1[o] = a;
@@ -698,26 +912,24 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
         v.y = v.y - f * (xn.y - x.y);
         u2[o] = v;
       }
-      // divergence of the level above (q+1), now that v(q) is final
       if (qp < np - 1) {
         const double th = dd * g.thu[q + 1];
         double2 dv;
         dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
         dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - v.y);
-        dmax = fmax(dmax, hypot(dv.x, dv.y));
+        dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
       }
       a_up = a; w_up = w; vup = v;
       xn = x;
     }
-    {  // divergence of the lowest level (v below is the wall, 0)
+    {
       const double th = dd * g.thu[1];
       const double2 vb = u2[c];
       double2 dv;
       dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
       dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
-      dmax = fmax(dmax, hypot(dv.x, dv.y));
+      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
     }
-    // ghost extrapolation of u and w, walls of v
     const int nu = g.nu;
     double2 t1 = u1[(size_t)nc + c], t3 = u3[(size_t)nc + c];
     u1[c] = cscale(t1, g.gwbc1);
@@ -751,15 +963,16 @@ __global__ void __launch_bounds__(NTHR) k_divmax(const double2 *__restrict__ u1,
       double2 dv;
       dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
       dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
-      dmax = fmax(dmax, hypot(dv.x, dv.y));
+      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
     }
   }
   dmax = warp_max(dmax);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
 }
 
+// err = max |div| (errbits holds the maximum of |div|^2)
 __global__ void k_err_from_bits(DevScalars *sc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) sc->err = __longlong_as_double((long long)sc->errbits);
+  if (threadIdx.x == 0 && blockIdx.x == 0) sc->err = sqrt(__longlong_as_double((long long)sc->errbits));
 }
 
 // host cfield [col][lev] <-> device [lev][col] (complex), tiled transpose
@@ -926,8 +1139,8 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__r
 // ============================================================================
 template <typename TN>
 __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
-                                                const double2 *__restrict__ u3, double2 *__restrict__ Nu1o,
-                                                double2 *__restrict__ Nu2o, double2 *__restrict__ Nu3o,
+                                                const double2 *__restrict__ u3, typename C2<TN>::t *__restrict__ Nu1o,
+                                                typename C2<TN>::t *__restrict__ Nu2o, typename C2<TN>::t *__restrict__ Nu3o,
                                                 const typename C2<TN>::t *__restrict__ N1xz, const typename C2<TN>::t *__restrict__ N2xz,
                                                 const typename C2<TN>::t *__restrict__ N3xz, const typename C2<TN>::t *__restrict__ uvf,
                                                 const typename C2<TN>::t *__restrict__ vvc, const typename C2<TN>::t *__restrict__ wvf,
@@ -952,14 +1165,14 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     const double th = g.thu[qu];
     for (int f = 0; f < 2; ++f) {
       const double2 *U = f ? u3 : u1;
-      double2 *No = f ? Nu3o : Nu1o;
+      typename ::C2<TN>::t *No = f ? Nu3o : Nu1o;
       const typename ::C2<TN>::t *X = f ? N3xz : N1xz;
       const typename ::C2<TN>::t *F = f ? wvf : uvf;
       const double C3 = f ? C3z : C3x;
       const double2 um = U[o - nc], u0 = U[o], up = U[o + nc];
       double2 L;
       L.x = (a * um.x + dg * u0.x) + cc * up.x; L.y = (a * um.y + dg * u0.y) + cc * up.y;
-      const double2 no = No[o];
+      const double2 no = ld2(No[o]);
       double2 du;
       du.x = (C1 * L.x + C2 * no.x) + (-C3 * pj.y);
       du.y = (C1 * L.y + C2 * no.y) + (C3 * pj.x);
@@ -967,7 +1180,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
       const double2 x = ld2(X[o]), fq = ld2(F[o]), fm = ld2(F[o - nc]);
       double2 n;
       n.x = x.x + (fq.x - fm.x) * th * g.dd; n.y = x.y + (fq.y - fm.y) * th * g.dd;
-      No[o] = n;  // N of this substep (the next substep's -cRK term)
+      No[o].x = n.x; No[o].y = n.y;  // N of this substep (the next substep's -cRK term)
       du.x = du.x + G * n.x; du.y = du.y + G * n.y;
       duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = du;
     }
@@ -981,7 +1194,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     L.x = (a * vm.x + dg * v0.x) + cc * vp.x; L.y = (a * vm.y + dg * v0.y) + cc * vp.y;
     const double C3 = -dR * g.dd * g.thv[qv];
     const double2 pp = p[(size_t)qv * nc + c], pm = p[(size_t)(qv - 1) * nc + c];
-    const double2 no = Nu2o[o];
+    const double2 no = ld2(Nu2o[o]);
     double2 du;
     du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
     du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
@@ -989,7 +1202,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     const double2 x = ld2(N2xz[o]), vp1 = ld2(vvc[o + nc]), vq = ld2(vvc[o]);
     double2 n;
     n.x = x.x + (vp1.x - vq.x) * th * g.dd; n.y = x.y + (vp1.y - vq.y) * th * g.dd;
-    Nu2o[o] = n;
+    Nu2o[o].x = n.x; Nu2o[o].y = n.y;
     du.x = du.x + G * n.x; du.y = du.y + G * n.y;
     duib[((size_t)s * 3 + 1) * nc + c] = du;
   }
