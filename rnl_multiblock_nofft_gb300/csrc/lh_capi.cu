@@ -28,8 +28,7 @@ struct lh_handle {
   double2 *u1, *u2, *u3, *p, *psi;
   void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
   double *dg1, *dg2, *dg3;  // factorised pressure matrices (constant)
-  float *a3f;  // FP32 scratch of the mixed-form solves
-  void *ysf;
+  void *ysf;  // FP32 scratch of the mixed-form solves
   void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
   double *a3s, *mfw;
   void *A, *B, *twx, *twz, *twx64, *twz64;
@@ -258,7 +257,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
   ZA(h->Nu1, vs * nu * nc); ZA(h->Nu3, vs * nu * nc); ZA(h->Nu2, vs * nv * nc);
   ZA(h->dg1, sizeof(double) * g.np * nc); ZA(h->dg2, sizeof(double) * g.np * nc); ZA(h->dg3, sizeof(double) * g.np * nc);
-  if (h->prec == LH_PREC_MIXED) { ZA(h->a3f, sizeof(float) * nu * nc); ZA(h->ysf, sizeof(float4) * nu * nc); }
+  if (h->prec == LH_PREC_MIXED) ZA(h->ysf, 2 * sizeof(float4) * nu * nc);
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
   ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
@@ -370,7 +369,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
 extern "C" int lh_destroy(lh_handle *h) {
   if (!h) return LH_EINVAL;
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
-  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->a3f, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
+  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
@@ -602,14 +601,14 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                          (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
                                                          h->ib ? h->d_ibslot_v : nullptr, h->duib));
   } else {
-    KL("k_helm_uw", k_helm_uw_mx<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, (float2 *)h->Nu1, (float2 *)h->Nu3,
-                                                           (const float2 *)h->N1xz, (const float2 *)h->N3xz,
-                                                           (const float2 *)h->uvf, (const float2 *)h->wvf, h->p, h->a3f,
-                                                           (float4 *)h->ysf, g, h->sc, kRK,
-                                                           h->ib ? h->d_ibslot_u : nullptr, h->duib));
-    KL("k_helm_v", k_helm_v_mx<<<nb, NTHR_H, 0, h->st>>>(h->u2, (float2 *)h->Nu2, (const float2 *)h->N2xz,
-                                                         (const float2 *)h->vvc, h->p, h->a3f, (float2 *)h->ysf, g,
-                                                         h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
+    const int nb2 = (2 * g.ncol + NTHR_H - 1) / NTHR_H;
+    KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2, 2), NTHR_H, 0, h->st>>>(
+                        (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
+                        (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,
+                        h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    KL("k_helm_v", k_helm_v_mx2<<<nb2, NTHR_H, 0, h->st>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
+                                                           (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysf,
+                                                           g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
   }
   if (g.flag_ctpress == 0) {
     const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
@@ -617,8 +616,11 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
   }
   KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
-  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
-                                                  h->sc, kRK));
+  {
+    const int nb2 = (2 * g.ncol + NTHR_H - 1) / NTHR_H;
+    KL("k_press", k_press2<<<nb2, NTHR_H, 0, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3, (double *)h->p,
+                                                      (double *)h->psi, h->dg1, h->dg2, h->dg3, g, h->sc, kRK));
+  }
   KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }

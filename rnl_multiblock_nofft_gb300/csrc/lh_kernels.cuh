@@ -525,22 +525,34 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
 // d(0) + gw1 d(1) = -(u(0) + gw1 u(1)) (and the top row alike). d is small, so
 // the right-hand side, the factorisation and both sweeps run in FP32; L(u) is
 // formed from FP64 neighbour differences (u(j+-1) - u(j)); u_new = u + d in FP64.
-// Scratch: ys [q][col] float4 (y of u and w), a3f [q][col] float.
 // ============================================================================
 __device__ __forceinline__ float2 f2d(double2 a) { return make_float2((float)a.x, (float)a.y); }
 __device__ __forceinline__ float2 f2sub(double2 a, double2 b) { return make_float2((float)(a.x - b.x), (float)(a.y - b.y)); }
 
-__global__ void __launch_bounds__(NTHR) k_helm_uw_mx(double2 *__restrict__ u1, double2 *__restrict__ u3,
-                                                     float2 *__restrict__ Nu1, float2 *__restrict__ Nu3,
-                                                     const float2 *__restrict__ N1xz, const float2 *__restrict__ N3xz,
-                                                     const float2 *__restrict__ uvf, const float2 *__restrict__ wvf,
-                                                     const double2 *__restrict__ p, float *__restrict__ a3f,
-                                                     float4 *__restrict__ ys, Geo g, const DevScalars *__restrict__ sc,
-                                                     int kRK, const int *__restrict__ ibslot_u,
-                                                     const double2 *__restrict__ duib) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// ============================================================================
+// Mixed-form solves with one lane per (column, real/imaginary part): the matrix
+// is real, so the two parts are independent systems; each lane repeats the FP32
+// factorisation. Scalar views: element (q, col, part) at (q*ncol + col)*2 + part.
+// ys2 holds (y(q), upper factor(q)) per lane.
+// k_helm_u_mx2: one field (u when F == 0, w when F == 2) per launch row (blockIdx.y).
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, double *__restrict__ u3,
+                                                     float *__restrict__ Nu1, float *__restrict__ Nu3,
+                                                     const float *__restrict__ N1xz, const float *__restrict__ N3xz,
+                                                     const float *__restrict__ uvf, const float *__restrict__ wvf,
+                                                     const double2 *__restrict__ p, float2 *__restrict__ ys2, Geo g,
+                                                     const DevScalars *__restrict__ sc, int kRK,
+                                                     const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
   if (c >= nc) return;
+  const int fw = blockIdx.y;  // 0: u, 1: w
+  double *u = fw ? u3 : u1;
+  float *Nu = fw ? Nu3 : Nu1;
+  const float *X = fw ? N3xz : N1xz;
+  const float *Fl = fw ? wvf : uvf;
+  float2 *ys = ys2 + (size_t)fw * g.nu * nc * 2;
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
   const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
@@ -549,104 +561,77 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw_mx(double2 *__restrict__ u1, d
   const double dt = sc->dt;
   const float dtf = (float)dt;
   const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
-  const float C3x = (float)(-dR * g.k1x[kx]), C3z = (float)(-dR * g.k1z[r]);
-  const float mp = (c == 0) ? (float)(-dR * sc->mpgx) : 0.f;
+  const float C3 = (float)(-dR * (fw ? g.k1z[r] : g.k1x[kx]));
+  const float mp = (c == 0 && fw == 0 && part == 0) ? (float)(-dR * sc->mpgx) : 0.f;
   const float dd = (float)g.dd;
   const int nu = g.nu;
   const double *d0 = g.d2u, *d1 = g.d2u + nu, *d2 = g.d2u + 2 * nu;
   const double gw1 = g.gw[1][0], gw2 = g.gw[1][1];
-  double2 um = u1[c], u0 = u1[(size_t)nc + c];
-  double2 wm = u3[c], w0 = u3[(size_t)nc + c];
-  // row 0
-  float2 yu = make_float2((float)(-(um.x + gw1 * u0.x)), (float)(-(um.y + gw1 * u0.y)));
-  float2 yw = make_float2((float)(-(wm.x + gw1 * w0.x)), (float)(-(wm.y + gw1 * w0.y)));
-  ys[c] = make_float4(yu.x, yu.y, yw.x, yw.y);
+  const size_t ci = (size_t)c * 2 + part;
+  const size_t lstride = (size_t)nc * 2;
+  double um = u[ci], u0 = u[lstride + ci];
+  float y = (float)(-(um + gw1 * u0));  // row 0
+  float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
-  float2 uvm = uvf[c], wvm = wvf[c];
+  float flm = Fl[ci];
   for (int q = 1; q <= nu - 2; ++q) {
-    const size_t o = (size_t)q * nc + c;
-    const double2 up1 = u1[o + nc], wp1 = u3[o + nc];
-    const float2 uvq = uvf[o], wvq = wvf[o];
+    const size_t e = (size_t)q * lstride + ci;
+    const double up1 = u[e + lstride];
+    const float flq = Fl[e];
     const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
     const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
-    const float2 dmu = f2sub(um, u0), dpu = f2sub(up1, u0), uq = f2d(u0);
-    const float2 dmw = f2sub(wm, w0), dpw = f2sub(wp1, w0), wq = f2d(w0);
-    float2 L1, L3;
-    L1.x = a * dmu.x + cc * dpu.x + sdg * uq.x; L1.y = a * dmu.y + cc * dpu.y + sdg * uq.y;
-    L3.x = a * dmw.x + cc * dpw.x + sdg * wq.x; L3.y = a * dmw.y + cc * dpw.y + sdg * wq.y;
-    float2 du1, du3;
+    const float L = a * (float)(um - u0) + cc * (float)(up1 - u0) + sdg * (float)u0;
+    float du;
     const int ibs = ibslot_u ? ibslot_u[q] : -1;
     if (ibs < 0) {
-      const float2 pj = f2d(p[(size_t)(q - 1) * nc + c]);
-      const float2 no1 = Nu1[o], no3 = Nu3[o];
-      du1.x = (C1 * L1.x + C2 * no1.x) + (-C3x * pj.y) + mp;
-      du1.y = (C1 * L1.y + C2 * no1.y) + (C3x * pj.x);
-      du3.x = (C1 * L3.x + C2 * no3.x) + (-C3z * pj.y);
-      du3.y = (C1 * L3.y + C2 * no3.y) + (C3z * pj.x);
-      const float th = (float)g.thu[q];
-      const float2 x1 = N1xz[o], x3 = N3xz[o];
-      float2 n1, n3;
-      n1.x = x1.x + (uvq.x - uvm.x) * th * dd; n1.y = x1.y + (uvq.y - uvm.y) * th * dd;
-      n3.x = x3.x + (wvq.x - wvm.x) * th * dd; n3.y = x3.y + (wvq.y - wvm.y) * th * dd;
-      Nu1[o] = n1;
-      Nu3[o] = n3;
-      du1.x += G * n1.x; du1.y += G * n1.y;
-      du3.x += G * n3.x; du3.y += G * n3.y;
+      const double2 pj = p[(size_t)(q - 1) * nc + c];
+      const float pt = part ? (float)pj.x : -(float)pj.y;  // i*C3*p: (-C3 p.y, C3 p.x)
+      du = (C1 * L + C2 * Nu[e]) + C3 * pt + mp;
+      const float n = X[e] + (flq - flm) * (float)g.thu[q] * dd;
+      Nu[e] = n;
+      du += G * n;
     } else {
-      du1 = f2d(duib[((size_t)ibs * 3 + 0) * nc + c]);
-      du3 = f2d(duib[((size_t)ibs * 3 + 2) * nc + c]);
+      const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+      du = (float)(part ? di.y : di.x);
     }
-    float2 r1, r3;
-    r1.x = dtf * du1.x + beta * L1.x; r1.y = dtf * du1.y + beta * L1.y;
-    r3.x = dtf * du3.x + beta * L3.x; r3.y = dtf * du3.y + beta * L3.y;
+    const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
     const float a2 = 1.f - beta * (b + k2f);
     const float a3p = a3raw * a2p;
-    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
     a2p = 1.f / (a2 - a1 * a3p);
-    yu.x = (r1.x - a1 * yu.x) * a2p; yu.y = (r1.y - a1 * yu.y) * a2p;
-    yw.x = (r3.x - a1 * yw.x) * a2p; yw.y = (r3.y - a1 * yw.y) * a2p;
-    ys[o] = make_float4(yu.x, yu.y, yw.x, yw.y);
+    y = (rr - a1 * y) * a2p;
+    yprev = y;
     a3raw = -beta * cc;
-    um = u0; u0 = up1; wm = w0; w0 = wp1;
-    uvm = uvq; wvm = wvq;
+    um = u0; u0 = up1;
+    flm = flq;
   }
-  {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1)); here um = u(n-2), u0 = u(n-1)
+  {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1))
     const int q = nu - 1;
     const float a1 = (float)gw2;
-    const float2 rl = make_float2((float)(-(gw2 * um.x + u0.x)), (float)(-(gw2 * um.y + u0.y)));
-    const float2 rw = make_float2((float)(-(gw2 * wm.x + w0.x)), (float)(-(gw2 * wm.y + w0.y)));
+    const float rl = (float)(-(gw2 * um + u0));
     const float a3p = a3raw * a2p;
-    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
     a2p = 1.f / (1.f - a1 * a3p);
-    yu.x = (rl.x - a1 * yu.x) * a2p; yu.y = (rl.y - a1 * yu.y) * a2p;
-    yw.x = (rw.x - a1 * yw.x) * a2p; yw.y = (rw.y - a1 * yw.y) * a2p;
-    double2 t = u1[(size_t)q * nc + c], s3 = u3[(size_t)q * nc + c];
-    t.x += (double)yu.x; t.y += (double)yu.y; s3.x += (double)yw.x; s3.y += (double)yw.y;
-    u1[(size_t)q * nc + c] = t;
-    u3[(size_t)q * nc + c] = s3;
+    y = (rl - a1 * y) * a2p;
+    u[(size_t)q * lstride + ci] = u0 + (double)y;
   }
-  float2 xu = yu, xw = yw;
+  float x = y;
   for (int q = nu - 2; q >= 0; --q) {
-    const size_t o = (size_t)q * nc + c;
-    const float a3p = a3f[o];
-    const float4 yy = ys[o];
-    xu.x = yy.x - a3p * xu.x; xu.y = yy.y - a3p * xu.y;
-    xw.x = yy.z - a3p * xw.x; xw.y = yy.w - a3p * xw.y;
-    double2 t = u1[o], s3 = u3[o];
-    t.x += (double)xu.x; t.y += (double)xu.y; s3.x += (double)xw.x; s3.y += (double)xw.y;
-    u1[o] = t;
-    u3[o] = s3;
+    const size_t e = (size_t)q * lstride + ci;
+    const float2 ya = ys[e];
+    x = ya.x - ya.y * x;
+    u[e] = u[e] + (double)x;
   }
 }
 
-__global__ void __launch_bounds__(NTHR) k_helm_v_mx(double2 *__restrict__ u2, float2 *__restrict__ Nu2,
-                                                    const float2 *__restrict__ N2xz, const float2 *__restrict__ vvc,
-                                                    const double2 *__restrict__ p, float *__restrict__ a3f,
-                                                    float2 *__restrict__ ys, Geo g, const DevScalars *__restrict__ sc,
-                                                    int kRK, const int *__restrict__ ibslot_v,
-                                                    const double2 *__restrict__ duib) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, float *__restrict__ Nu2,
+                                                     const float *__restrict__ N2xz, const float *__restrict__ vvc,
+                                                     const double *__restrict__ p, float2 *__restrict__ ys, Geo g,
+                                                     const DevScalars *__restrict__ sc, int kRK,
+                                                     const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
   if (c >= nc) return;
   const int r = c / g.N1h, kx = c - r * g.N1h;
@@ -660,68 +645,168 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx(double2 *__restrict__ u2, fl
   const float dd = (float)g.dd;
   const int nv = g.nv;
   const double *d0 = g.d2v, *d1 = g.d2v + nv, *d2 = g.d2v + 2 * nv;
-  double2 vm = u2[c], v0 = u2[(size_t)nc + c];
-  float2 y = make_float2((float)(-vm.x), (float)(-vm.y));  // row 0: d(0) = -v(0)
-  ys[c] = y;
+  const size_t ci = (size_t)c * 2 + part;
+  const size_t lstride = (size_t)nc * 2;
+  double vm = u2[ci], v0 = u2[lstride + ci];
+  float y = (float)(-vm);
+  float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
-  float2 vvq = vvc[(size_t)1 * nc + c];
+  float vvq = vvc[lstride + ci];
   for (int q = 1; q <= nv - 2; ++q) {
-    const size_t o = (size_t)q * nc + c;
-    const double2 vp1 = u2[o + nc];
-    const float2 vvp = vvc[o + nc];
+    const size_t e = (size_t)q * lstride + ci;
+    const double vp1 = u2[e + lstride];
+    const float vvp = vvc[e + lstride];
     const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
     const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
-    const float2 dm = f2sub(vm, v0), dp = f2sub(vp1, v0), vq = f2d(v0);
-    float2 L;
-    L.x = a * dm.x + cc * dp.x + sdg * vq.x; L.y = a * dm.y + cc * dp.y + sdg * vq.y;
-    float2 du;
+    const float L = a * (float)(vm - v0) + cc * (float)(vp1 - v0) + sdg * (float)v0;
+    float du;
     const int ibs = ibslot_v ? ibslot_v[q] : -1;
     if (ibs < 0) {
       const float C3 = (float)(-dR * g.dd * g.thv[q]);
-      const float2 pp = f2d(p[(size_t)q * nc + c]), pm = f2d(p[(size_t)(q - 1) * nc + c]);
-      const float2 no = Nu2[o];
-      du.x = (C1 * L.x + C2 * no.x) + C3 * (pp.x - pm.x);
-      du.y = (C1 * L.y + C2 * no.y) + C3 * (pp.y - pm.y);
-      const float th = (float)g.thv[q];
-      const float2 x2 = N2xz[o];
-      float2 n2;
-      n2.x = x2.x + (vvp.x - vvq.x) * th * dd; n2.y = x2.y + (vvp.y - vvq.y) * th * dd;
-      Nu2[o] = n2;
-      du.x += G * n2.x; du.y += G * n2.y;
+      const float pd = (float)p[e] - (float)p[e - lstride];
+      du = (C1 * L + C2 * Nu2[e]) + C3 * pd;
+      const float n = N2xz[e] + (vvp - vvq) * (float)g.thv[q] * dd;
+      Nu2[e] = n;
+      du += G * n;
     } else {
-      du = f2d(duib[((size_t)ibs * 3 + 1) * nc + c]);
+      const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
+      du = (float)(part ? di.y : di.x);
     }
-    float2 rr;
-    rr.x = dtf * du.x + beta * L.x; rr.y = dtf * du.y + beta * L.y;
+    const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
     const float a2 = 1.f - beta * (b + k2f);
     const float a3p = a3raw * a2p;
-    a3f[(size_t)(q - 1) * nc + c] = a3p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
     a2p = 1.f / (a2 - a1 * a3p);
-    y.x = (rr.x - a1 * y.x) * a2p; y.y = (rr.y - a1 * y.y) * a2p;
-    ys[o] = y;
+    y = (rr - a1 * y) * a2p;
+    yprev = y;
     a3raw = -beta * cc;
     vm = v0; v0 = vp1; vvq = vvp;
   }
   {  // last row: d(n-1) = -v(n-1)
     const int q = nv - 1;
     const float a3p = a3raw * a2p;
-    a3f[(size_t)(q - 1) * nc + c] = a3p;
-    y = make_float2((float)(-v0.x), (float)(-v0.y));
-    double2 t = u2[(size_t)q * nc + c];
-    t.x += (double)y.x; t.y += (double)y.y;
-    u2[(size_t)q * nc + c] = t;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+    y = (float)(-v0);
+    u2[(size_t)q * lstride + ci] = v0 + (double)y;
   }
-  float2 x = y;
+  float x = y;
   for (int q = nv - 2; q >= 0; --q) {
-    const size_t o = (size_t)q * nc + c;
-    const float a3p = a3f[o];
-    const float2 yy = ys[o];
-    x.x = yy.x - a3p * x.x; x.y = yy.y - a3p * x.y;
-    double2 t = u2[o];
-    t.x += (double)x.x; t.y += (double)x.y;
-    u2[o] = t;
+    const size_t e = (size_t)q * lstride + ci;
+    const float2 ya = ys[e];
+    x = ya.x - ya.y * x;
+    u2[e] = u2[e] + (double)x;
   }
+}
+
+// ============================================================================
+// Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
+// stored factors, p += psi, v_corr, and the divergence of the corrected field
+// (max |div|^2 -> errbits). FP64 in both forms. One lane per (column, real or
+// imaginary part); the two lanes of a column are neighbours in a warp and
+// exchange the other part with shuffles. All lanes run the loops; memory
+// accesses are guarded. p levels qp = 0..np-1 <-> u/v index q = qp + 1.
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double *__restrict__ u2,
+                                                 double *__restrict__ u3, double *__restrict__ p,
+                                                 double *__restrict__ psi, const double *__restrict__ dg1,
+                                                 const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
+                                                 DevScalars *sc, int kRK) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = tid >> 1, part = tid & 1;
+  const int nc = g.ncol;
+  const bool on = c < nc;
+  const int cc = on ? c : 0;
+  const int r = cc / g.N1h, kx = cc - r * g.N1h;
+  const double kxv = g.k1x[kx], kzv = g.k1z[r];
+  const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+  const double dtirk = sc->dti / aRb;
+  const double dt = sc->dt;
+  const int np = g.np;
+  const double dd = g.dd;
+  const size_t ci = (size_t)cc * 2 + part;
+  const size_t ls = (size_t)nc * 2;
+  const unsigned FULL = 0xffffffffu;
+  // i*k*a: part 0 -> -k*a.y, part 1 -> k*a.x ; `o` is the other part of a
+  double y = 0.0;
+  double vm = on ? u2[ci] : 0.0;
+  for (int qp = 0; qp < np; ++qp) {
+    const int q = qp + 1;
+    const size_t e = (size_t)q * ls + ci;
+    const double a = on ? u1[e] : 0.0, w = on ? u3[e] : 0.0, v = on ? u2[e] : 0.0;
+    const double ao = __shfl_xor_sync(FULL, a, 1), wo = __shfl_xor_sync(FULL, w, 1);
+    const double th = dd * g.thu[q];
+    const double dv = part ? (kxv * ao + kzv * wo) + th * (v - vm) : (-kxv * ao + -kzv * wo) + th * (v - vm);
+    vm = v;
+    double rhs = dtirk * dv;
+    if (qp == 0 && cc == 0) rhs = 0.0;
+    const double A1 = on ? dg1[(size_t)qp * nc + cc] : 0.0, a2p = on ? dg2[(size_t)qp * nc + cc] : 1.0;
+    y = (qp == 0) ? rhs * a2p : (rhs - A1 * y) * a2p;
+    if (on) psi[(size_t)qp * ls + ci] = y;
+  }
+  const double dtrk = dt * aRb;
+  const double dtrk2 = dtrk * dd;
+  const double kxd = dtrk * kxv, kzd = dtrk * kzv;
+  double xn = y;
+  double vup = 0.0, a_up = 0.0, w_up = 0.0, a_upo = 0.0, w_upo = 0.0;
+  double dmax = 0.0;
+  for (int qp = np - 1; qp >= 0; --qp) {
+    const int q = qp + 1;
+    const size_t e = (size_t)q * ls + ci;
+    double x;
+    if (qp == np - 1) x = xn;
+    else {
+      const double a3p = on ? dg3[(size_t)qp * nc + cc] : 0.0;
+      const double yy = on ? psi[(size_t)qp * ls + ci] : 0.0;
+      x = yy - a3p * xn;
+    }
+    if (on) {
+      psi[(size_t)qp * ls + ci] = x;
+      p[(size_t)qp * ls + ci] = p[(size_t)qp * ls + ci] + x;
+    }
+    const double xo = __shfl_xor_sync(FULL, x, 1);
+    double a = on ? u1[e] : 0.0, w = on ? u3[e] : 0.0;
+    // u -= (dtrk i kx) psi: part 0: u.x -= -kxd psi.y ; part 1: u.y -= kxd psi.x
+    if (part) { a = a - (kxd * xo); w = w - (kzd * xo); }
+    else { a = a - (-kxd * xo); w = w - (-kzd * xo); }
+    if (on) { u1[e] = a; u3[e] = w; }
+    double v = on ? u2[e] : 0.0;
+    if (q <= g.nv - 2) {
+      const double f = dtrk2 * g.thv[q];
+      v = v - f * (xn - x);
+      if (on) u2[e] = v;
+    }
+    const double ao = __shfl_xor_sync(FULL, a, 1), wo = __shfl_xor_sync(FULL, w, 1);
+    if (qp < np - 1) {
+      const double th = dd * g.thu[q + 1];
+      const double dv = part ? (kxv * a_upo + kzv * w_upo) + th * (vup - v) : (-kxv * a_upo + -kzv * w_upo) + th * (vup - v);
+      const double d2v = dv * dv + __shfl_xor_sync(FULL, dv * dv, 1);
+      if (on) dmax = fmax(dmax, d2v);
+    } else {
+      (void)__shfl_xor_sync(FULL, 0.0, 1);
+    }
+    a_up = a; w_up = w; a_upo = ao; w_upo = wo; vup = v;
+    xn = x;
+  }
+  {
+    const double th = dd * g.thu[1];
+    const double vb = on ? u2[ci] : 0.0;
+    const double dv = part ? (kxv * a_upo + kzv * w_upo) + th * (vup - vb) : (-kxv * a_upo + -kzv * w_upo) + th * (vup - vb);
+    const double d2v = dv * dv + __shfl_xor_sync(FULL, dv * dv, 1);
+    if (on) dmax = fmax(dmax, d2v);
+  }
+  (void)a_up; (void)w_up;
+  if (on) {
+    const int nu = g.nu;
+    u1[ci] = g.gwbc1 * u1[ls + ci];
+    u3[ci] = g.gwbc3 * u3[ls + ci];
+    u1[(size_t)(nu - 1) * ls + ci] = g.gwbc1 * u1[(size_t)(nu - 2) * ls + ci];
+    u3[(size_t)(nu - 1) * ls + ci] = g.gwbc3 * u3[(size_t)(nu - 2) * ls + ci];
+    u2[ci] = 0.0;
+    u2[(size_t)(g.nv - 1) * ls + ci] = 0.0;
+  }
+  dmax = warp_max(dmax);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
 }
 
 // ============================================================================
@@ -838,110 +923,6 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
     a3raw = A3;
   }
   dg3[(size_t)(np - 1) * nc + c] = 0.0;
-}
-
-// ============================================================================
-// Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
-// stored factors, p += psi, v_corr, and the divergence of the corrected field
-// (max |div|^2 -> errbits). One thread per column. p levels qp = 0..np-1 <->
-// u/v index q = qp + 1. `psi` holds the forward-sweep values, then psi.
-// ============================================================================
-__global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double2 *__restrict__ u2,
-                                                double2 *__restrict__ u3, double2 *__restrict__ p,
-                                                double2 *__restrict__ psi, const double *__restrict__ dg1,
-                                                const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
-                                                DevScalars *sc, int kRK) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nc = g.ncol;
-  double dmax = 0.0;
-  if (c < nc) {
-    const int r = c / g.N1h, kx = c - r * g.N1h;
-    const double kxv = g.k1x[kx], kzv = g.k1z[r];
-    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
-    const double dtirk = sc->dti / aRb;
-    const double dt = sc->dt;
-    const int np = g.np;
-    const double dd = g.dd;
-    double2 y = czero<double2>();
-    double2 vm = u2[c];
-    for (int qp = 0; qp < np; ++qp) {
-      const int q = qp + 1;
-      const size_t o = (size_t)q * nc + c;
-      const double2 a = u1[o], w = u3[o], v = u2[o];
-      const double th = dd * g.thu[q];
-      double2 dv;
-      dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
-      dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
-      vm = v;
-      double2 rhs;
-      rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
-      if (qp == 0 && c == 0) { rhs.x = 0.0; rhs.y = 0.0; }
-      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
-      if (qp == 0) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
-      else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
-      psi[(size_t)qp * nc + c] = y;
-    }
-    const double dtrk = dt * aRb;
-    const double dtrk2 = dtrk * dd;
-    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
-    double2 xn = y;
-    double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
-    for (int qp = np - 1; qp >= 0; --qp) {
-      const int q = qp + 1;
-      const size_t o = (size_t)q * nc + c;
-      double2 x;
-      if (qp == np - 1) x = xn;
-      else {
-        const double a3p = dg3[(size_t)qp * nc + c];
-        const double2 yy = psi[(size_t)qp * nc + c];
-        x.x = yy.x - a3p * xn.x; x.y = yy.y - a3p * xn.y;
-      }
-      psi[(size_t)qp * nc + c] = x;
-      double2 pp = p[(size_t)qp * nc + c];
-      pp.x = pp.x + x.x; pp.y = pp.y + x.y;
-      p[(size_t)qp * nc + c] = pp;
-      double2 a = u1[o], w = u3[o];
-      a.x = a.x - (-kxd * x.y); a.y = a.y - (kxd * x.x);
-      w.x = w.x - (-kzd * x.y); w.y = w.y - (kzd * x.x);
-      u1[o] = a;
-      u3[o] = w;
-      double2 v = u2[o];
-      if (q <= g.nv - 2) {
-        const double f = dtrk2 * g.thv[q];
-        v.x = v.x - f * (xn.x - x.x);
-        v.y = v.y - f * (xn.y - x.y);
-        u2[o] = v;
-      }
-      if (qp < np - 1) {
-        const double th = dd * g.thu[q + 1];
-        double2 dv;
-        dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
-        dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - v.y);
-        dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
-      }
-      a_up = a; w_up = w; vup = v;
-      xn = x;
-    }
-    {
-      const double th = dd * g.thu[1];
-      const double2 vb = u2[c];
-      double2 dv;
-      dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
-      dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
-      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
-    }
-    const int nu = g.nu;
-    double2 t1 = u1[(size_t)nc + c], t3 = u3[(size_t)nc + c];
-    u1[c] = cscale(t1, g.gwbc1);
-    u3[c] = cscale(t3, g.gwbc3);
-    t1 = u1[(size_t)(nu - 2) * nc + c]; t3 = u3[(size_t)(nu - 2) * nc + c];
-    u1[(size_t)(nu - 1) * nc + c] = cscale(t1, g.gwbc1);
-    u3[(size_t)(nu - 1) * nc + c] = cscale(t3, g.gwbc3);
-    u2[c] = czero<double2>();
-    u2[(size_t)(g.nv - 1) * nc + c] = czero<double2>();
-  }
-  dmax = warp_max(dmax);
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
 }
 
 __global__ void k_reset_err(DevScalars *sc) {
