@@ -35,6 +35,7 @@ struct lh_handle {
   size_t Abytes, Bbytes;
   long long graph_nodes_per_step;
   double *geo_pool;
+  float *geo_poolf;
   DevScalars *sc;
   double2 *stage;  // staging for transposes
   // immersed boundaries
@@ -234,6 +235,23 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   g.yu = P + o_yu; g.yv = P + o_yv; g.thu = P + o_thu; g.thv = P + o_thv; g.d2u = P + o_d2u; g.d2v = P + o_d2v;
   g.k1x = P + o_k1x; g.k2x = P + o_k2x; g.k1z = P + o_k1z; g.k2z = P + o_k2z;
   g.iua = P + o_iua; g.iub = P + o_iub; g.iud = P + o_iud; g.iva = P + o_iva; g.ivb = P + o_ivb; g.ivd = P + o_ivd;
+  {  // FP32 copies for the mixed form
+    std::vector<float> pf;
+    auto putf = [&](const double *src, size_t n) { size_t o = pf.size(); for (size_t i = 0; i < n; ++i) pf.push_back((float)src[i]); return o; };
+    std::vector<double> sdgu(nu, 0.0), sdgv(nv, 0.0);
+    for (int q = 0; q < nu; ++q) sdgu[q] = (cfg->dyu2i[q] + cfg->dyu2i[nu + q]) + cfg->dyu2i[2 * nu + q];
+    for (int q = 0; q < nv; ++q) sdgv[q] = (cfg->dyv2i[q] + cfg->dyv2i[nv + q]) + cfg->dyv2i[2 * nv + q];
+    size_t f_k1x = putf(cfg->k1x, g.N1h), f_k1z = putf(cfg->k1z, g.N2);
+    size_t f_iua = putf(iua.data(), nu), f_iub = putf(iub.data(), nu), f_iva = putf(iva.data(), nv), f_ivb = putf(ivb.data(), nv);
+    size_t f_thu = putf(cfg->dthdyu, nu), f_thv = putf(cfg->dthdyv, nv);
+    size_t f_d2u = putf(cfg->dyu2i, 3 * (size_t)nu), f_d2v = putf(cfg->dyv2i, 3 * (size_t)nv);
+    size_t f_su = putf(sdgu.data(), nu), f_sv = putf(sdgv.data(), nv);
+    h->geo_poolf = (float *)upload_vec(pf, ce);
+    if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+    float *F = h->geo_poolf;
+    g.k1xf = F + f_k1x; g.k1zf = F + f_k1z; g.iuaf = F + f_iua; g.iubf = F + f_iub; g.ivaf = F + f_iva; g.ivbf = F + f_ivb;
+    g.thuf = F + f_thu; g.thvf = F + f_thv; g.d2uf = F + f_d2u; g.d2vf = F + f_d2v; g.sdgu = F + f_su; g.sdgv = F + f_sv;
+  }
 
   const size_t vs = h->vsz;
 
@@ -370,7 +388,7 @@ extern "C" int lh_destroy(lh_handle *h) {
   if (!h) return LH_EINVAL;
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
-                  h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->sc, h->stage,
+                  h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
   for (void *b : bufs)

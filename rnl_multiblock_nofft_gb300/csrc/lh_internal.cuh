@@ -20,6 +20,9 @@ struct Geo {
   const double *iua, *iub, *iud;
   // v-level q (centre -> face): (iva*u[q+1] + ivb*u[q]) / ivd
   const double *iva, *ivb, *ivd;
+  // FP32 copies for the mixed form (no conversion in the kernels): wavenumbers,
+  // interpolation weights, metrics, difference coefficients and their row sums
+  const float *k1xf, *k1zf, *iuaf, *iubf, *ivaf, *ivbf, *thuf, *thvf, *d2uf, *d2vf, *sdgu, *sdgv;
   double Re, CFL, dtv, dd, dthetavi, alp, bet, Kib;
   double aRK[3], bRK[3], cRK[3], dRK[3], gRK[3];
   double gw[3][2];
@@ -36,6 +39,44 @@ struct DevScalars {
   int status;
   int pad;
 };
+
+// ---------------------------------------------------------------------------
+// double <-> float on the integer pipe. On this part conversion instructions
+// issue on the FP64 pipe, which the mixed form keeps for the arithmetic that
+// needs it; these do the IEEE-754 bit manipulation with integer operations.
+// d2f_alu: round to nearest even; |x| < 2^-126 becomes a signed zero; Inf/NaN
+// preserved. f2d_alu: exact (FP32 denormals read as zero).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float d2f_alu(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
+  const unsigned int sign = hi & 0x80000000u;
+  const int ed = (int)((hi >> 20) & 0x7ffu);
+  const int e = ed - 1023 + 127;
+  const unsigned int m = ((hi & 0x000fffffu) << 3) | (lo >> 29);
+  const unsigned int rest = lo & 0x1fffffffu;
+  unsigned int f = ((unsigned int)e << 23) | m;
+  f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  if (e <= 0) f = 0u;
+  if (e >= 255) f = (ed == 0x7ff && (((hi & 0x000fffffu) | lo) != 0u)) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float(sign | f);
+}
+__device__ __forceinline__ double f2d_alu(float x) {
+  const unsigned int u = __float_as_uint(x);
+  const unsigned int sign = u & 0x80000000u;
+  const unsigned int e = (u >> 23) & 0xffu;
+  const unsigned int m = u & 0x7fffffu;
+  unsigned int hi, lo;
+  if (e == 0u) { hi = sign; lo = 0u; }
+  else if (e == 255u) { hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u); lo = m << 29; }
+  else { hi = sign | ((e + 896u) << 20) | (m >> 3); lo = m << 29; }
+  return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+template <typename T> __device__ __forceinline__ T to_t(double x);
+template <> __device__ __forceinline__ double to_t<double>(double x) { return x; }
+template <> __device__ __forceinline__ float to_t<float>(double x) { return d2f_alu(x); }
+__device__ __forceinline__ double to_d(double x) { return x; }
+__device__ __forceinline__ double to_d(float x) { return f2d_alu(x); }
 
 // ---------------------------------------------------------------------------
 // complex helpers (double2 / float2)

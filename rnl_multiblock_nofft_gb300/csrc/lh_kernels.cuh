@@ -77,22 +77,34 @@ __global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1
     const int c = r * g.N1h + kx;
     V v;
     if (isU) {
-      if (f == 0) { const double2 x = u1[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
-      else if (f == 2) { const double2 x = u3[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
+      if (f == 0) { const double2 x = u1[(size_t)q * nc + c]; v.x = to_t<T>(x.x); v.y = to_t<T>(x.y); }
+      else if (f == 2) { const double2 x = u3[(size_t)q * nc + c]; v.x = to_t<T>(x.x); v.y = to_t<T>(x.y); }
       else {  // interp_v: v faces -> centre q
-        const T a = (T)g.iua[q], b = (T)g.iub[q];
         const double2 v0 = u2[(size_t)q * nc + c], vm = u2[(size_t)(q - 1) * nc + c];
-        v.x = a * (T)v0.x + b * (T)vm.x;
-        v.y = a * (T)v0.y + b * (T)vm.y;
+        if (sizeof(T) == 8) {
+          const double a = g.iua[q], b = g.iub[q];
+          v.x = (T)(a * v0.x + b * vm.x);
+          v.y = (T)(a * v0.y + b * vm.y);
+        } else {
+          const T a = (T)g.iuaf[q], b = (T)g.iubf[q];
+          v.x = a * to_t<T>(v0.x) + b * to_t<T>(vm.x);
+          v.y = a * to_t<T>(v0.y) + b * to_t<T>(vm.y);
+        }
       }
     } else {
-      if (f == 1) { const double2 x = u2[(size_t)q * nc + c]; v.x = (T)x.x; v.y = (T)x.y; }
+      if (f == 1) { const double2 x = u2[(size_t)q * nc + c]; v.x = to_t<T>(x.x); v.y = to_t<T>(x.y); }
       else {  // interp_u: centres -> face q
         const double2 *src = (f == 0) ? u1 : u3;
-        const T a = (T)g.iva[q], b = (T)g.ivb[q];
         const double2 up = src[(size_t)(q + 1) * nc + c], u0 = src[(size_t)q * nc + c];
-        v.x = a * (T)up.x + b * (T)u0.x;
-        v.y = a * (T)up.y + b * (T)u0.y;
+        if (sizeof(T) == 8) {
+          const double a = g.iva[q], b = g.ivb[q];
+          v.x = (T)(a * up.x + b * u0.x);
+          v.y = (T)(a * up.y + b * u0.y);
+        } else {
+          const T a = (T)g.ivaf[q], b = (T)g.ivbf[q];
+          v.x = a * to_t<T>(up.x) + b * to_t<T>(u0.x);
+          v.y = a * to_t<T>(up.y) + b * to_t<T>(u0.y);
+        }
       }
     }
     b0[prow(g, r) * KB + kk] = v;
@@ -165,13 +177,13 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
         const int l = l0 + 2 * pb;
         double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * G1;
         const V z = res[idx];
-        cp[(size_t)l * G1 + m] = (double)z.x;
-        cp[(size_t)(l + 1) * G1 + m] = (double)z.y;
+        cp[(size_t)l * G1 + m] = to_d(z.x);
+        cp[(size_t)(l + 1) * G1 + m] = to_d(z.y);
       }
     }
   }
   T m1 = 0, m2 = 0, m3 = 0;
-  const T thv = isU ? (T)0 : (T)g.thv[q];
+  const T thv = isU ? (T)0 : (sizeof(T) == 8 ? (T)g.thv[q] : (T)g.thvf[q]);
   for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
     const int pb = idx / G1, m = idx - pb * G1;
     const V u = res[(0 * PB + pb) * G1 + m], v = res[(1 * PB + pb) * G1 + m], w = res[(2 * PB + pb) * G1 + m];
@@ -202,8 +214,8 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
   if (doCFL) {
     m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
     if ((threadIdx.x & 31) == 0) {
-      if (isU) { atomic_max_pos(&sc->u1m, (double)m1); atomic_max_pos(&sc->u3m, (double)m3); }
-      else atomic_max_pos(&sc->u2m, (double)m2);
+      if (isU) { atomic_max_pos(&sc->u1m, to_d(m1)); atomic_max_pos(&sc->u3m, to_d(m3)); }
+      else atomic_max_pos(&sc->u2m, to_d(m2));
     }
   }
   __syncthreads();
@@ -263,7 +275,8 @@ __device__ __forceinline__ void zfwd_body(const typename C2<T>::t *__restrict__ 
     if (kx >= N1h) continue;
     const int row = prow(g, r);
     const int c = r * N1h + kx;
-    const T kxv = (T)g.k1x[kx], kzv = (T)g.k1z[r];
+    const T kxv = sizeof(T) == 8 ? (T)g.k1x[kx] : (T)g.k1xf[kx];
+    const T kzv = sizeof(T) == 8 ? (T)g.k1z[r] : (T)g.k1zf[r];
     const bool zr = (r == N2 / 2);  // der_x/der_z zero the kz = -N2/2 row
     if (NP == 4) {
       const V uu = cscale(res[row * NL + 0 * KB + kk], s2), uw = cscale(res[row * NL + 1 * KB + kk], s2);
@@ -570,7 +583,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   const size_t ci = (size_t)c * 2 + part;
   const size_t lstride = (size_t)nc * 2;
   double um = u[ci], u0 = u[lstride + ci];
-  float y = (float)(-(um + gw1 * u0));  // row 0
+  float y = d2f_alu(-(um + gw1 * u0));  // row 0
   float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
   float flm = Fl[ci];
@@ -578,21 +591,22 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     const size_t e = (size_t)q * lstride + ci;
     const double up1 = u[e + lstride];
     const float flq = Fl[e];
-    const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
-    const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
-    const float L = a * (float)(um - u0) + cc * (float)(up1 - u0) + sdg * (float)u0;
+    const float a = g.d2uf[q], b = g.d2uf[nu + q], cc = g.d2uf[2 * nu + q];
+    const float sdg = g.sdgu[q] + k2f;
+    const double dp = up1 - u0;
+    const float L = a * d2f_alu(um - u0) + cc * d2f_alu(dp) + sdg * d2f_alu(u0);
     float du;
     const int ibs = ibslot_u ? ibslot_u[q] : -1;
     if (ibs < 0) {
       const double2 pj = p[(size_t)(q - 1) * nc + c];
-      const float pt = part ? (float)pj.x : -(float)pj.y;  // i*C3*p: (-C3 p.y, C3 p.x)
+      const float pt = part ? d2f_alu(pj.x) : -d2f_alu(pj.y);  // i*C3*p: (-C3 p.y, C3 p.x)
       du = (C1 * L + C2 * Nu[e]) + C3 * pt + mp;
-      const float n = X[e] + (flq - flm) * (float)g.thu[q] * dd;
+      const float n = X[e] + (flq - flm) * g.thuf[q] * dd;
       Nu[e] = n;
       du += G * n;
     } else {
       const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
-      du = (float)(part ? di.y : di.x);
+      du = d2f_alu(part ? di.y : di.x);
     }
     const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
@@ -609,19 +623,19 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1))
     const int q = nu - 1;
     const float a1 = (float)gw2;
-    const float rl = (float)(-(gw2 * um + u0));
+    const float rl = d2f_alu(-(gw2 * um + u0));
     const float a3p = a3raw * a2p;
     ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
     a2p = 1.f / (1.f - a1 * a3p);
     y = (rl - a1 * y) * a2p;
-    u[(size_t)q * lstride + ci] = u0 + (double)y;
+    u[(size_t)q * lstride + ci] = u0 + f2d_alu(y);
   }
   float x = y;
   for (int q = nu - 2; q >= 0; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
     x = ya.x - ya.y * x;
-    u[e] = u[e] + (double)x;
+    u[e] = u[e] + f2d_alu(x);
   }
 }
 
@@ -648,7 +662,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   const size_t ci = (size_t)c * 2 + part;
   const size_t lstride = (size_t)nc * 2;
   double vm = u2[ci], v0 = u2[lstride + ci];
-  float y = (float)(-vm);
+  const float dRf = (float)dR;
+  float y = d2f_alu(-vm);
   float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
   float vvq = vvc[lstride + ci];
@@ -656,21 +671,21 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     const size_t e = (size_t)q * lstride + ci;
     const double vp1 = u2[e + lstride];
     const float vvp = vvc[e + lstride];
-    const float a = (float)d0[q], cc = (float)d2[q], b = (float)d1[q];
-    const float sdg = (float)((d0[q] + d1[q]) + d2[q]) + k2f;
-    const float L = a * (float)(vm - v0) + cc * (float)(vp1 - v0) + sdg * (float)v0;
+    const float a = g.d2vf[q], b = g.d2vf[nv + q], cc = g.d2vf[2 * nv + q];
+    const float sdg = g.sdgv[q] + k2f;
+    const float L = a * d2f_alu(vm - v0) + cc * d2f_alu(vp1 - v0) + sdg * d2f_alu(v0);
     float du;
     const int ibs = ibslot_v ? ibslot_v[q] : -1;
     if (ibs < 0) {
-      const float C3 = (float)(-dR * g.dd * g.thv[q]);
-      const float pd = (float)p[e] - (float)p[e - lstride];
+      const float C3 = -dRf * dd * g.thvf[q];
+      const float pd = d2f_alu(p[e]) - d2f_alu(p[e - lstride]);
       du = (C1 * L + C2 * Nu2[e]) + C3 * pd;
-      const float n = N2xz[e] + (vvp - vvq) * (float)g.thv[q] * dd;
+      const float n = N2xz[e] + (vvp - vvq) * g.thvf[q] * dd;
       Nu2[e] = n;
       du += G * n;
     } else {
       const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
-      du = (float)(part ? di.y : di.x);
+      du = d2f_alu(part ? di.y : di.x);
     }
     const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
@@ -687,15 +702,15 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     const int q = nv - 1;
     const float a3p = a3raw * a2p;
     ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
-    y = (float)(-v0);
-    u2[(size_t)q * lstride + ci] = v0 + (double)y;
+    y = d2f_alu(-v0);
+    u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
   }
   float x = y;
   for (int q = nv - 2; q >= 0; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
     x = ya.x - ya.y * x;
-    u2[e] = u2[e] + (double)x;
+    u2[e] = u2[e] + f2d_alu(x);
   }
 }
 
@@ -992,7 +1007,7 @@ __global__ void __launch_bounds__(NTHR) k_spec_zinv(const double2 *__restrict__ 
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= g.N1h) continue;
     const double2 val = S[r * g.N1h + kx];
-    V v; v.x = (T)val.x; v.y = (T)val.y;
+    V v; v.x = to_t<T>(val.x); v.y = to_t<T>(val.y);
     b0[prow(g, r) * KB + kk] = v;
   }
   __syncthreads();
@@ -1039,8 +1054,8 @@ __global__ void __launch_bounds__(NTHR) k_xinv_phys(const typename C2<T>::t *__r
     const int pb = idx / G1, m = idx - pb * G1;
     if (pb >= npairs) continue;
     const int l = l0 + 2 * pb;
-    P[(size_t)l * G1 + m] = (double)res[idx].x;
-    P[(size_t)(l + 1) * G1 + m] = (double)res[idx].y;
+    P[(size_t)l * G1 + m] = to_d(res[idx].x);
+    P[(size_t)(l + 1) * G1 + m] = to_d(res[idx].y);
   }
 }
 
@@ -1062,8 +1077,8 @@ __global__ void __launch_bounds__(NTHR) k_xfwd_phys(const double *__restrict__ p
     V z = czero<V>();
     if (pb < npairs) {
       const int l = l0 + 2 * pb;
-      z.x = (T)P[(size_t)l * G1 + m];
-      z.y = (T)P[(size_t)(l + 1) * G1 + m];
+      z.x = to_t<T>(P[(size_t)l * G1 + m]);
+      z.y = to_t<T>(P[(size_t)(l + 1) * G1 + m]);
     }
     b0[idx] = z;
   }
@@ -1108,7 +1123,7 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__r
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= N1h) continue;
     const V t = res[prow(g, r) * KB + kk];
-    double2 o; o.x = (double)t.x * s2; o.y = (double)t.y * s2;
+    double2 o; o.x = to_d(t.x) * s2; o.y = to_d(t.y) * s2;
     S[r * N1h + kx] = o;
   }
 }

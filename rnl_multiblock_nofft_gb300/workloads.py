@@ -56,6 +56,8 @@ WORKLOADS = {
     "M": dict(N=64, ny=97, posts=False, flpress=0, desc="mid smooth channel N 64x64, ny 97"),
     "MP": dict(N=64, ny=97, posts=True, flpress=0, post_period=16, post_points=8, post_height_plus=12.0,
                desc="mid textured channel N 64x64, ny 97, posts"),
+    "P": dict(N=192, ny=201, posts=False, flpress=0,
+              desc="profiling case: smooth channel N 192x192, ny 201 (state 0.27 GB, above L2)"),
 }
 
 
