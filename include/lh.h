@@ -76,7 +76,10 @@ typedef struct lh_config {
   const double *A_ib_u, *A_ib_v;  /* [nib_u], [nib_v] */
 } lh_config;
 
-/* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter). */
+/* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter).
+ * err = max |div u| of the state (error(), littleharsh.f90:342-375): the reference
+ * reads it only at the start of a step, so it is refreshed at the end of the third
+ * substep (and by lh_set_scalars). */
 typedef struct lh_scalars {
   double t, dt, dti, dtc, err, mpgx, QxT, Qx;
   int64_t iter;

@@ -24,6 +24,8 @@ struct lh_handle {
   int prec;  // LH_PREC_*
   size_t vsz;  // bytes of one complex value in the transforms
   cudaStream_t st;
+  cudaStream_t st2;            // side stream: mean-flow correction overlapped with the v solve
+  cudaEvent_t ev_fork, ev_join;
   // device buffers
   double2 *u1, *u2, *u3, *p, *psi;
   void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
@@ -360,8 +362,11 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     ZA(h->duphys, sizeof(double) * (size_t)h->nib * 3 * pp);
     ZA(h->duib, cz * (size_t)h->nib * 3 * nc);
   }
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
-    int rc = fail(h, LH_ECUDA, "cudaStreamCreate"); lh_destroy(h); return rc;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    int rc = fail(h, LH_ECUDA, "cudaStreamCreate/cudaEventCreate"); lh_destroy(h); return rc;
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
@@ -393,6 +398,9 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
   for (void *b : bufs)
     if (b) cudaFree(b);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->st2) cudaStreamDestroy(h->st2);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return LH_OK;
@@ -586,6 +594,26 @@ static int phys_to_spec(lh_handle *h, const double *phys, double2 *spec, int npl
 
 static const void *fp64_tw(lh_handle *h, bool x) { return x ? h->twx64 : h->twz64; }
 
+// flowrate_corr after solveU_W, on the side stream (joined before solveP); on the
+// main stream when kernels are being timed one by one
+static int meanflow_fork(lh_handle *h, int kRK) {
+  const Geo &g = h->g;
+  if (g.flag_ctpress != 0) return LH_OK;
+  const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
+  const int sm = mb <= 48 * 1024 ? 1 : 0;
+  if (h->prof) {
+    KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
+    return LH_OK;
+  }
+  CK(cudaEventRecord(h->ev_fork, h->st));
+  CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+  k_meanflow<<<1, 256, sm ? mb : 0, h->st2>>>(h->u1, g, h->sc, kRK, h->mfw, sm);
+  int rc = count_launch(h);
+  if (rc) return rc;
+  CK(cudaEventRecord(h->ev_join, h->st2));
+  return LH_OK;
+}
+
 template <typename T>
 static int substep_launches_t(lh_handle *h, int kRK) {
   typedef typename C2<T>::t V;
@@ -596,10 +624,18 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
   if (h->ib) {
     dim3 gd(nb, h->nib);
-    KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (V *)h->Nu1, (V *)h->Nu2, (V *)h->Nu3, (const V *)h->N1xz,
-                                                       (const V *)h->N2xz, (const V *)h->N3xz, (const V *)h->uvf,
-                                                       (const V *)h->vvc, (const V *)h->wvf, h->p, h->duib, h->d_iblev,
-                                                       h->nib, g, h->sc, kRK));
+    if (h->prec == LH_PREC_FP64) {
+      KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (V *)h->Nu1, (V *)h->Nu2, (V *)h->Nu3,
+                                                         (const V *)h->N1xz, (const V *)h->N2xz, (const V *)h->N3xz,
+                                                         (const V *)h->uvf, (const V *)h->vvc, (const V *)h->wvf, h->p,
+                                                         h->duib, h->d_iblev, h->nib, g, h->sc, kRK));
+    } else {
+      KL("k_ib_du", k_ib_du_mx<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (float2 *)h->Nu1, (float2 *)h->Nu2,
+                                                         (float2 *)h->Nu3, (const float2 *)h->N1xz, (const float2 *)h->N2xz,
+                                                         (const float2 *)h->N3xz, (const float2 *)h->uvf,
+                                                         (const float2 *)h->vvc, (const float2 *)h->wvf, h->p, h->duib,
+                                                         h->d_iblev, h->nib, g, h->sc, kRK));
+    }
     if ((rc = spec_to_phys<T>(h, h->duib, h->duphys, 3 * h->nib, h->A, h->twx, h->twz))) return rc;
     int ibu = (h->cfg.nib_u + 255) / 256, ibv = (h->cfg.nib_v + 255) / 256;
     if (h->cfg.nib_u > 0)
@@ -615,6 +651,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                            (const V *)h->N1xz, (const V *)h->N3xz, (const V *)h->uvf,
                                                            (const V *)h->wvf, h->p, h->a3s, g, h->sc, kRK,
                                                            h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    if ((rc = meanflow_fork(h, kRK))) return rc;
     KL("k_helm_v", k_helm_v<T><<<nb, NTHR_H, 0, h->st>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz,
                                                          (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
                                                          h->ib ? h->d_ibslot_v : nullptr, h->duib));
@@ -624,22 +661,17 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                         (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
                         (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,
                         h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    if ((rc = meanflow_fork(h, kRK))) return rc;
     KL("k_helm_v", k_helm_v_mx2<<<nb2, NTHR_H, 0, h->st>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
                                                            (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysf,
                                                            g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
   }
-  if (g.flag_ctpress == 0) {
-    const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
-    const int sm = mb <= 48 * 1024 ? 1 : 0;
-    KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
-  }
-  KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
-  {
-    const int nb2 = (2 * g.ncol + NTHR_H - 1) / NTHR_H;
-    KL("k_press", k_press2<<<nb2, NTHR_H, 0, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3, (double *)h->p,
-                                                      (double *)h->psi, h->dg1, h->dg2, h->dg3, g, h->sc, kRK));
-  }
-  KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
+  if (g.flag_ctpress == 0 && !h->prof) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
+  const int need_div = (kRK == 3) ? 1 : 0;
+  if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
+  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
+                                                  h->sc, kRK, need_div));
+  if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }
 

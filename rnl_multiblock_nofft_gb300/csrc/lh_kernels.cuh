@@ -13,8 +13,10 @@
 //   k_helm_uw   : RHS0_u1/u3 + der_yu_h + du += -gRK N + solveU_W, one thread per column
 //   k_helm_v    : RHS0_u2 + der_yv_h + du += -gRK N + solveV
 //   k_meanflow  : flowrate_corr on mode (0,0) (constant flow rate)
-//   k_press     : divergence + solveP (LUsolP with the factor rebuilt on the fly) + v_corr
-//                 + divergence of the corrected field (max |div| -> err)
+//   k_press     : divergence + solveP (LUsolP with the stored factors, k_build_dg) + v_corr
+//                 + divergence of the corrected field in the third substep (max |div| -> err)
+//   Mixed form (LH_PREC_MIXED): FP32 transforms, and k_helm_u_mx2 / k_helm_v_mx2 solve
+//   the Helmholtz systems for the increment in FP32 on top of the FP64 state.
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -715,116 +717,6 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
 }
 
 // ============================================================================
-// Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
-// stored factors, p += psi, v_corr, and the divergence of the corrected field
-// (max |div|^2 -> errbits). FP64 in both forms. One lane per (column, real or
-// imaginary part); the two lanes of a column are neighbours in a warp and
-// exchange the other part with shuffles. All lanes run the loops; memory
-// accesses are guarded. p levels qp = 0..np-1 <-> u/v index q = qp + 1.
-// ============================================================================
-__global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double *__restrict__ u2,
-                                                 double *__restrict__ u3, double *__restrict__ p,
-                                                 double *__restrict__ psi, const double *__restrict__ dg1,
-                                                 const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
-                                                 DevScalars *sc, int kRK) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = tid >> 1, part = tid & 1;
-  const int nc = g.ncol;
-  const bool on = c < nc;
-  const int cc = on ? c : 0;
-  const int r = cc / g.N1h, kx = cc - r * g.N1h;
-  const double kxv = g.k1x[kx], kzv = g.k1z[r];
-  const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
-  const double dtirk = sc->dti / aRb;
-  const double dt = sc->dt;
-  const int np = g.np;
-  const double dd = g.dd;
-  const size_t ci = (size_t)cc * 2 + part;
-  const size_t ls = (size_t)nc * 2;
-  const unsigned FULL = 0xffffffffu;
-  // i*k*a: part 0 -> -k*a.y, part 1 -> k*a.x ; `o` is the other part of a
-  double y = 0.0;
-  double vm = on ? u2[ci] : 0.0;
-  for (int qp = 0; qp < np; ++qp) {
-    const int q = qp + 1;
-    const size_t e = (size_t)q * ls + ci;
-    const double a = on ? u1[e] : 0.0, w = on ? u3[e] : 0.0, v = on ? u2[e] : 0.0;
-    const double ao = __shfl_xor_sync(FULL, a, 1), wo = __shfl_xor_sync(FULL, w, 1);
-    const double th = dd * g.thu[q];
-    const double dv = part ? (kxv * ao + kzv * wo) + th * (v - vm) : (-kxv * ao + -kzv * wo) + th * (v - vm);
-    vm = v;
-    double rhs = dtirk * dv;
-    if (qp == 0 && cc == 0) rhs = 0.0;
-    const double A1 = on ? dg1[(size_t)qp * nc + cc] : 0.0, a2p = on ? dg2[(size_t)qp * nc + cc] : 1.0;
-    y = (qp == 0) ? rhs * a2p : (rhs - A1 * y) * a2p;
-    if (on) psi[(size_t)qp * ls + ci] = y;
-  }
-  const double dtrk = dt * aRb;
-  const double dtrk2 = dtrk * dd;
-  const double kxd = dtrk * kxv, kzd = dtrk * kzv;
-  double xn = y;
-  double vup = 0.0, a_up = 0.0, w_up = 0.0, a_upo = 0.0, w_upo = 0.0;
-  double dmax = 0.0;
-  for (int qp = np - 1; qp >= 0; --qp) {
-    const int q = qp + 1;
-    const size_t e = (size_t)q * ls + ci;
-    double x;
-    if (qp == np - 1) x = xn;
-    else {
-      const double a3p = on ? dg3[(size_t)qp * nc + cc] : 0.0;
-      const double yy = on ? psi[(size_t)qp * ls + ci] : 0.0;
-      x = yy - a3p * xn;
-    }
-    if (on) {
-      psi[(size_t)qp * ls + ci] = x;
-      p[(size_t)qp * ls + ci] = p[(size_t)qp * ls + ci] + x;
-    }
-    const double xo = __shfl_xor_sync(FULL, x, 1);
-    double a = on ? u1[e] : 0.0, w = on ? u3[e] : 0.0;
-    // u -= (dtrk i kx) psi: part 0: u.x -= -kxd psi.y ; part 1: u.y -= kxd psi.x
-    if (part) { a = a - (kxd * xo); w = w - (kzd * xo); }
-    else { a = a - (-kxd * xo); w = w - (-kzd * xo); }
-    if (on) { u1[e] = a; u3[e] = w; }
-    double v = on ? u2[e] : 0.0;
-    if (q <= g.nv - 2) {
-      const double f = dtrk2 * g.thv[q];
-      v = v - f * (xn - x);
-      if (on) u2[e] = v;
-    }
-    const double ao = __shfl_xor_sync(FULL, a, 1), wo = __shfl_xor_sync(FULL, w, 1);
-    if (qp < np - 1) {
-      const double th = dd * g.thu[q + 1];
-      const double dv = part ? (kxv * a_upo + kzv * w_upo) + th * (vup - v) : (-kxv * a_upo + -kzv * w_upo) + th * (vup - v);
-      const double d2v = dv * dv + __shfl_xor_sync(FULL, dv * dv, 1);
-      if (on) dmax = fmax(dmax, d2v);
-    } else {
-      (void)__shfl_xor_sync(FULL, 0.0, 1);
-    }
-    a_up = a; w_up = w; a_upo = ao; w_upo = wo; vup = v;
-    xn = x;
-  }
-  {
-    const double th = dd * g.thu[1];
-    const double vb = on ? u2[ci] : 0.0;
-    const double dv = part ? (kxv * a_upo + kzv * w_upo) + th * (vup - vb) : (-kxv * a_upo + -kzv * w_upo) + th * (vup - vb);
-    const double d2v = dv * dv + __shfl_xor_sync(FULL, dv * dv, 1);
-    if (on) dmax = fmax(dmax, d2v);
-  }
-  (void)a_up; (void)w_up;
-  if (on) {
-    const int nu = g.nu;
-    u1[ci] = g.gwbc1 * u1[ls + ci];
-    u3[ci] = g.gwbc3 * u3[ls + ci];
-    u1[(size_t)(nu - 1) * ls + ci] = g.gwbc1 * u1[(size_t)(nu - 2) * ls + ci];
-    u3[(size_t)(nu - 1) * ls + ci] = g.gwbc3 * u3[(size_t)(nu - 2) * ls + ci];
-    u2[ci] = 0.0;
-    u2[(size_t)(g.nv - 1) * ls + ci] = 0.0;
-  }
-  dmax = warp_max(dmax);
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
-}
-
-// ============================================================================
 // flowrate_corr (littleharsh.f90:476-509) on mode (0,0) of u1. The block stages the
 // coefficients, the level widths and u(0,0) in `w` (shared memory when it fits,
 // else global scratch); thread 0 runs the recurrence and the sums in the
@@ -938,6 +830,112 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
     a3raw = A3;
   }
   dg3[(size_t)(np - 1) * nc + c] = 0.0;
+}
+
+// ============================================================================
+// Pressure: divergence, psi = dti/(a+b) div (gauge on (0,0)), LUsolP with the
+// stored factors, p += psi, v_corr, and the divergence of the corrected field
+// (max |div|^2 -> errbits) when need_div: the reference recomputes div after
+// every v_corr but only reads it (error()) at the start of a step, so it is
+// formed in the third substep. One thread per column. p levels qp = 0..np-1 <->
+// u/v index q = qp + 1. `psi` holds the forward-sweep values, then psi.
+// ============================================================================
+__global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double2 *__restrict__ u2,
+                                                double2 *__restrict__ u3, double2 *__restrict__ p,
+                                                double2 *__restrict__ psi, const double *__restrict__ dg1,
+                                                const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
+                                                DevScalars *sc, int kRK, int need_div) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nc = g.ncol;
+  double dmax = 0.0;
+  if (c < nc) {
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dtirk = sc->dti / aRb;
+    const double dt = sc->dt;
+    const int np = g.np;
+    const double dd = g.dd;
+    double2 y = czero<double2>();
+    double2 vm = u2[c];
+    for (int qp = 0; qp < np; ++qp) {
+      const int q = qp + 1;
+      const size_t o = (size_t)q * nc + c;
+      const double2 a = u1[o], w = u3[o], v = u2[o];
+      const double th = dd * g.thu[q];
+      double2 dv;
+      dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
+      dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
+      vm = v;
+      double2 rhs;
+      rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
+      if (qp == 0 && c == 0) { rhs.x = 0.0; rhs.y = 0.0; }
+      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
+      if (qp == 0) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
+      else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
+      psi[(size_t)qp * nc + c] = y;
+    }
+    const double dtrk = dt * aRb;
+    const double dtrk2 = dtrk * dd;
+    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
+    double2 xn = y;
+    double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
+    for (int qp = np - 1; qp >= 0; --qp) {
+      const int q = qp + 1;
+      const size_t o = (size_t)q * nc + c;
+      double2 x;
+      if (qp == np - 1) x = xn;
+      else {
+        const double a3p = dg3[(size_t)qp * nc + c];
+        const double2 yy = psi[(size_t)qp * nc + c];
+        x.x = yy.x - a3p * xn.x; x.y = yy.y - a3p * xn.y;
+      }
+      psi[(size_t)qp * nc + c] = x;
+      double2 pp = p[(size_t)qp * nc + c];
+      pp.x = pp.x + x.x; pp.y = pp.y + x.y;
+      p[(size_t)qp * nc + c] = pp;
+      double2 a = u1[o], w = u3[o];
+      a.x = a.x - (-kxd * x.y); a.y = a.y - (kxd * x.x);
+      w.x = w.x - (-kzd * x.y); w.y = w.y - (kzd * x.x);
+      u1[o] = a;
+      u3[o] = w;
+      double2 v = u2[o];
+      if (q <= g.nv - 2) {
+        const double f = dtrk2 * g.thv[q];
+        v.x = v.x - f * (xn.x - x.x);
+        v.y = v.y - f * (xn.y - x.y);
+        u2[o] = v;
+      }
+      if (need_div && qp < np - 1) {
+        const double th = dd * g.thu[q + 1];
+        double2 dv;
+        dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
+        dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - v.y);
+        dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
+      }
+      a_up = a; w_up = w; vup = v;
+      xn = x;
+    }
+    if (need_div) {
+      const double th = dd * g.thu[1];
+      const double2 vb = u2[c];
+      double2 dv;
+      dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
+      dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
+      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
+    }
+    const int nu = g.nu;
+    double2 t1 = u1[(size_t)nc + c], t3 = u3[(size_t)nc + c];
+    u1[c] = cscale(t1, g.gwbc1);
+    u3[c] = cscale(t3, g.gwbc3);
+    t1 = u1[(size_t)(nu - 2) * nc + c]; t3 = u3[(size_t)(nu - 2) * nc + c];
+    u1[(size_t)(nu - 1) * nc + c] = cscale(t1, g.gwbc1);
+    u3[(size_t)(nu - 1) * nc + c] = cscale(t3, g.gwbc3);
+    u2[c] = czero<double2>();
+    u2[(size_t)(g.nv - 1) * nc + c] = czero<double2>();
+  }
+  dmax = warp_max(dmax);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
 }
 
 __global__ void k_reset_err(DevScalars *sc) {
@@ -1201,6 +1199,84 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
     Nu2o[o].x = n.x; Nu2o[o].y = n.y;
     du.x = du.x + G * n.x; du.y = du.y + G * n.y;
     duib[((size_t)s * 3 + 1) * nc + c] = du;
+  }
+}
+
+// Mixed form of k_ib_du: the same right-hand side in FP32 (FP64 neighbour
+// differences for the Laplacian, integer-pipe conversions), N stored in FP32.
+__global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                   const double2 *__restrict__ u3, float2 *__restrict__ Nu1o,
+                                                   float2 *__restrict__ Nu2o, float2 *__restrict__ Nu3o,
+                                                   const float2 *__restrict__ N1xz, const float2 *__restrict__ N2xz,
+                                                   const float2 *__restrict__ N3xz, const float2 *__restrict__ uvf,
+                                                   const float2 *__restrict__ vvc, const float2 *__restrict__ wvf,
+                                                   const double2 *__restrict__ p, double2 *__restrict__ duib,
+                                                   const int *__restrict__ iblev, int nib, Geo g,
+                                                   const DevScalars *__restrict__ sc, int kRK) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  const int nc = g.ncol;
+  if (c >= nc || s >= nib) return;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
+  const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
+  const double dR = g.dRK[kRK - 1];
+  const float dRf = (float)dR;
+  const float G = (float)(-g.gRK[kRK - 1]);
+  const float dd = (float)g.dd;
+  const int qu = iblev[2 * s], qv = iblev[2 * s + 1];
+  if (qu > 0) {
+    const int nu = g.nu;
+    const size_t o = (size_t)qu * nc + c;
+    const float a = g.d2uf[qu], cc = g.d2uf[2 * nu + qu], sdg = g.sdgu[qu] + k2f;
+    const double2 pj = p[(size_t)(qu - 1) * nc + c];
+    const float pjx = d2f_alu(pj.x), pjy = d2f_alu(pj.y);
+    const float C3x = (float)(-dR * g.k1x[kx]), C3z = (float)(-dR * g.k1z[r]);
+    const float th = g.thuf[qu];
+    for (int f = 0; f < 2; ++f) {
+      const double2 *U = f ? u3 : u1;
+      float2 *No = f ? Nu3o : Nu1o;
+      const float2 *X = f ? N3xz : N1xz;
+      const float2 *F = f ? wvf : uvf;
+      const float C3 = f ? C3z : C3x;
+      const double2 um = U[o - nc], u0 = U[o], up = U[o + nc];
+      float2 L;
+      L.x = a * d2f_alu(um.x - u0.x) + cc * d2f_alu(up.x - u0.x) + sdg * d2f_alu(u0.x);
+      L.y = a * d2f_alu(um.y - u0.y) + cc * d2f_alu(up.y - u0.y) + sdg * d2f_alu(u0.y);
+      const float2 no = No[o];
+      float2 du;
+      du.x = (C1 * L.x + C2 * no.x) + (-C3 * pjy);
+      du.y = (C1 * L.y + C2 * no.y) + (C3 * pjx);
+      if (f == 0 && c == 0) du.x += (float)(-dR * sc->mpgx);
+      const float2 x = X[o], fq = F[o], fm = F[o - nc];
+      float2 n;
+      n.x = x.x + (fq.x - fm.x) * th * dd; n.y = x.y + (fq.y - fm.y) * th * dd;
+      No[o] = n;
+      du.x += G * n.x; du.y += G * n.y;
+      duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = make_double2(f2d_alu(du.x), f2d_alu(du.y));
+    }
+  }
+  if (qv > 0) {
+    const int nv = g.nv;
+    const size_t o = (size_t)qv * nc + c;
+    const float a = g.d2vf[qv], cc = g.d2vf[2 * nv + qv], sdg = g.sdgv[qv] + k2f;
+    const double2 vm = u2[o - nc], v0 = u2[o], vp = u2[o + nc];
+    float2 L;
+    L.x = a * d2f_alu(vm.x - v0.x) + cc * d2f_alu(vp.x - v0.x) + sdg * d2f_alu(v0.x);
+    L.y = a * d2f_alu(vm.y - v0.y) + cc * d2f_alu(vp.y - v0.y) + sdg * d2f_alu(v0.y);
+    const float C3 = -dRf * dd * g.thvf[qv];
+    const double2 pp = p[(size_t)qv * nc + c], pm = p[(size_t)(qv - 1) * nc + c];
+    const float2 no = Nu2o[o];
+    float2 du;
+    du.x = (C1 * L.x + C2 * no.x) + C3 * (d2f_alu(pp.x) - d2f_alu(pm.x));
+    du.y = (C1 * L.y + C2 * no.y) + C3 * (d2f_alu(pp.y) - d2f_alu(pm.y));
+    const float th = g.thvf[qv];
+    const float2 x = N2xz[o], vp1 = vvc[o + nc], vq = vvc[o];
+    float2 n;
+    n.x = x.x + (vp1.x - vq.x) * th * dd; n.y = x.y + (vp1.y - vq.y) * th * dd;
+    Nu2o[o] = n;
+    du.x += G * n.x; du.y += G * n.y;
+    duib[((size_t)s * 3 + 1) * nc + c] = make_double2(f2d_alu(du.x), f2d_alu(du.y));
   }
 }
 
