@@ -228,6 +228,52 @@ def time_steps(g, steps, torch):
     return e0.elapsed_time(e1), g.kernel_launches() - l0
 
 
+def run_ensemble(args, ws, rank, pg, torch, np):
+    """Config 3: 64 independent channels of uneven sizes, one graph launch per RK3
+    step of all of them (lh_batch_*). Points = the sum over channels."""
+    from rnl_multiblock_nofft_gb300.native import GpuBatch, GpuChannel
+    from rnl_multiblock_nofft_gb300.workloads import ensemble_setups, initial_field, initial_scalars
+    setups = ensemble_setups(64, seed=2000 + 1000 * rank)
+    pts = sum(s.mode_points() for s in setups)
+    forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
+    res = {}
+    for form in forms:
+        chans = []
+        for c, s in enumerate(setups):
+            g = GpuChannel(s, form)
+            g.upload_state(*initial_field(s, 2000 + c))
+            g.set_scalars(**initial_scalars(s))
+            chans.append(g)
+        b = GpuBatch(chans)
+        b.step(args.warmup)
+        b.synchronize()
+        barrier(pg)
+        stream = torch.cuda.ExternalStream(b.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = sum(g.kernel_launches() for g in chans)
+        e0.record(stream)
+        b.step(args.steps)
+        e1.record(stream)
+        b.synchronize()
+        torch.cuda.synchronize()
+        ms = reduce_max(pg, e0.elapsed_time(e1))
+        res[form] = {"value": ws * pts * 3 * args.steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / args.steps,
+                     "launches": sum(g.kernel_launches() for g in chans) - l0}
+        b.close()
+        for g in chans:
+            g.close()
+    head = "mixed" if "mixed" in res else forms[0]
+    line = {"metric": METRIC, "value": res[head]["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res[head]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32 transforms, f64 state",
+            "data": "synthetic ensemble (seeded grids, Re_tau, textures and fields)",
+            "config": {"workload": "C3: 64 channels, N in {32,48,64,96}, ny in {97,129,153}, Re_tau 120-300, posts",
+                       "form": head, "mode_points_per_substep": pts, "launch": "one CUDA graph per step"},
+            "gpu_launches": res[head]["launches"], "forms": res}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -251,6 +297,10 @@ def main():
     from rnl_multiblock_nofft_gb300.native import GpuChannel
     from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars, workload_setup
 
+    if args.workload == "C3":
+        run_ensemble(args, ws, rank, pg, torch, np)
+        barrier(pg)
+        return
     s = workload_setup(args.workload)
     ic = initial_field(s, 1000 + rank)
     sc0 = initial_scalars(s)
@@ -261,6 +311,7 @@ def main():
         g = GpuChannel(s, form)
         g.upload_state(*ic)
         g.set_scalars(**sc0)
+        g.autotune()
         g.step(args.warmup)
         g.synchronize()
         barrier(pg)

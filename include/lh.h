@@ -150,6 +150,24 @@ typedef struct lh_kernel_time {
 } lh_kernel_time;
 int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, int nmax, int *nout);
 
+/* Autotuner, no counterpart in the reference: times the candidate block sizes of
+ * the one-thread-per-column kernels (solves, pressure) on this handle's channel,
+ * keeps the fastest, and restores the state. Allocates a temporary copy of the
+ * state. Call before the first lh_step (or it recaptures the step graph). */
+int lh_autotune(lh_handle *h);
+
+/* Batches (the ensemble form; no counterpart in the reference): one RK3 step of
+ * each of `n` independent channels, of any sizes, captured once into a single
+ * CUDA graph in which every channel is a branch on its own stream, and replayed
+ * by lh_batch_step with one graph launch. The handles stay owned by the caller and
+ * must outlive the batch; upload their states before lh_batch_create. */
+typedef struct lh_batch lh_batch;
+int lh_batch_create(lh_handle *const *handles, int n, lh_batch **out);
+int lh_batch_step(lh_batch *b);
+int lh_batch_synchronize(lh_batch *b);
+int lh_batch_destroy(lh_batch *b);
+void *lh_batch_stream(lh_batch *b);
+
 /* ---- four_to_phys without a handle and without allocating ----
  * No counterpart in the reference. For callers that cannot call cudaMalloc: hosts
  * that own every byte of device memory themselves (a solver that sizes HBM once at

@@ -49,6 +49,7 @@ struct lh_handle {
   cudaGraphExec_t gexec;
   bool graph_ready;
   long long launches;
+  int tb_uw, tb_v, tb_p;  // threads per block of the one-thread-per-column kernels (lh_autotune)
   std::string err;
   // per-kernel timing (lh_profile_steps): events around each launch
   bool prof;
@@ -191,6 +192,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->vsz = (h->prec == LH_PREC_FP64) ? sizeof(double2) : sizeof(float2);
   h->graph_ready = false;
   h->launches = 0;
+  h->tb_uw = h->tb_v = h->tb_p = 128;
   if (!size_supported(cfg->Ngal1) || !size_supported(cfg->Ngal2)) {
     int rc = fail(h, LH_EINVAL, "Ngal must be one of 24 48 72 96 144 192 288 384 576 768 1152");
     delete h;
@@ -622,6 +624,8 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (rc) return rc;
   if (kRK == 1) KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc));
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
+  const int nbu = (g.ncol + h->tb_uw - 1) / h->tb_uw, nbv = (g.ncol + h->tb_v - 1) / h->tb_v;
+  const int nbp = (g.ncol + h->tb_p - 1) / h->tb_p;
   if (h->ib) {
     dim3 gd(nb, h->nib);
     if (h->prec == LH_PREC_FP64) {
@@ -647,29 +651,29 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     if ((rc = phys_to_spec<T>(h, h->duphys, h->duib, 3 * h->nib, h->B, h->twx, h->twz))) return rc;
   }
   if (h->prec == LH_PREC_FP64) {
-    KL("k_helm_uw", k_helm_uw<T><<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
+    KL("k_helm_uw", k_helm_uw<T><<<nbu, h->tb_uw, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
                                                            (const V *)h->N1xz, (const V *)h->N3xz, (const V *)h->uvf,
                                                            (const V *)h->wvf, h->p, h->a3s, g, h->sc, kRK,
                                                            h->ib ? h->d_ibslot_u : nullptr, h->duib));
     if ((rc = meanflow_fork(h, kRK))) return rc;
-    KL("k_helm_v", k_helm_v<T><<<nb, NTHR_H, 0, h->st>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz,
+    KL("k_helm_v", k_helm_v<T><<<nbv, h->tb_v, 0, h->st>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz,
                                                          (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
                                                          h->ib ? h->d_ibslot_v : nullptr, h->duib));
   } else {
-    const int nb2 = (2 * g.ncol + NTHR_H - 1) / NTHR_H;
-    KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2, 2), NTHR_H, 0, h->st>>>(
+    const int nb2u = (2 * g.ncol + h->tb_uw - 1) / h->tb_uw, nb2v = (2 * g.ncol + h->tb_v - 1) / h->tb_v;
+    KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2u, 2), h->tb_uw, 0, h->st>>>(
                         (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
                         (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,
                         h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
     if ((rc = meanflow_fork(h, kRK))) return rc;
-    KL("k_helm_v", k_helm_v_mx2<<<nb2, NTHR_H, 0, h->st>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
+    KL("k_helm_v", k_helm_v_mx2<<<nb2v, h->tb_v, 0, h->st>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
                                                            (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysf,
                                                            g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
   }
   if (g.flag_ctpress == 0 && !h->prof) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
-  KL("k_press", k_press<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
+  KL("k_press", k_press<<<nbp, h->tb_p, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
                                                   h->sc, kRK, need_div));
   if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
@@ -775,6 +779,146 @@ extern "C" int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int n
   if (need > h->Bbytes) return fail(h, LH_EINVAL, "too many planes for the scratch buffer");
   return phys_to_spec<double>(h, (const double *)phys, (double2 *)spec, nplanes, h->B, fp64_tw(h, true), fp64_tw(h, false));
 }
+
+// ---------------------------------------------------------------------------
+// Autotuner: threads per block of the one-thread-per-column kernels. Each
+// candidate runs one eager step with CUDA events around every launch on a copy of
+// the state; the state and the scalars are restored afterwards.
+// ---------------------------------------------------------------------------
+extern "C" int lh_autotune(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  const Geo &g = h->g;
+  const size_t nc = g.ncol, cz = sizeof(double2);
+  const size_t bu = cz * g.nu * nc, bv = cz * g.nv * nc, bp = cz * g.np * nc, bn = h->vsz * g.nu * nc,
+               bnv = h->vsz * g.nv * nc;
+  void *save = nullptr;
+  const size_t total = 2 * bu + bv + bp + 2 * bn + bnv + sizeof(DevScalars);
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaMalloc(&save, total));
+  char *sp = (char *)save;
+  void *src[] = {h->u1, h->u3, h->u2, h->p, h->Nu1, h->Nu3, h->Nu2, h->sc};
+  const size_t sz[] = {bu, bu, bv, bp, bn, bn, bnv, sizeof(DevScalars)};
+  auto copy_all = [&](bool to_save) -> cudaError_t {
+    size_t off = 0;
+    for (int i = 0; i < 8; ++i) {
+      cudaError_t e = to_save ? cudaMemcpyAsync(sp + off, src[i], sz[i], cudaMemcpyDeviceToDevice, h->st)
+                              : cudaMemcpyAsync(src[i], sp + off, sz[i], cudaMemcpyDeviceToDevice, h->st);
+      if (e != cudaSuccess) return e;
+      off += sz[i];
+    }
+    return cudaStreamSynchronize(h->st);
+  };
+  cudaError_t e = copy_all(true);
+  if (e != cudaSuccess) { cudaFree(save); return fail(h, LH_ECUDA, cudaGetErrorString(e)); }
+  const int cand[] = {64, 128, 256};
+  double best[3] = {1e30, 1e30, 1e30};
+  int pick[3] = {h->tb_uw, h->tb_v, h->tb_p};
+  const char *names[3] = {"k_helm_uw", "k_helm_v", "k_press"};
+  lh_kernel_time kt[64];
+  int rc = LH_OK;
+  for (int ci = 0; ci < 3 && rc == LH_OK; ++ci) {
+    h->tb_uw = h->tb_v = h->tb_p = cand[ci];
+    int n = 0;
+    rc = lh_profile_steps(h, 1, kt, 64, &n);
+    for (int k = 0; k < 3 && rc == LH_OK; ++k)
+      for (int i = 0; i < n; ++i)
+        if (strncmp(kt[i].name, names[k], 32) == 0 && kt[i].total_ms < best[k]) { best[k] = kt[i].total_ms; pick[k] = cand[ci]; }
+    if (copy_all(false) != cudaSuccess) rc = fail(h, LH_ECUDA, "state restore failed");
+  }
+  cudaFree(save);
+  h->tb_uw = pick[0]; h->tb_v = pick[1]; h->tb_p = pick[2];
+  if (h->graph_ready) {  // recapture with the chosen configuration
+    cudaGraphExecDestroy(h->gexec);
+    cudaGraphDestroy(h->graph);
+    h->graph_ready = false;
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Batches: one RK3 step of many independent channels (any sizes) as one CUDA
+// graph; every channel is a branch on its own stream.
+// ---------------------------------------------------------------------------
+struct lh_batch {
+  std::vector<lh_handle *> hs;
+  cudaStream_t root;
+  cudaEvent_t ev0;
+  std::vector<cudaEvent_t> evs;
+  cudaGraph_t graph;
+  cudaGraphExec_t gexec;
+  long long nodes;
+  std::string err;
+};
+
+extern "C" int lh_batch_create(lh_handle *const *handles, int n, lh_batch **out) {
+  if (!handles || n <= 0 || !out) return LH_EINVAL;
+  *out = nullptr;
+  lh_batch *b = new lh_batch();
+  b->hs.assign(handles, handles + n);
+  for (lh_handle *h : b->hs)
+    if (!h) { delete b; return LH_EINVAL; }
+  if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev0, cudaEventDisableTiming) != cudaSuccess) { delete b; return LH_ECUDA; }
+  b->evs.resize(n);
+  for (int i = 0; i < n; ++i)
+    if (cudaEventCreateWithFlags(&b->evs[i], cudaEventDisableTiming) != cudaSuccess) { delete b; return LH_ECUDA; }
+  for (lh_handle *h : b->hs)
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) { delete b; return LH_ECUDA; }
+  if (cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { delete b; return LH_ECUDA; }
+  cudaEventRecord(b->ev0, b->root);
+  int rc = LH_OK;
+  for (int i = 0; i < n && rc == LH_OK; ++i) {
+    lh_handle *h = b->hs[i];
+    cudaStreamWaitEvent(h->st, b->ev0, 0);
+    long long before = h->launches;
+    rc = step_launches(h);
+    h->launches = before;
+    cudaEventRecord(b->evs[i], h->st);
+    cudaStreamWaitEvent(b->root, b->evs[i], 0);
+  }
+  cudaGraph_t gr;
+  cudaError_t e = cudaStreamEndCapture(b->root, &gr);
+  if (rc != LH_OK || e != cudaSuccess) { delete b; return rc != LH_OK ? rc : LH_ECUDA; }
+  e = cudaGraphInstantiate(&b->gexec, gr, 0);
+  if (e != cudaSuccess) { cudaGraphDestroy(gr); delete b; return LH_ECUDA; }
+  b->graph = gr;
+  size_t nn = 0;
+  cudaGraphGetNodes(gr, nullptr, &nn);
+  b->nodes = (long long)nn;
+  *out = b;
+  return LH_OK;
+}
+
+extern "C" int lh_batch_step(lh_batch *b) {
+  if (!b) return LH_EINVAL;
+  if (cudaGraphLaunch(b->gexec, b->root) != cudaSuccess) return LH_ECUDA;
+  for (lh_handle *h : b->hs) h->launches += b->nodes / (long long)b->hs.size();
+  return LH_OK;
+}
+
+extern "C" int lh_batch_synchronize(lh_batch *b) {
+  if (!b) return LH_EINVAL;
+  if (cudaStreamSynchronize(b->root) != cudaSuccess) return LH_ECUDA;
+  int worst = LH_OK;
+  for (lh_handle *h : b->hs) {
+    int rc = lh_synchronize(h);
+    if (rc != LH_OK) worst = rc;
+  }
+  return worst;
+}
+
+extern "C" int lh_batch_destroy(lh_batch *b) {
+  if (!b) return LH_EINVAL;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (cudaEvent_t e : b->evs) if (e) cudaEventDestroy(e);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->root) cudaStreamDestroy(b->root);
+  delete b;
+  return LH_OK;
+}
+
+extern "C" void *lh_batch_stream(lh_batch *b) { return b ? (void *)b->root : nullptr; }
 
 // ===========================================================================
 // lh_four_to_phys_noalloc: the four_to_phys transform without a handle and

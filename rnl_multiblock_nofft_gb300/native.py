@@ -19,7 +19,8 @@ _lib = None
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
-           "lh_profile_steps", "lh_four_to_phys_noalloc")
+           "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
+           "lh_batch_synchronize", "lh_batch_destroy", "lh_batch_stream")
 
 
 class LhKernelTime(C.Structure):
@@ -61,6 +62,13 @@ def load(path: str = _LIB_PATH):
     L.lh_kernel_launches.restype = C.c_int64
     L.lh_profile_steps.argtypes = [vp, i, C.POINTER(LhKernelTime), i, C.POINTER(i)]
     L.lh_four_to_phys_noalloc.argtypes = [i, i, i, i, vp, vp, i, vp, C.POINTER(C.c_char_p)]
+    L.lh_autotune.argtypes = [vp]
+    L.lh_batch_create.argtypes = [C.POINTER(vp), i, C.POINTER(vp)]
+    L.lh_batch_step.argtypes = [vp]
+    L.lh_batch_synchronize.argtypes = [vp]
+    L.lh_batch_destroy.argtypes = [vp]
+    L.lh_batch_stream.argtypes = [vp]
+    L.lh_batch_stream.restype = vp
     _lib = L
     return L
 
@@ -148,6 +156,10 @@ class GpuChannel:
     def kernel_launches(self) -> int:
         return int(self.L.lh_kernel_launches(self.h))
 
+    def autotune(self):
+        """Pick the block sizes of the column kernels for this channel (state restored)."""
+        self._check(self.L.lh_autotune(self.h))
+
     def profile_steps(self, nsteps: int) -> dict:
         """{kernel name: (launches, total ms)} over `nsteps` eager steps."""
         buf = (LhKernelTime * 64)()
@@ -169,3 +181,44 @@ class GpuChannel:
 
     def phys_to_four(self, phys_ptr: int, spec_ptr: int, nplanes: int):
         self._check(self.L.lh_phys_to_four(self.h, C.c_void_p(phys_ptr), C.c_void_p(spec_ptr), nplanes))
+
+
+class GpuBatch:
+    """Many independent channels (any sizes) advanced together: one RK3 step of
+    every channel is one CUDA-graph launch (lh_batch_*). The GpuChannel objects
+    stay owned by the caller and must outlive the batch."""
+
+    def __init__(self, channels):
+        self.channels = list(channels)
+        self.L = load()
+        arr = (C.c_void_p * len(self.channels))(*[c.h.value for c in self.channels])
+        b = C.c_void_p()
+        rc = self.L.lh_batch_create(arr, len(self.channels), C.byref(b))
+        if rc != LH_OK:
+            raise LhError(rc, "lh_batch_create failed")
+        self.b = b
+
+    def step(self, n: int = 1):
+        for _ in range(n):
+            rc = self.L.lh_batch_step(self.b)
+            if rc != LH_OK:
+                raise LhError(rc, "lh_batch_step failed")
+
+    def synchronize(self):
+        rc = self.L.lh_batch_synchronize(self.b)
+        if rc != LH_OK:
+            raise LhError(rc, "lh_batch_synchronize failed")
+
+    def stream(self) -> int:
+        return int(self.L.lh_batch_stream(self.b) or 0)
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.lh_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

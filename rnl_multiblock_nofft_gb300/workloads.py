@@ -142,3 +142,29 @@ def initial_field(s: ChannelSetup, seed: int, amp: float = 0.1, kmax: int = 8):
 
 def initial_scalars(s: ChannelSetup) -> dict:
     return dict(t=0.0, dt=0.0, dti=0.0, dtc=0.0, mpgx=s.p.mpgx, iter=0, QxT=0.0)
+
+
+def ensemble_params(n: int = 64, seed: int = 2000):
+    """The batched ensemble: n independent channels with uneven grids drawn from a
+    seed: N in {32, 48, 64, 96} (Nx = Nz), ny in {97, 129, 153}, Re_tau in [120, 300],
+    square posts with a period of 8-24 physical points (a divisor of Ngal) and a solid
+    fraction of 0.1-0.5, 6 wall units high. Channel c uses seed + c for its field."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(n):
+        N = int(rng.choice([32, 48, 64, 96]))
+        ny = int(rng.choice([97, 129, 153]))
+        re_tau = float(rng.uniform(120.0, 300.0))
+        G = 3 * N // 2
+        periods = [d for d in range(8, 25) if G % d == 0]
+        period = int(rng.choice(periods))
+        frac = float(rng.uniform(0.1, 0.5))
+        npk = max(1, min(period - 1, int(round(period * math.sqrt(frac)))))
+        p = re_tau_params(N, ny, re_tau=re_tau, posts=True, post_period=period, post_points=npk,
+                          post_height_plus=6.0, flpress=0)
+        out.append(p)
+    return out
+
+
+def ensemble_setups(n: int = 64, seed: int = 2000):
+    return [build_setup(p) for p in ensemble_params(n, seed)]
