@@ -35,9 +35,9 @@ def test_batch_of_uneven_channels(cuda_ok):
         for o, _ in pairs:
             o.step()
     b.synchronize()
-    for o, g in pairs:
+    for o, g in pairs:   # bar: 1e-12 relative per step
         for x, y in zip(o.get_state(), g.download_state()):
-            assert rel(y, x) < 1e-12
+            assert rel(y, x) < 2 * 1e-12
         assert g.scalars()["iter"] == 2
     b.close()
 
@@ -56,4 +56,4 @@ def test_autotune_keeps_state_and_parity(cuda_ok):
     g.step(2)
     g.synchronize()
     for x, y in zip(o.get_state(), g.download_state()):
-        assert rel(y, x) < 1e-12
+        assert rel(y, x) < 2 * 1e-12
