@@ -30,7 +30,9 @@ def stale() -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and not stale():
         return LIB
-    cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+    # LH_NVCC_DEFINES: optional "-DNAME=VALUE ..." (tile budgets for tuning sweeps)
+    extra = os.environ.get("LH_NVCC_DEFINES", "").split()
+    cmd = [nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", *extra,
            "-o", LIB + ".tmp", os.path.join(CSRC, "lh_capi.cu"), "-lcudart"]
     if verbose:
         print(" ".join(cmd))

@@ -39,17 +39,27 @@ __device__ __forceinline__ T warp_max(T v) {
   return v;
 }
 
-// Lines per block of the transform kernels, from a shared-memory budget of two
-// blocks per SM (same values on the host and the device).
-#define LH_SMEM_BUDGET 98304
+// Lines per block of the transform kernels, from a shared-memory budget per
+// kernel (same values on the host and the device). The budgets set how many
+// blocks share an SM; the defaults are the fastest of a sweep on GB300 at C1.
+#ifndef LH_BUDGET_ZINV
+#define LH_BUDGET_ZINV 49152
+#endif
+#ifndef LH_BUDGET_XPASS
+#define LH_BUDGET_XPASS 49152
+#endif
+#ifndef LH_BUDGET_ZFWD
+#define LH_BUDGET_ZFWD 49152
+#endif
+__host__ __device__ constexpr int lh_clamp(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 template <typename V> __host__ __device__ constexpr int kb_zinv(int n) {
-  return (LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))) > 16 ? 16 : (LH_SMEM_BUDGET / (2 * n * (int)sizeof(V))));
+  return lh_clamp(LH_BUDGET_ZINV / (2 * n * (int)sizeof(V)), 1, 16);
 }
 template <typename V> __host__ __device__ constexpr int pb_xpass(int n) {
-  return (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) > 8 ? 8 : (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))));
+  return lh_clamp(LH_BUDGET_XPASS / (8 * n * (int)sizeof(V)), 1, 8);
 }
 template <typename V> __host__ __device__ constexpr int kb_zfwd(int n) {
-  return (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) < 1 ? 1 : ((LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))) > 8 ? 8 : (LH_SMEM_BUDGET / (8 * n * (int)sizeof(V))));
+  return lh_clamp(LH_BUDGET_ZFWD / (8 * n * (int)sizeof(V)), 1, 8);
 }
 
 // ============================================================================
