@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define LH_ABI_VERSION 1
+#define LH_ABI_VERSION 2
 
 enum {
   LH_OK = 0,
@@ -45,6 +45,11 @@ enum {
 enum {
   LH_PREC_FP64 = 0,    /* plain form: every kernel in FP64 */
   LH_PREC_MIXED = 1    /* precision form: FP32 transforms/products, FP64 state, solves and (0,0) mode */
+};
+
+enum {
+  LH_NONLIN_PRODUCTS = 0,  /* FFT products (ops_in_planes2) */
+  LH_NONLIN_TRIADS = 1     /* triad-list convolution (ops_in_planes) */
 };
 
 /* Everything the substep reads from `module declaration`, for one channel whose
@@ -74,6 +79,20 @@ typedef struct lh_config {
   const int32_t *list_ib_u;       /* [nib_u][6] : i, k, j, i1, k1, j1 (i,k 1-based physical) */
   const int32_t *list_ib_v;       /* [nib_v][6] */
   const double *A_ib_u, *A_ib_v;  /* [nib_u], [nib_v] */
+  /* Nonlinear-term form. LH_NONLIN_PRODUCTS: pseudo-spectral products with 3/2
+   * dealiasing (ops_in_planes2, FOU3D.f90:2090-2251). LH_NONLIN_TRIADS: the
+   * as-run triad-list convolution (ops_in_planes + nonlinInter, FOU3D.f90:1724-2088)
+   * over the interaction lists that nonlinRead loads (start.f90:2983-3069). */
+  int32_t nonlin_form;            /* LH_NONLIN_* */
+  int32_t triad_nx, triad_nz;     /* list header: largest |kx| and |kz| index (N1/2-1, N2/2-1) */
+  int32_t triad_nsets;            /* number of lists files (one per distinct plane) */
+  const int64_t *triad_off;       /* [nsets][9] triad offset of list `type` 1..9 in triad_data */
+  const int64_t *triad_len;       /* [nsets][9] number of triads L of that list */
+  const int8_t *triad_data;       /* list of L triads at offset o: bytes 4*o .. 4*o+4L-1, stored as
+                                     the lists file stores it (column-major list(L,4)): la[L],
+                                     ka[L], lp[L], kp[L]. Lists may share storage. */
+  const int32_t *triad_set_u;     /* [nyu] set (0-based) of each u level, -1 on the ghost levels */
+  const int32_t *triad_set_v;     /* [nyv] set of each v level, -1 on the wall levels */
 } lh_config;
 
 /* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter).

@@ -15,8 +15,10 @@
  *   littleharsh.f90:635-788  RHS0_u1 / RHS0_u2 / RHS0_u3
  *   littleharsh.f90:791-907  solveU_W / solveV
  *   littleharsh.f90:956-1052 v_corr
- *   FOU3D.f90:41-425         nonlinear (plain pseudo-spectral products, ops_in_planes2
- *                            FOU3D.f90:2090-2251, in place of the triad-list ops_in_planes)
+ *   FOU3D.f90:41-425         nonlinear, with either form of the products:
+ *   FOU3D.f90:2090-2251        ops_in_planes2 (pseudo-spectral products, 3/2 dealiasing)
+ *   FOU3D.f90:1724-2088        ops_in_planes + nonlinInter (the as-run triad-list
+ *                              convolution; lists as nonlinRead loads them, start.f90:2983-3069)
  *   FOU3D.f90:427-474        interp_u / interp_v
  *   FOU3D.f90:476-593        der_x / der_z
  *   FOU3D.f90:636-676        der_yu_h / der_yv_h
@@ -143,6 +145,10 @@ struct orc {
   cplx *uvf, *wvf, *vvc, *N1xz, *N2xz, *N3xz;
   double *DG; /* [np][ncol][3] factorised pressure matrices */
   double *phys_u1, *phys_u3, *phys_u2; /* physical planes, all levels (for IB) */
+  /* owned copies of the triad lists */
+  int8_t *tdata;
+  int64_t *toff, *tlen;
+  int32_t *tsu, *tsv;
   double t, dt, dti, dtc, err, mpgx, QxT, Qx;
   int64_t iter;
 };
@@ -208,6 +214,46 @@ static void build_DG(orc *O) {
   free(Db); free(Gb); free(Dt); free(Gt);
 }
 
+void orc_destroy(orc *O);
+
+/* Copies and checks the triad lists: header as nonlinRead checks it (start.f90:3040-3048),
+ * every triad inside the retained modes with a target x-mode la + lp >= 0. */
+static int copy_triads(orc *O, const lh_config *cfg) {
+  if (cfg->triad_nx != O->N1 / 2 - 1 || cfg->triad_nz != O->N2 / 2 - 1) return -1;
+  const int ns = cfg->triad_nsets, nx = cfg->triad_nx, nz = cfg->triad_nz;
+  if (ns <= 0 || !cfg->triad_off || !cfg->triad_len || !cfg->triad_data) return -1;
+  int64_t end = 0;
+  for (int i = 0; i < 9 * ns; ++i) {
+    if (cfg->triad_off[i] < 0 || cfg->triad_len[i] < 0) return -1;
+    int64_t e = cfg->triad_off[i] + cfg->triad_len[i];
+    if (e > end) end = e;
+  }
+  O->tdata = (int8_t *)malloc(4 * (size_t)end + 4);
+  O->toff = (int64_t *)malloc(sizeof(int64_t) * 9 * ns);
+  O->tlen = (int64_t *)malloc(sizeof(int64_t) * 9 * ns);
+  O->tsu = (int32_t *)malloc(sizeof(int32_t) * O->nu);
+  O->tsv = (int32_t *)malloc(sizeof(int32_t) * O->nv);
+  memcpy(O->tdata, cfg->triad_data, 4 * (size_t)end);
+  memcpy(O->toff, cfg->triad_off, sizeof(int64_t) * 9 * ns);
+  memcpy(O->tlen, cfg->triad_len, sizeof(int64_t) * 9 * ns);
+  memcpy(O->tsu, cfg->triad_set_u, sizeof(int32_t) * O->nu);
+  memcpy(O->tsv, cfg->triad_set_v, sizeof(int32_t) * O->nv);
+  for (int i = 0; i < 9 * ns; ++i) {
+    const int8_t *l = O->tdata + 4 * O->toff[i];
+    const int64_t L = O->tlen[i];
+    for (int64_t e = 0; e < L; ++e) {
+      int la = l[e], ka = l[L + e], lp = l[2 * L + e], kp = l[3 * L + e];
+      if (abs(la) > nx || abs(lp) > nx || abs(ka) > nz || abs(kp) > nz) return -1;
+      if (la + lp < 0 || la + lp > nx || abs(ka + kp) > nz) return -1;
+    }
+  }
+  for (int q = 1; q < O->nu - 1; ++q) if (O->tsu[q] < 0 || O->tsu[q] >= ns) return -1;
+  for (int q = 1; q < O->nv - 1; ++q) if (O->tsv[q] < 0 || O->tsv[q] >= ns) return -1;
+  O->c.triad_data = O->tdata; O->c.triad_off = O->toff; O->c.triad_len = O->tlen;
+  O->c.triad_set_u = O->tsu; O->c.triad_set_v = O->tsv;
+  return 0;
+}
+
 orc *orc_create(const lh_config *cfg) {
   orc *O = (orc *)calloc(1, sizeof(orc));
   if (!O) return NULL;
@@ -245,6 +291,7 @@ orc *orc_create(const lh_config *cfg) {
   O->phys_u1 = (double *)calloc(pp * O->nu, sizeof(double));
   O->phys_u3 = (double *)calloc(pp * O->nu, sizeof(double));
   O->phys_u2 = (double *)calloc(pp * O->nv, sizeof(double));
+  if (cfg->nonlin_form == LH_NONLIN_TRIADS && copy_triads(O, cfg)) { orc_destroy(O); return NULL; }
   build_DG(O);
   O->dt = 0; O->t = 0; O->mpgx = cfg->Re * 0; O->iter = 0;
   return O;
@@ -255,7 +302,8 @@ void orc_destroy(orc *O) {
   void *ptrs[] = {O->yu, O->yv, O->thu, O->thv, O->d2u, O->d2v, O->k1x, O->k2x, O->k1z, O->k2z,
                   O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
                   O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
-                  O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2};
+                  O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2,
+                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   plan_free(&O->px); plan_free(&O->pz);
   free(O);
@@ -349,6 +397,138 @@ static void derxz(const orc *O, const cplx *X, const cplx *Z, cplx *out) {
 }
 
 /* ------------------------------------------------------------------------- */
+/* triad-list products (ops_in_planes + nonlinInter, FOU3D.f90:1724-2088)      */
+/* ------------------------------------------------------------------------- */
+/* plane row of z-mode k in -N2/2..N2/2: kLkup (start.f90:1155-1163) on the compact
+ * [kz row][kx] plane, where row N2/2 holds kz = -N2/2 (= +N2/2) */
+static inline int krow(const orc *O, int k) { return k >= 0 ? k : k + O->N2; }
+
+/* nonlinInter (FOU3D.f90:1983-2012): X(la+lp, +-(ka+kp)) += A(la, +-ka) P(lp, +-kp) for every
+ * listed triad, mirrored pass p = 0 first; x-mode l < 0 reads conj of mode (|l|, -k).
+ * Evaluation order as the Fortran expression. */
+static void nonlin_inter(const orc *O, int set, int type, cplx *X, const cplx *A, const cplx *P) {
+  const int N1h = O->N1h;
+  const int64_t L = O->tlen[set * 9 + type - 1];
+  const int8_t *l = O->tdata + 4 * O->toff[set * 9 + type - 1];
+  double *x = (double *)X;
+  const double *a = (const double *)A, *pp = (const double *)P;
+  for (int64_t e = 0; e < L; ++e) {
+    const int la = l[e], ka0 = l[L + e], lp = l[2 * L + e], kp0 = l[3 * L + e];
+    const int sa = la < 0 ? -1 : 1, sp = lp < 0 ? -1 : 1;
+    const int ia = abs(la), ip = abs(lp), it = la + lp;
+    for (int p = 0; p <= 1; ++p) {
+      if (ka0 + kp0 == 0 && p == 1) continue;
+      const int pn = p * 2 - 1;
+      const int ka = krow(O, pn * sa * ka0), kp = krow(O, pn * sp * kp0), kt = krow(O, pn * (ka0 + kp0));
+      const double ar = a[2 * (ka * N1h + ia)], ai = a[2 * (ka * N1h + ia) + 1];
+      const double pr = pp[2 * (kp * N1h + ip)], pi = pp[2 * (kp * N1h + ip) + 1];
+      double *xt = x + 2 * (kt * N1h + it);
+      xt[0] = (xt[0] + ar * pr) - ((double)(sa * sp) * ai) * pi;
+      xt[1] = (xt[1] + ((double)sp * ar) * pi) + ((double)sa * ai) * pr;
+    }
+  }
+}
+
+/* zeroth mode of a product, sum over i = -N1/2..N1/2, k = klo..N2/2-1 of
+ * A(i, k) P(-i, -k) (FOU3D.f90:1755-1772, 1902-1920) */
+static void zeroth_mode(const orc *O, int klo, cplx *X, const cplx *A, const cplx *P) {
+  const int N1h = O->N1h;
+  const double *a = (const double *)A, *pp = (const double *)P;
+  double xr = creal(X[0]), xi = cimag(X[0]);
+  for (int i = -(O->N1 / 2); i <= O->N1 / 2; ++i)
+    for (int k = klo; k <= O->N2 / 2 - 1; ++k) {
+      const int sa = i < 0 ? -1 : 1, sp = -i < 0 ? -1 : 1;
+      const int ia = abs(i), ip = abs(i);
+      const int ka = krow(O, sa * k), kp = krow(O, sp * (-k));
+      const double ar = a[2 * (ka * N1h + ia)], ai = a[2 * (ka * N1h + ia) + 1];
+      const double pr = pp[2 * (kp * N1h + ip)], pi = pp[2 * (kp * N1h + ip) + 1];
+      xr = (xr + ar * pr) - ((double)(sa * sp) * ai) * pi;
+      xi = (xi + (ar * pi) * (double)sp) + ((double)sa * ai) * pr;
+    }
+  X[0] = CMPLX(xr, xi);
+}
+
+/* ops_in_planes: products of every u plane (uu, uw, vv, wu, ww) and v plane (uv, vu, vw,
+ * wv) by linear advection + zeroth mode + listed triads, then der_x / der_z; the physical
+ * planes feed dtc_calc and the immersed boundaries as in the transform form. */
+static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
+  const int nc = O->ncol, N2 = O->N2;
+  const size_t pp = (size_t)O->G1 * O->G2;
+  const int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3], vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
+  double u1m = *pu1m, u3m = *pu3m, u2m = *pu2m;
+#pragma omp parallel reduction(max : u1m, u3m, u2m)
+  {
+    pwork w; pwork_init(O, &w);
+    double *f = (double *)malloc(sizeof(double) * pp);
+    cplx *t1 = zalloc(nc), *t2 = zalloc(nc), *t3 = zalloc(nc), *t4 = zalloc(nc);
+#pragma omp for schedule(dynamic)
+    for (int j = ulo; j <= uhi; ++j) {
+      const int q = UIDX(j), set = O->tsu[q];
+      const cplx *U = PL(O->u1, q), *V = PL(O->u2i, q), *W = PL(O->u3, q);
+      cplx *uu = t1, *uw = t2, *wu = t3, *ww = t4, *vv = PL(O->vvc, q);
+      vv[0] = 0;
+      zeroth_mode(O, -(N2 / 2), vv, V, V);
+      const double u00 = creal(U[0]), v00 = creal(V[0]), w00 = creal(W[0]);
+      for (int c = 0; c < nc; ++c) {
+        const double ur = creal(U[c]), ui = cimag(U[c]), vr = creal(V[c]), vi = cimag(V[c]);
+        const double wr = creal(W[c]), wi = cimag(W[c]);
+        uu[c] = CMPLX(2 * (u00 * ur), 2 * (u00 * ui));
+        ww[c] = CMPLX(2 * (w00 * wr), 2 * (w00 * wi));
+        if (c != 0) vv[c] = CMPLX(2 * (v00 * vr), 2 * (v00 * vi));
+        uw[c] = CMPLX(u00 * wr + w00 * ur, u00 * wi + w00 * ui);
+        wu[c] = uw[c];
+      }
+      nonlin_inter(O, set, 1, uu, U, U);
+      nonlin_inter(O, set, 3, uw, W, U);
+      nonlin_inter(O, set, 5, vv, V, V);
+      nonlin_inter(O, set, 7, wu, U, W);
+      nonlin_inter(O, set, 9, ww, W, W);
+      derxz(O, uu, uw, PL(O->N1xz, q));
+      derxz(O, wu, ww, PL(O->N3xz, q));
+      four_to_phys_plane(O, U, f, &w);
+      for (size_t e = 0; e < pp; ++e) if (fabs(f[e]) > u1m) u1m = fabs(f[e]);
+      memcpy(O->phys_u1 + pp * q, f, sizeof(double) * pp);
+      four_to_phys_plane(O, W, f, &w);
+      for (size_t e = 0; e < pp; ++e) if (fabs(f[e]) > u3m) u3m = fabs(f[e]);
+      memcpy(O->phys_u3 + pp * q, f, sizeof(double) * pp);
+    }
+#pragma omp for schedule(dynamic)
+    for (int j = vlo; j <= vhi; ++j) {
+      const int q = UIDX(j), set = O->tsv[q];
+      const cplx *Ui = PL(O->u1i, q), *V = PL(O->u2, q), *Wi = PL(O->u3i, q);
+      cplx *uv = PL(O->uvf, q), *wv = PL(O->wvf, q), *vu = t1, *vw = t2;
+      uv[0] = 0;
+      wv[0] = 0;
+      zeroth_mode(O, -(N2 / 2 - 1), uv, Ui, V);
+      zeroth_mode(O, -(N2 / 2 - 1), wv, Wi, V);
+      const double u00 = creal(Ui[0]), v00 = creal(V[0]), w00 = creal(Wi[0]);
+      for (int c = 0; c < nc; ++c) {
+        const double ur = creal(Ui[c]), ui = cimag(Ui[c]), vr = creal(V[c]), vi = cimag(V[c]);
+        const double wr = creal(Wi[c]), wi = cimag(Wi[c]);
+        vu[c] = CMPLX(u00 * vr + v00 * ur, u00 * vi + v00 * ui);
+        vw[c] = CMPLX(v00 * wr + w00 * vr, v00 * wi + w00 * vi);
+        if (c != 0) { uv[c] = vu[c]; wv[c] = vw[c]; }
+      }
+      nonlin_inter(O, set, 2, uv, V, Ui);
+      nonlin_inter(O, set, 4, vu, Ui, V);
+      nonlin_inter(O, set, 6, vw, Wi, V);
+      nonlin_inter(O, set, 8, wv, V, Wi);
+      derxz(O, vu, vw, PL(O->N2xz, q));
+      four_to_phys_plane(O, V, f, &w);
+      const double th = O->thv[q];
+      for (size_t e = 0; e < pp; ++e) {
+        double a = fabs(f[e]) * th;
+        if (a > u2m) u2m = a;
+      }
+      memcpy(O->phys_u2 + pp * q, f, sizeof(double) * pp);
+    }
+    free(f); free(t1); free(t2); free(t3); free(t4);
+    pwork_free(&w);
+  }
+  *pu1m = u1m; *pu3m = u3m; *pu2m = u2m;
+}
+
+/* ------------------------------------------------------------------------- */
 /* nonlinear (FOU3D.f90:41-425 with ops_in_planes2)                          */
 /* ------------------------------------------------------------------------- */
 static void nonlinear(orc *O, int kRK) {
@@ -385,6 +565,8 @@ static void nonlinear(orc *O, int kRK) {
   int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3];
   int vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
 
+  if (O->c.nonlin_form == LH_NONLIN_TRIADS) triad_products(O, &u1m, &u3m, &u2m);
+  else
 #pragma omp parallel reduction(max : u1m, u3m, u2m)
   {
     pwork w; pwork_init(O, &w);

@@ -57,12 +57,13 @@ class Oracle:
     """One channel on the CPU oracle. State arrays use the host cfield layout
     (complex128 [ncols, nlevels])."""
 
-    def __init__(self, setup: ChannelSetup, threads: int = 0):
+    def __init__(self, setup: ChannelSetup, threads: int = 0, triads=None):
+        """`triads` (a TriadLists) selects the triad-list nonlinear term."""
         self.s = setup
         L = lib()
         if threads:
             L.orc_set_threads(threads)
-        cfg, self._keep = make_config(setup)
+        cfg, self._keep = make_config(setup, triads=triads)
         self._cfg = cfg
         self.h = L.orc_create(C.byref(cfg))
         if not self.h:

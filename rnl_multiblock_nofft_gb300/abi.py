@@ -8,12 +8,15 @@ import numpy as np
 
 from .setup_grid import UGRID, VGRID, ChannelSetup
 
-LH_ABI_VERSION = 1
+LH_ABI_VERSION = 2
 LH_OK, LH_EINVAL, LH_ENONFINITE, LH_ETIMEOUT, LH_ECUDA, LH_ENOMEM = 0, -1, -2, -3, -4, -5
 LH_PREC_FP64, LH_PREC_MIXED = 0, 1
+LH_NONLIN_PRODUCTS, LH_NONLIN_TRIADS = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
+_lp = C.POINTER(C.c_int64)
+_bp = C.POINTER(C.c_int8)
 
 
 class LhConfig(C.Structure):
@@ -34,6 +37,9 @@ class LhConfig(C.Structure):
         ("flag_ctpress", C.c_int32), ("ib_enable", C.c_int32),
         ("nib_u", C.c_int32), ("nib_v", C.c_int32),
         ("list_ib_u", _ip), ("list_ib_v", _ip), ("A_ib_u", _dp), ("A_ib_v", _dp),
+        ("nonlin_form", C.c_int32), ("triad_nx", C.c_int32), ("triad_nz", C.c_int32),
+        ("triad_nsets", C.c_int32), ("triad_off", _lp), ("triad_len", _lp), ("triad_data", _bp),
+        ("triad_set_u", _ip), ("triad_set_v", _ip),
     ]
 
 
@@ -50,8 +56,9 @@ def _ptr(a: np.ndarray, typ):
     return a.ctypes.data_as(typ)
 
 
-def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64):
-    """Returns (LhConfig, keepalive) for a single-resolution channel."""
+def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
+    """Returns (LhConfig, keepalive) for a single-resolution channel. `triads` (a
+    triads.TriadLists) selects the triad-list nonlinear form; None the FFT products."""
     if s.multiblock:
         raise ValueError("bands with different x/z resolution are not supported by this build")
     keep = []
@@ -100,6 +107,19 @@ def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64):
     c.list_ib_v = i32(lv.reshape(-1) if len(lv) else np.zeros(6, np.int32))
     c.A_ib_u = d(s.A_ib[UGRID] if len(lu) else np.zeros(1))
     c.A_ib_v = d(s.A_ib[VGRID] if len(lv) else np.zeros(1))
+    c.nonlin_form = LH_NONLIN_PRODUCTS
+    if triads is not None:
+        pk = triads.pack(s)
+        c.nonlin_form = LH_NONLIN_TRIADS
+        c.triad_nx, c.triad_nz = pk["nx"], pk["nz"]
+        c.triad_nsets = len(pk["off"])
+        for name, typ in (("off", _lp), ("len", _lp), ("data", _bp)):
+            keep.append(pk[name])
+        c.triad_off = _ptr(pk["off"], _lp)
+        c.triad_len = _ptr(pk["len"], _lp)
+        c.triad_data = _ptr(pk["data"], _bp)
+        c.triad_set_u = i32(pk["set_u"])
+        c.triad_set_v = i32(pk["set_v"])
     return c, keep
 
 
