@@ -18,7 +18,8 @@
  *    order of proc_lims_columns with one process (start.f90:1610-1631):
  *    column = ikz * (N1/2+1) + ikx, ikz = 0..N2-1 in k1F_z order.
  *  - All entry points return LH_OK or a negative error code; lh_last_error()
- *    returns a message for the last failure on that handle.
+ *    returns a message for the last failure on that handle, lh_last_error(NULL)
+ *    the last failure on the calling thread (e.g. of lh_create).
  *  - One handle per host thread. No internal threads.
  */
 #ifndef LH_H

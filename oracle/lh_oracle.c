@@ -740,7 +740,6 @@ static double flowrateIm(const orc *O) {
 }
 
 static void divergence(orc *O) {
-  const int nc = O->ncol;
   const double dd = O->c.ddthetavi;
   for (int j = O->c.N4[0] + 1; j <= O->c.N4[3]; ++j) {
     double th = dd * O->thu[UIDX(j)];

@@ -10,6 +10,7 @@
 #include "lh_internal.cuh"
 
 #include "lh_kernels.cuh"
+#include "lh_triads.cuh"
 
 namespace {
 const int NTHR_H = 256;
@@ -45,6 +46,14 @@ struct lh_handle {
   int *d_lu, *d_lv, *d_capslot, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
   double *d_Au, *d_Av, *cap, *duphys;
   double2 *duib;
+  // triad-list nonlinear form
+  int triad;
+  TriadGeo tg;
+  uint32_t *d_terms;
+  int *d_wb, *d_lid;
+  int tri_threads;
+  size_t tri_smem;
+  long long tri_nterms;
   cudaGraph_t graph;
   cudaGraphExec_t gexec;
   bool graph_ready;
@@ -57,8 +66,12 @@ struct lh_handle {
   const char *cur_name;
 };
 
+// message of the last failure on this host thread (lh_last_error(NULL))
+static thread_local std::string t_last_err;
+
 static int fail(lh_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
+  t_last_err = msg;
   return code;
 }
 
@@ -175,16 +188,19 @@ static int set_smem_attrs_all(lh_handle *h) {
 
 extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   lh_handle *h = nullptr;
-  if (!cfg || !out) return LH_EINVAL;
+  if (!cfg || !out) return fail(nullptr, LH_EINVAL, "null argument");
   *out = nullptr;
-  if (cfg->abi_version != LH_ABI_VERSION) return LH_EINVAL;
-  if (cfg->precision != LH_PREC_FP64 && cfg->precision != LH_PREC_MIXED) return LH_EINVAL;
+  if (cfg->abi_version != LH_ABI_VERSION) return fail(nullptr, LH_EINVAL, "abi_version mismatch");
+  if (cfg->precision != LH_PREC_FP64 && cfg->precision != LH_PREC_MIXED)
+    return fail(nullptr, LH_EINVAL, "unknown precision");
+  if (cfg->nonlin_form != LH_NONLIN_PRODUCTS && cfg->nonlin_form != LH_NONLIN_TRIADS)
+    return fail(nullptr, LH_EINVAL, "unknown nonlinear form");
   if (cfg->N1 <= 0 || cfg->N2 <= 0 || (cfg->N1 & 1) || (cfg->N2 & 1) || cfg->Ngal1 <= cfg->N1 ||
       cfg->Ngal2 <= cfg->N2 || (cfg->Ngal1 & 1) || (cfg->Ngal2 & 1) || cfg->dny < 0)
-    return LH_EINVAL;
+    return fail(nullptr, LH_EINVAL, "bad N / Ngal / dny");
   if (cfg->nyu != cfg->N4[3] + 1 - cfg->N4[0] + 1 || cfg->nyv != cfg->N3[3] + 1 - cfg->N3[0] + 1 ||
       cfg->nyv != cfg->nyu - 1 || cfg->N4[0] != -cfg->dny || cfg->N3[0] != -cfg->dny || cfg->nyu < 5)
-    return LH_EINVAL;
+    return fail(nullptr, LH_EINVAL, "band limits inconsistent with nyu / nyv / dny");
   h = new lh_handle();
   memset(&h->g, 0, sizeof(Geo));
   h->cfg = *cfg;
@@ -372,6 +388,34 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
+  h->triad = (cfg->nonlin_form == LH_NONLIN_TRIADS) ? 1 : 0;
+  h->d_terms = nullptr; h->d_wb = h->d_lid = nullptr; h->tri_nterms = 0;
+  if (h->triad) {  // expand and upload the triad lists (nonlinRead, start.f90:2983-3069)
+    TriadHost th;
+    std::string e = build_triads(cfg, g, th);
+    if (!e.empty()) { rc = fail(h, LH_EINVAL, e); lh_destroy(h); return rc; }
+    h->d_terms = (uint32_t *)upload_vec(th.terms, ce);
+    if (ce == cudaSuccess) h->d_wb = (int *)upload_vec(th.wb, ce);
+    if (ce == cudaSuccess) h->d_lid = (int *)upload_vec(th.lid, ce);
+    if (ce != cudaSuccess) {
+      rc = fail(h, ce == cudaErrorMemoryAllocation ? LH_ENOMEM : LH_ECUDA, std::string("triad lists: ") + cudaGetErrorString(ce));
+      lh_destroy(h);
+      return rc;
+    }
+    h->tg.terms = h->d_terms; h->tg.wb = h->d_wb; h->tg.lid = h->d_lid;
+    h->tg.Tw = th.Tw; h->tg.T = th.T; h->tg.nx = cfg->triad_nx; h->tg.nz = cfg->triad_nz; h->tg.P = th.P;
+    h->tri_nterms = th.nterms;
+    h->tri_threads = std::min(32 * th.Tw, 512);
+    h->tri_smem = (size_t)(3 * th.P + 1) * h->vsz;
+    int lim = 0;
+    if (smem_optin(&lim) || h->tri_smem > (size_t)lim) {
+      rc = fail(h, LH_EINVAL, "plane too large for the triad form (shared memory)"); lh_destroy(h); return rc;
+    }
+    cudaError_t ea = (h->prec == LH_PREC_FP64)
+                         ? cudaFuncSetAttribute(k_triad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->tri_smem)
+                         : cudaFuncSetAttribute(k_triad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->tri_smem);
+    if (ea != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ea)); lh_destroy(h); return rc; }
+  }
   {  // pressure factors, once (start.f90:656-658)
     const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
     k_build_dg<<<nb, NTHR_H, 0, h->st>>>(h->dg1, h->dg2, h->dg3, g);
@@ -387,6 +431,9 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->cfg.k1x = h->cfg.k2x = h->cfg.k1z = h->cfg.k2z = nullptr;
   h->cfg.list_ib_u = h->cfg.list_ib_v = nullptr;
   h->cfg.A_ib_u = h->cfg.A_ib_v = nullptr;
+  h->cfg.triad_off = h->cfg.triad_len = nullptr;
+  h->cfg.triad_data = nullptr;
+  h->cfg.triad_set_u = h->cfg.triad_set_v = nullptr;
   *out = h;
   return LH_OK;
 }
@@ -397,7 +444,7 @@ extern "C" int lh_destroy(lh_handle *h) {
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
-                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib};
+                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -408,7 +455,7 @@ extern "C" int lh_destroy(lh_handle *h) {
   return LH_OK;
 }
 
-extern "C" const char *lh_last_error(lh_handle *h) { return h ? h->err.c_str() : "null handle"; }
+extern "C" const char *lh_last_error(lh_handle *h) { return h ? h->err.c_str() : t_last_err.c_str(); }
 
 extern "C" void *lh_stream(lh_handle *h) { return h ? (void *)h->st : nullptr; }
 
@@ -538,6 +585,29 @@ static int nonlinear_transforms(lh_handle *h, int kRK) {
   return rc;
 }
 
+// triad-list form (ops_in_planes): the products come from the lists; the inverse
+// transforms still run where the physical velocities are needed (dtc_calc at kRK = 1)
+template <typename T>
+static int triad_nonlinear(lh_handle *h, int kRK) {
+  typedef typename C2<T>::t V;
+  const Geo &g = h->g;
+  const int nslots = g.nuI + g.nvI;
+  int rc = LH_OK;
+  if (kRK == 1) {
+    KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc));
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, nslots));
+    if (rc) return rc;
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G1, rc = launch_xpass<T, N>(h, nslots, 1));
+    if (rc) return rc;
+  }
+  KL("k_triad", k_triad<T><<<nslots, h->tri_threads, h->tri_smem, h->st>>>(
+                    h->u1, h->u2, h->u3, g, h->tg, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
+                    (V *)h->vvc, (V *)h->wvf));
+  return LH_OK;
+}
+
 // plane transforms through scratch buffers in precision T (leaves: FP64; immersed
 // boundaries: the form's transform precision)
 template <typename T, int N>
@@ -620,7 +690,7 @@ template <typename T>
 static int substep_launches_t(lh_handle *h, int kRK) {
   typedef typename C2<T>::t V;
   const Geo &g = h->g;
-  int rc = nonlinear_transforms<T>(h, kRK);
+  int rc = h->triad ? triad_nonlinear<T>(h, kRK) : nonlinear_transforms<T>(h, kRK);
   if (rc) return rc;
   if (kRK == 1) KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc));
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
@@ -844,6 +914,14 @@ struct lh_batch {
   cudaStream_t root;
   cudaEvent_t ev0;
   std::vector<cudaEvent_t> evs;
+  // triad-list nonlinear form
+  int triad;
+  TriadGeo tg;
+  uint32_t *d_terms;
+  int *d_wb, *d_lid;
+  int tri_threads;
+  size_t tri_smem;
+  long long tri_nterms;
   cudaGraph_t graph;
   cudaGraphExec_t gexec;
   long long nodes;

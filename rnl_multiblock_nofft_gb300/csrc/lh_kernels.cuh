@@ -590,7 +590,6 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   const float mp = (c == 0 && fw == 0 && part == 0) ? (float)(-dR * sc->mpgx) : 0.f;
   const float dd = (float)g.dd;
   const int nu = g.nu;
-  const double *d0 = g.d2u, *d1 = g.d2u + nu, *d2 = g.d2u + 2 * nu;
   const double gw1 = g.gw[1][0], gw2 = g.gw[1][1];
   const size_t ci = (size_t)c * 2 + part;
   const size_t lstride = (size_t)nc * 2;
@@ -670,7 +669,6 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
   const float dd = (float)g.dd;
   const int nv = g.nv;
-  const double *d0 = g.d2v, *d1 = g.d2v + nv, *d2 = g.d2v + 2 * nv;
   const size_t ci = (size_t)c * 2 + part;
   const size_t lstride = (size_t)nc * 2;
   double vm = u2[ci], v0 = u2[lstride + ci];

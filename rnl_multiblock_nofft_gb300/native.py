@@ -83,17 +83,19 @@ class GpuChannel:
     State arrays on the host use the reference's cfield layout: complex128
     [ncols, nlevels] (level fastest), one column per (kx, kz) mode."""
 
-    def __init__(self, setup: ChannelSetup, precision: str = "fp64"):
+    def __init__(self, setup: ChannelSetup, precision: str = "fp64", triads=None):
+        """`triads` (triads.TriadLists) selects the as-run triad-list nonlinear term
+        (ops_in_planes); None the pseudo-spectral products (ops_in_planes2)."""
         self.s = setup
         self.L = load()
         prec = {"fp64": LH_PREC_FP64, "mixed": LH_PREC_MIXED}[precision]
         self.precision = precision
-        cfg, self._keep = make_config(setup, prec)
+        cfg, self._keep = make_config(setup, prec, triads=triads)
         self._cfg = cfg
         h = C.c_void_p()
         rc = self.L.lh_create(C.byref(cfg), C.byref(h))
         if rc != LH_OK:
-            raise LhError(rc, "lh_create failed (is a CUDA device present?)")
+            raise LhError(rc, "lh_create failed: " + self.L.lh_last_error(None).decode())
         self.h = h
         self.shapes = cfield_shape(setup)
 
