@@ -1,14 +1,15 @@
 """Throughput of the RK3 substep on one GB300 (or N replicas, one per GPU).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload C1] [--form both|fp64|mixed]
+                    [--workload C1] [--form both|fp64|mixed] [--nonlin products|triads]
 
 Metric: Mpts*substeps/s = N1*N2*ny mode-points per RK3 substep, 3 substeps per step.
 `value` is the headline form (mixed when its velocity error against the FP64 form
 stays within 1e-5, else FP64) with the state resident in HBM; `e2e` is the same
 metric through the C ABI with the state copied from pinned host memory and back
 every step. The path does not shard (replicas only): with N > 1 every rank runs its
-own channel and `value` sums the replicas.
+own channel and `value` sums the replicas. `--nonlin triads` runs the as-run
+triad-list nonlinear term (complete lists, threshold 0) instead of the products.
 """
 from __future__ import annotations
 
@@ -151,6 +152,31 @@ def algorithmic_bytes(s, kernel: str, form: str) -> float:
     return float("nan")
 
 
+def triad_lists(args, s):
+    if args.nonlin != "triads":
+        return None
+    from rnl_multiblock_nofft_gb300.triads import TriadLists
+    return TriadLists.complete(s)
+
+
+def triad_terms(s, tl) -> int:
+    """Multiply-adds of complex values per substep in the triad sums: every list
+    triad counts twice (both z-signs) except those with ka + kp = 0."""
+    from rnl_multiblock_nofft_gb300.triads import U_TYPES, V_TYPES, plane_files
+    fu, fv = plane_files(s)
+    cache = {}
+    n = 0
+    for files, types in ((fu[1:-1], U_TYPES), (fv[1:-1], V_TYPES)):
+        for j in files:
+            for t in types:
+                a = tl.files[int(j)][t - 1]
+                k = id(a)
+                if k not in cache:
+                    cache[k] = 2 * len(a) - int(((a[:, 1].astype(int) + a[:, 3]) == 0).sum())
+                n += cache[k]
+    return n
+
+
 def run_reference(args, ws, rank):
     """The reference's CPU path on the host cores: the Fortran/MPI reference cannot
     be built here (no Fortran compiler), so its restatement (the oracle) runs on
@@ -162,7 +188,7 @@ def run_reference(args, ws, rank):
     from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars, workload_setup
     s = workload_setup(args.workload)
     cores = os.cpu_count() or 1
-    o = Oracle(s, threads=cores)
+    o = Oracle(s, threads=cores, triads=triad_lists(args, s))
     o.set_state(*initial_field(s, 1000))
     o.set_scalars(**initial_scalars(s))
     k = 0
@@ -194,14 +220,14 @@ def workload_desc(name):
     return WORKLOADS[name]["desc"]
 
 
-def cpu_baseline(s, budget_s: float = 20.0):
+def cpu_baseline(s, budget_s: float = 20.0, triads=None):
     """Oracle on the host cores, bounded: RK3 substeps of the same workload until
     ~budget_s of CPU work (at least one)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
     from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars
     cores = os.cpu_count() or 1
-    o = Oracle(s, threads=cores)
+    o = Oracle(s, threads=cores, triads=triads)
     o.set_state(*initial_field(s, 1000))
     o.set_scalars(**initial_scalars(s))
     n, t0 = 0, time.perf_counter()
@@ -282,6 +308,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="C1")
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--nonlin", default="products", choices=["products", "triads"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -302,13 +329,14 @@ def main():
         barrier(pg)
         return
     s = workload_setup(args.workload)
+    tl = triad_lists(args, s)
     ic = initial_field(s, 1000 + rank)
     sc0 = initial_scalars(s)
     pts = s.mode_points()
     forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
     res, states = {}, {}
     for form in forms:
-        g = GpuChannel(s, form)
+        g = GpuChannel(s, form, triads=tl)
         g.upload_state(*ic)
         g.set_scalars(**sc0)
         g.autotune()
@@ -345,7 +373,7 @@ def main():
     R = res[head]
 
     # e2e through the C ABI: pinned host state in, step, state out, every step
-    g = GpuChannel(s, head)
+    g = GpuChannel(s, head, triads=tl)
     shapes = g.shapes
     pinned = [torch.empty(sh + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
               for sh in shapes]
@@ -400,8 +428,16 @@ def main():
                           "kernel_ms_per_step": {k: v[1] for k, v in r["kernels"].items()}}
                       for f, r in res.items()},
             "mixed_rel_err_vs_fp64": relerr}
+    if tl is not None:
+        nt = triad_terms(s, tl)
+        tk = R["kernels"].get("k_triad")
+        line["config"]["nonlinear"] = ("triad lists (ops_in_planes), complete (threshold 0): "
+                                       f"{tl.n_triads() // max(1, len(tl.files))} triads per file")
+        line["triads"] = {"complex_macs_per_substep": nt,
+                          "k_triad_ms_per_step": tk[1] if tk else None,
+                          "gflops": (8 * nt * 3 / (tk[1] * 1e-3) / 1e9) if tk else None}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(s)
+        line["cpu_baseline"] = cpu_baseline(s, triads=tl)
     if rank == 0:
         print(json.dumps(line), flush=True)
     barrier(pg)

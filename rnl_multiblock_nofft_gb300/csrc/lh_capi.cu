@@ -50,7 +50,7 @@ struct lh_handle {
   int triad;
   TriadGeo tg;
   uint32_t *d_terms;
-  int *d_wb, *d_lid;
+  int *d_wb, *d_lid, *d_tmap;
   int tri_threads;
   size_t tri_smem;
   long long tri_nterms;
@@ -389,7 +389,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
   h->triad = (cfg->nonlin_form == LH_NONLIN_TRIADS) ? 1 : 0;
-  h->d_terms = nullptr; h->d_wb = h->d_lid = nullptr; h->tri_nterms = 0;
+  h->d_terms = nullptr; h->d_wb = h->d_lid = h->d_tmap = nullptr; h->tri_nterms = 0;
   if (h->triad) {  // expand and upload the triad lists (nonlinRead, start.f90:2983-3069)
     TriadHost th;
     std::string e = build_triads(cfg, g, th);
@@ -397,12 +397,13 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     h->d_terms = (uint32_t *)upload_vec(th.terms, ce);
     if (ce == cudaSuccess) h->d_wb = (int *)upload_vec(th.wb, ce);
     if (ce == cudaSuccess) h->d_lid = (int *)upload_vec(th.lid, ce);
+    if (ce == cudaSuccess) h->d_tmap = (int *)upload_vec(th.tmap, ce);
     if (ce != cudaSuccess) {
       rc = fail(h, ce == cudaErrorMemoryAllocation ? LH_ENOMEM : LH_ECUDA, std::string("triad lists: ") + cudaGetErrorString(ce));
       lh_destroy(h);
       return rc;
     }
-    h->tg.terms = h->d_terms; h->tg.wb = h->d_wb; h->tg.lid = h->d_lid;
+    h->tg.terms = h->d_terms; h->tg.wb = h->d_wb; h->tg.lid = h->d_lid; h->tg.tmap = h->d_tmap;
     h->tg.Tw = th.Tw; h->tg.T = th.T; h->tg.nx = cfg->triad_nx; h->tg.nz = cfg->triad_nz; h->tg.P = th.P;
     h->tri_nterms = th.nterms;
     h->tri_threads = std::min(32 * th.Tw, 512);
@@ -444,7 +445,7 @@ extern "C" int lh_destroy(lh_handle *h) {
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
-                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid};
+                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -914,14 +915,6 @@ struct lh_batch {
   cudaStream_t root;
   cudaEvent_t ev0;
   std::vector<cudaEvent_t> evs;
-  // triad-list nonlinear form
-  int triad;
-  TriadGeo tg;
-  uint32_t *d_terms;
-  int *d_wb, *d_lid;
-  int tri_threads;
-  size_t tri_smem;
-  long long tri_nterms;
   cudaGraph_t graph;
   cudaGraphExec_t gexec;
   long long nodes;

@@ -15,7 +15,9 @@
 // with a stable counting sort (so every target sums its terms in the reference's
 // order), and laid out warp-striped: the 32 targets of a warp own rows of 32
 // terms, row i holding term i of each lane (padding terms read a zero slot), so
-// every warp load of terms is one coalesced 128-byte line. A term is 32 bits:
+// every warp load of terms is one coalesced 128-byte line. Targets are assigned to
+// thread slots in decreasing order of their complete-list term count, so the lanes
+// of a warp carry similar counts and little padding. A term is 32 bits:
 // two 15-bit shared-memory indices (field * P + row * (N1/2+1) + |l|) and two
 // conjugate flags. One block per plane stages the plane's three velocity fields
 // (interpolated where the stagger needs it, FOU3D.f90:427-474) in shared memory;
@@ -35,6 +37,7 @@ struct TriadGeo {
   const uint32_t *terms;  // warp-striped term rows, 32 terms per row
   const int *wb;          // [nlists][Tw+1] first row of each warp of each expanded list
   const int *lid;         // [(nu + nv) * 9] expanded list of (level, type), -1 if none
+  const int *tmap;        // [T] target of each thread slot (slots ordered by expected term count)
   int Tw, T, nx, nz, P;   // warps, targets, list header, plane size (N2 * (N1/2+1))
 };
 
@@ -161,9 +164,10 @@ __global__ void __launch_bounds__(512) k_triad(const double2 *__restrict__ u1, c
   const int *lid = tg.lid + (size_t)(isU ? q : g.nu + q) * 9;
   const int lane = threadIdx.x & 31;
   // targets: (lt, kt) with list terms
-  for (int tt = threadIdx.x; tt < tg.Tw * 32; tt += blockDim.x) {
-    if (tt >= tg.T) continue;
-    const int w = tt >> 5;
+  for (int sl = threadIdx.x; sl < tg.Tw * 32; sl += blockDim.x) {
+    if (sl >= tg.T) continue;
+    const int w = sl >> 5;
+    const int tt = tg.tmap[sl];
     const int lt = tt / kw, kt = tt - lt * kw - tg.nz;
     const int r = tri_krow(kt, N2), c = r * N1h + lt;
     const bool z0 = (lt == 0 && kt == 0);
@@ -232,6 +236,7 @@ struct TriadHost {
   std::vector<uint32_t> terms;
   std::vector<int> wb;   // [nlists][Tw+1]
   std::vector<int> lid;  // [(nu + nv) * 9]
+  std::vector<int> tmap;  // [T] slot -> target
   int Tw = 0, T = 0, P = 0, nlists = 0;
   long long nterms = 0;  // list terms (both passes), without padding
 };
@@ -260,6 +265,13 @@ static std::string build_triads(const lh_config *cfg, const Geo &g, TriadHost &t
   const int kw = 2 * nz + 1;
   th.T = (nx + 1) * kw;
   th.Tw = (th.T + 31) / 32;
+  // slots: targets by decreasing complete-list count (2nx+1-lt)(2nz+1-|kt|), stable
+  th.tmap.resize(th.T);
+  for (int t = 0; t < th.T; ++t) th.tmap[t] = t;
+  auto key = [&](int t) { const int lt = t / kw, kt = t - lt * kw - nz; return (2 * nx + 1 - lt) * (kw - abs(kt)); };
+  std::stable_sort(th.tmap.begin(), th.tmap.end(), [&](int a, int b) { return key(a) > key(b); });
+  std::vector<int> slot_of(th.T);
+  for (int sl = 0; sl < th.T; ++sl) slot_of[th.tmap[sl]] = sl;
   const uint32_t zero = (uint32_t)(3 * th.P);
   const uint32_t pad = zero | (zero << 16);
   th.lid.assign((size_t)(g.nu + g.nv) * 9, -1);
@@ -287,11 +299,11 @@ static std::string build_triads(const lh_config *cfg, const Geo &g, TriadHost &t
         const int ra = tri_krow(pn * sa * ka0, N2), rp = tri_krow(pn * sp * kp0, N2);
         const uint32_t ia = (uint32_t)(fa * th.P + ra * N1h + abs(la)) | (la < 0 ? 0x8000u : 0u);
         const uint32_t ip = (uint32_t)(fp * th.P + rp * N1h + abs(lp)) | (lp < 0 ? 0x8000u : 0u);
-        tgt.push_back((la + lp) * kw + pn * (ka0 + kp0) + nz);
+        tgt.push_back(slot_of[(la + lp) * kw + pn * (ka0 + kp0) + nz]);
         code.push_back(ia | (ip << 16));
       }
     }
-    // stable counting sort by target, then warp striping
+    // stable counting sort by slot, then warp striping
     cnt.assign(th.Tw * 32, 0);
     for (int t : tgt) ++cnt[t];
     start.assign(th.Tw * 32 + 1, 0);
