@@ -94,6 +94,10 @@ typedef struct lh_config {
                                      ka[L], lp[L], kp[L]. Lists may share storage. */
   const int32_t *triad_set_u;     /* [nyu] set (0-based) of each u level, -1 on the ghost levels */
   const int32_t *triad_set_v;     /* [nyv] set of each v level, -1 on the wall levels */
+  /* Multiblock: N1, N2, Ngal1, Ngal2 above are the wall bands' (bands 1 and 3,
+   * N(1:2,1), Ngal(1:2,1)); these are the core band's (band 2). Equal values give a
+   * single-resolution channel. The core modes must be a subset of the wall modes. */
+  int32_t N1c, N2c, Ngal1c, Ngal2c;
 } lh_config;
 
 /* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter).
@@ -123,6 +127,19 @@ const char *lh_last_error(lh_handle *h);
 int lh_upload_state(lh_handle *h, const double *u1, const double *u2,
                     const double *u3, const double *p);
 int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p);
+
+/* Per-band state, the reference's cfield of one band (u1(iband)%f etc.,
+ * declaration.f90:137-139): band 1 (bottom wall band) and 3 (top) hold the short
+ * columns (wall-band modes the core band lacks) over their jlim levels
+ * (start.f90:1675-1709); band 2 the long columns over all levels. Columns in the
+ * order of columns_i/k with one process (start.f90:1566-1609): row-major over
+ * (kz index, kx) of the wall-band modes. Shapes [ncols_b][nlev_b] complex(8),
+ * nlev_b = jlim(2,grid,b) - jlim(1,grid,b) + 1 for u/w, v and p. Bands 1 and 3
+ * are empty for a single-resolution channel, and band 2 is then lh_upload_state's
+ * layout. Blocking. */
+int lh_upload_band(lh_handle *h, int band, const double *u1, const double *u2,
+                   const double *u3, const double *p);
+int lh_download_band(lh_handle *h, int band, double *u1, double *u2, double *u3, double *p);
 
 /* Scalars: lh_set_scalars also (re)computes Qx, and QxT when flag_ctpress == 0,
  * as getini does (start.f90:2170-2176), and the initial divergence. */

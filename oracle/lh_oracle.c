@@ -138,7 +138,13 @@ struct orc {
   double *yu, *yv, *thu, *thv, *d2u, *d2v, *k1x, *k2x, *k1z, *k2z, *Au, *Av;
   int32_t *lu, *lv;
   int N1, N2, N1h, G1, G2, dny, nu, nv, np, ncol, nn;
-  fftplan px, pz; /* complex plans of length G1 and G2 */
+  fftplan px, pz; /* complex plans of length G1 and G2 (wall bands) */
+  /* multiblock: core band (band 2) resolution, its plans, the long-column flags of
+   * the wall-band mode grid and jlim(lo/hi, grid, band) (start.f90:1675-1709) */
+  int mb, N1c, N2c, G1c, G2c;
+  fftplan pxc, pzc;
+  unsigned char *lng;
+  int bj[3][3][2]; /* [band 0..2][grid: 0 u, 1 v, 2 p][lo, hi], reference j */
   cplx *u1, *u2, *u3, *p;
   cplx *Nu1, *Nu2, *Nu3, *du1, *du2, *du3, *psi, *div;
   cplx *u1i, *u2i, *u3i; /* u1,u3 at v levels; u2 at u levels */
@@ -157,6 +163,12 @@ struct orc {
 #define PIDX(j) ((j) + O->dny - 1)      /* p level j -> array index */
 #define PL(F, idx) ((F) + (size_t)(idx) * O->ncol)
 
+/* column segments: a long column has one (band 2), a short column two (bands 1, 3) */
+static inline int col_bands(const orc *O, int c, int b[2]) {
+  if (!O->mb || O->lng[c]) { b[0] = 1; return 1; }
+  b[0] = 0; b[1] = 2; return 2;
+}
+
 static double *dupd(const double *s, size_t n) {
   double *d = (double *)malloc(sizeof(double) * (n ? n : 1));
   if (n) memcpy(d, s, sizeof(double) * n);
@@ -165,27 +177,30 @@ static double *dupd(const double *s, size_t n) {
 
 static cplx *zalloc(size_t n) { return (cplx *)calloc(n ? n : 1, sizeof(cplx)); }
 
-/* pressure matrix, LU_buildP + LU_decP (tridLU_3D.f90:333-407, 477-518) */
+/* pressure matrices of every band's columns over jlim(1:2, pgrid, band), LU_buildP +
+ * LU_decP (tridLU_3D.f90:333-407, 477-518); gauge on mode (0,0) of band 2 */
 static void build_DG(orc *O) {
   const double dd = O->c.ddthetavi;
-  int ns = O->c.N4[0] + 1, ne = O->c.N4[3];
-  int n = ne - ns + 1;
-  double *Db = (double *)malloc(sizeof(double) * (n + 2)); /* index m - (ns-1) */
-  double *Gb = (double *)malloc(sizeof(double) * (n + 2));
-  double *Dt = (double *)malloc(sizeof(double) * (n + 2));
-  double *Gt = (double *)malloc(sizeof(double) * (n + 2));
+  for (int c = 0; c < O->ncol; ++c) {
+    int bs[2];
+    const int nsg = col_bands(O, c, bs);
+    const int r = c / O->N1h, kx = c % O->N1h;
+    const double k2x = O->k2x[kx], k2z = O->k2z[r];
+    for (int sgi = 0; sgi < nsg; ++sgi) {
+      const int b = bs[sgi];
+      const int ns = O->bj[b][2][0], ne = O->bj[b][2][1], n = ne - ns + 1;
+      double *Db = (double *)malloc(sizeof(double) * (n + 2)); /* index m - (ns-1) */
+      double *Gb = (double *)malloc(sizeof(double) * (n + 2));
+      double *Dt = (double *)malloc(sizeof(double) * (n + 2));
+      double *Gt = (double *)malloc(sizeof(double) * (n + 2));
 #define X(m) ((m) - (ns - 1))
-  for (int j = ns; j <= ne; ++j) {
-    Db[X(j - 1)] = -dd * O->thu[UIDX(j)];
-    Gb[X(j)] = -dd * O->thv[UIDX(j)];
-    Dt[X(j)] = dd * O->thu[UIDX(j)];
-    Gt[X(j + 1)] = dd * O->thv[UIDX(j)];
-  }
-  for (int kz = 0; kz < O->N2; ++kz)
-    for (int kx = 0; kx < O->N1h; ++kx) {
-      int col = kz * O->N1h + kx;
-      double k2x = O->k2x[kx], k2z = O->k2z[kz];
-#define A(c, j) O->DG[((size_t)((j) - ns) * O->ncol + col) * 3 + (c) - 1]
+      for (int j = ns; j <= ne; ++j) {
+        Db[X(j - 1)] = -dd * O->thu[UIDX(j)];
+        Gb[X(j)] = -dd * O->thv[UIDX(j)];
+        Dt[X(j)] = dd * O->thu[UIDX(j)];
+        Gt[X(j + 1)] = dd * O->thv[UIDX(j)];
+      }
+#define A(cc, j) O->DG[((size_t)PIDX(j) * O->ncol + c) * 3 + (cc) - 1]
       A(1, ns) = 0.0;
       A(2, ns) = (Dt[X(ns)] * Gb[X(ns)]) + k2x + k2z;
       A(3, ns) = (Dt[X(ns)] * Gt[X(ns + 1)]);
@@ -197,7 +212,7 @@ static void build_DG(orc *O) {
         A(1, j) = (Db[X(j - 1)] * Gb[X(j - 1)]);
         A(3, j) = (Dt[X(j)] * Gt[X(j + 1)]);
       }
-      if (col == 0) { /* gauge of mode (0,0), tridLU_3D.f90:384-390 */
+      if (c == 0 && b == 1) { /* gauge of mode (0,0), tridLU_3D.f90:384-390 */
         double h = O->yu[UIDX(1 + 1)] - O->yu[UIDX(1)];
         A(1, ns) = 0.0;
         A(2, ns) = 1.0 / (h * h);
@@ -209,9 +224,10 @@ static void build_DG(orc *O) {
         A(2, j) = 1.0 / (A(2, j) - A(1, j) * A(3, j - 1));
       }
 #undef A
-    }
 #undef X
-  free(Db); free(Gb); free(Dt); free(Gt);
+      free(Db); free(Gb); free(Dt); free(Gt);
+    }
+  }
 }
 
 void orc_destroy(orc *O);
@@ -262,6 +278,25 @@ orc *orc_create(const lh_config *cfg) {
   O->G1 = cfg->Ngal1; O->G2 = cfg->Ngal2; O->dny = cfg->dny;
   O->nu = cfg->nyu; O->nv = cfg->nyv; O->np = cfg->nyu - 2; O->nn = cfg->nn;
   O->ncol = O->N1h * O->N2;
+  O->N1c = cfg->N1c; O->N2c = cfg->N2c; O->G1c = cfg->Ngal1c; O->G2c = cfg->Ngal2c;
+  O->mb = (O->N1c != O->N1 || O->N2c != O->N2 || O->G1c != O->G1 || O->G2c != O->G2);
+  if (O->N1c <= 0 || O->N2c <= 0 || O->N1c > O->N1 || O->N2c > O->N2 || (O->N1c & 1) || (O->N2c & 1) ||
+      O->G1c <= O->N1c || O->G2c <= O->N2c || (O->mb && cfg->nonlin_form == LH_NONLIN_TRIADS)) {
+    free(O);
+    return NULL;
+  }
+  {
+    const int *N3 = cfg->N3, *N4 = cfg->N4;
+    const int bj[3][3][2] = {{{N4[0], N4[1] + 1}, {N3[0], N3[1] + 1}, {N4[0] + 1, N4[1]}},
+                             {{N4[0], N4[3] + 1}, {N3[0], N3[3] + 1}, {N4[0] + 1, N4[3]}},
+                             {{N4[2], N4[3] + 1}, {N3[2], N3[3] + 1}, {N4[2] + 1, N4[3]}}};
+    memcpy(O->bj, bj, sizeof(bj));
+    O->lng = (unsigned char *)malloc((size_t)O->ncol);
+    for (int c = 0; c < O->ncol; ++c) {
+      const int r = c / O->N1h, kx = c % O->N1h;
+      O->lng[c] = (kx <= O->N1c / 2) && (r < O->N2c / 2 || r >= O->N2 - O->N2c / 2);
+    }
+  }
   O->yu = dupd(cfg->yu, O->nu); O->yv = dupd(cfg->yv, O->nv);
   O->thu = dupd(cfg->dthdyu, O->nu); O->thv = dupd(cfg->dthdyv, O->nv);
   O->d2u = dupd(cfg->dyu2i, 3 * (size_t)O->nu); O->d2v = dupd(cfg->dyv2i, 3 * (size_t)O->nv);
@@ -276,7 +311,9 @@ orc *orc_create(const lh_config *cfg) {
   O->c.dyu2i = O->d2u; O->c.dyv2i = O->d2v; O->c.k1x = O->k1x; O->c.k2x = O->k2x;
   O->c.k1z = O->k1z; O->c.k2z = O->k2z; O->c.list_ib_u = O->lu; O->c.list_ib_v = O->lv;
   O->c.A_ib_u = O->Au; O->c.A_ib_v = O->Av;
-  if (plan_init(&O->px, O->G1) || plan_init(&O->pz, O->G2)) return NULL;
+  if (plan_init(&O->px, O->G1) || plan_init(&O->pz, O->G2) || plan_init(&O->pxc, O->G1c) ||
+      plan_init(&O->pzc, O->G2c))
+    return NULL;
   size_t nc = (size_t)O->ncol;
   O->u1 = zalloc(nc * O->nu); O->u3 = zalloc(nc * O->nu); O->u2 = zalloc(nc * O->nv);
   O->p = zalloc(nc * O->np);
@@ -303,19 +340,38 @@ void orc_destroy(orc *O) {
                   O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
                   O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
                   O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2,
-                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv};
+                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
-  plan_free(&O->px); plan_free(&O->pz);
+  plan_free(&O->px); plan_free(&O->pz); plan_free(&O->pxc); plan_free(&O->pzc);
   free(O);
 }
 
 /* ------------------------------------------------------------------------- */
 /* transforms of one plane                                                     */
 /* ------------------------------------------------------------------------- */
-/* plane row (0-based, physical z index) of column kz-index r (0-based) */
-static inline int prow(const orc *O, int r) { return r < O->N2 / 2 ? r : r - O->N2 + O->G2; }
+/* A plane's resolution: the wall bands' (every mode of the wall-band grid) or the
+ * core band's (the long columns only). Mode (r, kx) of a view, r its own kz index,
+ * lives at wall-grid column frow(r) * (N1/2+1) + kx (the dk shift, start.f90:1722-1734). */
+typedef struct { int N1h, N2, G1, G2; const fftplan *px, *pz; } pview;
+static inline size_t vcol(const orc *O, const pview *v, int r, int kx) {
+  const int fr = r < v->N2 / 2 ? r : r + O->N2 - v->N2;
+  return (size_t)fr * O->N1h + kx;
+}
+static inline void view_of(const orc *O, int fine, pview *v) {
+  if (fine) { v->N1h = O->N1h; v->N2 = O->N2; v->G1 = O->G1; v->G2 = O->G2; v->px = &O->px; v->pz = &O->pz; }
+  else { v->N1h = O->N1c / 2 + 1; v->N2 = O->N2c; v->G1 = O->G1c; v->G2 = O->G2c; v->px = &O->pxc; v->pz = &O->pzc; }
+}
+/* band of planes (proc_lims_planes, start.f90:1836-1916): u plane j is a wall-band plane
+ * for j <= N(4,1) or j > N(4,2); v plane j for j <= N(3,1) or j > N(3,2) */
+static inline int fine_u(const orc *O, int j) { return !O->mb || j <= O->c.N4[1] || j > O->c.N4[2]; }
+static inline int fine_v(const orc *O, int j) { return !O->mb || j <= O->c.N3[1] || j > O->c.N3[2]; }
 
-/* work buffers for one thread */
+/* plane row (0-based, physical z index) of kz-index r of a view */
+static inline int prow(const pview *v, int r) { return r < v->N2 / 2 ? r : r - v->N2 + v->G2; }
+
+
+
+/* work buffers for one thread (sized for the wall-band planes, the largest) */
 typedef struct { cplx *A; cplx *line; cplx *tmp; } pwork;
 
 static void pwork_init(const orc *O, pwork *w) {
@@ -326,17 +382,17 @@ static void pwork_init(const orc *O, pwork *w) {
 }
 static void pwork_free(pwork *w) { free(w->A); free(w->line); free(w->tmp); }
 
-/* four_to_phys (FOU3D.f90:738-781): spectral plane S[kz][kx] -> phys[l][m] (G2 x G1).
- * z: backward complex transform of the N1/2+1 retained x-modes; x: backward real
- * transform of every row, Im of x-modes 0 and G1/2 ignored. */
-static void four_to_phys_plane(const orc *O, const cplx *S, double *phys, pwork *w) {
-  const int G1 = O->G1, G2 = O->G2, Gh = G1 / 2 + 1, N1h = O->N1h;
+/* four_to_phys (FOU3D.f90:738-781): the modes of view v of spectral plane S -> phys[l][m]
+ * (G2 x G1 of the view). z: backward complex transform of the N1/2+1 retained x-modes; x:
+ * backward real transform of every row, Im of x-modes 0 and G1/2 ignored. */
+static void four_to_phys_plane(const orc *O, const pview *v, const cplx *S, double *phys, pwork *w) {
+  const int G1 = v->G1, G2 = v->G2, Gh = G1 / 2 + 1, N1h = v->N1h;
   memset(w->A, 0, sizeof(cplx) * (size_t)G2 * Gh);
   for (int kx = 0; kx < N1h; ++kx) {
     for (int l = 0; l < G2; ++l) w->line[l] = 0;
-    for (int r = 0; r < O->N2; ++r) w->line[prow(O, r)] = S[(size_t)r * N1h + kx];
+    for (int r = 0; r < v->N2; ++r) w->line[prow(v, r)] = S[vcol(O, v, r, kx)];
     w->line[G2 / 2] = 0; /* zeroed z 'oddball' row */
-    fft_inplace(&O->pz, w->line, +1, w->tmp);
+    fft_inplace(v->pz, w->line, +1, w->tmp);
     for (int l = 0; l < G2; ++l) w->A[(size_t)l * Gh + kx] = w->line[l];
   }
   /* x: pair rows (a, b) into one complex backward transform */
@@ -350,7 +406,7 @@ static void four_to_phys_plane(const orc *O, const cplx *S, double *phys, pwork 
       w->line[k] = ak + I * bk;
       if (k > 0 && k < G1 / 2) w->line[G1 - k] = conj(ak) + I * conj(bk);
     }
-    fft_inplace(&O->px, w->line, +1, w->tmp);
+    fft_inplace(v->px, w->line, +1, w->tmp);
     for (int m = 0; m < G1; ++m) {
       phys[(size_t)l * G1 + m] = creal(w->line[m]);
       if (b) phys[(size_t)(l + 1) * G1 + m] = cimag(w->line[m]);
@@ -358,16 +414,16 @@ static void four_to_phys_plane(const orc *O, const cplx *S, double *phys, pwork 
   }
 }
 
-/* phys_to_four (FOU3D.f90:2253-2272) restricted to the retained modes: returns
- * C[kz-index r][kx] for all N2 column rows (the zeroed row G2/2 is never retained). */
-static void phys_to_four_plane(const orc *O, const double *phys, cplx *C, pwork *w) {
-  const int G1 = O->G1, G2 = O->G2, Gh = G1 / 2 + 1, N1h = O->N1h;
+/* phys_to_four (FOU3D.f90:2253-2272) restricted to the retained modes of view v: writes
+ * C at the view's columns for all its N2 rows (the zeroed row G2/2 is never retained). */
+static void phys_to_four_plane(const orc *O, const pview *v, const double *phys, cplx *C, pwork *w) {
+  const int G1 = v->G1, G2 = v->G2, Gh = G1 / 2 + 1, N1h = v->N1h;
   const double s1 = 1.0 / G1, s2 = 1.0 / G2;
   for (int l = 0; l < G2; l += 2) {
     int hasb = (l + 1 < G2);
     for (int m = 0; m < G1; ++m)
       w->line[m] = phys[(size_t)l * G1 + m] + I * (hasb ? phys[(size_t)(l + 1) * G1 + m] : 0.0);
-    fft_inplace(&O->px, w->line, -1, w->tmp);
+    fft_inplace(v->px, w->line, -1, w->tmp);
     for (int k = 0; k <= G1 / 2; ++k) {
       cplx z = w->line[k], zc = conj(w->line[(G1 - k) % G1]);
       cplx A = 0.5 * (z + zc), B = -0.5 * I * (z - zc);
@@ -379,19 +435,19 @@ static void phys_to_four_plane(const orc *O, const double *phys, cplx *C, pwork 
   }
   for (int kx = 0; kx < N1h; ++kx) {
     for (int l = 0; l < G2; ++l) w->line[l] = w->A[(size_t)l * Gh + kx];
-    fft_inplace(&O->pz, w->line, -1, w->tmp);
-    for (int r = 0; r < O->N2; ++r) C[(size_t)r * N1h + kx] = w->line[prow(O, r)] * s2;
+    fft_inplace(v->pz, w->line, -1, w->tmp);
+    for (int r = 0; r < v->N2; ++r) C[vcol(O, v, r, kx)] = w->line[prow(v, r)] * s2;
   }
 }
 
-/* der_x / der_z (FOU3D.f90:476-593) of retained-mode planes, summed:
- * out = i kx * X + i kz * Z, with the row kz = -N2/2 (column r = N2/2) zeroed. */
-static void derxz(const orc *O, const cplx *X, const cplx *Z, cplx *out) {
-  for (int r = 0; r < O->N2; ++r)
-    for (int kx = 0; kx < O->N1h; ++kx) {
-      size_t c = (size_t)r * O->N1h + kx;
-      if (r == O->N2 / 2) { out[c] = 0; continue; }
-      cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[r];
+/* der_x / der_z (FOU3D.f90:476-593) of the view's modes, summed:
+ * out = i kx * X + i kz * Z, with the row kz = -N2/2 of the view zeroed. */
+static void derxz(const orc *O, const pview *v, const cplx *X, const cplx *Z, cplx *out) {
+  for (int r = 0; r < v->N2; ++r)
+    for (int kx = 0; kx < v->N1h; ++kx) {
+      size_t c = vcol(O, v, r, kx);
+      if (r == v->N2 / 2) { out[c] = 0; continue; }
+      cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[c / O->N1h];
       out[c] = kxF * X[c] + kzF * Z[c];
     }
 }
@@ -456,6 +512,8 @@ static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
   const size_t pp = (size_t)O->G1 * O->G2;
   const int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3], vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
   double u1m = *pu1m, u3m = *pu3m, u2m = *pu2m;
+  pview vf;
+  view_of(O, 1, &vf);
 #pragma omp parallel reduction(max : u1m, u3m, u2m)
   {
     pwork w; pwork_init(O, &w);
@@ -483,12 +541,12 @@ static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
       nonlin_inter(O, set, 5, vv, V, V);
       nonlin_inter(O, set, 7, wu, U, W);
       nonlin_inter(O, set, 9, ww, W, W);
-      derxz(O, uu, uw, PL(O->N1xz, q));
-      derxz(O, wu, ww, PL(O->N3xz, q));
-      four_to_phys_plane(O, U, f, &w);
+      derxz(O, &vf, uu, uw, PL(O->N1xz, q));
+      derxz(O, &vf, wu, ww, PL(O->N3xz, q));
+      four_to_phys_plane(O, &vf, U, f, &w);
       for (size_t e = 0; e < pp; ++e) if (fabs(f[e]) > u1m) u1m = fabs(f[e]);
       memcpy(O->phys_u1 + pp * q, f, sizeof(double) * pp);
-      four_to_phys_plane(O, W, f, &w);
+      four_to_phys_plane(O, &vf, W, f, &w);
       for (size_t e = 0; e < pp; ++e) if (fabs(f[e]) > u3m) u3m = fabs(f[e]);
       memcpy(O->phys_u3 + pp * q, f, sizeof(double) * pp);
     }
@@ -513,8 +571,8 @@ static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
       nonlin_inter(O, set, 4, vu, Ui, V);
       nonlin_inter(O, set, 6, vw, Wi, V);
       nonlin_inter(O, set, 8, wv, V, Wi);
-      derxz(O, vu, vw, PL(O->N2xz, q));
-      four_to_phys_plane(O, V, f, &w);
+      derxz(O, &vf, vu, vw, PL(O->N2xz, q));
+      four_to_phys_plane(O, &vf, V, f, &w);
       const double th = O->thv[q];
       for (size_t e = 0; e < pp; ++e) {
         double a = fabs(f[e]) * th;
@@ -534,33 +592,34 @@ static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
 static void nonlinear(orc *O, int kRK) {
   const int nc = O->ncol;
   const double dd = O->c.ddthetavi;
-  /* interp_u (u1,u3 -> v levels) and interp_v (u2 -> u levels), FOU3D.f90:427-474 */
-  for (int jv = O->c.N3[0]; jv <= O->c.N3[3] + 1; ++jv) {
-    double yv = O->yv[UIDX(jv)], yuj = O->yu[UIDX(jv)], yu1 = O->yu[UIDX(jv + 1)];
-    for (int c = 0; c < nc; ++c) {
-      cplx a = PL(O->u1, UIDX(jv + 1))[c], b = PL(O->u1, UIDX(jv))[c];
-      PL(O->u1i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * b) / (yu1 - yuj);
-      a = PL(O->u3, UIDX(jv + 1))[c]; b = PL(O->u3, UIDX(jv))[c];
-      PL(O->u3i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * b) / (yu1 - yuj);
-    }
-  }
-  for (int ju = O->c.N4[0] + 1; ju <= O->c.N4[3]; ++ju) {
-    double yuj = O->yu[UIDX(ju)], yvm = O->yv[UIDX(ju - 1)], yvj = O->yv[UIDX(ju)];
-    for (int c = 0; c < nc; ++c)
-      PL(O->u2i, UIDX(ju))[c] = ((yuj - yvm) * PL(O->u2, UIDX(ju))[c]
-                                 + (yvj - yuj) * PL(O->u2, UIDX(ju - 1))[c]) / (yvj - yvm);
-  }
-  {
-    int lo = O->c.N4[0], hi = O->c.N4[3] + 1, vlo = O->c.N3[0], vhi = O->c.N3[3] + 1;
-    for (int c = 0; c < nc; ++c) {
+  /* interp_u (u1,u3 -> v levels) and interp_v (u2 -> u levels) of every band's columns
+   * over the band's levels, FOU3D.f90:427-474 */
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nc; ++c) {
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      for (int jv = O->bj[b][1][0]; jv <= O->bj[b][1][1]; ++jv) {
+        double yv = O->yv[UIDX(jv)], yuj = O->yu[UIDX(jv)], yu1 = O->yu[UIDX(jv + 1)];
+        cplx a = PL(O->u1, UIDX(jv + 1))[c], bb = PL(O->u1, UIDX(jv))[c];
+        PL(O->u1i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * bb) / (yu1 - yuj);
+        a = PL(O->u3, UIDX(jv + 1))[c]; bb = PL(O->u3, UIDX(jv))[c];
+        PL(O->u3i, UIDX(jv))[c] = ((yv - yuj) * a + (yu1 - yv) * bb) / (yu1 - yuj);
+      }
+      const int lo = O->bj[b][0][0], hi = O->bj[b][0][1], vlo = O->bj[b][1][0], vhi = O->bj[b][1][1];
+      for (int ju = lo + 1; ju <= hi - 1; ++ju) {
+        double yuj = O->yu[UIDX(ju)], yvm = O->yv[UIDX(ju - 1)], yvj = O->yv[UIDX(ju)];
+        PL(O->u2i, UIDX(ju))[c] = ((yuj - yvm) * PL(O->u2, UIDX(ju))[c]
+                                   + (yvj - yuj) * PL(O->u2, UIDX(ju - 1))[c]) / (yvj - yvm);
+      }
       cplx i1 = PL(O->u2i, UIDX(lo + 1))[c], i2 = PL(O->u2i, UIDX(hi - 1))[c];
-      PL(O->u2i, UIDX(lo))[c] = O->c.gw_interp[1][0] * (PL(O->u2, UIDX(vlo))[c] - i1) + i1;
-      PL(O->u2i, UIDX(hi))[c] = O->c.gw_interp[1][1] * (PL(O->u2, UIDX(vhi))[c] - i2) + i2;
+      PL(O->u2i, UIDX(lo))[c] = O->c.gw_interp[b][0] * (PL(O->u2, UIDX(vlo))[c] - i1) + i1;
+      PL(O->u2i, UIDX(hi))[c] = O->c.gw_interp[b][1] * (PL(O->u2, UIDX(vhi))[c] - i2) + i2;
     }
   }
 
-  const int G1 = O->G1, G2 = O->G2;
-  const size_t pp = (size_t)G1 * G2;
+  const size_t ppF = (size_t)O->G1 * O->G2;
   double u1m = 0.0, u3m = 0.0, u2m = 1e-6;
   int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3];
   int vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
@@ -570,16 +629,19 @@ static void nonlinear(orc *O, int kRK) {
 #pragma omp parallel reduction(max : u1m, u3m, u2m)
   {
     pwork w; pwork_init(O, &w);
-    double *f1 = (double *)malloc(sizeof(double) * pp), *f2 = (double *)malloc(sizeof(double) * pp);
-    double *f3 = (double *)malloc(sizeof(double) * pp);
-    double *q1 = (double *)malloc(sizeof(double) * pp), *q2 = (double *)malloc(sizeof(double) * pp);
-    double *q3 = (double *)malloc(sizeof(double) * pp), *q4 = (double *)malloc(sizeof(double) * pp);
+    double *f1 = (double *)malloc(sizeof(double) * ppF), *f2 = (double *)malloc(sizeof(double) * ppF);
+    double *f3 = (double *)malloc(sizeof(double) * ppF);
+    double *q1 = (double *)malloc(sizeof(double) * ppF), *q2 = (double *)malloc(sizeof(double) * ppF);
+    double *q3 = (double *)malloc(sizeof(double) * ppF), *q4 = (double *)malloc(sizeof(double) * ppF);
     cplx *c1 = zalloc(nc), *c2 = zalloc(nc), *c3 = zalloc(nc), *c4 = zalloc(nc);
 #pragma omp for schedule(dynamic)
     for (int ju = ulo; ju <= uhi; ++ju) {
-      four_to_phys_plane(O, PL(O->u1, UIDX(ju)), f1, &w);
-      four_to_phys_plane(O, PL(O->u2i, UIDX(ju)), f2, &w);
-      four_to_phys_plane(O, PL(O->u3, UIDX(ju)), f3, &w);
+      pview v;
+      view_of(O, fine_u(O, ju), &v);
+      const size_t pp = (size_t)v.G1 * v.G2;
+      four_to_phys_plane(O, &v, PL(O->u1, UIDX(ju)), f1, &w);
+      four_to_phys_plane(O, &v, PL(O->u2i, UIDX(ju)), f2, &w);
+      four_to_phys_plane(O, &v, PL(O->u3, UIDX(ju)), f3, &w);
       for (size_t e = 0; e < pp; ++e) {
         q1[e] = f1[e] * f1[e];
         q2[e] = f1[e] * f3[e];
@@ -588,20 +650,23 @@ static void nonlinear(orc *O, int kRK) {
         if (fabs(f1[e]) > u1m) u1m = fabs(f1[e]);
         if (fabs(f3[e]) > u3m) u3m = fabs(f3[e]);
       }
-      memcpy(O->phys_u1 + pp * UIDX(ju), f1, sizeof(double) * pp);
-      memcpy(O->phys_u3 + pp * UIDX(ju), f3, sizeof(double) * pp);
-      phys_to_four_plane(O, q1, c1, &w);
-      phys_to_four_plane(O, q2, c2, &w);
-      phys_to_four_plane(O, q3, PL(O->vvc, UIDX(ju)), &w);
-      phys_to_four_plane(O, q4, c4, &w);
-      derxz(O, c1, c2, PL(O->N1xz, UIDX(ju)));
-      derxz(O, c2, c4, PL(O->N3xz, UIDX(ju)));
+      memcpy(O->phys_u1 + ppF * UIDX(ju), f1, sizeof(double) * pp);
+      memcpy(O->phys_u3 + ppF * UIDX(ju), f3, sizeof(double) * pp);
+      phys_to_four_plane(O, &v, q1, c1, &w);
+      phys_to_four_plane(O, &v, q2, c2, &w);
+      phys_to_four_plane(O, &v, q3, PL(O->vvc, UIDX(ju)), &w);
+      phys_to_four_plane(O, &v, q4, c4, &w);
+      derxz(O, &v, c1, c2, PL(O->N1xz, UIDX(ju)));
+      derxz(O, &v, c2, c4, PL(O->N3xz, UIDX(ju)));
     }
 #pragma omp for schedule(dynamic)
     for (int jv = vlo; jv <= vhi; ++jv) {
-      four_to_phys_plane(O, PL(O->u1i, UIDX(jv)), f1, &w);
-      four_to_phys_plane(O, PL(O->u2, UIDX(jv)), f2, &w);
-      four_to_phys_plane(O, PL(O->u3i, UIDX(jv)), f3, &w);
+      pview v;
+      view_of(O, fine_v(O, jv), &v);
+      const size_t pp = (size_t)v.G1 * v.G2;
+      four_to_phys_plane(O, &v, PL(O->u1i, UIDX(jv)), f1, &w);
+      four_to_phys_plane(O, &v, PL(O->u2, UIDX(jv)), f2, &w);
+      four_to_phys_plane(O, &v, PL(O->u3i, UIDX(jv)), f3, &w);
       double th = O->thv[UIDX(jv)];
       for (size_t e = 0; e < pp; ++e) {
         q1[e] = f1[e] * f2[e];
@@ -609,10 +674,10 @@ static void nonlinear(orc *O, int kRK) {
         double a = fabs(f2[e]) * th;
         if (a > u2m) u2m = a;
       }
-      memcpy(O->phys_u2 + pp * UIDX(jv), f2, sizeof(double) * pp);
-      phys_to_four_plane(O, q1, PL(O->uvf, UIDX(jv)), &w);
-      phys_to_four_plane(O, q2, PL(O->wvf, UIDX(jv)), &w);
-      derxz(O, PL(O->uvf, UIDX(jv)), PL(O->wvf, UIDX(jv)), PL(O->N2xz, UIDX(jv)));
+      memcpy(O->phys_u2 + ppF * UIDX(jv), f2, sizeof(double) * pp);
+      phys_to_four_plane(O, &v, q1, PL(O->uvf, UIDX(jv)), &w);
+      phys_to_four_plane(O, &v, q2, PL(O->wvf, UIDX(jv)), &w);
+      derxz(O, &v, PL(O->uvf, UIDX(jv)), PL(O->wvf, UIDX(jv)), PL(O->N2xz, UIDX(jv)));
     }
     free(f1); free(f2); free(f3); free(q1); free(q2); free(q3); free(q4);
     free(c1); free(c2); free(c3); free(c4);
@@ -624,21 +689,27 @@ static void nonlinear(orc *O, int kRK) {
   memset(PL(O->uvf, UIDX(O->c.N3[3] + 1)), 0, sizeof(cplx) * nc);
   memset(PL(O->wvf, UIDX(O->c.N3[3] + 1)), 0, sizeof(cplx) * nc);
 
-  /* y-derivatives and assembly (FOU3D.f90:262-283, 636-676) */
-  for (int ju = ulo; ju <= uhi; ++ju) {
-    double th = O->thu[UIDX(ju)];
-    for (int c = 0; c < nc; ++c) {
-      cplx d1 = (PL(O->uvf, UIDX(ju))[c] - PL(O->uvf, UIDX(ju - 1))[c]) * th * dd;
-      cplx d3 = (PL(O->wvf, UIDX(ju))[c] - PL(O->wvf, UIDX(ju - 1))[c]) * th * dd;
-      PL(O->Nu1, UIDX(ju))[c] = PL(O->N1xz, UIDX(ju))[c] + d1;
-      PL(O->Nu3, UIDX(ju))[c] = PL(O->N3xz, UIDX(ju))[c] + d3;
-    }
-  }
-  for (int jv = vlo; jv <= vhi; ++jv) {
-    double th = O->thv[UIDX(jv)];
-    for (int c = 0; c < nc; ++c) {
-      cplx d2 = (PL(O->vvc, UIDX(jv + 1))[c] - PL(O->vvc, UIDX(jv))[c]) * th * dd;
-      PL(O->Nu2, UIDX(jv))[c] = PL(O->N2xz, UIDX(jv))[c] + d2;
+  /* y-derivatives and assembly over every band's interior levels (FOU3D.f90:262-283,
+   * 636-676); a short column's band-end flux level lies on a core plane, which holds
+   * no short modes: its flux is zero, as the reference's transposes leave it */
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nc; ++c) {
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      for (int ju = O->bj[b][0][0] + 1; ju <= O->bj[b][0][1] - 1; ++ju) {
+        double th = O->thu[UIDX(ju)];
+        cplx d1 = (PL(O->uvf, UIDX(ju))[c] - PL(O->uvf, UIDX(ju - 1))[c]) * th * dd;
+        cplx d3 = (PL(O->wvf, UIDX(ju))[c] - PL(O->wvf, UIDX(ju - 1))[c]) * th * dd;
+        PL(O->Nu1, UIDX(ju))[c] = PL(O->N1xz, UIDX(ju))[c] + d1;
+        PL(O->Nu3, UIDX(ju))[c] = PL(O->N3xz, UIDX(ju))[c] + d3;
+      }
+      for (int jv = O->bj[b][1][0] + 1; jv <= O->bj[b][1][1] - 1; ++jv) {
+        double th = O->thv[UIDX(jv)];
+        cplx d2 = (PL(O->vvc, UIDX(jv + 1))[c] - PL(O->vvc, UIDX(jv))[c]) * th * dd;
+        PL(O->Nu2, UIDX(jv))[c] = PL(O->N2xz, UIDX(jv))[c] + d2;
+      }
     }
   }
 
@@ -666,10 +737,12 @@ static void imm_bounds(orc *O, cplx *du, const double *uphys, int nlist, const i
 #pragma omp parallel
     {
       pwork w; pwork_init(O, &w);
+      pview vf;
+      view_of(O, 1, &vf);
       double *ph = (double *)malloc(sizeof(double) * pp);
 #pragma omp for schedule(dynamic)
       for (int j = ranges[rg][0]; j <= ranges[rg][1]; ++j) {
-        four_to_phys_plane(O, PL(du, UIDX(j)), ph, &w);
+        four_to_phys_plane(O, &vf, PL(du, UIDX(j)), ph, &w);
         for (int e = 0; e < nlist; ++e) {
           const int32_t *L = list + 6 * (size_t)e;
           if (L[2] != j) continue;
@@ -677,7 +750,7 @@ static void imm_bounds(orc *O, cplx *du, const double *uphys, int nlist, const i
           double u = uphys[pp * UIDX(j) + (size_t)(L[1] - 1) * G1 + (L[0] - 1)];
           ph[(size_t)(L[1] - 1) * G1 + (L[0] - 1)] = Kibdt * (V - u);
         }
-        phys_to_four_plane(O, ph, PL(du, UIDX(j)), &w);
+        phys_to_four_plane(O, &vf, ph, PL(du, UIDX(j)), &w);
       }
       free(ph);
       pwork_free(&w);
@@ -741,12 +814,15 @@ static double flowrateIm(const orc *O) {
 
 static void divergence(orc *O) {
   const double dd = O->c.ddthetavi;
-  for (int j = O->c.N4[0] + 1; j <= O->c.N4[3]; ++j) {
-    double th = dd * O->thu[UIDX(j)];
-    for (int r = 0; r < O->N2; ++r)
-      for (int kx = 0; kx < O->N1h; ++kx) {
-        int c = r * O->N1h + kx;
-        cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[r];
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < O->ncol; ++c) {
+    const int r = c / O->N1h, kx = c % O->N1h;
+    cplx kxF = I * O->k1x[kx], kzF = I * O->k1z[r];
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi)
+      for (int j = O->bj[bs[sgi]][2][0]; j <= O->bj[bs[sgi]][2][1]; ++j) {
+        double th = dd * O->thu[UIDX(j)];
         PL(O->div, PIDX(j))[c] = kxF * PL(O->u1, UIDX(j))[c] + kzF * PL(O->u3, UIDX(j))[c]
                                  + th * (PL(O->u2, UIDX(j))[c] - PL(O->u2, UIDX(j - 1))[c]);
       }
@@ -765,17 +841,19 @@ int orc_substep(orc *O, int kRK) {
   const int nc = O->ncol, N1h = O->N1h;
   const double C1 = O->c.aRK[kRK - 1] / O->c.Re, C2 = -O->c.cRK[kRK - 1];
   const double dR = O->c.dRK[kRK - 1];
-  const int ulo = O->c.N4[0] + 1, uhi = O->c.N4[3], vlo = O->c.N3[0] + 1, vhi = O->c.N3[3];
 
-  /* RHS0_u1 / RHS0_u3 (littleharsh.f90:635-679, 739-788) */
+  /* RHS0_u1 / RHS0_u3 / RHS0_u2 (littleharsh.f90:635-788) over every band's interior levels */
 #pragma omp parallel for schedule(static)
-  for (int j = ulo; j <= uhi; ++j) {
-    const double a = O->d2u[0 * O->nu + UIDX(j)], b = O->d2u[1 * O->nu + UIDX(j)];
-    const double cc = O->d2u[2 * O->nu + UIDX(j)];
-    for (int r = 0; r < O->N2; ++r)
-      for (int kx = 0; kx < N1h; ++kx) {
-        int c = r * N1h + kx;
-        double dg = O->k2x[kx] + O->k2z[r] + b;
+  for (int c = 0; c < nc; ++c) {
+    const int r = c / N1h, kx = c % N1h;
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      for (int j = O->bj[b][0][0] + 1; j <= O->bj[b][0][1] - 1; ++j) {
+        const double a = O->d2u[0 * O->nu + UIDX(j)], bb = O->d2u[1 * O->nu + UIDX(j)];
+        const double cc = O->d2u[2 * O->nu + UIDX(j)];
+        double dg = O->k2x[kx] + O->k2z[r] + bb;
         cplx L1 = a * PL(O->u1, UIDX(j - 1))[c] + dg * PL(O->u1, UIDX(j))[c] + cc * PL(O->u1, UIDX(j + 1))[c];
         cplx L3 = a * PL(O->u3, UIDX(j - 1))[c] + dg * PL(O->u3, UIDX(j))[c] + cc * PL(O->u3, UIDX(j + 1))[c];
         cplx C3x = -dR * (I * O->k1x[kx]);
@@ -783,23 +861,18 @@ int orc_substep(orc *O, int kRK) {
         cplx pj = PL(O->p, PIDX(j))[c];
         PL(O->du1, UIDX(j))[c] = C1 * L1 + C2 * PL(O->Nu1, UIDX(j))[c] + C3x * pj;
         PL(O->du3, UIDX(j))[c] = C1 * L3 + C2 * PL(O->Nu3, UIDX(j))[c] + C3z * pj;
+        if (c == 0) PL(O->du1, UIDX(j))[0] = PL(O->du1, UIDX(j))[0] + (-dR * O->mpgx);
       }
-    PL(O->du1, UIDX(j))[0] = PL(O->du1, UIDX(j))[0] + (-dR * O->mpgx);
-  }
-  /* RHS0_u2 (littleharsh.f90:681-737) */
-#pragma omp parallel for schedule(static)
-  for (int j = vlo; j <= vhi; ++j) {
-    const double a = O->d2v[0 * O->nv + UIDX(j)], b = O->d2v[1 * O->nv + UIDX(j)];
-    const double cc = O->d2v[2 * O->nv + UIDX(j)];
-    const double C3 = -dR * O->c.ddthetavi * O->thv[UIDX(j)];
-    for (int r = 0; r < O->N2; ++r)
-      for (int kx = 0; kx < N1h; ++kx) {
-        int c = r * N1h + kx;
-        double dg = O->k2x[kx] + O->k2z[r] + b;
+      for (int j = O->bj[b][1][0] + 1; j <= O->bj[b][1][1] - 1; ++j) {
+        const double a = O->d2v[0 * O->nv + UIDX(j)], bb = O->d2v[1 * O->nv + UIDX(j)];
+        const double cc = O->d2v[2 * O->nv + UIDX(j)];
+        const double C3 = -dR * O->c.ddthetavi * O->thv[UIDX(j)];
+        double dg = O->k2x[kx] + O->k2z[r] + bb;
         cplx L2 = a * PL(O->u2, UIDX(j - 1))[c] + dg * PL(O->u2, UIDX(j))[c] + cc * PL(O->u2, UIDX(j + 1))[c];
         PL(O->du2, UIDX(j))[c] = C1 * L2 + C2 * PL(O->Nu2, UIDX(j))[c]
                                  + C3 * (PL(O->p, PIDX(j + 1))[c] - PL(O->p, PIDX(j))[c]);
       }
+    }
   }
 
   nonlinear(O, kRK);
@@ -807,14 +880,19 @@ int orc_substep(orc *O, int kRK) {
   /* du += -gRK * Nu (FOU3D.f90:399-410) */
   const double G = -O->c.gRK[kRK - 1];
 #pragma omp parallel for schedule(static)
-  for (int j = ulo; j <= uhi; ++j)
-    for (int c = 0; c < nc; ++c) {
-      PL(O->du1, UIDX(j))[c] = PL(O->du1, UIDX(j))[c] + G * PL(O->Nu1, UIDX(j))[c];
-      PL(O->du3, UIDX(j))[c] = PL(O->du3, UIDX(j))[c] + G * PL(O->Nu3, UIDX(j))[c];
+  for (int c = 0; c < nc; ++c) {
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      for (int j = O->bj[b][0][0] + 1; j <= O->bj[b][0][1] - 1; ++j) {
+        PL(O->du1, UIDX(j))[c] = PL(O->du1, UIDX(j))[c] + G * PL(O->Nu1, UIDX(j))[c];
+        PL(O->du3, UIDX(j))[c] = PL(O->du3, UIDX(j))[c] + G * PL(O->Nu3, UIDX(j))[c];
+      }
+      for (int j = O->bj[b][1][0] + 1; j <= O->bj[b][1][1] - 1; ++j)
+        PL(O->du2, UIDX(j))[c] = PL(O->du2, UIDX(j))[c] + G * PL(O->Nu2, UIDX(j))[c];
     }
-#pragma omp parallel for schedule(static)
-  for (int j = vlo; j <= vhi; ++j)
-    for (int c = 0; c < nc; ++c) PL(O->du2, UIDX(j))[c] = PL(O->du2, UIDX(j))[c] + G * PL(O->Nu2, UIDX(j))[c];
+  }
 
   if (O->c.ib_enable && O->dny > 0) {
     int d = O->dny, nn = O->nn;
@@ -823,117 +901,128 @@ int orc_substep(orc *O, int kRK) {
     imm_bounds(O, O->du3, O->phys_u3, O->c.nib_u, O->lu, O->Au, -d + 1, 0, nn + 2, nn + 1 + d);
   }
 
-  /* solveU_W (littleharsh.f90:791-828, tridLU_3D.f90:55-132, 257-291) */
+  /* solveU_W and solveV per band (littleharsh.f90:791-907, tridLU_3D.f90:55-189, 257-329):
+   * rows jlim(1)..jlim(2) of the band, BC rows [1, gridweighting(b,1)] and
+   * [gridweighting(b,2), 1] for u and w, identity rows for v */
   const double dt = O->dt;
   const double beta = O->c.bRK[kRK - 1] * dt / O->c.Re;
-  const int lo = O->c.N4[0], hi = O->c.N4[3] + 1, n = hi - lo + 1;
 #pragma omp parallel
   {
-    double *a1 = (double *)malloc(sizeof(double) * n), *a2 = (double *)malloc(sizeof(double) * n);
-    double *a3 = (double *)malloc(sizeof(double) * n);
+    const int nmax = O->nu + 2;
+    double *a1 = (double *)malloc(sizeof(double) * nmax), *a2 = (double *)malloc(sizeof(double) * nmax);
+    double *a3 = (double *)malloc(sizeof(double) * nmax);
 #pragma omp for schedule(static)
     for (int c = 0; c < nc; ++c) {
       int r = c / N1h, kx = c % N1h;
-      PL(O->du1, UIDX(lo))[c] = 0; PL(O->du3, UIDX(lo))[c] = 0;
-      for (int j = lo + 1; j <= hi - 1; ++j) {
-        PL(O->du1, UIDX(j))[c] = PL(O->u1, UIDX(j))[c] + dt * PL(O->du1, UIDX(j))[c];
-        PL(O->du3, UIDX(j))[c] = PL(O->u3, UIDX(j))[c] + dt * PL(O->du3, UIDX(j))[c];
-      }
-      PL(O->du1, UIDX(hi))[c] = 0; PL(O->du3, UIDX(hi))[c] = 0;
       double k2x = O->k2x[kx], k2z = O->k2z[r];
-      a1[0] = 0.0; a2[0] = 1.0; a3[0] = O->c.gw[1][0];
-      for (int j = lo + 1; j <= hi - 1; ++j) {
-        int q = j - lo;
-        a1[q] = -beta * O->d2u[0 * O->nu + UIDX(j)];
-        a2[q] = 1.0 - beta * (O->d2u[1 * O->nu + UIDX(j)] + k2x + k2z);
-        a3[q] = -beta * O->d2u[2 * O->nu + UIDX(j)];
+      int bs[2];
+      const int ns = col_bands(O, c, bs);
+      for (int sgi = 0; sgi < ns; ++sgi) {
+        const int b = bs[sgi];
+        int lo = O->bj[b][0][0], hi = O->bj[b][0][1], n = hi - lo + 1;
+        PL(O->du1, UIDX(lo))[c] = 0; PL(O->du3, UIDX(lo))[c] = 0;
+        for (int j = lo + 1; j <= hi - 1; ++j) {
+          PL(O->du1, UIDX(j))[c] = PL(O->u1, UIDX(j))[c] + dt * PL(O->du1, UIDX(j))[c];
+          PL(O->du3, UIDX(j))[c] = PL(O->u3, UIDX(j))[c] + dt * PL(O->du3, UIDX(j))[c];
+        }
+        PL(O->du1, UIDX(hi))[c] = 0; PL(O->du3, UIDX(hi))[c] = 0;
+        a1[0] = 0.0; a2[0] = 1.0; a3[0] = O->c.gw[b][0];
+        for (int j = lo + 1; j <= hi - 1; ++j) {
+          int q = j - lo;
+          a1[q] = -beta * O->d2u[0 * O->nu + UIDX(j)];
+          a2[q] = 1.0 - beta * (O->d2u[1 * O->nu + UIDX(j)] + k2x + k2z);
+          a3[q] = -beta * O->d2u[2 * O->nu + UIDX(j)];
+        }
+        a1[n - 1] = O->c.gw[b][1]; a2[n - 1] = 1.0; a3[n - 1] = 0.0;
+        lu_dec(a1, a2, a3, n);
+        for (int j = 0; j < n; ++j) {
+          PL(O->u1, UIDX(lo + j))[c] = PL(O->du1, UIDX(lo + j))[c];
+          PL(O->u3, UIDX(lo + j))[c] = PL(O->du3, UIDX(lo + j))[c];
+        }
+        lu_sol(a1, a2, a3, PL(O->u1, UIDX(lo)) + c, n, (size_t)nc);
+        lu_sol(a1, a2, a3, PL(O->u3, UIDX(lo)) + c, n, (size_t)nc);
+
+        int vlo0 = O->bj[b][1][0], vhi0 = O->bj[b][1][1], nvv = vhi0 - vlo0 + 1;
+        PL(O->du2, UIDX(vlo0))[c] = 0;
+        for (int j = vlo0 + 1; j <= vhi0 - 1; ++j)
+          PL(O->du2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] + dt * PL(O->du2, UIDX(j))[c];
+        PL(O->du2, UIDX(vhi0))[c] = 0;
+        a1[0] = 0.0; a2[0] = 1.0; a3[0] = 0.0;
+        for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
+          int q = j - vlo0;
+          a1[q] = -beta * O->d2v[0 * O->nv + UIDX(j)];
+          a2[q] = 1.0 - beta * (O->d2v[1 * O->nv + UIDX(j)] + k2x + k2z);
+          a3[q] = -beta * O->d2v[2 * O->nv + UIDX(j)];
+        }
+        a1[nvv - 1] = 0.0; a2[nvv - 1] = 1.0; a3[nvv - 1] = 0.0;
+        lu_dec(a1, a2, a3, nvv);
+        for (int j = 0; j < nvv; ++j) PL(O->u2, UIDX(vlo0 + j))[c] = PL(O->du2, UIDX(vlo0 + j))[c];
+        lu_sol(a1, a2, a3, PL(O->u2, UIDX(vlo0)) + c, nvv, (size_t)nc);
       }
-      a1[n - 1] = O->c.gw[1][1]; a2[n - 1] = 1.0; a3[n - 1] = 0.0;
-      lu_dec(a1, a2, a3, n);
-      for (int j = 0; j < n; ++j) {
-        PL(O->u1, UIDX(lo + j))[c] = PL(O->du1, UIDX(lo + j))[c];
-        PL(O->u3, UIDX(lo + j))[c] = PL(O->du3, UIDX(lo + j))[c];
-      }
-      lu_sol(a1, a2, a3, PL(O->u1, UIDX(lo)) + c, n, (size_t)nc);
-      lu_sol(a1, a2, a3, PL(O->u3, UIDX(lo)) + c, n, (size_t)nc);
-    }
-    free(a1); free(a2); free(a3);
-  }
-  /* solveV (littleharsh.f90:877-907, tridLU_3D.f90:135-189, 294-329) */
-  const int vlo0 = O->c.N3[0], vhi0 = O->c.N3[3] + 1, nvv = vhi0 - vlo0 + 1;
-#pragma omp parallel
-  {
-    double *a1 = (double *)malloc(sizeof(double) * nvv), *a2 = (double *)malloc(sizeof(double) * nvv);
-    double *a3 = (double *)malloc(sizeof(double) * nvv);
-#pragma omp for schedule(static)
-    for (int c = 0; c < nc; ++c) {
-      int r = c / N1h, kx = c % N1h;
-      PL(O->du2, UIDX(vlo0))[c] = 0;
-      for (int j = vlo0 + 1; j <= vhi0 - 1; ++j)
-        PL(O->du2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] + dt * PL(O->du2, UIDX(j))[c];
-      PL(O->du2, UIDX(vhi0))[c] = 0;
-      double k2x = O->k2x[kx], k2z = O->k2z[r];
-      a1[0] = 0.0; a2[0] = 1.0; a3[0] = 0.0;
-      for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
-        int q = j - vlo0;
-        a1[q] = -beta * O->d2v[0 * O->nv + UIDX(j)];
-        a2[q] = 1.0 - beta * (O->d2v[1 * O->nv + UIDX(j)] + k2x + k2z);
-        a3[q] = -beta * O->d2v[2 * O->nv + UIDX(j)];
-      }
-      a1[nvv - 1] = 0.0; a2[nvv - 1] = 1.0; a3[nvv - 1] = 0.0;
-      lu_dec(a1, a2, a3, nvv);
-      for (int j = 0; j < nvv; ++j) PL(O->u2, UIDX(vlo0 + j))[c] = PL(O->du2, UIDX(vlo0 + j))[c];
-      lu_sol(a1, a2, a3, PL(O->u2, UIDX(vlo0)) + c, nvv, (size_t)nc);
     }
     free(a1); free(a2); free(a3);
   }
 
   if (O->c.flag_ctpress == 0) flowrate_corr(O, kRK);
 
-  /* solveP (littleharsh.f90:581-633) */
+  /* solveP (littleharsh.f90:581-633): per band, LUsolP over jlim(1:2, pgrid, b) */
   divergence(O);
   const double dtirk = O->dti / (O->c.aRK[kRK - 1] + O->c.bRK[kRK - 1]);
-  const int pns = O->c.N4[0] + 1, pne = O->c.N4[3], npn = pne - pns + 1;
   for (size_t e = 0; e < (size_t)nc * O->np; ++e) O->psi[e] = dtirk * O->div[e];
-  PL(O->psi, PIDX(pns))[0] = 0.0;
+  PL(O->psi, PIDX(O->c.N4[0] + 1))[0] = 0.0;
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < nc; ++c) {
-    cplx *x = PL(O->psi, PIDX(pns)) + c;
-    const double *D = O->DG;
-#define DGA(cc, q) D[((size_t)(q) * nc + c) * 3 + (cc) - 1]
-    x[0] = x[0] * DGA(2, 0);
-    for (int q = 1; q < npn; ++q) x[(size_t)q * nc] = (x[(size_t)q * nc] - DGA(1, q) * x[(size_t)(q - 1) * nc]) * DGA(2, q);
-    for (int q = npn - 2; q >= 0; --q) x[(size_t)q * nc] = x[(size_t)q * nc] - DGA(3, q) * x[(size_t)(q + 1) * nc];
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      const int q0 = PIDX(O->bj[b][2][0]), npn = O->bj[b][2][1] - O->bj[b][2][0] + 1;
+      cplx *x = PL(O->psi, q0) + c;
+      const double *D = O->DG;
+#define DGA(cc, q) D[((size_t)(q0 + (q)) * nc + c) * 3 + (cc) - 1]
+      x[0] = x[0] * DGA(2, 0);
+      for (int q = 1; q < npn; ++q) x[(size_t)q * nc] = (x[(size_t)q * nc] - DGA(1, q) * x[(size_t)(q - 1) * nc]) * DGA(2, q);
+      for (int q = npn - 2; q >= 0; --q) x[(size_t)q * nc] = x[(size_t)q * nc] - DGA(3, q) * x[(size_t)(q + 1) * nc];
 #undef DGA
+    }
   }
   for (size_t e = 0; e < (size_t)nc * O->np; ++e) O->p[e] = O->p[e] + O->psi[e];
 
-  /* v_corr (littleharsh.f90:956-1052) */
+  /* v_corr (littleharsh.f90:956-1052): interior of every band; the wall ghosts of
+   * bands 1, 2 (bottom) and 2, 3 (top) from gridweighting_bc; v = 0 at band ends */
   const double dtrk = dt * (O->c.aRK[kRK - 1] + O->c.bRK[kRK - 1]);
+  const double dtrk_u2 = dtrk * O->c.ddthetavi;
 #pragma omp parallel for schedule(static)
-  for (int j = lo + 1; j <= hi - 1; ++j)
-    for (int r = 0; r < O->N2; ++r)
-      for (int kx = 0; kx < N1h; ++kx) {
-        int c = r * N1h + kx;
-        cplx kxc = (cplx)dtrk * (I * O->k1x[kx]);
-        cplx kzc = (cplx)dtrk * (I * O->k1z[r]);
+  for (int c = 0; c < nc; ++c) {
+    const int r = c / N1h, kx = c % N1h;
+    cplx kxc = (cplx)dtrk * (I * O->k1x[kx]);
+    cplx kzc = (cplx)dtrk * (I * O->k1z[r]);
+    int bs[2];
+    const int ns = col_bands(O, c, bs);
+    for (int sgi = 0; sgi < ns; ++sgi) {
+      const int b = bs[sgi];
+      const int lo = O->bj[b][0][0], hi = O->bj[b][0][1];
+      for (int j = lo + 1; j <= hi - 1; ++j) {
         PL(O->u1, UIDX(j))[c] = PL(O->u1, UIDX(j))[c] - kxc * PL(O->psi, PIDX(j))[c];
         PL(O->u3, UIDX(j))[c] = PL(O->u3, UIDX(j))[c] - kzc * PL(O->psi, PIDX(j))[c];
       }
-  for (int c = 0; c < nc; ++c) {
-    PL(O->u1, UIDX(lo))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(lo + 1))[c];
-    PL(O->u1, UIDX(hi))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(hi - 1))[c];
-    PL(O->u3, UIDX(lo))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(lo + 1))[c];
-    PL(O->u3, UIDX(hi))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(hi - 1))[c];
+      if (b <= 1) {
+        PL(O->u1, UIDX(lo))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(lo + 1))[c];
+        PL(O->u3, UIDX(lo))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(lo + 1))[c];
+      }
+      if (b >= 1) {
+        PL(O->u1, UIDX(hi))[c] = O->c.gw_bc_u1 * PL(O->u1, UIDX(hi - 1))[c];
+        PL(O->u3, UIDX(hi))[c] = O->c.gw_bc_u3 * PL(O->u3, UIDX(hi - 1))[c];
+      }
+      const int vlo0 = O->bj[b][1][0], vhi0 = O->bj[b][1][1];
+      for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
+        double f = dtrk_u2 * O->thv[UIDX(j)];
+        PL(O->u2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] - f * (PL(O->psi, PIDX(j + 1))[c] - PL(O->psi, PIDX(j))[c]);
+      }
+      PL(O->u2, UIDX(vlo0))[c] = 0;
+      PL(O->u2, UIDX(vhi0))[c] = 0;
+    }
   }
-  const double dtrk_u2 = dtrk * O->c.ddthetavi;
-#pragma omp parallel for schedule(static)
-  for (int j = vlo0 + 1; j <= vhi0 - 1; ++j) {
-    double f = dtrk_u2 * O->thv[UIDX(j)];
-    for (int c = 0; c < nc; ++c)
-      PL(O->u2, UIDX(j))[c] = PL(O->u2, UIDX(j))[c] - f * (PL(O->psi, PIDX(j + 1))[c] - PL(O->psi, PIDX(j))[c]);
-  }
-  for (int c = 0; c < nc; ++c) { PL(O->u2, UIDX(vlo0))[c] = 0; PL(O->u2, UIDX(vhi0))[c] = 0; }
   divergence(O);
   return 0;
 }
@@ -981,6 +1070,40 @@ int orc_get_state(orc *O, double *u1, double *u2, double *u3, double *p) {
   if (p) get_field(O, O->p, O->np, p);
   return 0;
 }
+/* one band's cfield f(level, column) <-> the wall-grid layout: the band's columns in
+ * wall-grid order (columns_i/k, start.f90:1566-1609) over its jlim levels */
+static int band_io(orc *O, int band, int put, double *u1, double *u2, double *u3, double *p) {
+  if (band < 1 || band > 3) return -1;
+  const int b = band - 1;
+  cplx *F[4] = {O->u1, O->u2, O->u3, O->p};
+  double *H[4] = {u1, u2, u3, p};
+  const int grid[4] = {0, 1, 0, 2};
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    const int lo = O->bj[b][grid[f]][0], hi = O->bj[b][grid[f]][1], nl = hi - lo + 1;
+    const int base = (f == 3) ? PIDX(lo) : UIDX(lo);
+    size_t k = 0;
+    for (int c = 0; c < O->ncol; ++c) {
+      const int isl = !O->mb || O->lng[c];
+      if ((b == 1) != isl) continue;
+      for (int l = 0; l < nl; ++l) {
+        double *h = H[f] + 2 * (k * nl + l);
+        cplx *d = &F[f][(size_t)(base + l) * O->ncol + c];
+        if (put) *d = h[0] + I * h[1];
+        else { h[0] = creal(*d); h[1] = cimag(*d); }
+      }
+      ++k;
+    }
+  }
+  return 0;
+}
+int orc_set_band(orc *O, int band, const double *u1, const double *u2, const double *u3, const double *p) {
+  return band_io(O, band, 1, (double *)u1, (double *)u2, (double *)u3, (double *)p);
+}
+int orc_get_band(orc *O, int band, double *u1, double *u2, double *u3, double *p) {
+  return band_io(O, band, 0, u1, u2, u3, p);
+}
+
 /* Nu1/Nu2/Nu3 of the last substep, same layout (levels of u, v, u) */
 int orc_get_nonlinear(orc *O, double *n1, double *n2, double *n3) {
   if (n1) get_field(O, O->Nu1, O->nu, n1);
@@ -1012,9 +1135,11 @@ int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes) {
 #pragma omp parallel
   {
     pwork w; pwork_init(O, &w);
+    pview vf;
+    view_of(O, 1, &vf);
 #pragma omp for
     for (int q = 0; q < nplanes; ++q)
-      four_to_phys_plane(O, (const cplx *)spec + ns * q, phys + pp * q, &w);
+      four_to_phys_plane(O, &vf, (const cplx *)spec + ns * q, phys + pp * q, &w);
     pwork_free(&w);
   }
   return 0;
@@ -1024,9 +1149,11 @@ int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes) {
 #pragma omp parallel
   {
     pwork w; pwork_init(O, &w);
+    pview vf;
+    view_of(O, 1, &vf);
 #pragma omp for
     for (int q = 0; q < nplanes; ++q)
-      phys_to_four_plane(O, phys + pp * q, (cplx *)spec + ns * q, &w);
+      phys_to_four_plane(O, &vf, phys + pp * q, (cplx *)spec + ns * q, &w);
     pwork_free(&w);
   }
   return 0;

@@ -9,6 +9,8 @@ orc *orc_create(const lh_config *cfg);
 void orc_destroy(orc *O);
 int orc_set_state(orc *O, const double *u1, const double *u2, const double *u3, const double *p);
 int orc_get_state(orc *O, double *u1, double *u2, double *u3, double *p);
+int orc_set_band(orc *O, int band, const double *u1, const double *u2, const double *u3, const double *p);
+int orc_get_band(orc *O, int band, double *u1, double *u2, double *u3, double *p);
 int orc_get_nonlinear(orc *O, double *n1, double *n2, double *n3);
 int orc_set_scalars(orc *O, const lh_scalars *s);
 int orc_get_scalars(orc *O, lh_scalars *s);

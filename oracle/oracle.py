@@ -36,6 +36,8 @@ def lib():
         L.orc_create.restype = vp
         L.orc_create.argtypes = [vp]
         L.orc_destroy.argtypes = [vp]
+        for f in ("orc_set_band", "orc_get_band"):
+            getattr(L, f).argtypes = [vp, C.c_int] + [dp] * 4
         for f in ("orc_set_state", "orc_get_state", "orc_get_nonlinear"):
             getattr(L, f).argtypes = [vp] + [dp] * (4 if f != "orc_get_nonlinear" else 3)
         L.orc_set_scalars.argtypes = [vp, vp]
@@ -83,6 +85,24 @@ class Oracle:
             if a is not None and a.shape != sh:
                 raise ValueError(f"shape {a.shape} != {sh}")
         lib().orc_set_state(self.h, *[_dptr(a) for a in arrs])
+
+    def set_bands(self, bands: dict):
+        """{band: (u1, u2, u3, p)} in the bands' cfield layouts (ChannelSetup.band_shapes)."""
+        for b, arrs in bands.items():
+            arrs = [np.ascontiguousarray(a, np.complex128) for a in arrs]
+            for a, sh in zip(arrs, self.s.band_shapes(b)):
+                if a.shape != sh:
+                    raise ValueError(f"band {b}: shape {a.shape} != {sh}")
+            if lib().orc_set_band(self.h, b, *[_dptr(a) for a in arrs]) != 0:
+                raise ValueError("orc_set_band failed")
+
+    def get_bands(self) -> dict:
+        out = {}
+        for b in (1, 2, 3):
+            arrs = [np.zeros(sh, np.complex128) for sh in self.s.band_shapes(b)]
+            lib().orc_get_band(self.h, b, *[_dptr(a) for a in arrs])
+            out[b] = arrs
+        return out
 
     def get_state(self):
         out = [np.zeros(sh, np.complex128) for sh in self.shapes]

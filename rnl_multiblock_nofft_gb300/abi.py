@@ -40,6 +40,7 @@ class LhConfig(C.Structure):
         ("nonlin_form", C.c_int32), ("triad_nx", C.c_int32), ("triad_nz", C.c_int32),
         ("triad_nsets", C.c_int32), ("triad_off", _lp), ("triad_len", _lp), ("triad_data", _bp),
         ("triad_set_u", _ip), ("triad_set_v", _ip),
+        ("N1c", C.c_int32), ("N2c", C.c_int32), ("Ngal1c", C.c_int32), ("Ngal2c", C.c_int32),
     ]
 
 
@@ -57,10 +58,9 @@ def _ptr(a: np.ndarray, typ):
 
 
 def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
-    """Returns (LhConfig, keepalive) for a single-resolution channel. `triads` (a
-    triads.TriadLists) selects the triad-list nonlinear form; None the FFT products."""
-    if s.multiblock:
-        raise ValueError("bands with different x/z resolution are not supported by this build")
+    """Returns (LhConfig, keepalive) for a channel (single-resolution or multiblock).
+    `triads` (a triads.TriadLists) selects the triad-list nonlinear form; None the
+    FFT products."""
     keep = []
 
     def d(a):
@@ -78,6 +78,7 @@ def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
     c.precision = precision
     c.N1, c.N2 = s.N1, s.N2
     c.Ngal1, c.Ngal2 = s.G1, s.G2
+    c.N1c, c.N2c, c.Ngal1c, c.Ngal2c = s.N1c, s.N2c, s.G1c, s.G2c
     c.dny, c.nn = s.dny, s.nn
     for b in range(4):
         c.N3[b] = int(s.N[2, b])
@@ -124,5 +125,6 @@ def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
 
 
 def cfield_shape(s: ChannelSetup):
-    """Host cfield shapes (ncols, nlevels) of u1, u2, u3, p."""
+    """Host cfield shapes (ncols, nlevels) of u1, u2, u3, p (single-resolution
+    channels; multiblock channels use ChannelSetup.band_shapes)."""
     return ((s.ncols, s.nyu), (s.ncols, s.nyv), (s.ncols, s.nyu), (s.ncols, s.nyu - 2))

@@ -46,6 +46,15 @@ struct lh_handle {
   int *d_lu, *d_lv, *d_capslot, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
   double *d_Au, *d_Av, *cap, *duphys;
   double2 *duib;
+  // plane views of the nonlinear launches: wall-band planes, then core planes
+  // (multiblock); one view when single-resolution
+  Geo gv[2];
+  int nviews;
+  int *d_slotq, *d_capv;    // slot -> level of the views; capture slot of view 0's slots
+  void *twv[2][2];          // twiddles of the views (x, z) in the transform precision
+  int2 *d_vcol;             // virtual columns of the solve kernels (multiblock)
+  int *d_bcols;             // long columns, then short columns (band I/O)
+  int nlong, nshort;
   // triad-list nonlinear form
   int triad;
   TriadGeo tg;
@@ -178,7 +187,8 @@ static int set_smem_attrs_all(lh_handle *h) {
   int lim = 0;
   if (smem_optin(&lim)) return fail(h, LH_ECUDA, "cudaDeviceGetAttribute");
   cudaError_t e = cudaSuccess;
-  for (int n : {h->g.G1, h->g.G2}) {
+  for (int n : {h->g.G1, h->g.G2, h->gv[1].G1, h->gv[1].G2}) {
+    if (n <= 0) continue;
     LH_DISPATCH(n, e = set_attrs_sized<double, N>(lim); if (e == cudaSuccess) e = set_attrs_sized<float, N>(lim));
     if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
   }
@@ -201,6 +211,17 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   if (cfg->nyu != cfg->N4[3] + 1 - cfg->N4[0] + 1 || cfg->nyv != cfg->N3[3] + 1 - cfg->N3[0] + 1 ||
       cfg->nyv != cfg->nyu - 1 || cfg->N4[0] != -cfg->dny || cfg->N3[0] != -cfg->dny || cfg->nyu < 5)
     return fail(nullptr, LH_EINVAL, "band limits inconsistent with nyu / nyv / dny");
+  const int mb = (cfg->N1c != cfg->N1 || cfg->N2c != cfg->N2 || cfg->Ngal1c != cfg->Ngal1 || cfg->Ngal2c != cfg->Ngal2);
+  if (mb) {
+    if (cfg->N1c <= 0 || cfg->N2c <= 0 || cfg->N1c > cfg->N1 || cfg->N2c > cfg->N2 || (cfg->N1c & 1) ||
+        (cfg->N2c & 1) || cfg->Ngal1c <= cfg->N1c || cfg->Ngal2c <= cfg->N2c || !size_supported(cfg->Ngal1c) ||
+        !size_supported(cfg->Ngal2c))
+      return fail(nullptr, LH_EINVAL, "core band: need N1c <= N1, N2c <= N2, even, Ngal1c/Ngal2c supported sizes");
+    if (cfg->N4[2] <= cfg->N4[1] + 1 || cfg->N3[2] <= cfg->N3[1] + 1 || cfg->N4[1] <= cfg->N4[0] + 1)
+      return fail(nullptr, LH_EINVAL, "multiblock: every band needs interior levels");
+    if (cfg->nonlin_form == LH_NONLIN_TRIADS)
+      return fail(nullptr, LH_EINVAL, "triad lists need one x/z resolution in every band");
+  }
   h = new lh_handle();
   memset(&h->g, 0, sizeof(Geo));
   h->cfg = *cfg;
@@ -226,6 +247,41 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   for (int b = 0; b < 3; ++b) { g.gw[b][0] = cfg->gw[b][0]; g.gw[b][1] = cfg->gw[b][1]; }
   g.gwbc1 = cfg->gw_bc_u1; g.gwbc3 = cfg->gw_bc_u3;
+  // multiblock description: wall-band grid, band level ranges (jlim, start.f90:1675-1709)
+  g.mb = mb;
+  g.N1hF = g.N1h; g.N2F = g.N2; g.ncolF = g.ncol;
+  g.slotq = nullptr;
+  {
+    const int d = cfg->dny, *N3 = cfg->N3, *N4 = cfg->N4;
+    const int bq[3][6] = {{N4[0] + d, N4[1] + 1 + d, N3[0] + d, N3[1] + 1 + d, N4[0] + d, N4[1] + d - 1},
+                          {N4[0] + d, N4[3] + 1 + d, N3[0] + d, N3[3] + 1 + d, N4[0] + d, N4[3] + d - 1},
+                          {N4[2] + d, N4[3] + 1 + d, N3[2] + d, N3[3] + 1 + d, N4[2] + d, N4[3] + d - 1}};
+    memcpy(g.bq, bq, sizeof(bq));
+  }
+  // long columns (modes of the core band) and short columns (wall bands only)
+  std::vector<int> longc, shortc;
+  for (int c = 0; c < g.ncol; ++c) {
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const bool lg = !mb || (kx <= cfg->N1c / 2 && (r < cfg->N2c / 2 || r >= g.N2 - cfg->N2c / 2));
+    (lg ? longc : shortc).push_back(c);
+  }
+  h->nlong = (int)longc.size(); h->nshort = (int)shortc.size();
+  g.nvc = mb ? h->nlong + 2 * h->nshort : g.ncol;
+  g.vcol = nullptr;
+  // plane views: u planes N(4,0)+1..N(4,1), N(4,2)+1..N(4,3) and v planes N(3,0)+1..N(3,1),
+  // N(3,2)+1..N(3,3) are wall-band planes (proc_lims_planes, start.f90:1836-1916)
+  std::vector<int> vsl[2][2];
+  for (int q = 1; q <= g.nu - 2; ++q) {
+    const int j = q - cfg->dny;
+    vsl[(!mb || j <= cfg->N4[1] || j > cfg->N4[2]) ? 0 : 1][0].push_back(q);
+  }
+  for (int q = 1; q <= g.nv - 2; ++q) {
+    const int j = q - cfg->dny;
+    vsl[(!mb || j <= cfg->N3[1] || j > cfg->N3[2]) ? 0 : 1][1].push_back(q);
+  }
+  h->nviews = mb ? 2 : 1;
+  // view sizes (the views themselves are filled once the geometry pools exist)
+  const int vN1h[2] = {g.N1h, cfg->N1c / 2 + 1}, vG2[2] = {g.G2, cfg->Ngal2c};
   g.flag_ctpress = cfg->flag_ctpress;
   const int nu = g.nu, nv = g.nv;
   // geometry pool: yu yv thu thv d2u(3nu) d2v(3nv) k1x k2x k1z k2z iua iub iud iva ivb ivd
@@ -300,8 +356,17 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
   ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
   ZA(h->mfw, sizeof(double) * 6 * (size_t)(g.nn + 3));
-  h->Abytes = vs * (size_t)(g.nuI + g.nvI) * 3 * g.G2 * g.N1h;
-  h->Bbytes = vs * (size_t)(4 * g.nuI + 2 * g.nvI) * g.N1h * g.G2;
+  h->Abytes = h->Bbytes = 0;
+  for (int vi = 0; vi < h->nviews; ++vi) {
+    const size_t nuv = vsl[vi][0].size(), nvv = vsl[vi][1].size();
+    h->Abytes = std::max(h->Abytes, vs * (nuv + nvv) * 3 * vG2[vi] * vN1h[vi]);
+    h->Bbytes = std::max(h->Bbytes, vs * (4 * nuv + 2 * nvv) * vN1h[vi] * vG2[vi]);
+  }
+  {  // the immersed-boundary round trip transforms 3 * 2 * dny planes through A and B
+    const size_t ibp = (cfg->ib_enable && cfg->dny > 0) ? (size_t)6 * cfg->dny : 0;
+    h->Abytes = std::max(h->Abytes, sizeof(double2) * ibp * g.G2 * g.N1h);
+    h->Bbytes = std::max(h->Bbytes, sizeof(double2) * ibp * g.G2 * g.N1h);
+  }
   ZA(h->A, h->Abytes);
   ZA(h->B, h->Bbytes);
   ZA(h->sc, sizeof(DevScalars));
@@ -330,6 +395,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->d_lu = h->d_lv = h->d_capslot = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
   h->d_Au = h->d_Av = h->cap = h->duphys = nullptr;
   h->duib = nullptr;
+  std::vector<int> lev2cap_u(nu, -1), lev2cap_v(nv, -1);  // captured physical planes of the IB forcing
   if (h->ib) {
     const int d = cfg->dny;
     h->nib = 2 * d;
@@ -341,14 +407,13 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
       ibslot_u[qu] = s; ibslot_v[qv] = s;
     }
     // captured levels: u ib levels + the two tip reference levels; v ib levels
-    std::vector<int> capslot(g.nuI + g.nvI, -1), lev2cap_u(nu, -1), lev2cap_v(nv, -1);
     int nc2 = 0;
     for (int q = 1; q <= nu - 2; ++q) {
       bool need = ibslot_u[q] >= 0 || q == d + 1 || q == cfg->nn + 1 + d;
-      if (need) { capslot[q - 1] = nc2; lev2cap_u[q] = nc2; ++nc2; }
+      if (need) { lev2cap_u[q] = nc2; ++nc2; }
     }
     for (int q = 1; q <= nv - 2; ++q)
-      if (ibslot_v[q] >= 0) { capslot[g.nuI + q - 1] = nc2; lev2cap_v[q] = nc2; ++nc2; }
+      if (ibslot_v[q] >= 0) { lev2cap_v[q] = nc2; ++nc2; }
     h->ncap = nc2;
     std::vector<int> lu(cfg->list_ib_u, cfg->list_ib_u + 6 * (size_t)cfg->nib_u);
     std::vector<int> lv(cfg->list_ib_v, cfg->list_ib_v + 6 * (size_t)cfg->nib_v);
@@ -370,7 +435,6 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     std::vector<double> Au(cfg->A_ib_u, cfg->A_ib_u + cfg->nib_u), Av(cfg->A_ib_v, cfg->A_ib_v + cfg->nib_v);
     h->d_lu = (int *)upload_vec(lu, ce); h->d_lv = (int *)upload_vec(lv, ce);
     h->d_Au = (double *)upload_vec(Au, ce); h->d_Av = (double *)upload_vec(Av, ce);
-    h->d_capslot = (int *)upload_vec(capslot, ce);
     h->d_ibslot_u = (int *)upload_vec(ibslot_u, ce); h->d_ibslot_v = (int *)upload_vec(ibslot_v, ce);
     h->d_iblev = (int *)upload_vec(iblev, ce);
     h->d_lev2cap_u = (int *)upload_vec(lev2cap_u, ce); h->d_lev2cap_v = (int *)upload_vec(lev2cap_v, ce);
@@ -385,6 +449,58 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
       cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
     int rc = fail(h, LH_ECUDA, "cudaStreamCreate/cudaEventCreate"); lh_destroy(h); return rc;
+  }
+  {  // views: slot tables, capture slots of view 0, twiddles; solve segments; band columns
+    std::vector<int> slotq, capv;
+    size_t off[2];
+    for (int vi = 0; vi < 2; ++vi) {
+      off[vi] = slotq.size();
+      slotq.insert(slotq.end(), vsl[vi][0].begin(), vsl[vi][0].end());
+      slotq.insert(slotq.end(), vsl[vi][1].begin(), vsl[vi][1].end());
+    }
+    for (int q : vsl[0][0]) capv.push_back(lev2cap_u[q]);
+    for (int q : vsl[0][1]) capv.push_back(lev2cap_v[q]);
+    // every captured level must be a plane of view 0 (the immersed region is in the wall bands)
+    int ncapv = 0;
+    for (int x : capv) ncapv += (x >= 0);
+    if (ncapv != h->ncap) { int rc = fail(h, LH_EINVAL, "immersed region outside the wall bands"); lh_destroy(h); return rc; }
+    h->d_slotq = (int *)upload_vec(slotq, ce);
+    if (ce == cudaSuccess) h->d_capv = (int *)upload_vec(capv, ce);
+    std::vector<int2> vcol;
+    if (mb) {
+      for (int c : longc) vcol.push_back(make_int2(c, 1));
+      for (int c : shortc) vcol.push_back(make_int2(c, 0));
+      for (int c : shortc) vcol.push_back(make_int2(c, 2));
+      if (ce == cudaSuccess) h->d_vcol = (int2 *)upload_vec(vcol, ce);
+    }
+    std::vector<int> bcols(longc);
+    bcols.insert(bcols.end(), shortc.begin(), shortc.end());
+    if (ce == cudaSuccess) h->d_bcols = (int *)upload_vec(bcols, ce);
+    h->twv[0][0] = h->twx; h->twv[0][1] = h->twz;
+    h->twv[1][0] = h->twv[1][1] = nullptr;
+    if (mb && ce == cudaSuccess) {
+      if (h->prec == LH_PREC_FP64) {
+        std::vector<double> tx, tz;
+        twiddles(cfg->Ngal1c, tx); twiddles(cfg->Ngal2c, tz);
+        h->twv[1][0] = upload_vec(tx, ce); if (ce == cudaSuccess) h->twv[1][1] = upload_vec(tz, ce);
+      } else {
+        std::vector<float> tx, tz;
+        twiddles(cfg->Ngal1c, tx); twiddles(cfg->Ngal2c, tz);
+        h->twv[1][0] = upload_vec(tx, ce); if (ce == cudaSuccess) h->twv[1][1] = upload_vec(tz, ce);
+      }
+    }
+    if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
+    g.vcol = mb ? h->d_vcol : nullptr;
+    for (int vi = 0; vi < 2; ++vi) {
+      Geo &gv = h->gv[vi];
+      gv = g;
+      gv.nuI = (int)vsl[vi][0].size(); gv.nvI = (int)vsl[vi][1].size();
+      gv.slotq = mb ? h->d_slotq + off[vi] : nullptr;
+      if (vi == 1) {
+        gv.N1 = cfg->N1c; gv.N2 = cfg->N2c; gv.N1h = cfg->N1c / 2 + 1;
+        gv.G1 = cfg->Ngal1c; gv.G2 = cfg->Ngal2c; gv.ncol = gv.N1h * gv.N2;
+      }
+    }
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
@@ -418,7 +534,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     if (ea != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ea)); lh_destroy(h); return rc; }
   }
   {  // pressure factors, once (start.f90:656-658)
-    const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
+    const int nb = (g.nvc + NTHR_H - 1) / NTHR_H;
     k_build_dg<<<nb, NTHR_H, 0, h->st>>>(h->dg1, h->dg2, h->dg3, g);
     cudaError_t e = cudaStreamSynchronize(h->st);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -445,7 +561,8 @@ extern "C" int lh_destroy(lh_handle *h) {
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
-                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap};
+                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
+                  h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1]};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -489,6 +606,7 @@ static int get_field(lh_handle *h, const double2 *srcd, int nlev, double *dst) {
 
 extern "C" int lh_upload_state(lh_handle *h, const double *u1, const double *u2, const double *u3, const double *p) {
   if (!h) return LH_EINVAL;
+  if (h->g.mb) return fail(h, LH_EINVAL, "multiblock channel: use lh_upload_band");
   int rc;
   if (u1 && (rc = put_field(h, h->u1, h->g.nu, u1))) return rc;
   if (u2 && (rc = put_field(h, h->u2, h->g.nv, u2))) return rc;
@@ -500,11 +618,62 @@ extern "C" int lh_upload_state(lh_handle *h, const double *u1, const double *u2,
 
 extern "C" int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p) {
   if (!h) return LH_EINVAL;
+  if (h->g.mb) return fail(h, LH_EINVAL, "multiblock channel: use lh_download_band");
   int rc;
   if (u1) { if ((rc = get_field(h, h->u1, h->g.nu, u1))) return rc; CK(cudaStreamSynchronize(h->st)); }
   if (u2) { if ((rc = get_field(h, h->u2, h->g.nv, u2))) return rc; CK(cudaStreamSynchronize(h->st)); }
   if (u3) { if ((rc = get_field(h, h->u3, h->g.nu, u3))) return rc; CK(cudaStreamSynchronize(h->st)); }
   if (p) { if ((rc = get_field(h, h->p, h->g.np, p))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  return LH_OK;
+}
+
+// one band's cfield [column][level] (staged on the device) <-> the wall-grid layout
+static int band_field(lh_handle *h, int band, int field, double2 *dev, const double *hin, double *hout) {
+  const int b = band - 1;
+  const int ncb = (band == 2) ? h->nlong : h->nshort;
+  const int *cols = h->d_bcols + ((band == 2) ? 0 : h->nlong);
+  const int lo = h->g.bq[b][field == 3 ? 4 : (field == 1 ? 2 : 0)];
+  const int hi = h->g.bq[b][field == 3 ? 5 : (field == 1 ? 3 : 1)];
+  const int nl = hi - lo + 1;
+  const size_t n = (size_t)ncb * nl;
+  if (n == 0) return LH_OK;
+  const int nb = (int)((n + NTHR_H - 1) / NTHR_H);
+  if (hin) {
+    CK(cudaMemcpyAsync(h->stage, hin, sizeof(double2) * n, cudaMemcpyHostToDevice, h->st));
+    KL("k_band_io", k_band_io<<<nb, NTHR_H, 0, h->st>>>(dev, h->stage, cols, ncb, nl, lo, h->g.ncol, 1));
+  } else {
+    KL("k_band_io", k_band_io<<<nb, NTHR_H, 0, h->st>>>(dev, h->stage, cols, ncb, nl, lo, h->g.ncol, 0));
+    CK(cudaMemcpyAsync(hout, h->stage, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return LH_OK;
+}
+
+extern "C" int lh_upload_band(lh_handle *h, int band, const double *u1, const double *u2, const double *u3,
+                              const double *p) {
+  if (!h) return LH_EINVAL;
+  if (band < 1 || band > 3) return fail(h, LH_EINVAL, "band must be 1, 2 or 3");
+  double2 *F[4] = {h->u1, h->u2, h->u3, h->p};
+  const double *H[4] = {u1, u2, u3, p};
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    int rc = band_field(h, band, f, F[f], H[f], nullptr);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));  // the staging buffer is reused by the next field
+  }
+  return LH_OK;
+}
+
+extern "C" int lh_download_band(lh_handle *h, int band, double *u1, double *u2, double *u3, double *p) {
+  if (!h) return LH_EINVAL;
+  if (band < 1 || band > 3) return fail(h, LH_EINVAL, "band must be 1, 2 or 3");
+  double2 *F[4] = {h->u1, h->u2, h->u3, h->p};
+  double *H[4] = {u1, u2, u3, p};
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    int rc = band_field(h, band, f, F[f], nullptr, H[f]);
+    if (rc) return rc;
+  }
   return LH_OK;
 }
 
@@ -516,7 +685,7 @@ extern "C" int lh_set_scalars(lh_handle *h, const lh_scalars *s) {
   d.QxT = s->QxT; d.Qx = s->Qx; d.iter = s->iter;
   CK(cudaMemcpyAsync(h->sc, &d, sizeof(d), cudaMemcpyHostToDevice, h->st));
   KL("k_flowrate", k_flowrate<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc, h->g.flag_ctpress != 1 ? 1 : 0));
-  const int nb = (h->g.ncol + NTHR_H - 1) / NTHR_H;
+  const int nb = (h->g.nvc + NTHR_H - 1) / NTHR_H;
   KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   KL("k_divmax", k_divmax<<<nb, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, h->g, h->sc));
   KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
@@ -538,52 +707,61 @@ extern "C" int lh_get_scalars(lh_handle *h, lh_scalars *s) {
 // one substep
 // ---------------------------------------------------------------------------
 template <typename T, int N>
-static int launch_zinv(lh_handle *h, int nslots) {
+static int launch_zinv(lh_handle *h, const Geo &g, int nslots, const void *twz) {
   typedef typename C2<T>::t V;
   constexpr int KB = kb_zinv<V>(N);
-  const Geo &g = h->g;
   dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
   KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
-                      h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)h->twz));
+                      h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)twz));
   return LH_OK;
 }
 template <typename T, int N>
-static int launch_xpass(lh_handle *h, int nslots, int doCFL) {
+static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const int *capslot, const void *twx) {
   typedef typename C2<T>::t V;
   constexpr int PB = pb_xpass<V>(N);
-  const Geo &g = h->g;
   dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
   KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, NTHR_H, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
-                       (const V *)h->A, (V *)h->B, g, (const V *)h->twx, doCFL, h->sc,
-                       h->ib ? h->d_capslot : nullptr, h->cap));
+                       (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, h->cap));
   return LH_OK;
 }
 template <typename T, int N>
-static int launch_zfwd(lh_handle *h, int nslots) {
+static int launch_zfwd(lh_handle *h, const Geo &g, int nslots, const void *twz) {
   typedef typename C2<T>::t V;
   constexpr int KB = kb_zfwd<V>(N);
-  const Geo &g = h->g;
   dim3 grid((g.N1h + KB - 1) / KB, nslots);
   KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, NTHR_H, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
-                      (const V *)h->B, g, (const V *)h->twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
+                      (const V *)h->B, g, (const V *)twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
                       (V *)h->vvc, (V *)h->wvf));
   return LH_OK;
 }
 
+// inverse transforms, products (and CFL maxima at kRK = 1) of one view's planes
+template <typename T>
+static int view_products(lh_handle *h, int vi, int kRK, bool forward) {
+  const Geo &g = h->gv[vi];
+  const int nslots = g.nuI + g.nvI;
+  if (nslots == 0) return LH_OK;
+  const int *capslot = (h->ib && vi == 0) ? h->d_capv : nullptr;
+  int rc = LH_EINVAL;
+  const void *twx = h->twv[vi][0], *twz = h->twv[vi][1];
+  LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, g, nslots, twz));
+  if (rc) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(g.G1, rc = launch_xpass<T, N>(h, g, nslots, kRK == 1 ? 1 : 0, capslot, twx));
+  if (rc || !forward) return rc;
+  rc = LH_EINVAL;
+  LH_DISPATCH(g.G2, rc = launch_zfwd<T, N>(h, g, nslots, twz));
+  return rc;
+}
+
 template <typename T>
 static int nonlinear_transforms(lh_handle *h, int kRK) {
-  const Geo &g = h->g;
-  const int nslots = g.nuI + g.nvI;
-  int rc = LH_EINVAL;
   if (kRK == 1) KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc));
-  LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, nslots));
-  if (rc) return rc;
-  rc = LH_EINVAL;
-  LH_DISPATCH(g.G1, rc = launch_xpass<T, N>(h, nslots, kRK == 1 ? 1 : 0));
-  if (rc) return rc;
-  rc = LH_EINVAL;
-  LH_DISPATCH(g.G2, rc = launch_zfwd<T, N>(h, nslots));
-  return rc;
+  for (int vi = 0; vi < h->nviews; ++vi) {
+    const int rc = view_products<T>(h, vi, kRK, true);
+    if (rc) return rc;
+  }
+  return LH_OK;
 }
 
 // triad-list form (ops_in_planes): the products come from the lists; the inverse
@@ -593,14 +771,9 @@ static int triad_nonlinear(lh_handle *h, int kRK) {
   typedef typename C2<T>::t V;
   const Geo &g = h->g;
   const int nslots = g.nuI + g.nvI;
-  int rc = LH_OK;
   if (kRK == 1) {
     KL("k_reset_cfl", k_reset_cfl<<<1, 32, 0, h->st>>>(h->sc));
-    rc = LH_EINVAL;
-    LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, nslots));
-    if (rc) return rc;
-    rc = LH_EINVAL;
-    LH_DISPATCH(g.G1, rc = launch_xpass<T, N>(h, nslots, 1));
+    const int rc = view_products<T>(h, 0, kRK, false);
     if (rc) return rc;
   }
   KL("k_triad", k_triad<T><<<nslots, h->tri_threads, h->tri_smem, h->st>>>(
@@ -695,8 +868,8 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (rc) return rc;
   if (kRK == 1) KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc));
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
-  const int nbu = (g.ncol + h->tb_uw - 1) / h->tb_uw, nbv = (g.ncol + h->tb_v - 1) / h->tb_v;
-  const int nbp = (g.ncol + h->tb_p - 1) / h->tb_p;
+  const int nbu = (g.nvc + h->tb_uw - 1) / h->tb_uw, nbv = (g.nvc + h->tb_v - 1) / h->tb_v;
+  const int nbp = (g.nvc + h->tb_p - 1) / h->tb_p;
   if (h->ib) {
     dim3 gd(nb, h->nib);
     if (h->prec == LH_PREC_FP64) {
@@ -731,7 +904,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                          (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
                                                          h->ib ? h->d_ibslot_v : nullptr, h->duib));
   } else {
-    const int nb2u = (2 * g.ncol + h->tb_uw - 1) / h->tb_uw, nb2v = (2 * g.ncol + h->tb_v - 1) / h->tb_v;
+    const int nb2u = (2 * g.nvc + h->tb_uw - 1) / h->tb_uw, nb2v = (2 * g.nvc + h->tb_v - 1) / h->tb_v;
     KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2u, 2), h->tb_uw, 0, h->st>>>(
                         (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
                         (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,

@@ -28,7 +28,38 @@ struct Geo {
   double gw[3][2];
   double gwbc1, gwbc3;
   int flag_ctpress;
+  // ---- multiblock and plane views ----
+  // The state lives on the wall-band mode grid: level stride ncolF = N1hF * N2F columns
+  // (column = kz row * N1hF + kx). A nonlinear launch sees one class of planes (a
+  // "view"): N1h, N2, G1, G2 and ncol are the view's, mode (r, kx) of the view is
+  // wall-grid column gcol(); slotq maps the launch's slots to levels (null: slot + 1
+  // for u slots, slot - nuI + 1 for v slots).
+  int mb;
+  int N1hF, N2F, ncolF;
+  const int *slotq;
+  // Column segments of the solve kernels: virtual column vc -> (column, band 0..2);
+  // a long column has band 1 (all levels), a short column bands 0 and 2 (the wall
+  // bands' levels). vcol null: vc = column, band 1.
+  int nvc;
+  const int2 *vcol;
+  int bq[3][6];  // per band: u lo, u hi, v lo, v hi, p lo, p hi (array indices, inclusive)
 };
+
+// wall-grid column of mode (r, kx) of the view g (r: the view's own kz row)
+__host__ __device__ __forceinline__ int gcol(const Geo &g, int r, int kx) {
+  return (r < g.N2 / 2 ? r : r + g.N2F - g.N2) * g.N1hF + kx;
+}
+// wall-grid kz row of the view's row r (index of k1z)
+__host__ __device__ __forceinline__ int grow(const Geo &g, int r) { return r < g.N2 / 2 ? r : r + g.N2F - g.N2; }
+// level of a nonlinear slot
+__device__ __forceinline__ int slot_level(const Geo &g, int slot, bool isU) {
+  return g.slotq ? g.slotq[slot] : (isU ? slot + 1 : slot - g.nuI + 1);
+}
+// column and band of a virtual column
+__device__ __forceinline__ void vcol_of(const Geo &g, int vc, int &c, int &b) {
+  if (g.vcol) { const int2 e = g.vcol[vc]; c = e.x; b = e.y; }
+  else { c = vc; b = 1; }
+}
 
 // Scalars kept on the device (no host round trip inside a step).
 struct DevScalars {

@@ -79,14 +79,14 @@ __global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1
   V *b1 = b0 + KB * N;
   const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
   const bool isU = slot < g.nuI;
-  const int q = isU ? slot + 1 : slot - g.nuI + 1;
-  const int nc = g.ncol;
+  const int q = slot_level(g, slot, isU);
+  const int nc = g.ncolF;
   for (int i = threadIdx.x; i < KB * N; i += blockDim.x) b0[i] = czero<V>();
   __syncthreads();
   for (int idx = threadIdx.x; idx < g.N2 * KB; idx += blockDim.x) {
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= g.N1h) continue;
-    const int c = r * g.N1h + kx;
+    const int c = gcol(g, r, kx);
     V v;
     if (isU) {
       if (f == 0) { const double2 x = u1[(size_t)q * nc + c]; v.x = to_t<T>(x.x); v.y = to_t<T>(x.y); }
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
   V *b1 = b0 + 4 * PB * G1;
   const int slot = blockIdx.y;
   const bool isU = slot < g.nuI;
-  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int q = slot_level(g, slot, isU);
   const int l0 = blockIdx.x * PB * 2;
   const int npairs = min(PB, (G2 - l0) / 2);
   const size_t fstride = (size_t)G2 * N1h;
@@ -281,14 +281,14 @@ __device__ __forceinline__ void zfwd_body(const typename C2<T>::t *__restrict__ 
   __syncthreads();
   V *res = line_fft<false, N, NL, true>(b0, b1, twz);
   const T s2 = (T)1 / (T)N;
-  const size_t off = (size_t)q * g.ncol;
+  const size_t off = (size_t)q * g.ncolF;
   for (int idx = threadIdx.x; idx < N2 * KB; idx += blockDim.x) {
     const int r = idx / KB, kk = idx - r * KB, kx = kx0 + kk;
     if (kx >= N1h) continue;
     const int row = prow(g, r);
-    const int c = r * N1h + kx;
+    const int c = gcol(g, r, kx), rg = grow(g, r);
     const T kxv = sizeof(T) == 8 ? (T)g.k1x[kx] : (T)g.k1xf[kx];
-    const T kzv = sizeof(T) == 8 ? (T)g.k1z[r] : (T)g.k1zf[r];
+    const T kzv = sizeof(T) == 8 ? (T)g.k1z[rg] : (T)g.k1zf[rg];
     const bool zr = (r == N2 / 2);  // der_x/der_z zero the kz = -N2/2 row
     if (NP == 4) {
       const V uu = cscale(res[row * NL + 0 * KB + kk], s2), uw = cscale(res[row * NL + 1 * KB + kk], s2);
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_nl(const typename C2<T>::t *__res
                                                   typename C2<T>::t *__restrict__ vvc, typename C2<T>::t *__restrict__ wvf) {
   const int slot = blockIdx.y;
   const bool isU = slot < g.nuI;
-  const int q = isU ? slot + 1 : slot - g.nuI + 1;
+  const int q = slot_level(g, slot, isU);
   const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
   if (isU) zfwd_body<T, N, 4>(B, g, twz, slot, q, pbase, N1xz, N2xz, N3xz, uvf, vvc, wvf);
   else zfwd_body<T, N, 2>(B, g, twz, slot, q, pbase, N1xz, N2xz, N3xz, uvf, vvc, wvf);
@@ -373,9 +373,12 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
                                                   const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
                                                   const DevScalars *__restrict__ sc, int kRK,
                                                   const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = g.ncol;
-  if (c >= nc) return;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  const int qlo = g.bq[bd][0], qhi = g.bq[bd][1];
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const double k2x = g.k2x[kx], k2z = g.k2z[r];
   const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1];
@@ -386,16 +389,17 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
   const double mp = (c == 0) ? -dR * sc->mpgx : 0.0;
   const int nu = g.nu;
   const double *d0 = g.d2u, *d1 = g.d2u + nu, *d2 = g.d2u + 2 * nu;
-  // row 0: [1, gw(2,1)], rhs 0
-  double a3raw = g.gw[1][0];
+  // first row: [1, gw(b,1)], rhs 0
+  double a3raw = g.gw[bd][0];
   double a2p = 1.0;  // 1/a2(0)
   double2 y1 = czero<double2>(), y3 = czero<double2>();
-  double2 um1 = u1[c], u0 = u1[(size_t)nc + c];
-  double2 wm1 = u3[c], w0 = u3[(size_t)nc + c];
-  u1[c] = y1;
-  u3[c] = y3;
-  double2 uvm = ld2(uvf[c]), wvm = ld2(wvf[c]);
-  for (int q = 1; q <= nu - 2; ++q) {
+  const size_t o0 = (size_t)qlo * nc + c;
+  double2 um1 = u1[o0], u0 = u1[o0 + nc];
+  double2 wm1 = u3[o0], w0 = u3[o0 + nc];
+  u1[o0] = y1;
+  u3[o0] = y3;
+  double2 uvm = ld2(uvf[o0]), wvm = ld2(wvf[o0]);
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t o = (size_t)q * nc + c;
     const double2 up1 = u1[o + nc], wp1 = u3[o + nc];
     const double2 uvq = ld2(uvf[o]), wvq = ld2(wvf[o]);
@@ -442,9 +446,9 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
     um1 = u0; u0 = up1; wm1 = w0; w0 = wp1;
     uvm = uvq; wvm = wvq;
   }
-  {  // last row: [gw(2,2), 1], rhs 0
-    const int q = nu - 1;
-    const double a1 = g.gw[1][1];
+  {  // last row: [gw(b,2), 1], rhs 0
+    const int q = qhi;
+    const double a1 = g.gw[bd][1];
     const double a3p = a3raw * a2p;
     a3s[(size_t)(q - 1) * nc + c] = a3p;
     a2p = 1.0 / (1.0 - a1 * a3p);
@@ -454,7 +458,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_uw(double2 *__restrict__ u1, doub
     u3[(size_t)q * nc + c] = y3;
   }
   double2 x1 = y1, x3 = y3;
-  for (int q = nu - 2; q >= 0; --q) {
+  for (int q = qhi - 1; q >= qlo; --q) {
     const size_t o = (size_t)q * nc + c;
     const double a3p = a3s[o];
     const double2 yy1 = u1[o], yy3 = u3[o];
@@ -474,9 +478,12 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
                                                  const double2 *__restrict__ p, double *__restrict__ a3s, Geo g,
                                                  const DevScalars *__restrict__ sc, int kRK,
                                                  const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = g.ncol;
-  if (c >= nc) return;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  const int qlo = g.bq[bd][2], qhi = g.bq[bd][3];
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const double k2x = g.k2x[kx], k2z = g.k2z[r];
   const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1];
@@ -487,10 +494,11 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
   const double *d0 = g.d2v, *d1 = g.d2v + nv, *d2 = g.d2v + 2 * nv;
   double a3raw = 0.0, a2p = 1.0;
   double2 y = czero<double2>();
-  double2 vm1 = u2[c], v0 = u2[(size_t)nc + c];
-  u2[c] = y;
-  double2 vvq = ld2(vvc[(size_t)1 * nc + c]);  // vv at u level q (interior starts at 1)
-  for (int q = 1; q <= nv - 2; ++q) {
+  const size_t o0 = (size_t)qlo * nc + c;
+  double2 vm1 = u2[o0], v0 = u2[o0 + nc];
+  u2[o0] = y;
+  double2 vvq = ld2(vvc[o0 + nc]);  // vv at u level q (interior starts at qlo + 1)
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t o = (size_t)q * nc + c;
     const double2 vp1 = u2[o + nc];
     const double2 vvp = ld2(vvc[o + nc]);  // vv at u level q+1
@@ -527,7 +535,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
     vm1 = v0; v0 = vp1; vvq = vvp;
   }
   {
-    const int q = nv - 1;
+    const int q = qhi;
     const double a3p = a3raw * a2p;
     a3s[(size_t)(q - 1) * nc + c] = a3p;
     a2p = 1.0 / (1.0 - 0.0 * a3p);
@@ -535,7 +543,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
     u2[(size_t)q * nc + c] = y;
   }
   double2 x = y;
-  for (int q = nv - 2; q >= 0; --q) {
+  for (int q = qhi - 1; q >= qlo; --q) {
     const size_t o = (size_t)q * nc + c;
     const double a3p = a3s[o];
     const double2 yy = u2[o];
@@ -569,9 +577,12 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
                                                      const DevScalars *__restrict__ sc, int kRK,
                                                      const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = tid >> 1, part = tid & 1;
+  const int vc = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
-  if (c >= nc) return;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  const int qlo = g.bq[bd][0], qhi = g.bq[bd][1];
   const int fw = blockIdx.y;  // 0: u, 1: w
   double *u = fw ? u3 : u1;
   float *Nu = fw ? Nu3 : Nu1;
@@ -590,15 +601,16 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   const float mp = (c == 0 && fw == 0 && part == 0) ? (float)(-dR * sc->mpgx) : 0.f;
   const float dd = (float)g.dd;
   const int nu = g.nu;
-  const double gw1 = g.gw[1][0], gw2 = g.gw[1][1];
-  const size_t ci = (size_t)c * 2 + part;
+  const double gw1 = g.gw[bd][0], gw2 = g.gw[bd][1];
   const size_t lstride = (size_t)nc * 2;
-  double um = u[ci], u0 = u[lstride + ci];
-  float y = d2f_alu(-(um + gw1 * u0));  // row 0
+  const size_t ci = (size_t)c * 2 + part;
+  const size_t e0 = (size_t)qlo * lstride + ci;
+  double um = u[e0], u0 = u[e0 + lstride];
+  float y = d2f_alu(-(um + gw1 * u0));  // first row
   float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
-  float flm = Fl[ci];
-  for (int q = 1; q <= nu - 2; ++q) {
+  float flm = Fl[e0];
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t e = (size_t)q * lstride + ci;
     const double up1 = u[e + lstride];
     const float flq = Fl[e];
@@ -632,7 +644,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     flm = flq;
   }
   {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1))
-    const int q = nu - 1;
+    const int q = qhi;
     const float a1 = (float)gw2;
     const float rl = d2f_alu(-(gw2 * um + u0));
     const float a3p = a3raw * a2p;
@@ -642,7 +654,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     u[(size_t)q * lstride + ci] = u0 + f2d_alu(y);
   }
   float x = y;
-  for (int q = nu - 2; q >= 0; --q) {
+  for (int q = qhi - 1; q >= qlo; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
     x = ya.x - ya.y * x;
@@ -656,9 +668,12 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
                                                      const DevScalars *__restrict__ sc, int kRK,
                                                      const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = tid >> 1, part = tid & 1;
+  const int vc = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
-  if (c >= nc) return;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  const int qlo = g.bq[bd][2], qhi = g.bq[bd][3];
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
   const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
@@ -671,13 +686,14 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   const int nv = g.nv;
   const size_t ci = (size_t)c * 2 + part;
   const size_t lstride = (size_t)nc * 2;
-  double vm = u2[ci], v0 = u2[lstride + ci];
+  const size_t e0 = (size_t)qlo * lstride + ci;
+  double vm = u2[e0], v0 = u2[e0 + lstride];
   const float dRf = (float)dR;
   float y = d2f_alu(-vm);
   float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
-  float vvq = vvc[lstride + ci];
-  for (int q = 1; q <= nv - 2; ++q) {
+  float vvq = vvc[e0 + lstride];
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t e = (size_t)q * lstride + ci;
     const double vp1 = u2[e + lstride];
     const float vvp = vvc[e + lstride];
@@ -709,14 +725,14 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     vm = v0; v0 = vp1; vvq = vvp;
   }
   {  // last row: d(n-1) = -v(n-1)
-    const int q = nv - 1;
+    const int q = qhi;
     const float a3p = a3raw * a2p;
     ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
     y = d2f_alu(-v0);
     u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
   }
   float x = y;
-  for (int q = nv - 2; q >= 0; --q) {
+  for (int q = qhi - 1; q >= qlo; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
     x = ya.x - ya.y * x;
@@ -799,24 +815,26 @@ __global__ void k_step_end(DevScalars *sc) {
 // ============================================================================
 __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, double *__restrict__ dg2,
                                                    double *__restrict__ dg3, Geo g) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = g.ncol;
-  if (c >= nc) return;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  const int plo = g.bq[bd][4], phi = g.bq[bd][5];
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const double k2x = g.k2x[kx], k2z = g.k2z[r];
   const double dd = g.dd;
-  const int np = g.np;
   double a3raw = 0.0, a2p = 0.0;
-  for (int qp = 0; qp < np; ++qp) {
+  for (int qp = plo; qp <= phi; ++qp) {
     const int q = qp + 1;
     const double Dt = dd * g.thu[q];
     const double Gb = -dd * g.thv[q];
     double A1, A2, A3;
-    if (qp == 0) {
+    if (qp == plo) {
       A1 = 0.0;
       A2 = (Dt * Gb) + k2x + k2z;
       A3 = (Dt * (dd * g.thv[q]));
-      if (c == 0) {  // gauge of mode (0,0)
+      if (c == 0 && bd == 1) {  // gauge of mode (0,0)
         const double h = g.yu[2 + g.dny] - g.yu[1 + g.dny];
         A1 = 0.0; A2 = 1.0 / (h * h); A3 = 0.0;
       }
@@ -824,10 +842,10 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
       const double Db = -dd * g.thu[q];
       const double Gt = dd * g.thv[q - 1];
       const double Gbm = -dd * g.thv[q - 1];
-      if (qp == np - 1) { A2 = (Db * Gt) + k2x + k2z; A1 = (Db * Gbm); A3 = 0.0; }
+      if (qp == phi) { A2 = (Db * Gt) + k2x + k2z; A1 = (Db * Gbm); A3 = 0.0; }
       else { A2 = (Db * Gt) + (Dt * Gb) + k2x + k2z; A1 = (Db * Gbm); A3 = (Dt * (dd * g.thv[q])); }
     }
-    if (qp == 0) a2p = 1.0 / A2;
+    if (qp == plo) a2p = 1.0 / A2;
     else {
       const double a3p = a3raw * a2p;
       dg3[(size_t)(qp - 1) * nc + c] = a3p;
@@ -837,7 +855,7 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
     dg2[(size_t)qp * nc + c] = a2p;
     a3raw = A3;
   }
-  dg3[(size_t)(np - 1) * nc + c] = 0.0;
+  dg3[(size_t)phi * nc + c] = 0.0;
 }
 
 // ============================================================================
@@ -853,20 +871,23 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
                                                 double2 *__restrict__ psi, const double *__restrict__ dg1,
                                                 const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
                                                 DevScalars *sc, int kRK, int need_div) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
   const int nc = g.ncol;
   double dmax = 0.0;
-  if (c < nc) {
+  if (vc < g.nvc) {
+    int c, bd;
+    vcol_of(g, vc, c, bd);
+    const int plo = g.bq[bd][4], phi = g.bq[bd][5];
+    const int ulo = g.bq[bd][0], uhi = g.bq[bd][1], vlo = g.bq[bd][2], vhi = g.bq[bd][3];
     const int r = c / g.N1h, kx = c - r * g.N1h;
     const double kxv = g.k1x[kx], kzv = g.k1z[r];
     const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
     const double dtirk = sc->dti / aRb;
     const double dt = sc->dt;
-    const int np = g.np;
     const double dd = g.dd;
     double2 y = czero<double2>();
-    double2 vm = u2[c];
-    for (int qp = 0; qp < np; ++qp) {
+    double2 vm = u2[(size_t)plo * nc + c];
+    for (int qp = plo; qp <= phi; ++qp) {
       const int q = qp + 1;
       const size_t o = (size_t)q * nc + c;
       const double2 a = u1[o], w = u3[o], v = u2[o];
@@ -877,9 +898,9 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
       vm = v;
       double2 rhs;
       rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
-      if (qp == 0 && c == 0) { rhs.x = 0.0; rhs.y = 0.0; }
+      if (qp == plo && c == 0 && bd == 1) { rhs.x = 0.0; rhs.y = 0.0; }
       const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
-      if (qp == 0) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
+      if (qp == plo) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
       else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
       psi[(size_t)qp * nc + c] = y;
     }
@@ -888,11 +909,11 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
     const double kxd = dtrk * kxv, kzd = dtrk * kzv;
     double2 xn = y;
     double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
-    for (int qp = np - 1; qp >= 0; --qp) {
+    for (int qp = phi; qp >= plo; --qp) {
       const int q = qp + 1;
       const size_t o = (size_t)q * nc + c;
       double2 x;
-      if (qp == np - 1) x = xn;
+      if (qp == phi) x = xn;
       else {
         const double a3p = dg3[(size_t)qp * nc + c];
         const double2 yy = psi[(size_t)qp * nc + c];
@@ -908,13 +929,13 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
       u1[o] = a;
       u3[o] = w;
       double2 v = u2[o];
-      if (q <= g.nv - 2) {
+      if (q <= vhi - 1) {
         const double f = dtrk2 * g.thv[q];
         v.x = v.x - f * (xn.x - x.x);
         v.y = v.y - f * (xn.y - x.y);
         u2[o] = v;
       }
-      if (need_div && qp < np - 1) {
+      if (need_div && qp < phi) {
         const double th = dd * g.thu[q + 1];
         double2 dv;
         dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
@@ -925,22 +946,27 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
       xn = x;
     }
     if (need_div) {
-      const double th = dd * g.thu[1];
-      const double2 vb = u2[c];
+      const double th = dd * g.thu[plo + 1];
+      const double2 vb = u2[(size_t)plo * nc + c];
       double2 dv;
       dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
       dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
       dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
     }
-    const int nu = g.nu;
-    double2 t1 = u1[(size_t)nc + c], t3 = u3[(size_t)nc + c];
-    u1[c] = cscale(t1, g.gwbc1);
-    u3[c] = cscale(t3, g.gwbc3);
-    t1 = u1[(size_t)(nu - 2) * nc + c]; t3 = u3[(size_t)(nu - 2) * nc + c];
-    u1[(size_t)(nu - 1) * nc + c] = cscale(t1, g.gwbc1);
-    u3[(size_t)(nu - 1) * nc + c] = cscale(t3, g.gwbc3);
-    u2[c] = czero<double2>();
-    u2[(size_t)(g.nv - 1) * nc + c] = czero<double2>();
+    // wall ghosts: bands 1, 2 at the bottom, bands 2, 3 at the top (the short columns'
+    // interface ghosts keep the values of their Helmholtz boundary rows); v = 0 at band ends
+    if (bd <= 1) {
+      const double2 t1 = u1[(size_t)(ulo + 1) * nc + c], t3 = u3[(size_t)(ulo + 1) * nc + c];
+      u1[(size_t)ulo * nc + c] = cscale(t1, g.gwbc1);
+      u3[(size_t)ulo * nc + c] = cscale(t3, g.gwbc3);
+    }
+    if (bd >= 1) {
+      const double2 t1 = u1[(size_t)(uhi - 1) * nc + c], t3 = u3[(size_t)(uhi - 1) * nc + c];
+      u1[(size_t)uhi * nc + c] = cscale(t1, g.gwbc1);
+      u3[(size_t)uhi * nc + c] = cscale(t3, g.gwbc3);
+    }
+    u2[(size_t)vlo * nc + c] = czero<double2>();
+    u2[(size_t)vhi * nc + c] = czero<double2>();
   }
   dmax = warp_max(dmax);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
@@ -953,12 +979,14 @@ __global__ void k_reset_err(DevScalars *sc) {
 // max |div| of the current state (getini's divergence + error())
 __global__ void __launch_bounds__(NTHR) k_divmax(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                  const double2 *__restrict__ u3, Geo g, DevScalars *sc) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
   double dmax = 0.0;
-  if (c < g.ncol) {
+  if (vc < g.nvc) {
+    int c, bd;
+    vcol_of(g, vc, c, bd);
     const int r = c / g.N1h, kx = c - r * g.N1h;
     const double kxv = g.k1x[kx], kzv = g.k1z[r];
-    for (int q = 1; q <= g.nu - 2; ++q) {
+    for (int q = g.bq[bd][4] + 1; q <= g.bq[bd][5] + 1; ++q) {
       const size_t o = (size_t)q * g.ncol + c;
       const double2 a = u1[o], w = u3[o], v = u2[o], vm = u2[o - g.ncol];
       const double th = g.dd * g.thu[q];
@@ -975,6 +1003,17 @@ __global__ void __launch_bounds__(NTHR) k_divmax(const double2 *__restrict__ u1,
 // err = max |div| (errbits holds the maximum of |div|^2)
 __global__ void k_err_from_bits(DevScalars *sc) {
   if (threadIdx.x == 0 && blockIdx.x == 0) sc->err = sqrt(__longlong_as_double((long long)sc->errbits));
+}
+
+// one band's host cfield [k][l] (staged) <-> device [lev0 + l][cols[k]]; put = 1 writes the device
+__global__ void k_band_io(double2 *__restrict__ dev, double2 *__restrict__ stage, const int *__restrict__ cols,
+                          int ncb, int nlev, int lev0, int ncol, int put) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)ncb * nlev) return;
+  const int k = (int)(i / nlev), l = (int)(i - (size_t)k * nlev);
+  double2 *d = dev + (size_t)(lev0 + l) * ncol + cols[k];
+  if (put) *d = stage[i];
+  else stage[i] = *d;
 }
 
 // host cfield [col][lev] <-> device [lev][col] (complex), tiled transpose

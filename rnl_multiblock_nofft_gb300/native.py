@@ -17,6 +17,7 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
 _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
+           "lh_upload_band", "lh_download_band",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
@@ -48,6 +49,8 @@ def load(path: str = _LIB_PATH):
     L.lh_last_error.restype = C.c_char_p
     L.lh_upload_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_download_state.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_upload_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
+    L.lh_download_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_set_scalars.argtypes = [vp, C.POINTER(LhScalars)]
     L.lh_get_scalars.argtypes = [vp, C.POINTER(LhScalars)]
     L.lh_substep.argtypes = [vp, i]
@@ -131,6 +134,24 @@ class GpuChannel:
             if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
                 raise ValueError("download buffers must be C-contiguous complex128 of the state shapes")
         self._check(self.L.lh_download_state(self.h, *[_dptr(a) for a in out]))
+        return out
+
+    def upload_bands(self, bands: dict):
+        """{band: (u1, u2, u3, p)} in the bands' cfield layouts (ChannelSetup.band_shapes);
+        the per-band upload of a multiblock channel (lh_upload_band)."""
+        for b, arrs in bands.items():
+            arrs = [np.ascontiguousarray(a, np.complex128) if a is not None else None for a in arrs]
+            for a, sh in zip(arrs, self.s.band_shapes(b)):
+                if a is not None and a.shape != sh:
+                    raise ValueError(f"band {b}: shape {a.shape} != {sh}")
+            self._check(self.L.lh_upload_band(self.h, b, *[_dptr(a) for a in arrs]))
+
+    def download_bands(self) -> dict:
+        out = {}
+        for b in (1, 2, 3):
+            arrs = [np.zeros(sh, np.complex128) for sh in self.s.band_shapes(b)]
+            self._check(self.L.lh_download_band(self.h, b, *[_dptr(a) for a in arrs]))
+            out[b] = arrs
         return out
 
     def set_scalars(self, **kw):

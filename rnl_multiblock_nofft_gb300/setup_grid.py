@@ -143,10 +143,62 @@ class ChannelSetup:
     def multiblock(self) -> bool:
         return bool(self.N[0, 1] != self.N[0, 2] or self.N[1, 1] != self.N[1, 2])
 
+    # ---- core band (band 2); equal to the above for one resolution ----
+    @property
+    def N1c(self) -> int:
+        return int(self.N[0, 2])
+
+    @property
+    def N2c(self) -> int:
+        return int(self.N[1, 2])
+
+    @property
+    def G1c(self) -> int:
+        return int(self.Ngal[0, 2])
+
+    @property
+    def G2c(self) -> int:
+        return int(self.Ngal[1, 2])
+
+    def is_long(self) -> np.ndarray:
+        """Per column of the wall-band mode grid (row kz index r = 0..N2-1 in k1F_z
+        order, kx = 0..N1/2 fastest): True for the long columns (modes the core band
+        also holds, start.f90:1596-1609), False for the short ones (wall bands only)."""
+        N1h, N2 = self.N1 // 2 + 1, self.N2
+        r = np.arange(N2)[:, None]
+        kx = np.arange(N1h)[None, :]
+        rz = (r < self.N2c // 2) | (r >= N2 - self.N2c // 2)
+        return ((kx <= self.N1c // 2) & rz).reshape(-1)
+
+    def band_cols(self, band: int) -> np.ndarray:
+        """Columns of band 1..3 as indices into the wall-band mode grid, in the order of
+        columns_i/k with one process (start.f90:1566-1609): row-major over (r, kx)."""
+        lng = self.is_long()
+        idx = np.arange(lng.size)
+        return idx[lng] if band == 2 else idx[~lng]
+
+    def band_levels(self, band: int, grid: int) -> tuple:
+        """(lo, hi) array indices (j + dny) of jlim(1:2, grid, band)."""
+        lo, hi = self.jlim[:, grid - 1, band - 1]
+        return int(lo) + self.dny, int(hi) + self.dny
+
+    def band_shapes(self, band: int):
+        """Host cfield shapes of (u1, u2, u3, p) of one band: [columns][levels]."""
+        nc = len(self.band_cols(band))
+        out = []
+        for grid in (UGRID, VGRID, UGRID, PGRID):
+            lo, hi = self.band_levels(band, grid)
+            out.append((nc, hi - lo + 1))
+        return tuple(out)
+
     def mode_points(self) -> int:
         """Retained mode-points of one substep: sum over the nominal y-levels
-        (``ny`` of the configuration) of N1*N2."""
-        return int(self.N1 * self.N2 * self.p.ny)
+        (``ny`` of the configuration, v levels 0..ny-1) of N1*N2 of the level's band."""
+        if not self.multiblock:
+            return int(self.N1 * self.N2 * self.p.ny)
+        j = np.arange(self.p.ny)
+        wall = (j <= self.N[2, 1]) | (j > self.N[2, 2])
+        return int(np.where(wall, self.N1 * self.N2, self.N1c * self.N2c).sum())
 
 
 def _ygrid(p: ChannelParams, N: np.ndarray, posth_abs: float):

@@ -58,6 +58,15 @@ WORKLOADS = {
                desc="mid textured channel N 64x64, ny 97, posts"),
     "P": dict(N=192, ny=201, posts=False, flpress=0,
               desc="profiling case: smooth channel N 192x192, ny 201 (state 0.27 GB, above L2)"),
+    "C4": dict(N=768, Nz=384, ny=385, re_tau=550.0, posts=True, post_period=24, post_points=12,
+               post_height_plus=6.0, flpress=0, core=(384, 192),
+               desc="multiblock channel: wall bands N 768x384, core band N 384x192, ny 385, Re_tau 550, "
+                    "12x12-point posts on a 24-point period, 6 wall units high"),
+    "MB": dict(N=32, ny=65, posts=False, flpress=0, core=(16, 16),
+               desc="small multiblock channel: wall bands N 32x32, core band N 16x16, ny 65"),
+    "MBP": dict(N=32, ny=65, posts=True, flpress=0, post_period=8, post_points=4, post_height_plus=20.0,
+                core=(16, 16),
+                desc="small multiblock channel with posts: wall bands N 32x32, core N 16x16, ny 65"),
 }
 
 
@@ -66,7 +75,12 @@ def workload_params(name: str) -> ChannelParams:
     w.pop("desc")
     N = w.pop("N")
     ny = w.pop("ny")
-    return re_tau_params(N, ny, **w)
+    core = w.pop("core", None)
+    p = re_tau_params(N, ny, **w)
+    if core is not None:
+        p.Ngalx = (p.Ngalx[0], 3 * core[0] // 2)
+        p.Ngalz = (p.Ngalz[0], 3 * core[1] // 2)
+    return p
 
 
 def workload_setup(name: str) -> ChannelSetup:
@@ -138,6 +152,89 @@ def initial_field(s: ChannelSetup, seed: int, amp: float = 0.1, kmax: int = 8):
     u3[:, :, -1] = s.gw_bc_u3 * u3[:, :, -2]
     p = np.zeros((N2 * N1h, nu - 2), np.complex128)
     return (u1.reshape(N2 * N1h, nu), u2.reshape(N2 * N1h, nv), u3.reshape(N2 * N1h, nu), p)
+
+
+def _fine_field(s: ChannelSetup, seed: int, amp: float, kmax: int):
+    """initial_field on the wall-band mode grid, all levels: (u1, u2, u3) [N2][N1h][lev]."""
+    u1, u2, u3, _ = initial_field(s, seed, amp, kmax)
+    N1h, N2 = s.N1 // 2 + 1, s.N2
+    return (u1.reshape(N2, N1h, -1), u2.reshape(N2, N1h, -1), u3.reshape(N2, N1h, -1))
+
+
+def initial_field_bands(s: ChannelSetup, seed: int, amp: float = 0.1, kmax: int = 8,
+                        short_amp: float = 0.02) -> dict:
+    """Per-band initial state {band: (u1, u2, u3, p)} in the bands' cfield layouts
+    (ChannelSetup.band_shapes). Long columns (band 2) carry initial_field's laminar
+    profile and perturbation; the short columns of bands 1 and 3 a divergence-free
+    perturbation of relative amplitude `short_amp` confined to their band: v with the
+    envelope (y - y_lo)^2 (y_hi - y)^2 between the band's end v levels (where v = 0),
+    (u, w) built from it as in initial_field, ghosts from the band's boundary rows."""
+    rng = np.random.default_rng(seed + 7919)
+    u1f, u2f, u3f, _ = initial_field(s, seed, amp, kmax)
+    lng = s.is_long()
+    out = {}
+    nu, nv = s.nyu, s.nyv
+    th = s.dthdyu * s.ddthetavi
+    for band in (1, 2, 3):
+        cols = s.band_cols(band)
+        shp = s.band_shapes(band)
+        if band == 2:
+            a = [u1f[cols], u2f[cols], u3f[cols]]
+            (lo, hi) = s.band_levels(2, 2)
+            out[band] = (a[0][:, lo:hi + 1], a[1], a[2][:, lo:hi + 1], np.zeros(shp[3], np.complex128))
+            continue
+        ulo, uhi = s.band_levels(band, 2)
+        vlo, vhi = s.band_levels(band, 1)
+        U1 = np.zeros((len(cols), nu), np.complex128)
+        U3 = np.zeros_like(U1)
+        U2 = np.zeros((len(cols), nv), np.complex128)
+        yv = s.yv
+        env = np.zeros(nv)
+        env[vlo:vhi + 1] = (yv[vlo:vhi + 1] - yv[vlo]) ** 2 * (yv[vhi] - yv[vlo:vhi + 1]) ** 2
+        env /= max(env.max(), 1e-300)
+        yu = s.yu
+        envu = np.clip((yu - yv[vlo]) * (yv[vhi] - yu), 0.0, None) ** 2
+        envu /= max(envu.max(), 1e-300)
+        N1h = s.N1 // 2 + 1
+        for i, c in enumerate(cols):
+            r, kx = divmod(int(c), N1h)
+            if kx == 0 and r > s.N2 // 2:
+                continue  # kx = 0 modes filled by Hermitian symmetry below
+            k1x, k1z = s.k1x[kx], s.k1z[r]
+            k2 = k1x * k1x + k1z * k1z
+            v = short_amp * (rng.normal() + 1j * rng.normal()) * env
+            D = np.zeros(nu, np.complex128)
+            D[1:-1] = (v[1:] - v[:-1]) * th[1:-1]
+            ph = np.zeros(nu, np.complex128)
+            ph[ulo + 1:uhi] = (short_amp / math.sqrt(k2)) * (rng.normal() + 1j * rng.normal()) * envu[ulo + 1:uhi]
+            U1[i] = 1j * k1x * D / k2 + k1z * ph
+            U3[i] = 1j * k1z * D / k2 - k1x * ph
+            U2[i] = v
+        # kx = 0 columns: Hermitian partner of row r is row N2 - r
+        pos = {int(c): i for i, c in enumerate(cols)}
+        for i, c in enumerate(cols):
+            r, kx = divmod(int(c), N1h)
+            if kx == 0 and r > s.N2 // 2:
+                j = pos.get((s.N2 - r) * N1h)
+                if j is not None:
+                    U1[i], U2[i], U3[i] = np.conj(U1[j]), np.conj(U2[j]), np.conj(U3[j])
+        for U in (U1, U3):
+            U[:, :ulo + 1] = 0.0
+            U[:, uhi:] = 0.0
+        # ghosts: wall ghosts from gridweighting_bc, interface ghosts from the band's BC row
+        b = band - 1
+        if band == 1:
+            U1[:, ulo] = s.gw_bc_u1 * U1[:, ulo + 1]
+            U3[:, ulo] = s.gw_bc_u3 * U3[:, ulo + 1]
+            U1[:, uhi] = -s.gw[b, 1] * U1[:, uhi - 1]
+            U3[:, uhi] = -s.gw[b, 1] * U3[:, uhi - 1]
+        else:
+            U1[:, uhi] = s.gw_bc_u1 * U1[:, uhi - 1]
+            U3[:, uhi] = s.gw_bc_u3 * U3[:, uhi - 1]
+            U1[:, ulo] = -s.gw[b, 0] * U1[:, ulo + 1]
+            U3[:, ulo] = -s.gw[b, 0] * U3[:, ulo + 1]
+        out[band] = (U1[:, ulo:uhi + 1], U2[:, vlo:vhi + 1], U3[:, ulo:uhi + 1], np.zeros(shp[3], np.complex128))
+    return out
 
 
 def initial_scalars(s: ChannelSetup) -> dict:
