@@ -14,6 +14,7 @@ triad-list nonlinear term (complete lists, threshold 0) instead of the products.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -21,6 +22,8 @@ import subprocess
 import sys
 import tempfile
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -126,29 +129,55 @@ def traffic_table():
     return out
 
 
-def algorithmic_bytes(s, kernel: str, form: str) -> float:
-    """Compulsory HBM bytes of one launch: every input and output element once.
-    Spectral fields are complex128; the transform intermediates are complex128 in
-    the FP64 form and complex64 in the mixed form."""
-    nc = s.ncols
+def plane_views(s):
+    """(u planes, v planes, N1h, G2, modes per plane) of each plane class: wall-band
+    planes, then core planes (multiblock only)."""
     nuI, nvI = s.nyu - 2, s.nyv - 2
-    G1, G2, N1h = s.G1, s.G2, s.N1 // 2 + 1
+    if not s.multiblock:
+        return [(nuI, nvI, s.N1 // 2 + 1, s.G2, s.ncols)]
+    d = s.dny
+    ju = np.arange(1, s.nyu - 1) - d
+    jv = np.arange(1, s.nyv - 1) - d
+    fu = int(((ju <= s.N[3, 1]) | (ju > s.N[3, 2])).sum())
+    fv = int(((jv <= s.N[2, 1]) | (jv > s.N[2, 2])).sum())
+    return [(fu, fv, s.N1 // 2 + 1, s.G2, s.ncols),
+            (nuI - fu, nvI - fv, s.N1c // 2 + 1, s.G2c, (s.N1c // 2 + 1) * s.N2c)]
+
+
+def column_levels(s, grid: int) -> int:
+    """Sum over the solve segments of (levels of `grid`): long columns span the channel,
+    short columns their two wall bands."""
+    tot = 0
+    for b in (1, 2, 3):
+        lo, hi = s.band_levels(b, grid)
+        tot += len(s.band_cols(b)) * (hi - lo + 1)
+    return tot
+
+
+def algorithmic_bytes(s, kernel: str, form: str) -> float:
+    """Compulsory HBM bytes of one substep's launches of a kernel: every input and
+    output element once. Spectral fields are complex128; the transform intermediates
+    are complex128 in the FP64 form and complex64 in the mixed form."""
     vs = 16 if form == "fp64" else 8
-    A = (nuI + nvI) * 3 * G2 * N1h * vs
-    B = (4 * nuI + 2 * nvI) * N1h * G2 * vs
     z = 16
-    if kernel == "k_zinv_nl":
-        return (nuI + nvI) * 3 * nc * z + A
-    if kernel == "k_xpass_nl":
-        return A + B
-    if kernel == "k_zfwd_nl":
-        return B + (nuI + nvI) * 3 * nc * z
+    tot = 0.0
+    for nuI, nvI, N1h, G2, ncv in plane_views(s):
+        A = (nuI + nvI) * 3 * G2 * N1h * vs
+        B = (4 * nuI + 2 * nvI) * N1h * G2 * vs
+        if kernel == "k_zinv_nl":
+            tot += (nuI + nvI) * 3 * ncv * z + A
+        elif kernel == "k_xpass_nl":
+            tot += A + B
+        elif kernel == "k_zfwd_nl":
+            tot += B + (nuI + nvI) * 3 * ncv * z
+    if kernel in ("k_zinv_nl", "k_xpass_nl", "k_zfwd_nl"):
+        return tot
     if kernel == "k_helm_uw":
-        return s.nyu * nc * z * 13
+        return column_levels(s, 2) * z * 13
     if kernel == "k_helm_v":
-        return s.nyv * nc * z * 7
+        return column_levels(s, 1) * z * 7
     if kernel == "k_press":
-        return s.nyu * nc * z * 8
+        return column_levels(s, 2) * z * 8
     return float("nan")
 
 
@@ -177,6 +206,14 @@ def triad_terms(s, tl) -> int:
     return n
 
 
+def oracle_initial_state(o, s):
+    from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_field_bands
+    if s.multiblock:
+        o.set_bands(initial_field_bands(s, 1000))
+    else:
+        o.set_state(*initial_field(s, 1000))
+
+
 def run_reference(args, ws, rank):
     """The reference's CPU path on the host cores: the Fortran/MPI reference cannot
     be built here (no Fortran compiler), so its restatement (the oracle) runs on
@@ -189,7 +226,7 @@ def run_reference(args, ws, rank):
     s = workload_setup(args.workload)
     cores = os.cpu_count() or 1
     o = Oracle(s, threads=cores, triads=triad_lists(args, s))
-    o.set_state(*initial_field(s, 1000))
+    oracle_initial_state(o, s)
     o.set_scalars(**initial_scalars(s))
     k = 0
     for _ in range(args.warmup):
@@ -228,7 +265,7 @@ def cpu_baseline(s, budget_s: float = 20.0, triads=None):
     from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_scalars
     cores = os.cpu_count() or 1
     o = Oracle(s, threads=cores, triads=triads)
-    o.set_state(*initial_field(s, 1000))
+    oracle_initial_state(o, s)
     o.set_scalars(**initial_scalars(s))
     n, t0 = 0, time.perf_counter()
     while True:
@@ -330,14 +367,23 @@ def main():
         return
     s = workload_setup(args.workload)
     tl = triad_lists(args, s)
-    ic = initial_field(s, 1000 + rank)
+    mb = s.multiblock
+    if mb:
+        from rnl_multiblock_nofft_gb300.workloads import initial_field_bands
+        icb = initial_field_bands(s, 1000 + rank)
+        ic = [a for b in (1, 2, 3) for a in icb[b]]
+    else:
+        ic = initial_field(s, 1000 + rank)
     sc0 = initial_scalars(s)
     pts = s.mode_points()
     forms = ["fp64", "mixed"] if args.form == "both" else [args.form]
     res, states = {}, {}
     for form in forms:
         g = GpuChannel(s, form, triads=tl)
-        g.upload_state(*ic)
+        if mb:
+            g.upload_bands(icb)
+        else:
+            g.upload_state(*ic)
         g.set_scalars(**sc0)
         g.autotune()
         g.step(args.warmup)
@@ -350,7 +396,7 @@ def main():
         ms = reduce_max(pg, ms)
         res[form] = {"ms": ms, "launches": launches, "clocks": clocks,
                      "value": ws * pts * 3 * args.steps / (ms * 1e-3) / 1e6}
-        states[form] = g.download_state()
+        states[form] = ([a for b in (1, 2, 3) for a in g.download_bands()[b]] if mb else g.download_state())
         sc = g.scalars()
         res[form]["scalars"] = {k: sc[k] for k in ("t", "dt", "err", "Qx", "iter")}
         # per-kernel times (eager, events around each launch) for the roofline
@@ -364,7 +410,10 @@ def main():
     relerr = None
     if "fp64" in states and "mixed" in states:
         relerr = {}
-        for f, a, b in zip(("u1", "u2", "u3", "p"), states["fp64"], states["mixed"]):
+        nf = 4
+        for i, f in enumerate(("u1", "u2", "u3", "p")):
+            a = np.concatenate([x.ravel() for x in states["fp64"][i::nf]])
+            b = np.concatenate([x.ravel() for x in states["mixed"][i::nf]])
             relerr[f] = float(np.linalg.norm(b - a) / np.linalg.norm(a))
     vel_err = max(relerr[f] for f in ("u1", "u2", "u3")) if relerr else None
     head = "mixed" if ("mixed" in res and (relerr is None or vel_err <= 1e-5)) else "fp64"
@@ -374,24 +423,38 @@ def main():
 
     # e2e through the C ABI: pinned host state in, step, state out, every step
     g = GpuChannel(s, head, triads=tl)
-    shapes = g.shapes
-    pinned = [torch.empty(sh + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
-              for sh in shapes]
+    shapes = [sh for b in (1, 2, 3) for sh in s.band_shapes(b)] if mb else list(g.shapes)
+    pin = lambda sh: torch.empty(tuple(sh) + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+    pinned = [pin(sh) for sh in shapes]
     for dst, src in zip(pinned, ic):
         dst[...] = src
-    g.upload_state(*pinned)
+    pinned_out = [pin(sh) for sh in shapes]
+
+    def put(arrs):
+        if mb:
+            g.upload_bands({b: arrs[4 * (b - 1):4 * b] for b in (1, 2, 3)})
+        else:
+            g.upload_state(*arrs)
+
+    def get(arrs):
+        if mb:
+            for b in (1, 2, 3):
+                g._check(g.L.lh_download_band(g.h, b, *[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                                                         for a in arrs[4 * (b - 1):4 * b]]))
+        else:
+            g.download_state(out=arrs)
+
+    put(pinned)
     g.set_scalars(**sc0)
     g.step(1)
     g.synchronize()
     barrier(pg)
-    pinned_out = [torch.empty(sh + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
-                  for sh in shapes]
     nb = sum(a.nbytes for a in pinned)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        g.upload_state(*pinned)
+        put(pinned)
         g.step(1)
-        g.download_state(out=pinned_out)   # the step's result read back to the host
+        get(pinned_out)   # the step's result read back to the host
     g.synchronize()
     e2e_s = reduce_max(pg, time.perf_counter() - t0)
     g.close()
@@ -404,9 +467,10 @@ def main():
     dom = max(kern.items(), key=lambda kv: kv[1][1])
     dname, (dlaunch, dms) = dom
     avg_ms = dms / dlaunch
-    alg = algorithmic_bytes(s, dname, head)
+    alg_step = 3 * algorithmic_bytes(s, dname, head)   # the profiled step has 3 substeps
+    alg = alg_step / dlaunch
     peak, peak_kind = measured_peaks()
-    achieved = alg / (avg_ms * 1e-3) / 1e9
+    achieved = alg_step / (dms * 1e-3) / 1e9
     tt = traffic_table().get((dname, head))
     step_total = sum(v[1] for v in kern.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -420,6 +484,7 @@ def main():
             "data": "synthetic (seeded perturbed laminar channel, see rnl_multiblock_nofft_gb300/workloads.py)",
             "config": {"workload": f"{args.workload}: {workload_desc(args.workload)}", "form": head,
                        "mode_points_per_substep": pts, "N1": s.N1, "N2": s.N2, "ny": s.p.ny,
+                       "core_band": [s.N1c, s.N2c] if mb else None,
                        "ny_with_immersed_region": s.nyv, "Ngal": [s.G1, s.G2],
                        "l2": "inputs larger than L2 (state ~%.0f MB)" % (sum(a.nbytes for a in ic) / 1e6),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
