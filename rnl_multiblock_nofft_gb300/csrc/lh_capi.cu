@@ -31,9 +31,9 @@ struct lh_handle {
   double2 *u1, *u2, *u3, *p, *psi;
   void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
   double *dg1, *dg2, *dg3;  // factorised pressure matrices (constant)
-  void *ysf;  // FP32 scratch of the mixed-form solves
+  void *ysf, *ysv;  // FP32 scratch of the mixed-form solves (u and w; v)
   void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
-  double *a3s, *mfw;
+  double *a3s, *a3v, *mfw;
   void *A, *B, *twx, *twz, *twx64, *twz64;
   size_t Abytes, Bbytes;
   long long graph_nodes_per_step;
@@ -351,10 +351,10 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
   ZA(h->Nu1, vs * nu * nc); ZA(h->Nu3, vs * nu * nc); ZA(h->Nu2, vs * nv * nc);
   ZA(h->dg1, sizeof(double) * g.np * nc); ZA(h->dg2, sizeof(double) * g.np * nc); ZA(h->dg3, sizeof(double) * g.np * nc);
-  if (h->prec == LH_PREC_MIXED) ZA(h->ysf, 2 * sizeof(float4) * nu * nc);
+  if (h->prec == LH_PREC_MIXED) { ZA(h->ysf, 2 * sizeof(float4) * nu * nc); ZA(h->ysv, 2 * sizeof(float2) * nv * nc); }
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
-  ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc);
+  ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc); ZA(h->a3v, sizeof(double) * nv * nc);
   ZA(h->mfw, sizeof(double) * 6 * (size_t)(g.nn + 3));
   h->Abytes = h->Bbytes = 0;
   for (int vi = 0; vi < h->nviews; ++vi) {
@@ -562,7 +562,8 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
-                  h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1]};
+                  h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
+                  h->ysv, h->a3v};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -842,21 +843,13 @@ static const void *fp64_tw(lh_handle *h, bool x) { return x ? h->twx64 : h->twz6
 
 // flowrate_corr after solveU_W, on the side stream (joined before solveP); on the
 // main stream when kernels are being timed one by one
-static int meanflow_fork(lh_handle *h, int kRK) {
+// flowrate_corr on the main stream, after the u solve (constant flow rate only)
+static int meanflow(lh_handle *h, int kRK) {
   const Geo &g = h->g;
   if (g.flag_ctpress != 0) return LH_OK;
   const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
   const int sm = mb <= 48 * 1024 ? 1 : 0;
-  if (h->prof) {
-    KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
-    return LH_OK;
-  }
-  CK(cudaEventRecord(h->ev_fork, h->st));
-  CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
-  k_meanflow<<<1, 256, sm ? mb : 0, h->st2>>>(h->u1, g, h->sc, kRK, h->mfw, sm);
-  int rc = count_launch(h);
-  if (rc) return rc;
-  CK(cudaEventRecord(h->ev_join, h->st2));
+  KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));
   return LH_OK;
 }
 
@@ -894,27 +887,41 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                           h->d_ibslot_v, h->d_lev2cap_v, g, h->sc));
     if ((rc = phys_to_spec<T>(h, h->duphys, h->duib, 3 * h->nib, h->B, h->twx, h->twz))) return rc;
   }
+  // The u/w and v solves are independent: v runs on the side stream while u/w and the
+  // mean-flow correction (which follows u) run on the main stream; each solve has its
+  // own scratch. (Sequential on the main stream while per-kernel times are profiled.)
+  const bool fork = !h->prof;
+  cudaStream_t sv = fork ? h->st2 : h->st;
+  if (fork) {
+    CK(cudaEventRecord(h->ev_fork, h->st));
+    CK(cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+  }
+  if (!fork) prof_begin(h, "k_helm_v");
+  if (h->prec == LH_PREC_FP64) {
+    k_helm_v<T><<<nbv, h->tb_v, 0, sv>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz, (const V *)h->vvc, h->p,
+                                         h->a3v, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib);
+  } else {
+    const int nb2v = (2 * g.nvc + h->tb_v - 1) / h->tb_v;
+    k_helm_v_mx2<<<nb2v, h->tb_v, 0, sv>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
+                                           (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysv, g, h->sc,
+                                           kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib);
+  }
+  if ((rc = count_launch(h))) return rc;
+  if (fork) CK(cudaEventRecord(h->ev_join, h->st2));
   if (h->prec == LH_PREC_FP64) {
     KL("k_helm_uw", k_helm_uw<T><<<nbu, h->tb_uw, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
                                                            (const V *)h->N1xz, (const V *)h->N3xz, (const V *)h->uvf,
                                                            (const V *)h->wvf, h->p, h->a3s, g, h->sc, kRK,
                                                            h->ib ? h->d_ibslot_u : nullptr, h->duib));
-    if ((rc = meanflow_fork(h, kRK))) return rc;
-    KL("k_helm_v", k_helm_v<T><<<nbv, h->tb_v, 0, h->st>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz,
-                                                         (const V *)h->vvc, h->p, h->a3s, g, h->sc, kRK,
-                                                         h->ib ? h->d_ibslot_v : nullptr, h->duib));
   } else {
-    const int nb2u = (2 * g.nvc + h->tb_uw - 1) / h->tb_uw, nb2v = (2 * g.nvc + h->tb_v - 1) / h->tb_v;
+    const int nb2u = (2 * g.nvc + h->tb_uw - 1) / h->tb_uw;
     KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2u, 2), h->tb_uw, 0, h->st>>>(
                         (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
                         (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,
                         h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
-    if ((rc = meanflow_fork(h, kRK))) return rc;
-    KL("k_helm_v", k_helm_v_mx2<<<nb2v, h->tb_v, 0, h->st>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
-                                                           (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysf,
-                                                           g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib));
   }
-  if (g.flag_ctpress == 0 && !h->prof) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
+  if ((rc = meanflow(h, kRK))) return rc;
+  if (fork) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   KL("k_press", k_press<<<nbp, h->tb_p, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
