@@ -862,7 +862,6 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (kRK == 1) KL("k_dt", k_dt<<<1, 32, 0, h->st>>>(g, h->sc));
   const int nb = (g.ncol + NTHR_H - 1) / NTHR_H;
   const int nbu = (g.nvc + h->tb_uw - 1) / h->tb_uw, nbv = (g.nvc + h->tb_v - 1) / h->tb_v;
-  const int nbp = (g.nvc + h->tb_p - 1) / h->tb_p;
   if (h->ib) {
     dim3 gd(nb, h->nib);
     if (h->prec == LH_PREC_FP64) {
@@ -924,8 +923,10 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (fork) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
-  KL("k_press", k_press<<<nbp, h->tb_p, 0, h->st>>>(h->u1, h->u2, h->u3, h->p, h->psi, h->dg1, h->dg2, h->dg3, g,
-                                                  h->sc, kRK, need_div));
+  const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
+  KL("k_press", k_press2<<<nbp2, h->tb_p, 0, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
+                                                    (double *)h->p, (double *)h->psi, h->dg1, h->dg2, h->dg3, g,
+                                                    h->sc, kRK, need_div));
   if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }

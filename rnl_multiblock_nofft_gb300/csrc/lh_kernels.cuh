@@ -610,6 +610,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
   float flm = Fl[e0];
+#pragma unroll 4
   for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t e = (size_t)q * lstride + ci;
     const double up1 = u[e + lstride];
@@ -654,6 +655,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     u[(size_t)q * lstride + ci] = u0 + f2d_alu(y);
   }
   float x = y;
+#pragma unroll 4
   for (int q = qhi - 1; q >= qlo; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
@@ -693,6 +695,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
   float vvq = vvc[e0 + lstride];
+#pragma unroll 4
   for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t e = (size_t)q * lstride + ci;
     const double vp1 = u2[e + lstride];
@@ -732,6 +735,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
   }
   float x = y;
+#pragma unroll 4
   for (int q = qhi - 1; q >= qlo; --q) {
     const size_t e = (size_t)q * lstride + ci;
     const float2 ya = ys[e];
@@ -887,6 +891,9 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
     const double dd = g.dd;
     double2 y = czero<double2>();
     double2 vm = u2[(size_t)plo * nc + c];
+    // unrolled so the loads of several levels are in flight together (the column
+    // kernels run few warps per SM; memory-level parallelism hides the latency)
+#pragma unroll 4
     for (int qp = plo; qp <= phi; ++qp) {
       const int q = qp + 1;
       const size_t o = (size_t)q * nc + c;
@@ -909,6 +916,7 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
     const double kxd = dtrk * kxv, kzd = dtrk * kzv;
     double2 xn = y;
     double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
+#pragma unroll 4
     for (int qp = phi; qp >= plo; --qp) {
       const int q = qp + 1;
       const size_t o = (size_t)q * nc + c;
@@ -968,6 +976,111 @@ __global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double
     u2[(size_t)vlo * nc + c] = czero<double2>();
     u2[(size_t)vhi * nc + c] = czero<double2>();
   }
+  dmax = warp_max(dmax);
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
+}
+
+// k_press with one lane per (column, real/imaginary part): the pressure matrix is real,
+// so the two parts are independent systems; the i*k couplings of the divergence and of
+// v_corr exchange the other part through a shuffle within the lane pair. Twice the
+// warps of k_press for the same columns (the solves are latency-bound at C1 sizes).
+// Scalar views: element (level, col, part) at (level*ncol + col)*2 + part.
+__global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double *__restrict__ u2,
+                                                 double *__restrict__ u3, double *__restrict__ p,
+                                                 double *__restrict__ psi, const double *__restrict__ dg1,
+                                                 const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
+                                                 DevScalars *sc, int kRK, int need_div) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = tid >> 1, part = tid & 1;
+  const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
+  const int nc = g.ncol;
+  double dmax = 0.0;
+  if (vc < g.nvc) {
+    int c, bd;
+    vcol_of(g, vc, c, bd);
+    const int plo = g.bq[bd][4], phi = g.bq[bd][5];
+    const int ulo = g.bq[bd][0], uhi = g.bq[bd][1], vlo = g.bq[bd][2], vhi = g.bq[bd][3];
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    // i*k*z: real part -k*z.y, imaginary part k*z.x; lane `part` reads the other part
+    const double sgn = part ? 1.0 : -1.0;
+    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dtirk = sc->dti / aRb;
+    const double dt = sc->dt;
+    const double dd = g.dd;
+    const size_t ls = (size_t)nc * 2;
+    const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
+    double y = 0.0;
+    double vm = u2[(size_t)plo * ls + ci];
+#pragma unroll 4
+    for (int qp = plo; qp <= phi; ++qp) {
+      const int q = qp + 1;
+      const size_t e = (size_t)q * ls;
+      const double ao = u1[e + co], wo = u3[e + co], v = u2[e + ci];
+      const double th = dd * g.thu[q];
+      const double dv = sgn * (kxv * ao + kzv * wo) + th * (v - vm);
+      vm = v;
+      double rhs = dtirk * dv;
+      if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
+      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
+      y = (qp == plo) ? rhs * a2p : (rhs - A1 * y) * a2p;
+      psi[(size_t)qp * ls + ci] = y;
+    }
+    const double dtrk = dt * aRb;
+    const double dtrk2 = dtrk * dd;
+    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
+    double xn = y;
+    double vup = 0.0, aup_o = 0.0, wup_o = 0.0;
+#pragma unroll 4
+    for (int qp = phi; qp >= plo; --qp) {
+      const int q = qp + 1;
+      const size_t e = (size_t)q * ls;
+      double x;
+      if (qp == phi) x = xn;
+      else x = psi[(size_t)qp * ls + ci] - dg3[(size_t)qp * nc + c] * xn;
+      psi[(size_t)qp * ls + ci] = x;
+      p[(size_t)qp * ls + ci] += x;
+      // u -= dtrk i kx psi: the real part gains kxd*psi.y, the imaginary part loses kxd*psi.x
+      const double xo = __shfl_xor_sync(pm, x, 1);
+      const double a = u1[e + ci] - sgn * kxd * xo;
+      const double w = u3[e + ci] - sgn * kzd * xo;
+      u1[e + ci] = a;
+      u3[e + ci] = w;
+      double v = u2[e + ci];
+      if (q <= vhi - 1) {
+        v = v - dtrk2 * g.thv[q] * (xn - x);
+        u2[e + ci] = v;
+      }
+      // divergence of the corrected field at the level above (p level qp + 1)
+      const double ao = __shfl_xor_sync(pm, a, 1), wo = __shfl_xor_sync(pm, w, 1);
+      if (need_div && qp < phi) {
+        const double th = dd * g.thu[q + 1];
+        const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - v);
+        const double d2 = dvp * dvp;
+        dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+      }
+      aup_o = ao; wup_o = wo; vup = v;
+      xn = x;
+    }
+    if (need_div) {
+      const double th = dd * g.thu[plo + 1];
+      const double vb = u2[(size_t)plo * ls + ci];
+      const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - vb);
+      const double d2 = dvp * dvp;
+      dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+    }
+    if (bd <= 1) {
+      u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
+      u3[(size_t)ulo * ls + ci] = g.gwbc3 * u3[(size_t)(ulo + 1) * ls + ci];
+    }
+    if (bd >= 1) {
+      u1[(size_t)uhi * ls + ci] = g.gwbc1 * u1[(size_t)(uhi - 1) * ls + ci];
+      u3[(size_t)uhi * ls + ci] = g.gwbc3 * u3[(size_t)(uhi - 1) * ls + ci];
+    }
+    u2[(size_t)vlo * ls + ci] = 0.0;
+    u2[(size_t)vhi * ls + ci] = 0.0;
+  }
+  // |div|^2 = re^2 + im^2 per level, summed over the lane pair above
   dmax = warp_max(dmax);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
 }
