@@ -116,9 +116,9 @@ template <typename T> struct C2;
 template <> struct C2<double> { typedef double2 t; };
 template <> struct C2<float> { typedef float2 t; };
 
-template <typename V> __device__ __forceinline__ V cadd(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
-template <typename V> __device__ __forceinline__ V csub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
-template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+template <typename V> __host__ __device__ __forceinline__ V cadd(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename V> __host__ __device__ __forceinline__ V csub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename V> __host__ __device__ __forceinline__ V cmul(V a, V b) {
   V r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
 }
 template <typename V, typename S> __device__ __forceinline__ V cscale(V a, S s) { V r; r.x = a.x * s; r.y = a.y * s; return r; }
@@ -133,8 +133,49 @@ template <typename V, typename S> __device__ __forceinline__ V cimul(S k, V a) {
 // INV = true: backward (exp(+i)), unscaled. Returns the buffer holding the result.
 // ---------------------------------------------------------------------------
 template <int R, bool INV, typename V>
-__device__ __forceinline__ void dftR(V *v) {
-  if (R == 2) {
+__host__ __device__ __forceinline__ void dftR(V *v) {
+  if (R == 8) {
+    // two radix-4 DFTs on the even and odd elements, then W8^k on the odd ones
+    typedef decltype(v[0].x) S;
+    const S h = (S)0.70710678118654752440084436210485;  // 1/sqrt(2)
+    V e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    dftR<4, INV>(e);
+    dftR<4, INV>(o);
+    V t1, t2, t3;
+    // forward W8 = (1 - i)/sqrt2, W8^2 = -i, W8^3 = (-1 - i)/sqrt2; backward conjugate
+    if (INV) {
+      t1.x = h * (o[1].x - o[1].y); t1.y = h * (o[1].x + o[1].y);
+      t2.x = -o[2].y; t2.y = o[2].x;
+      t3.x = -h * (o[3].x + o[3].y); t3.y = h * (o[3].x - o[3].y);
+    } else {
+      t1.x = h * (o[1].x + o[1].y); t1.y = h * (o[1].y - o[1].x);
+      t2.x = o[2].y; t2.y = -o[2].x;
+      t3.x = h * (o[3].y - o[3].x); t3.y = -h * (o[3].x + o[3].y);
+    }
+    v[0] = cadd(e[0], o[0]); v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], t1); v[5] = csub(e[1], t1);
+    v[2] = cadd(e[2], t2); v[6] = csub(e[2], t2);
+    v[3] = cadd(e[3], t3); v[7] = csub(e[3], t3);
+  } else if (R == 6) {
+    // two radix-3 DFTs on the even and odd elements, then W6^k on the odd ones
+    typedef decltype(v[0].x) S;
+    const S s3 = (S)0.86602540378443864676372317075294;  // sin(2 pi / 6)
+    V e[3] = {v[0], v[2], v[4]}, o[3] = {v[1], v[3], v[5]};
+    dftR<3, INV>(e);
+    dftR<3, INV>(o);
+    V t1, t2;
+    // forward W6 = (1/2, -s3), W6^2 = (-1/2, -s3); backward conjugate
+    if (INV) {
+      t1.x = (S)0.5 * o[1].x - s3 * o[1].y; t1.y = (S)0.5 * o[1].y + s3 * o[1].x;
+      t2.x = (S)-0.5 * o[2].x - s3 * o[2].y; t2.y = (S)-0.5 * o[2].y + s3 * o[2].x;
+    } else {
+      t1.x = (S)0.5 * o[1].x + s3 * o[1].y; t1.y = (S)0.5 * o[1].y - s3 * o[1].x;
+      t2.x = (S)-0.5 * o[2].x + s3 * o[2].y; t2.y = (S)-0.5 * o[2].y - s3 * o[2].x;
+    }
+    v[0] = cadd(e[0], o[0]); v[3] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], t1); v[4] = csub(e[1], t1);
+    v[2] = cadd(e[2], t2); v[5] = csub(e[2], t2);
+  } else if (R == 2) {
     V a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
@@ -164,7 +205,7 @@ __device__ __forceinline__ void dftR(V *v) {
 
 // ---------------------------------------------------------------------------
 // N and NL are compile-time (index arithmetic becomes shifts and multiplies); the
-// radices run 4, ..., 4, [2], 3, ..., 3. IL selects the layout
+// radices run 8, ..., then 6, 4, 2 or 3 as the remaining length allows (384 = 8*8*6). IL selects the layout
 // of the lines in shared memory: IL = false, line-contiguous (element e of line
 // l at l*N + e, threads over e); IL = true, interleaved (at e*NL + l, threads
 // over l first), which makes every stage's loads and stores bank-conflict free.
@@ -205,7 +246,7 @@ __device__ __forceinline__ V *fft_rec_c(V *a, V *b, const V *__restrict__ tw) {
     return a;
   } else {
     constexpr int rem = N / Ns;
-    constexpr int R = (rem % 4 == 0) ? 4 : ((rem % 2 == 0) ? 2 : 3);
+    constexpr int R = (rem % 8 == 0) ? 8 : ((rem % 6 == 0) ? 6 : ((rem % 4 == 0) ? 4 : ((rem % 2 == 0) ? 2 : 3)));
     fft_stage_c<R, INV, N, Ns, NL, IL>(a, b, tw);
     __syncthreads();
     return fft_rec_c<INV, N, Ns * R, NL, IL>(b, a, tw);
