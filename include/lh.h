@@ -98,6 +98,9 @@ typedef struct lh_config {
    * N(1:2,1), Ngal(1:2,1)); these are the core band's (band 2). Equal values give a
    * single-resolution channel. The core modes must be a subset of the wall modes. */
   int32_t N1c, N2c, Ngal1c, Ngal2c;
+  /* Post tiles of the wall texture (ntilex, ntilez of boundary_post_coll.f90; 0 = none):
+   * the tile-conditioned statistics average over them. */
+  int32_t ntilex, ntilez;
 } lh_config;
 
 /* Scalars of the time integration (module declaration: t, dt, dti, dtc, err, mpgx, QxT, Qx, iter).
@@ -172,6 +175,25 @@ void *lh_stream(lh_handle *h);
  * (FOU3D.f90:766-781, 2253-2272) over cft/rft (cft_buff.f:1-65, rft_buff.f:24-86). */
 int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int nplanes);
 int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes);
+
+/* ---- statistics (stats.f90:1-107), accumulated on the device ----
+ * lh_stats_accumulate adds the current state's statistics (istat += 1), as stats() does
+ * when called from nonlinear at kRK = 1 (FOU3D.f90:298-373), over the interior planes:
+ * per level, sums over the physical plane of quantities
+ *   0 U, 1 U^2, 2 W, 3 W^2, 4 U V, 5 U W   (u levels; V interpolated to the centres)
+ *   6 V, 7 V^2, 8 V W                      (v levels; W interpolated to the faces)
+ * and the same nine sums conditioned on the position inside a post tile (conddown1/2,
+ * condup1/2, stats.f90:109-250): wall-band planes only, indexed by the distance j1 = 1..
+ * from the wall, the top band mirrored onto the bottom with the sign of V flipped. The
+ * pressure and vorticity statistics are not formed. Sums are in FP64 from planes in the
+ * form's transform precision. */
+int lh_stats_accumulate(lh_handle *h);
+int lh_stats_reset(lh_handle *h);
+/* ncl: conditioned levels; dnx, dnz: tile size in physical points (0 without tiles) */
+int lh_stats_dims(lh_handle *h, int *ncl, int *dnx, int *dnz);
+/* plane: [9][nyu] (u-level quantities at u index j+dny, v-level ones at v index j+dny);
+ * cond: [9][ncl][dnz][dnx] (may be NULL); istat: number of accumulations. Blocking. */
+int lh_stats_get(lh_handle *h, double *plane, double *cond, int64_t *istat);
 
 /* Number of CUDA kernel launches issued by the handle since creation (graph
  * replays count every kernel node). */

@@ -145,6 +145,10 @@ struct orc {
   fftplan pxc, pzc;
   unsigned char *lng;
   int bj[3][3][2]; /* [band 0..2][grid: 0 u, 1 v, 2 p][lo, hi], reference j */
+  /* statistics (stats.f90): plane sums [9][nu], tile-conditioned sums [9][ncl][dnz][dnx] */
+  double *st_pl, *st_cd;
+  int st_ncl, st_dnx, st_dnz;
+  int64_t istat;
   cplx *u1, *u2, *u3, *p;
   cplx *Nu1, *Nu2, *Nu3, *du1, *du2, *du3, *psi, *div;
   cplx *u1i, *u2i, *u3i; /* u1,u3 at v levels; u2 at u levels */
@@ -340,7 +344,7 @@ void orc_destroy(orc *O) {
                   O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
                   O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
                   O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2,
-                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng};
+                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng, O->st_pl, O->st_cd};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   plan_free(&O->px); plan_free(&O->pz); plan_free(&O->pxc); plan_free(&O->pzc);
   free(O);
@@ -589,11 +593,10 @@ static void triad_products(orc *O, double *pu1m, double *pu3m, double *pu2m) {
 /* ------------------------------------------------------------------------- */
 /* nonlinear (FOU3D.f90:41-425 with ops_in_planes2)                          */
 /* ------------------------------------------------------------------------- */
-static void nonlinear(orc *O, int kRK) {
+/* interp_u (u1,u3 -> v levels) and interp_v (u2 -> u levels) of every band's columns
+ * over the band's levels, FOU3D.f90:427-474 */
+static void interp_all(orc *O) {
   const int nc = O->ncol;
-  const double dd = O->c.ddthetavi;
-  /* interp_u (u1,u3 -> v levels) and interp_v (u2 -> u levels) of every band's columns
-   * over the band's levels, FOU3D.f90:427-474 */
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < nc; ++c) {
     int bs[2];
@@ -618,6 +621,12 @@ static void nonlinear(orc *O, int kRK) {
       PL(O->u2i, UIDX(hi))[c] = O->c.gw_interp[b][1] * (PL(O->u2, UIDX(vhi))[c] - i2) + i2;
     }
   }
+}
+
+static void nonlinear(orc *O, int kRK) {
+  const int nc = O->ncol;
+  const double dd = O->c.ddthetavi;
+  interp_all(O);
 
   const size_t ppF = (size_t)O->G1 * O->G2;
   double u1m = 0.0, u3m = 0.0, u2m = 1e-6;
@@ -1156,6 +1165,117 @@ int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes) {
       phys_to_four_plane(O, &vf, phys + pp * q, (cplx *)spec + ns * q, &w);
     pwork_free(&w);
   }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* statistics (stats.f90:1-250) of the current state over the interior planes  */
+/* ------------------------------------------------------------------------- */
+static void stats_alloc(orc *O) {
+  const int *N3 = O->c.N3, *N4 = O->c.N4;
+  int ncl = N4[1] - N4[0];
+  if (N4[3] - N4[2] > ncl) ncl = N4[3] - N4[2];
+  if (N3[1] - N3[0] > ncl) ncl = N3[1] - N3[0];
+  if (N3[3] - N3[2] > ncl) ncl = N3[3] - N3[2];
+  const int tx = O->c.ntilex, tz = O->c.ntilez;
+  O->st_ncl = ncl;
+  O->st_dnx = (tx > 0 && tz > 0) ? O->G1 / tx : 0;
+  O->st_dnz = (tx > 0 && tz > 0) ? O->G2 / tz : 0;
+  O->st_pl = (double *)calloc((size_t)9 * O->nu, sizeof(double));
+  O->st_cd = (double *)calloc((size_t)9 * ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1), sizeof(double));
+  O->istat = 0;
+}
+
+/* one plane's sums: the plane statistics of stats(), and conddown/condup
+ * (stats.f90:109-250) on wall-band planes: tile position (i, k) = (m mod dnx, l mod dnz),
+ * level j1 = j - Ny(grid,0) at the bottom, Ny(grid,nband) + 1 - j at the top, where V
+ * enters with the sign -1 (xsign) */
+static void stats_plane(orc *O, int isU, int j, const double *a, const double *b, const double *c3, int G1,
+                        int G2, int fine) {
+  const size_t pp = (size_t)G1 * G2;
+  double s[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+  double *P = O->st_pl;
+  const int q = UIDX(j), nu = O->nu;
+  for (size_t e = 0; e < pp; ++e) {
+    if (isU) {
+      s[0] += a[e]; s2[0] += a[e] * a[e];
+      s[1] += c3[e]; s2[1] += c3[e] * c3[e];
+      s[2] += a[e] * b[e];
+      s2[2] += a[e] * c3[e];
+    } else {
+      s[0] += b[e]; s2[0] += b[e] * b[e];
+      s[1] += b[e] * c3[e];
+    }
+  }
+  if (isU) {
+    P[0 * nu + q] += s[0]; P[1 * nu + q] += s2[0]; P[2 * nu + q] += s[1]; P[3 * nu + q] += s2[1];
+    P[4 * nu + q] += s[2]; P[5 * nu + q] += s2[2];
+  } else {
+    P[6 * nu + q] += s[0]; P[7 * nu + q] += s2[0]; P[8 * nu + q] += s[1];
+  }
+  const int dnx = O->st_dnx, dnz = O->st_dnz;
+  if (!dnx || !fine) return;
+  const int *NN = isU ? O->c.N4 : O->c.N3;
+  int j1, sv;
+  if (j <= NN[1]) { j1 = j - NN[0]; sv = 1; }
+  else if (j > NN[2]) { j1 = NN[3] + 1 - j; sv = -1; }
+  else return;
+  const int ncl = O->st_ncl;
+#define CD(qty, k, i) O->st_cd[(((size_t)(qty) * ncl + (j1 - 1)) * dnz + (k)) * dnx + (i)]
+  for (int l = 0; l < G2; ++l)
+    for (int m = 0; m < G1; ++m) {
+      const size_t e = (size_t)l * G1 + m;
+      const int i = m % dnx, k = l % dnz;
+      if (isU) {
+        CD(0, k, i) += a[e]; CD(1, k, i) += a[e] * a[e];
+        CD(2, k, i) += c3[e]; CD(3, k, i) += c3[e] * c3[e];
+        CD(4, k, i) += a[e] * (b[e] * sv); CD(5, k, i) += a[e] * c3[e];
+      } else {
+        CD(6, k, i) += b[e] * sv; CD(7, k, i) += b[e] * b[e];
+        CD(8, k, i) += (b[e] * sv) * c3[e];
+      }
+    }
+#undef CD
+}
+
+int orc_stats_accumulate(orc *O) {
+  if (!O->st_pl) stats_alloc(O);
+  interp_all(O);
+  const size_t ppF = (size_t)O->G1 * O->G2;
+  double *f1 = (double *)malloc(sizeof(double) * ppF), *f2 = (double *)malloc(sizeof(double) * ppF);
+  double *f3 = (double *)malloc(sizeof(double) * ppF);
+  pwork w; pwork_init(O, &w);
+  for (int j = O->c.N4[0] + 1; j <= O->c.N4[3]; ++j) {
+    pview v;
+    const int fine = fine_u(O, j);
+    view_of(O, fine, &v);
+    four_to_phys_plane(O, &v, PL(O->u1, UIDX(j)), f1, &w);
+    four_to_phys_plane(O, &v, PL(O->u2i, UIDX(j)), f2, &w);
+    four_to_phys_plane(O, &v, PL(O->u3, UIDX(j)), f3, &w);
+    stats_plane(O, 1, j, f1, f2, f3, v.G1, v.G2, fine);
+  }
+  for (int j = O->c.N3[0] + 1; j <= O->c.N3[3]; ++j) {
+    pview v;
+    const int fine = fine_v(O, j);
+    view_of(O, fine, &v);
+    four_to_phys_plane(O, &v, PL(O->u1i, UIDX(j)), f1, &w);
+    four_to_phys_plane(O, &v, PL(O->u2, UIDX(j)), f2, &w);
+    four_to_phys_plane(O, &v, PL(O->u3i, UIDX(j)), f3, &w);
+    stats_plane(O, 0, j, f1, f2, f3, v.G1, v.G2, fine);
+  }
+  pwork_free(&w);
+  free(f1); free(f2); free(f3);
+  O->istat += 1;
+  return 0;
+}
+
+int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims) {
+  if (!O->st_pl) stats_alloc(O);
+  if (plane) memcpy(plane, O->st_pl, sizeof(double) * 9 * (size_t)O->nu);
+  const size_t nc = (size_t)9 * O->st_ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1);
+  if (cond && O->st_dnx) memcpy(cond, O->st_cd, sizeof(double) * nc);
+  if (istat) *istat = O->istat;
+  if (dims) { dims[0] = O->st_ncl; dims[1] = O->st_dnx; dims[2] = O->st_dnz; }
   return 0;
 }
 

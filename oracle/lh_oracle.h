@@ -19,4 +19,7 @@ int orc_step(orc *O);
 int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes);
 int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes);
 int orc_set_threads(int n);
+int orc_stats_accumulate(orc *O);
+/* dims: ncl, dnx, dnz */
+int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims);
 #endif

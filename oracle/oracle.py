@@ -47,6 +47,8 @@ def lib():
         L.orc_four_to_phys.argtypes = [vp, dp, dp, C.c_int]
         L.orc_phys_to_four.argtypes = [vp, dp, dp, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_stats_accumulate.argtypes = [vp]
+        L.orc_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -134,6 +136,20 @@ class Oracle:
         for _ in range(n):
             if lib().orc_step(self.h) != 0:
                 raise RuntimeError("orc_step failed")
+
+    def stats_accumulate(self):
+        lib().orc_stats_accumulate(self.h)
+
+    def stats(self):
+        """(plane [9][nyu], cond [9][ncl][dnz][dnx] or None, istat)"""
+        dims = (C.c_int * 3)()
+        lib().orc_stats_get(self.h, None, None, None, dims)
+        ncl, dnx, dnz = dims[0], dims[1], dims[2]
+        plane = np.zeros((9, self.s.nyu))
+        cond = np.zeros((9, ncl, dnz, dnx)) if dnx else None
+        ist = C.c_int64()
+        lib().orc_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist), dims)
+        return plane, cond, ist.value
 
     def four_to_phys(self, spec: np.ndarray) -> np.ndarray:
         spec = np.ascontiguousarray(spec, np.complex128)

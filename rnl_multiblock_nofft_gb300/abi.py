@@ -41,6 +41,7 @@ class LhConfig(C.Structure):
         ("triad_nsets", C.c_int32), ("triad_off", _lp), ("triad_len", _lp), ("triad_data", _bp),
         ("triad_set_u", _ip), ("triad_set_v", _ip),
         ("N1c", C.c_int32), ("N2c", C.c_int32), ("Ngal1c", C.c_int32), ("Ngal2c", C.c_int32),
+        ("ntilex", C.c_int32), ("ntilez", C.c_int32),
     ]
 
 
@@ -79,6 +80,8 @@ def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
     c.N1, c.N2 = s.N1, s.N2
     c.Ngal1, c.Ngal2 = s.G1, s.G2
     c.N1c, c.N2c, c.Ngal1c, c.Ngal2c = s.N1c, s.N2c, s.G1c, s.G2c
+    if p_has_tiles(s):
+        c.ntilex, c.ntilez = int(s.p.ntilex), int(s.p.ntilez)
     c.dny, c.nn = s.dny, s.nn
     for b in range(4):
         c.N3[b] = int(s.N[2, b])
@@ -122,6 +125,11 @@ def make_config(s: ChannelSetup, precision: int = LH_PREC_FP64, triads=None):
         c.triad_set_u = i32(pk["set_u"])
         c.triad_set_v = i32(pk["set_v"])
     return c, keep
+
+
+def p_has_tiles(s: ChannelSetup) -> bool:
+    p = s.p
+    return p.geometry_type == 2 and p.ntilex > 0 and p.ntilez > 0 and s.G1 % p.ntilex == 0 and s.G2 % p.ntilez == 0
 
 
 def cfield_shape(s: ChannelSetup):

@@ -55,6 +55,10 @@ struct lh_handle {
   int2 *d_vcol;             // virtual columns of the solve kernels (multiblock)
   int *d_bcols;             // long columns, then short columns (band I/O)
   int nlong, nshort;
+  // statistics
+  double *st_pl, *st_cd;
+  int st_ncl, st_dnx, st_dnz, st_ntx;
+  long long istat;
   // triad-list nonlinear form
   int triad;
   TriadGeo tg;
@@ -167,6 +171,8 @@ static cudaError_t set_attrs_sized(int lim) {
   const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv_nl<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass_nl<T, N>, A, lim);
+  // k_xstats also holds a small static reduction array
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xstats<T, N>, A, lim - 1024);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_nl<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<T, N>, A, lim);
@@ -502,6 +508,18 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
       }
     }
   }
+  {  // statistics accumulators
+    const int *N3 = cfg->N3, *N4 = cfg->N4;
+    int ncl = std::max(std::max(N4[1] - N4[0], N4[3] - N4[2]), std::max(N3[1] - N3[0], N3[3] - N3[2]));
+    const bool tiles = cfg->ntilex > 0 && cfg->ntilez > 0 && g.G1 % cfg->ntilex == 0 && g.G2 % cfg->ntilez == 0;
+    h->st_ncl = ncl;
+    h->st_ntx = tiles ? cfg->ntilex : 0;
+    h->st_dnx = tiles ? g.G1 / cfg->ntilex : 0;
+    h->st_dnz = tiles ? g.G2 / cfg->ntilez : 0;
+    h->istat = 0;
+    ZA(h->st_pl, sizeof(double) * 9 * (size_t)nu);
+    ZA(h->st_cd, sizeof(double) * 9 * (size_t)ncl * (tiles ? (size_t)h->st_dnx * h->st_dnz : 1));
+  }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
   h->triad = (cfg->nonlin_form == LH_NONLIN_TRIADS) ? 1 : 0;
@@ -563,7 +581,7 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
                   h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
-                  h->ysv, h->a3v};
+                  h->ysv, h->a3v, h->st_pl, h->st_cd};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -1006,6 +1024,70 @@ extern "C" int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, i
   *nout = n;
   if (rc != LH_OK) return rc;
   if (e != cudaSuccess) return fail(h, LH_ECUDA, cudaGetErrorString(e));
+  return LH_OK;
+}
+
+// statistics of the current state: the inverse transforms of the nonlinear stage, then
+// the sums of stats.f90 (k_xstats), per plane class
+template <typename T, int N>
+static int launch_xstats(lh_handle *h, const Geo &g, int nslots, const void *twx) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = pb_xpass<V>(N);
+  dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
+  KL("k_xstats", k_xstats<T, N><<<grid, NTHR_H, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
+                     (const V *)h->A, g, (const V *)twx, h->st_pl, h->st_cd, h->st_ncl, h->st_dnx, h->st_dnz,
+                     h->st_ntx));
+  return LH_OK;
+}
+template <typename T>
+static int stats_launches(lh_handle *h) {
+  for (int vi = 0; vi < h->nviews; ++vi) {
+    const Geo &g = h->gv[vi];
+    const int nslots = g.nuI + g.nvI;
+    if (nslots == 0) continue;
+    int rc = LH_EINVAL;
+    LH_DISPATCH(g.G2, rc = launch_zinv<T, N>(h, g, nslots, h->twv[vi][1]));
+    if (rc) return rc;
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G1, rc = launch_xstats<T, N>(h, g, nslots, h->twv[vi][0]));
+    if (rc) return rc;
+  }
+  return LH_OK;
+}
+
+extern "C" int lh_stats_accumulate(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  const int rc = (h->prec == LH_PREC_FP64) ? stats_launches<double>(h) : stats_launches<float>(h);
+  if (rc) return rc;
+  h->istat += 1;
+  return LH_OK;
+}
+
+extern "C" int lh_stats_reset(lh_handle *h) {
+  if (!h) return LH_EINVAL;
+  const size_t ncd = 9 * (size_t)h->st_ncl * (h->st_dnx ? (size_t)h->st_dnx * h->st_dnz : 1);
+  CK(cudaMemsetAsync(h->st_pl, 0, sizeof(double) * 9 * (size_t)h->g.nu, h->st));
+  CK(cudaMemsetAsync(h->st_cd, 0, sizeof(double) * ncd, h->st));
+  h->istat = 0;
+  return LH_OK;
+}
+
+extern "C" int lh_stats_dims(lh_handle *h, int *ncl, int *dnx, int *dnz) {
+  if (!h) return LH_EINVAL;
+  if (ncl) *ncl = h->st_ncl;
+  if (dnx) *dnx = h->st_dnx;
+  if (dnz) *dnz = h->st_dnz;
+  return LH_OK;
+}
+
+extern "C" int lh_stats_get(lh_handle *h, double *plane, double *cond, int64_t *istat) {
+  if (!h) return LH_EINVAL;
+  if (plane) CK(cudaMemcpyAsync(plane, h->st_pl, sizeof(double) * 9 * (size_t)h->g.nu, cudaMemcpyDeviceToHost, h->st));
+  if (cond && h->st_dnx)
+    CK(cudaMemcpyAsync(cond, h->st_cd, sizeof(double) * 9 * (size_t)h->st_ncl * h->st_dnx * h->st_dnz,
+                       cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (istat) *istat = h->istat;
   return LH_OK;
 }
 

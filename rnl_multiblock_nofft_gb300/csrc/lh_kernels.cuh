@@ -253,6 +253,105 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
 }
 
 // ============================================================================
+// Statistics (stats.f90:1-250) of one plane class: the x pass's gather and inverse
+// transform, then the plane sums (per level) and the tile-conditioned sums (wall-band
+// planes: conddown1/2 at the bottom, condup1/2 mirrored at the top with V's sign
+// flipped). u slots hold (u, v interpolated, w), v slots (u interpolated, v, w
+// interpolated). Sums: block reduction, one FP64 atomic per quantity and block; the
+// conditioned sums add the ntilex tiles of a row in registers first.
+// pl: [9][nu]; cd: [9][ncl][dnz][dnx].
+// ============================================================================
+template <typename T, int N>
+__global__ void __launch_bounds__(NTHR) k_xstats(const typename C2<T>::t *__restrict__ A, Geo g,
+                                                 const typename C2<T>::t *__restrict__ twx, double *__restrict__ pl,
+                                                 double *__restrict__ cd, int ncl, int dnx, int dnz, int ntx) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = pb_xpass<V>(N);
+  constexpr int G1 = N, H = N / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[NTHR / 32][6];
+  const int G2 = g.G2, N1h = g.N1h;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + 4 * PB * G1;
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const int l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const size_t fstride = (size_t)G2 * N1h;
+  const V *Af = A + (size_t)slot * 3 * fstride;
+  for (int idx = threadIdx.x; idx < 3 * PB * G1; idx += blockDim.x) {
+    const int line = idx / G1, m = idx - line * G1;
+    const int f = line / PB, pb = line - f * PB;
+    V z = czero<V>();
+    if (pb < npairs) {
+      const int l = l0 + 2 * pb;
+      int k = m;
+      bool conjpart = false;
+      if (m > H) { k = G1 - m; conjpart = true; }
+      if (k < N1h) {
+        V a = Af[f * fstride + (size_t)l * N1h + k];
+        V b = Af[f * fstride + (size_t)(l + 1) * N1h + k];
+        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
+        if (!conjpart) { z.x = a.x - b.y; z.y = a.y + b.x; }
+        else { z.x = a.x + b.y; z.y = -a.y + b.x; }
+      }
+    }
+    b0[idx] = z;
+  }
+  __syncthreads();
+  const V *res = line_fft<true, N, 3 * PB, false>(b0, b1, twx);
+  // plane sums
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    if (pb >= npairs) continue;
+    const V u = res[(0 * PB + pb) * G1 + m], v = res[(1 * PB + pb) * G1 + m], w = res[(2 * PB + pb) * G1 + m];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const double a = to_d(h ? u.y : u.x), b = to_d(h ? v.y : v.x), c = to_d(h ? w.y : w.x);
+      if (isU) { s[0] += a; s[1] += a * a; s[2] += c; s[3] += c * c; s[4] += a * b; s[5] += a * c; }
+      else { s[0] += b; s[1] += b * b; s[2] += b * c; }
+    }
+  }
+  const int nq = isU ? 6 : 3, qb = isU ? 0 : 6;
+  for (int t = 0; t < nq; ++t) {
+    double x = s[t];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][t] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    double x = 0;
+    for (int wi = 0; wi < (int)(blockDim.x >> 5); ++wi) x += red[wi][threadIdx.x];
+    atomicAdd(&pl[(size_t)(qb + threadIdx.x) * g.nu + q], x);
+  }
+  // tile-conditioned sums on the wall-band planes
+  if (!dnx) return;
+  const int j = q - g.dny;
+  const int *NN = isU ? g.N4 : g.N3;
+  int j1, sv;
+  if (j <= NN[1]) { j1 = j - NN[0]; sv = 1; }
+  else if (j > NN[2]) { j1 = NN[3] + 1 - j; sv = -1; }
+  else return;
+  for (int idx = threadIdx.x; idx < 2 * npairs * dnx; idx += blockDim.x) {
+    const int rr = idx / dnx, i = idx - rr * dnx;
+    const int pb = rr >> 1, h = rr & 1;
+    const int k = (l0 + rr) % dnz;
+    double c[6] = {0, 0, 0, 0, 0, 0};
+    for (int ix = 0; ix < ntx; ++ix) {
+      const int m = i + dnx * ix;
+      const V u = res[(0 * PB + pb) * G1 + m], v = res[(1 * PB + pb) * G1 + m], w = res[(2 * PB + pb) * G1 + m];
+      const double a = to_d(h ? u.y : u.x), b = to_d(h ? v.y : v.x) * sv, cc = to_d(h ? w.y : w.x);
+      if (isU) { c[0] += a; c[1] += a * a; c[2] += cc; c[3] += cc * cc; c[4] += a * b; c[5] += a * cc; }
+      else { c[0] += b; c[1] += b * b; c[2] += b * cc; }
+    }
+    for (int t = 0; t < nq; ++t)
+      atomicAdd(&cd[(((size_t)(qb + t) * ncl + (j1 - 1)) * dnz + k) * dnx + i], c[t]);
+  }
+}
+
+// ============================================================================
 // T3: forward z transforms + der_x/der_z. grid: x = kx group (KB), y = level slot.
 // u level: products uu, uw, vv, ww -> N1xz, N3xz, vvc.   v level: uv, wv -> N2xz, uvf, wvf.
 // Outputs are complex in the transform precision (TO = T).

@@ -17,7 +17,8 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
 _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
-           "lh_upload_band", "lh_download_band",
+           "lh_upload_band", "lh_download_band", "lh_stats_accumulate", "lh_stats_reset", "lh_stats_dims",
+           "lh_stats_get",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
@@ -50,6 +51,10 @@ def load(path: str = _LIB_PATH):
     L.lh_upload_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_download_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_upload_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
+    L.lh_stats_accumulate.argtypes = [vp]
+    L.lh_stats_reset.argtypes = [vp]
+    L.lh_stats_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.lh_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
     L.lh_download_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_set_scalars.argtypes = [vp, C.POINTER(LhScalars)]
     L.lh_get_scalars.argtypes = [vp, C.POINTER(LhScalars)]
@@ -153,6 +158,23 @@ class GpuChannel:
             self._check(self.L.lh_download_band(self.h, b, *[_dptr(a) for a in arrs]))
             out[b] = arrs
         return out
+
+    # ---- statistics (stats.f90) ----
+    def stats_accumulate(self):
+        self._check(self.L.lh_stats_accumulate(self.h))
+
+    def stats_reset(self):
+        self._check(self.L.lh_stats_reset(self.h))
+
+    def stats(self):
+        """(plane [9][nyu], cond [9][ncl][dnz][dnx] or None, istat); see include/lh.h."""
+        ncl, dnx, dnz = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.lh_stats_dims(self.h, C.byref(ncl), C.byref(dnx), C.byref(dnz)))
+        plane = np.zeros((9, self.s.nyu))
+        cond = np.zeros((9, ncl.value, dnz.value, dnx.value)) if dnx.value else None
+        ist = C.c_int64()
+        self._check(self.L.lh_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist)))
+        return plane, cond, ist.value
 
     def set_scalars(self, **kw):
         s = LhScalars()
