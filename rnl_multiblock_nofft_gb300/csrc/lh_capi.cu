@@ -522,6 +522,10 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
+  if (cudaFuncSetAttribute((const void *)k_meanflow_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) !=
+      cudaSuccess) {
+    rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_meanflow_pcr)"); lh_destroy(h); return rc;
+  }
   h->triad = (cfg->nonlin_form == LH_NONLIN_TRIADS) ? 1 : 0;
   h->d_terms = nullptr; h->d_wb = h->d_lid = h->d_tmap = nullptr; h->tri_nterms = 0;
   if (h->triad) {  // expand and upload the triad lists (nonlinRead, start.f90:2983-3069)
@@ -865,6 +869,11 @@ static const void *fp64_tw(lh_handle *h, bool x) { return x ? h->twx64 : h->twz6
 static int meanflow(lh_handle *h, int kRK) {
   const Geo &g = h->g;
   if (g.flag_ctpress != 0) return LH_OK;
+  const size_t pcr = 8 * sizeof(double) * (size_t)(g.nn + 3);
+  if (pcr <= 96 * 1024) {  // parallel cyclic reduction in one block
+    KL("k_meanflow", k_meanflow_pcr<<<1, 512, pcr, h->st>>>(h->u1, g, h->sc, kRK));
+    return LH_OK;
+  }
   const size_t mb = 6 * sizeof(double) * (size_t)(g.nn + 3);
   const int sm = mb <= 48 * 1024 ? 1 : 0;
   KL("k_meanflow", k_meanflow<<<1, 256, sm ? mb : 0, h->st>>>(h->u1, g, h->sc, kRK, h->mfw, sm));

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
       oth[(1 * PB + pb) * G1 + m] = p1;
       oth[(2 * PB + pb) * G1 + m] = p2;
       oth[(3 * PB + pb) * G1 + m] = p3;
-      if (valid) {
+      if (valid && doCFL) {
         m1 = fmax(m1, fmax(fabs(u.x), fabs(u.y)));
         m3 = fmax(m3, fmax(fabs(w.x), fabs(w.y)));
       }
@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
       p1.x = w.x * v.x; p1.y = w.y * v.y;
       oth[(0 * PB + pb) * G1 + m] = p0;
       oth[(1 * PB + pb) * G1 + m] = p1;
-      if (valid) m2 = fmax(m2, fmax(fabs(v.x), fabs(v.y)) * thv);
+      if (valid && doCFL) m2 = fmax(m2, fmax(fabs(v.x), fabs(v.y)) * thv);
     }
   }
   if (doCFL) {
@@ -892,6 +892,79 @@ __global__ void k_meanflow(double2 *__restrict__ u1, Geo g, DevScalars *sc, int 
   __syncthreads();
   const double gg = gg_sh;
   for (int j = threadIdx.x; j <= nn + 2; j += blockDim.x) u1[(size_t)(j + dny) * nc].x = ur[j] + gg * u11[j];
+}
+
+// flowrate_corr with the tridiagonal system solved by parallel cyclic reduction in one
+// block (log2(n) steps) instead of k_meanflow's serial recurrence (its FP64 divisions
+// were the latency); same system and correction, the solution's rounding differs.
+// Shared memory: 8 n doubles (two copies of the four diagonals/rhs).
+__global__ void __launch_bounds__(512) k_meanflow_pcr(double2 *__restrict__ u1, Geo g, DevScalars *sc, int kRK) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double gg_sh;
+  const int nn = g.nn, n = nn + 3, dny = g.dny, nc = g.ncol, nu = g.nu;
+  double *A = reinterpret_cast<double *>(smem_raw), *B = A + n, *Cc = B + n, *D = Cc + n;
+  double *A2 = D + n, *B2 = A2 + n, *C2b = B2 + n, *D2 = C2b + n;
+  const double dt = sc->dt;
+  const double bdt = -g.dRK[kRK - 1] * dt;
+  const double beta = g.bRK[kRK - 1] * dt / g.Re;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    if (j == 0) { A[j] = 0.0; B[j] = 1.0; Cc[j] = g.gw[1][0]; D[j] = 0.0; }
+    else if (j == nn + 2) { A[j] = g.gw[1][1]; B[j] = 1.0; Cc[j] = 0.0; D[j] = 0.0; }
+    else {
+      A[j] = -beta * g.d2u[j + dny];
+      B[j] = 1.0 - beta * g.d2u[nu + j + dny];
+      Cc[j] = -beta * g.d2u[2 * nu + j + dny];
+      D[j] = bdt;
+    }
+  }
+  __syncthreads();
+  for (int st = 1; st < n; st *= 2) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int im = i - st, ip = i + st;
+      double a = 0.0, b = B[i], c = 0.0, d = D[i];
+      if (im >= 0) {
+        const double al = -A[i] / B[im];
+        a = al * A[im];
+        b += al * Cc[im];
+        d += al * D[im];
+      }
+      if (ip < n) {
+        const double ga = -Cc[i] / B[ip];
+        c = ga * Cc[ip];
+        b += ga * A[ip];
+        d += ga * D[ip];
+      }
+      A2[i] = a; B2[i] = b; C2b[i] = c; D2[i] = d;
+    }
+    __syncthreads();
+    double *t;
+    t = A; A = A2; A2 = t;
+    t = B; B = B2; B2 = t;
+    t = Cc; Cc = C2b; C2b = t;
+    t = D; D = D2; D2 = t;
+  }
+  // u11 = D / B; the flow-rate sums Qx1 = sum dy u11, Qx0 = sum dy u(0,0) (j = 1..nn+1)
+  // run serially in the reference's order: QxT - Qx0 cancels, so its rounding matters
+  // (the level widths and u(0,0) are staged in shared memory first: the serial loop then
+  // runs on shared-memory loads)
+  double *dy = A2, *ur = B2;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    D[j] = D[j] / B[j];
+    dy[j] = (j >= 1 && j <= nn + 1) ? (g.yv[j + dny] - g.yv[j - 1 + dny]) : 0.0;
+    ur[j] = u1[(size_t)(j + dny) * nc].x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double Qx1 = 0.0, Qx0 = 0.0;
+    for (int j = 1; j <= nn + 1; ++j) Qx1 = Qx1 + dy[j] * D[j];
+    for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + dy[j] * ur[j];
+    const double gg = (sc->QxT - Qx0) / Qx1;
+    sc->mpgx = sc->mpgx + gg;
+    gg_sh = gg;
+  }
+  __syncthreads();
+  const double gg = gg_sh;
+  for (int j = threadIdx.x; j <= nn + 2; j += blockDim.x) u1[(size_t)(j + dny) * nc].x += gg * D[j];
 }
 
 // flowrateIm of u1 (0,0): Qx (meanflow_ctP, littleharsh.f90:529-545; getini)
