@@ -214,6 +214,9 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   if (cfg->N1 <= 0 || cfg->N2 <= 0 || (cfg->N1 & 1) || (cfg->N2 & 1) || cfg->Ngal1 <= cfg->N1 ||
       cfg->Ngal2 <= cfg->N2 || (cfg->Ngal1 & 1) || (cfg->Ngal2 & 1) || cfg->dny < 0)
     return fail(nullptr, LH_EINVAL, "bad N / Ngal / dny");
+  if (cfg->N1 != 2 * (cfg->Ngal1 / 3) || cfg->N2 != 2 * (cfg->Ngal2 / 3) || cfg->N1c != 2 * (cfg->Ngal1c / 3) ||
+      cfg->N2c != 2 * (cfg->Ngal2c / 3))
+    return fail(nullptr, LH_EINVAL, "N must be 2 (Ngal / 3) in every band (start.f90:110-114)");
   if (cfg->nyu != cfg->N4[3] + 1 - cfg->N4[0] + 1 || cfg->nyv != cfg->N3[3] + 1 - cfg->N3[0] + 1 ||
       cfg->nyv != cfg->nyu - 1 || cfg->N4[0] != -cfg->dny || cfg->N3[0] != -cfg->dny || cfg->nyu < 5)
     return fail(nullptr, LH_EINVAL, "band limits inconsistent with nyu / nyv / dny");

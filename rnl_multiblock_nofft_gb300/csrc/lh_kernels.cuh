@@ -235,10 +235,13 @@ __global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__re
   const int nprod = isU ? 4 : 2;
   const T s1 = (T)1 / (T)G1;
   const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
-  // separate the two rows of each pair, keep kx = 0..N1h-1; kx fastest (coalesced rows)
-  for (int idx = threadIdx.x; idx < nprod * PB * 2 * N1h; idx += blockDim.x) {
-    const int k = idx % N1h;
-    const int rest = idx / N1h;
+  // separate the two rows of each pair, keep kx = 0..N1h-1; kx fastest (coalesced rows).
+  // N1 = 2 (Ngal1 / 3) (lh_create checks it), so N1h = G1 / 3 + 1 is a compile-time
+  // constant here and the index split needs no runtime division.
+  constexpr int NH = G1 / 3 + 1;
+  for (int idx = threadIdx.x; idx < nprod * PB * 2 * NH; idx += blockDim.x) {
+    const int k = idx % NH;
+    const int rest = idx / NH;
     const int half = rest & 1;
     const int pb = (rest >> 1) % PB, p = (rest >> 1) / PB;
     if (pb >= npairs) continue;
