@@ -170,6 +170,10 @@ def algorithmic_bytes(s, kernel: str, form: str) -> float:
             tot += A + B
         elif kernel == "k_zfwd_nl":
             tot += B + (nuI + nvI) * 3 * ncv * z
+    if kernel == "k_xpass_nl" and s.dny > 0 and s.p.ib_enable and s.p.geometry_type == 2:
+        # physical planes of the immersed-boundary levels (and the two tip levels) captured
+        # for the forcing: 3 fields, FP64
+        tot += (4 * s.dny + 2) * 3 * s.G1 * s.G2 * 8
     if kernel in ("k_zinv_nl", "k_xpass_nl", "k_zfwd_nl"):
         return tot
     if kernel == "k_helm_uw":
