@@ -737,7 +737,7 @@ static int launch_zinv(lh_handle *h, const Geo &g, int nslots, const void *twz) 
   typedef typename C2<T>::t V;
   constexpr int KB = kb_zinv<V>(N);
   dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
-  KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
+  KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, LH_ZINV_THREADS, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
                       h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)twz));
   return LH_OK;
 }
@@ -746,7 +746,7 @@ static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const
   typedef typename C2<T>::t V;
   constexpr int PB = pb_xpass<V>(N);
   dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
-  KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, NTHR_H, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
+  KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, LH_XPASS_THREADS, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
                        (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, h->cap));
   return LH_OK;
 }
@@ -755,7 +755,7 @@ static int launch_zfwd(lh_handle *h, const Geo &g, int nslots, const void *twz) 
   typedef typename C2<T>::t V;
   constexpr int KB = kb_zfwd<V>(N);
   dim3 grid((g.N1h + KB - 1) / KB, nslots);
-  KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, NTHR_H, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
+  KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, LH_ZFWD_THREADS, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
                       (const V *)h->B, g, (const V *)twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
                       (V *)h->vvc, (V *)h->wvf));
   return LH_OK;

@@ -46,7 +46,7 @@ __device__ __forceinline__ T warp_max(T v) {
 #define LH_BUDGET_ZINV 49152
 #endif
 #ifndef LH_BUDGET_XPASS
-#define LH_BUDGET_XPASS 49152
+#define LH_BUDGET_XPASS 24576
 #endif
 #ifndef LH_BUDGET_ZFWD
 #define LH_BUDGET_ZFWD 49152
@@ -68,8 +68,14 @@ template <typename V> __host__ __device__ constexpr int kb_zfwd(int n) {
 // A layout: [(slot*3 + f)][l][kx], l = 0..G2-1, kx = 0..N1h-1.
 // Lines are interleaved in shared memory (element l of line kk at l*KB + kk).
 // ============================================================================
+#ifndef LH_ZINV_THREADS
+#define LH_ZINV_THREADS 256
+#endif
+#ifndef LH_ZFWD_THREADS
+#define LH_ZFWD_THREADS 256
+#endif
 template <typename T, int N>
-__global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+__global__ void __launch_bounds__(LH_ZINV_THREADS) k_zinv_nl(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                   const double2 *__restrict__ u3, typename C2<T>::t *__restrict__ A,
                                                   Geo g, const typename C2<T>::t *__restrict__ twz) {
   typedef typename C2<T>::t V;
@@ -136,8 +142,13 @@ __global__ void __launch_bounds__(NTHR) k_zinv_nl(const double2 *__restrict__ u1
 // B layout: [pslot][l][kx]; pslot = slot*4 + p (u levels), nuI*4 + (slot-nuI)*2 + p (v).
 // capture (optional): physical velocities of selected levels, [cap][f][l][m].
 // ============================================================================
+// x pass: one row pair per block (FP32) in 4 warps: a Stockham pass over the few lines
+// of a block then spreads evenly over the threads (the fastest of a sweep at C1)
+#ifndef LH_XPASS_THREADS
+#define LH_XPASS_THREADS 128
+#endif
 template <typename T, int N>
-__global__ void __launch_bounds__(NTHR) k_xpass_nl(const typename C2<T>::t *__restrict__ A,
+__global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2<T>::t *__restrict__ A,
                                                    typename C2<T>::t *__restrict__ B, Geo g,
                                                    const typename C2<T>::t *__restrict__ twx, int doCFL,
                                                    DevScalars *sc, const int *__restrict__ capslot,
@@ -415,7 +426,7 @@ __device__ __forceinline__ void zfwd_body(const typename C2<T>::t *__restrict__ 
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(NTHR) k_zfwd_nl(const typename C2<T>::t *__restrict__ B, Geo g,
+__global__ void __launch_bounds__(LH_ZFWD_THREADS) k_zfwd_nl(const typename C2<T>::t *__restrict__ B, Geo g,
                                                   const typename C2<T>::t *__restrict__ twz,
                                                   typename C2<T>::t *__restrict__ N1xz, typename C2<T>::t *__restrict__ N2xz,
                                                   typename C2<T>::t *__restrict__ N3xz, typename C2<T>::t *__restrict__ uvf,
