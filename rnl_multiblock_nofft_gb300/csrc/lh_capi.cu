@@ -43,7 +43,7 @@ struct lh_handle {
   double2 *stage;  // staging for transposes
   // immersed boundaries
   int ib, nib, ncap;
-  int *d_lu, *d_lv, *d_capslot, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
+  int *d_lu, *d_lv, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
   double *d_Au, *d_Av, *cap, *duphys;
   double2 *duib;
   // plane views of the nonlinear launches: wall-band planes, then core planes
@@ -401,7 +401,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   // immersed boundaries
   h->ib = (cfg->ib_enable && cfg->dny > 0) ? 1 : 0;
   h->nib = 0; h->ncap = 0;
-  h->d_lu = h->d_lv = h->d_capslot = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
+  h->d_lu = h->d_lv = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
   h->d_Au = h->d_Av = h->cap = h->duphys = nullptr;
   h->duib = nullptr;
   std::vector<int> lev2cap_u(nu, -1), lev2cap_v(nv, -1);  // captured physical planes of the IB forcing
@@ -585,7 +585,7 @@ extern "C" int lh_destroy(lh_handle *h) {
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
-                  h->d_lu, h->d_lv, h->d_capslot, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
+                  h->d_lu, h->d_lv, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
                   h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
                   h->ysv, h->a3v, h->st_pl, h->st_cd};

@@ -1053,123 +1053,13 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
 // stored factors, p += psi, v_corr, and the divergence of the corrected field
 // (max |div|^2 -> errbits) when need_div: the reference recomputes div after
 // every v_corr but only reads it (error()) at the start of a step, so it is
-// formed in the third substep. One thread per column. p levels qp = 0..np-1 <->
-// u/v index q = qp + 1. `psi` holds the forward-sweep values, then psi.
+// formed in the third substep. p levels qp <-> u/v index q = qp + 1;
+// `psi` holds the forward-sweep values, then psi.
 // ============================================================================
-__global__ void __launch_bounds__(NTHR) k_press(double2 *__restrict__ u1, double2 *__restrict__ u2,
-                                                double2 *__restrict__ u3, double2 *__restrict__ p,
-                                                double2 *__restrict__ psi, const double *__restrict__ dg1,
-                                                const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
-                                                DevScalars *sc, int kRK, int need_div) {
-  const int vc = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nc = g.ncol;
-  double dmax = 0.0;
-  if (vc < g.nvc) {
-    int c, bd;
-    vcol_of(g, vc, c, bd);
-    const int plo = g.bq[bd][4], phi = g.bq[bd][5];
-    const int ulo = g.bq[bd][0], uhi = g.bq[bd][1], vlo = g.bq[bd][2], vhi = g.bq[bd][3];
-    const int r = c / g.N1h, kx = c - r * g.N1h;
-    const double kxv = g.k1x[kx], kzv = g.k1z[r];
-    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
-    const double dtirk = sc->dti / aRb;
-    const double dt = sc->dt;
-    const double dd = g.dd;
-    double2 y = czero<double2>();
-    double2 vm = u2[(size_t)plo * nc + c];
-    // unrolled so the loads of several levels are in flight together (the column
-    // kernels run few warps per SM; memory-level parallelism hides the latency)
-#pragma unroll 4
-    for (int qp = plo; qp <= phi; ++qp) {
-      const int q = qp + 1;
-      const size_t o = (size_t)q * nc + c;
-      const double2 a = u1[o], w = u3[o], v = u2[o];
-      const double th = dd * g.thu[q];
-      double2 dv;
-      dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
-      dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
-      vm = v;
-      double2 rhs;
-      rhs.x = dtirk * dv.x; rhs.y = dtirk * dv.y;
-      if (qp == plo && c == 0 && bd == 1) { rhs.x = 0.0; rhs.y = 0.0; }
-      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
-      if (qp == plo) { y.x = rhs.x * a2p; y.y = rhs.y * a2p; }
-      else { y.x = (rhs.x - A1 * y.x) * a2p; y.y = (rhs.y - A1 * y.y) * a2p; }
-      psi[(size_t)qp * nc + c] = y;
-    }
-    const double dtrk = dt * aRb;
-    const double dtrk2 = dtrk * dd;
-    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
-    double2 xn = y;
-    double2 vup = czero<double2>(), a_up = czero<double2>(), w_up = czero<double2>();
-#pragma unroll 4
-    for (int qp = phi; qp >= plo; --qp) {
-      const int q = qp + 1;
-      const size_t o = (size_t)q * nc + c;
-      double2 x;
-      if (qp == phi) x = xn;
-      else {
-        const double a3p = dg3[(size_t)qp * nc + c];
-        const double2 yy = psi[(size_t)qp * nc + c];
-        x.x = yy.x - a3p * xn.x; x.y = yy.y - a3p * xn.y;
-      }
-      psi[(size_t)qp * nc + c] = x;
-      double2 pp = p[(size_t)qp * nc + c];
-      pp.x = pp.x + x.x; pp.y = pp.y + x.y;
-      p[(size_t)qp * nc + c] = pp;
-      double2 a = u1[o], w = u3[o];
-      a.x = a.x - (-kxd * x.y); a.y = a.y - (kxd * x.x);
-      w.x = w.x - (-kzd * x.y); w.y = w.y - (kzd * x.x);
-      u1[o] = a;
-      u3[o] = w;
-      double2 v = u2[o];
-      if (q <= vhi - 1) {
-        const double f = dtrk2 * g.thv[q];
-        v.x = v.x - f * (xn.x - x.x);
-        v.y = v.y - f * (xn.y - x.y);
-        u2[o] = v;
-      }
-      if (need_div && qp < phi) {
-        const double th = dd * g.thu[q + 1];
-        double2 dv;
-        dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - v.x);
-        dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - v.y);
-        dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
-      }
-      a_up = a; w_up = w; vup = v;
-      xn = x;
-    }
-    if (need_div) {
-      const double th = dd * g.thu[plo + 1];
-      const double2 vb = u2[(size_t)plo * nc + c];
-      double2 dv;
-      dv.x = (-kxv * a_up.y + -kzv * w_up.y) + th * (vup.x - vb.x);
-      dv.y = (kxv * a_up.x + kzv * w_up.x) + th * (vup.y - vb.y);
-      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
-    }
-    // wall ghosts: bands 1, 2 at the bottom, bands 2, 3 at the top (the short columns'
-    // interface ghosts keep the values of their Helmholtz boundary rows); v = 0 at band ends
-    if (bd <= 1) {
-      const double2 t1 = u1[(size_t)(ulo + 1) * nc + c], t3 = u3[(size_t)(ulo + 1) * nc + c];
-      u1[(size_t)ulo * nc + c] = cscale(t1, g.gwbc1);
-      u3[(size_t)ulo * nc + c] = cscale(t3, g.gwbc3);
-    }
-    if (bd >= 1) {
-      const double2 t1 = u1[(size_t)(uhi - 1) * nc + c], t3 = u3[(size_t)(uhi - 1) * nc + c];
-      u1[(size_t)uhi * nc + c] = cscale(t1, g.gwbc1);
-      u3[(size_t)uhi * nc + c] = cscale(t3, g.gwbc3);
-    }
-    u2[(size_t)vlo * nc + c] = czero<double2>();
-    u2[(size_t)vhi * nc + c] = czero<double2>();
-  }
-  dmax = warp_max(dmax);
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
-}
-
-// k_press with one lane per (column, real/imaginary part): the pressure matrix is real,
-// so the two parts are independent systems; the i*k couplings of the divergence and of
-// v_corr exchange the other part through a shuffle within the lane pair. Twice the
-// warps of k_press for the same columns (the solves are latency-bound at C1 sizes).
+// One lane per (column, real/imaginary part): the pressure matrix is real, so the two
+// parts are independent systems; the i*k couplings of the divergence and of v_corr
+// exchange the other part through a shuffle within the lane pair. Two lanes per column
+// double the warps in flight (the solves are latency-bound at the 384x192 wall grid).
 // Scalar views: element (level, col, part) at (level*ncol + col)*2 + part.
 __global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double *__restrict__ u2,
                                                  double *__restrict__ u3, double *__restrict__ p,
