@@ -145,10 +145,17 @@ struct orc {
   fftplan pxc, pzc;
   unsigned char *lng;
   int bj[3][3][2]; /* [band 0..2][grid: 0 u, 1 v, 2 p][lo, hi], reference j */
-  /* statistics (stats.f90): plane sums [9][nu], tile-conditioned sums [9][ncl][dnz][dnx] */
+  /* statistics (stats.f90): plane sums [11][nu], tile-conditioned sums [9][ncl][dnz][dnx] */
   double *st_pl, *st_cd;
   int st_ncl, st_dnx, st_dnz;
   int64_t istat;
+  /* spectra (spectra.f90): sp(level, long column) of U, V, W, UV, P, level fastest */
+  double *sp[5];
+  int sp_nl[5], nlong;
+  /* slip statistics (sl_stats2.f90): [wall 0 bottom, 1 top][u1_itp, du1dy, u3_itp, du3dy][column] */
+  cplx *slip;
+  /* plans of the unpadded N grids (four_to_phys_N): wall bands and core band */
+  fftplan pxN, pzN, pxNc, pzNc;
   cplx *u1, *u2, *u3, *p;
   cplx *Nu1, *Nu2, *Nu3, *du1, *du2, *du3, *psi, *div;
   cplx *u1i, *u2i, *u3i; /* u1,u3 at v levels; u2 at u levels */
@@ -316,7 +323,8 @@ orc *orc_create(const lh_config *cfg) {
   O->c.k1z = O->k1z; O->c.k2z = O->k2z; O->c.list_ib_u = O->lu; O->c.list_ib_v = O->lv;
   O->c.A_ib_u = O->Au; O->c.A_ib_v = O->Av;
   if (plan_init(&O->px, O->G1) || plan_init(&O->pz, O->G2) || plan_init(&O->pxc, O->G1c) ||
-      plan_init(&O->pzc, O->G2c))
+      plan_init(&O->pzc, O->G2c) || plan_init(&O->pxN, O->N1) || plan_init(&O->pzN, O->N2) ||
+      plan_init(&O->pxNc, O->N1c) || plan_init(&O->pzNc, O->N2c))
     return NULL;
   size_t nc = (size_t)O->ncol;
   O->u1 = zalloc(nc * O->nu); O->u3 = zalloc(nc * O->nu); O->u2 = zalloc(nc * O->nv);
@@ -344,9 +352,11 @@ void orc_destroy(orc *O) {
                   O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
                   O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
                   O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2,
-                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng, O->st_pl, O->st_cd};
+                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng, O->st_pl, O->st_cd,
+                  O->sp[0], O->sp[1], O->sp[2], O->sp[3], O->sp[4], O->slip};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   plan_free(&O->px); plan_free(&O->pz); plan_free(&O->pxc); plan_free(&O->pzc);
+  plan_free(&O->pxN); plan_free(&O->pzN); plan_free(&O->pxNc); plan_free(&O->pzNc);
   free(O);
 }
 
@@ -1181,9 +1191,20 @@ static void stats_alloc(orc *O) {
   O->st_ncl = ncl;
   O->st_dnx = (tx > 0 && tz > 0) ? O->G1 / tx : 0;
   O->st_dnz = (tx > 0 && tz > 0) ? O->G2 / tz : 0;
-  O->st_pl = (double *)calloc((size_t)9 * O->nu, sizeof(double));
+  O->st_pl = (double *)calloc((size_t)11 * O->nu, sizeof(double));
   O->st_cd = (double *)calloc((size_t)9 * ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1), sizeof(double));
   O->istat = 0;
+  O->nlong = 0;
+  for (int c = 0; c < O->ncol; ++c) O->nlong += (!O->mb || O->lng[c]);
+  /* band 2's levels: jlim(1:2, grid, midband) (start.f90:1675-1709) */
+  const int nl[5] = {O->bj[1][0][1] - O->bj[1][0][0] + 1, O->bj[1][1][1] - O->bj[1][1][0] + 1,
+                     O->bj[1][0][1] - O->bj[1][0][0] + 1, O->bj[1][0][1] - O->bj[1][0][0] + 1,
+                     O->bj[1][2][1] - O->bj[1][2][0] + 1};
+  for (int q = 0; q < 5; ++q) {
+    O->sp_nl[q] = nl[q];
+    O->sp[q] = (double *)calloc((size_t)nl[q] * O->nlong, sizeof(double));
+  }
+  O->slip = zalloc((size_t)8 * O->ncol);
 }
 
 /* one plane's sums: the plane statistics of stats(), and conddown/condup
@@ -1238,6 +1259,102 @@ static void stats_plane(orc *O, int isU, int j, const double *a, const double *b
 #undef CD
 }
 
+/* omega_x at v plane j (FOU3D.f90:300-327): -der_z_N(v) + der_yv_h_wx(w) in the plane band's
+ * unpadded N1 x N2 layout, four_to_phys_N (FOU3D.f90:786-804: z backward complex transform
+ * of the N1/2+1 x-modes, no zeroed row, then x backward real transform), summed over the
+ * N1 x N2 points in the order of stats.f90:56-63 (k outer, i inner). */
+static void wx_plane(orc *O, int j, double *phys, pwork *w, double *ps, double *ps2) {
+  const int fine = fine_v(O, j);
+  const int N1 = fine ? O->N1 : O->N1c, N2 = fine ? O->N2 : O->N2c, N1h = N1 / 2 + 1;
+  const fftplan *px = fine ? &O->pxN : &O->pxNc, *pz = fine ? &O->pzN : &O->pzNc;
+  pview v;
+  view_of(O, fine, &v);
+  const int q = UIDX(j);
+  const double fy = O->thv[q] * O->c.ddthetavi;
+  for (int kx = 0; kx < N1h; ++kx) {
+    for (int r = 0; r < N2; ++r) {
+      const size_t c = vcol(O, &v, r, kx);
+      const int fr = (int)(c / O->N1h);
+      const cplx dz = (I * O->k1z[fr]) * PL(O->u2, q)[c];
+      const cplx dy = (PL(O->u3, q + 1)[c] - PL(O->u3, q)[c]) * fy;
+      w->line[r] = -dz + dy;
+    }
+    fft_inplace(pz, w->line, +1, w->tmp);
+    for (int l = 0; l < N2; ++l) w->A[(size_t)l * N1h + kx] = w->line[l];
+  }
+  for (int l = 0; l < N2; ++l) {
+    const cplx *a = w->A + (size_t)l * N1h;
+    for (int k = 0; k < N1; ++k) w->line[k] = 0;
+    for (int k = 0; k <= N1 / 2; ++k) {
+      cplx ak = a[k];
+      if (k == 0 || k == N1 / 2) ak = creal(ak);
+      w->line[k] = ak;
+      if (k > 0 && k < N1 / 2) w->line[N1 - k] = conj(ak);
+    }
+    fft_inplace(px, w->line, +1, w->tmp);
+    for (int m = 0; m < N1; ++m) phys[(size_t)l * N1 + m] = creal(w->line[m]);
+  }
+  double s = 0, s2 = 0;
+  for (int l = 0; l < N2; ++l)
+    for (int m = 0; m < N1; ++m) {
+      const double x = phys[(size_t)l * N1 + m];
+      s += x;
+      s2 += x * x;
+    }
+  *ps = s;
+  *ps2 = s2;
+}
+
+/* spectra (spectra.f90:1-56): buildsp / buildspUV over band 2's columns (the long
+ * columns, in the order of columns_long_list) and levels, sp(j, column) += |u|^2,
+ * spUV += Re u1 Re u2_itp + Im u1 Im u2_itp (u2_itp: v interpolated to the centres) */
+static void spectra_accumulate(orc *O) {
+  const int ulo = UIDX(O->bj[1][0][0]), vlo = UIDX(O->bj[1][1][0]), plo = PIDX(O->bj[1][2][0]);
+  int k = 0;
+  for (int c = 0; c < O->ncol; ++c) {
+    if (O->mb && !O->lng[c]) continue;
+    double *sU = O->sp[0] + (size_t)k * O->sp_nl[0], *sV = O->sp[1] + (size_t)k * O->sp_nl[1];
+    double *sW = O->sp[2] + (size_t)k * O->sp_nl[2], *sUV = O->sp[3] + (size_t)k * O->sp_nl[3];
+    double *sP = O->sp[4] + (size_t)k * O->sp_nl[4];
+    for (int l = 0; l < O->sp_nl[0]; ++l) {
+      const cplx a = PL(O->u1, ulo + l)[c], b = PL(O->u3, ulo + l)[c], v = PL(O->u2i, ulo + l)[c];
+      sU[l] = sU[l] + creal(a) * creal(a) + cimag(a) * cimag(a);
+      sW[l] = sW[l] + creal(b) * creal(b) + cimag(b) * cimag(b);
+      sUV[l] = sUV[l] + creal(a) * creal(v) + cimag(a) * cimag(v);
+    }
+    for (int l = 0; l < O->sp_nl[1]; ++l) {
+      const cplx a = PL(O->u2, vlo + l)[c];
+      sV[l] = sV[l] + creal(a) * creal(a) + cimag(a) * cimag(a);
+    }
+    for (int l = 0; l < O->sp_nl[4]; ++l) {
+      const cplx a = PL(O->p, plo + l)[c];
+      sP[l] = sP[l] + creal(a) * creal(a) + cimag(a) * cimag(a);
+    }
+    ++k;
+  }
+}
+
+/* sl_stats / inst_sl_stats (sl_stats2.f90:33-121, inst_sl_stats.f90:1-62) at the two wall
+ * faces jlim(1, vgrid, 2) and jlim(2, vgrid, 2), every column of the wall-band grid (the
+ * columns of bands 1+2 at the bottom, 2+3 at the top): u1_itp, du1dy, u3_itp, du3dy with
+ * du/dy = (u(j+1) - u(j)) dthdyv(j) ddthetavi, negated at the top. out: [2][4][ncol];
+ * acc: add (sl_stats) or overwrite (inst_sl_stats). interp_all must have run. */
+static void slip_planes(orc *O, cplx *out, int acc) {
+  const int jw[2] = {O->c.N3[0], O->c.N3[3] + 1};
+  const double sg[2] = {1.0, -1.0};
+  const size_t nc = (size_t)O->ncol;
+  for (int w = 0; w < 2; ++w) {
+    const int q = UIDX(jw[w]);
+    const double fy = O->thv[q] * O->c.ddthetavi;
+    cplx *o = out + (size_t)w * 4 * nc;
+    for (size_t c = 0; c < nc; ++c) {
+      const cplx v[4] = {PL(O->u1i, q)[c], sg[w] * ((PL(O->u1, q + 1)[c] - PL(O->u1, q)[c]) * fy),
+                         PL(O->u3i, q)[c], sg[w] * ((PL(O->u3, q + 1)[c] - PL(O->u3, q)[c]) * fy)};
+      for (int f = 0; f < 4; ++f) o[f * nc + c] = acc ? o[f * nc + c] + v[f] : v[f];
+    }
+  }
+}
+
 int orc_stats_accumulate(orc *O) {
   if (!O->st_pl) stats_alloc(O);
   interp_all(O);
@@ -1263,19 +1380,63 @@ int orc_stats_accumulate(orc *O) {
     four_to_phys_plane(O, &v, PL(O->u3i, UIDX(j)), f3, &w);
     stats_plane(O, 0, j, f1, f2, f3, v.G1, v.G2, fine);
   }
+  for (int j = O->c.N3[0]; j <= O->c.N3[3] + 1; ++j) {
+    double s = 0, s2 = 0;
+    wx_plane(O, j, f1, &w, &s, &s2);
+    O->st_pl[9 * (size_t)O->nu + UIDX(j)] += s;
+    O->st_pl[10 * (size_t)O->nu + UIDX(j)] += s2;
+  }
   pwork_free(&w);
   free(f1); free(f2); free(f3);
+  spectra_accumulate(O);
+  slip_planes(O, O->slip, 1);
   O->istat += 1;
   return 0;
 }
 
 int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims) {
   if (!O->st_pl) stats_alloc(O);
-  if (plane) memcpy(plane, O->st_pl, sizeof(double) * 9 * (size_t)O->nu);
+  if (plane) memcpy(plane, O->st_pl, sizeof(double) * 11 * (size_t)O->nu);
   const size_t nc = (size_t)9 * O->st_ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1);
   if (cond && O->st_dnx) memcpy(cond, O->st_cd, sizeof(double) * nc);
   if (istat) *istat = O->istat;
   if (dims) { dims[0] = O->st_ncl; dims[1] = O->st_dnx; dims[2] = O->st_dnz; }
+  return 0;
+}
+
+/* sp(level, long column) of U, V, W, UV, P (NULL skips one); nl: band 2's level counts */
+int orc_spectra_get(orc *O, double *sU, double *sV, double *sW, double *sUV, double *sP, int *nl, int *nlong) {
+  if (!O->st_pl) stats_alloc(O);
+  double *dst[5] = {sU, sV, sW, sUV, sP};
+  for (int q = 0; q < 5; ++q) {
+    if (dst[q]) memcpy(dst[q], O->sp[q], sizeof(double) * (size_t)O->sp_nl[q] * O->nlong);
+    if (nl) nl[q] = O->sp_nl[q];
+  }
+  if (nlong) *nlong = O->nlong;
+  return 0;
+}
+
+/* accumulated slip statistics [2][4][ncol] complex (NULL skips) */
+int orc_slip_get(orc *O, double *acc) {
+  if (!O->st_pl) stats_alloc(O);
+  if (acc) memcpy(acc, O->slip, sizeof(cplx) * 8 * (size_t)O->ncol);
+  return 0;
+}
+
+/* instantaneous slip planes of the current state [2][4][ncol] complex */
+int orc_slip_planes(orc *O, double *out) {
+  interp_all(O);
+  slip_planes(O, (cplx *)out, 0);
+  return 0;
+}
+
+int orc_stats_reset(orc *O) {
+  if (!O->st_pl) stats_alloc(O);
+  memset(O->st_pl, 0, sizeof(double) * 11 * (size_t)O->nu);
+  memset(O->st_cd, 0, sizeof(double) * 9 * (size_t)O->st_ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1));
+  for (int q = 0; q < 5; ++q) memset(O->sp[q], 0, sizeof(double) * (size_t)O->sp_nl[q] * O->nlong);
+  memset(O->slip, 0, sizeof(cplx) * 8 * (size_t)O->ncol);
+  O->istat = 0;
   return 0;
 }
 

@@ -20,6 +20,10 @@ int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes);
 int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes);
 int orc_set_threads(int n);
 int orc_stats_accumulate(orc *O);
-/* dims: ncl, dnx, dnz */
+/* plane: [11][nu]; dims: ncl, dnx, dnz */
 int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims);
+int orc_stats_reset(orc *O);
+int orc_spectra_get(orc *O, double *sU, double *sV, double *sW, double *sUV, double *sP, int *nl, int *nlong);
+int orc_slip_get(orc *O, double *acc);
+int orc_slip_planes(orc *O, double *out);
 #endif

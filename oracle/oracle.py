@@ -49,6 +49,10 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_stats_accumulate.argtypes = [vp]
         L.orc_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+        L.orc_stats_reset.argtypes = [vp]
+        L.orc_spectra_get.argtypes = [vp] + [dp] * 5 + [C.POINTER(C.c_int)] * 2
+        L.orc_slip_get.argtypes = [vp, dp]
+        L.orc_slip_planes.argtypes = [vp, dp]
         _lib = L
     return _lib
 
@@ -140,12 +144,38 @@ class Oracle:
     def stats_accumulate(self):
         lib().orc_stats_accumulate(self.h)
 
+    def stats_reset(self):
+        lib().orc_stats_reset(self.h)
+
+    def spectra(self) -> dict:
+        """Accumulated sp(level, long column) of spectra.f90, as {"U", "V", "W", "UV", "P"}:
+        arrays [long column][level of band 2]."""
+        nl = (C.c_int * 5)()
+        nlong = C.c_int()
+        lib().orc_spectra_get(self.h, None, None, None, None, None, nl, C.byref(nlong))
+        out = {k: np.zeros((nlong.value, nl[q])) for q, k in enumerate(("U", "V", "W", "UV", "P"))}
+        lib().orc_spectra_get(self.h, *[_dptr(out[k]) for k in ("U", "V", "W", "UV", "P")], None, None)
+        return out
+
+    def slip(self) -> np.ndarray:
+        """Accumulated slip statistics: complex [wall (bottom, top)][u1_itp, du1dy, u3_itp,
+        du3dy][N2][N1/2+1]"""
+        out = np.zeros((2, 4, self.s.N2, self.s.N1 // 2 + 1), np.complex128)
+        lib().orc_slip_get(self.h, _dptr(out.view(np.float64)))
+        return out
+
+    def slip_planes(self) -> np.ndarray:
+        """Instantaneous slip planes of the current state, laid out as slip()"""
+        out = np.zeros((2, 4, self.s.N2, self.s.N1 // 2 + 1), np.complex128)
+        lib().orc_slip_planes(self.h, _dptr(out.view(np.float64)))
+        return out
+
     def stats(self):
-        """(plane [9][nyu], cond [9][ncl][dnz][dnx] or None, istat)"""
+        """(plane [11][nyu], cond [9][ncl][dnz][dnx] or None, istat)"""
         dims = (C.c_int * 3)()
         lib().orc_stats_get(self.h, None, None, None, dims)
         ncl, dnx, dnz = dims[0], dims[1], dims[2]
-        plane = np.zeros((9, self.s.nyu))
+        plane = np.zeros((11, self.s.nyu))
         cond = np.zeros((9, ncl, dnz, dnx)) if dnx else None
         ist = C.c_int64()
         lib().orc_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist), dims)
