@@ -176,24 +176,47 @@ void *lh_stream(lh_handle *h);
 int lh_four_to_phys(lh_handle *h, const void *spec, void *phys, int nplanes);
 int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes);
 
-/* ---- statistics (stats.f90:1-107), accumulated on the device ----
- * lh_stats_accumulate adds the current state's statistics (istat += 1), as stats() does
- * when called from nonlinear at kRK = 1 (FOU3D.f90:298-373), over the interior planes:
- * per level, sums over the physical plane of quantities
- *   0 U, 1 U^2, 2 W, 3 W^2, 4 U V, 5 U W   (u levels; V interpolated to the centres)
- *   6 V, 7 V^2, 8 V W                      (v levels; W interpolated to the faces)
- * and the same nine sums conditioned on the position inside a post tile (conddown1/2,
- * condup1/2, stats.f90:109-250): wall-band planes only, indexed by the distance j1 = 1..
- * from the wall, the top band mirrored onto the bottom with the sign of V flipped. The
- * pressure and vorticity statistics are not formed. Sums are in FP64 from planes in the
- * form's transform precision. */
+/* ---- statistics (stats.f90, spectra.f90, sl_stats2.f90), accumulated on the device ----
+ * lh_stats_accumulate adds the current state's statistics (istat += 1), as the statistics
+ * step of nonlinear does at kRK = 1 when flagst is set (FOU3D.f90:127-130, 298-373):
+ * stats(), spectra() and sl_stats() together.
+ * Plane sums (stats.f90:1-107), per level:
+ *   0 U, 1 U^2, 2 W, 3 W^2, 4 U V, 5 U W   (interior u levels; V interpolated to the centres)
+ *   6 V, 7 V^2, 8 V W                      (interior v levels; W interpolated to the faces)
+ *   9 omega_x, 10 omega_x^2                (every v level: omega_x = -dv/dz + dw/dy on the
+ *                                           plane's unpadded N1 x N2 grid, FOU3D.f90:300-327)
+ * and the sums 0-8 conditioned on the position inside a post tile (conddown1/2, condup1/2,
+ * stats.f90:109-250): wall-band planes only, indexed by the distance j1 = 1.. from the
+ * wall, the top band mirrored onto the bottom with the sign of V flipped. Sums 0-8 are in
+ * FP64 from planes in the form's transform precision; 9-10 from the FP64 state. The
+ * pressure sums are not formed: the reference's come from ppPL, which holds the spectral
+ * packing of p (FOU3D.f90:156-157), not a physical field. */
 int lh_stats_accumulate(lh_handle *h);
+/* zeroes every accumulator (plane, conditioned, spectra, slip) and istat */
 int lh_stats_reset(lh_handle *h);
 /* ncl: conditioned levels; dnx, dnz: tile size in physical points (0 without tiles) */
 int lh_stats_dims(lh_handle *h, int *ncl, int *dnx, int *dnz);
-/* plane: [9][nyu] (u-level quantities at u index j+dny, v-level ones at v index j+dny);
+/* plane: [11][nyu] (u-level quantities at u index j+dny, v-level ones at v index j+dny);
  * cond: [9][ncl][dnz][dnx] (may be NULL); istat: number of accumulations. Blocking. */
 int lh_stats_get(lh_handle *h, double *plane, double *cond, int64_t *istat);
+
+/* Spectra (spectra.f90:1-56, buildsp / buildspUV): over band 2 (the long columns, in the
+ * order of columns_long_list, start.f90:1606-1631) and band 2's levels jlim(1:2, grid, 2),
+ * sp(j, column) += |u|^2 of U, V, W, P, and spUV += Re u1 Re v + Im u1 Im v with v
+ * interpolated to the centres. nlev: [5] level counts of U, V, W, UV, P; nlong: columns. */
+int lh_spectra_dims(lh_handle *h, int *nlev, int *nlong);
+/* each array [nlong][nlev[q]] (level fastest, the layout of sp(j, column)); NULL skips one.
+ * Folding onto |kz| for the file is the host's (recvwrspec, spectra.f90:124-182). Blocking. */
+int lh_spectra_get(lh_handle *h, double *spU, double *spV, double *spW, double *spUV, double *spP);
+
+/* Slip statistics (sl_stats2.f90:33-121) at the wall faces jlim(1, vgrid, 2) (bottom) and
+ * jlim(2, vgrid, 2) (top), every mode of the wall-band grid: u1 and u3 interpolated to the
+ * face and du1/dy, du3/dy = (u(j+1) - u(j)) dthdyv(j) ddthetavi, negated at the top.
+ * acc: [2 faces][4: u1, du1dy, u3, du3dy][N2][N1+2] (re/im of x-modes 0..N1/2, the
+ * bslip_*_M layout), accumulated by lh_stats_accumulate. Blocking. */
+int lh_slip_get(lh_handle *h, double *acc);
+/* the same four planes of the current state, not accumulated (inst_sl_stats.f90:1-62) */
+int lh_slip_planes(lh_handle *h, double *out);
 
 /* Number of CUDA kernel launches issued by the handle since creation (graph
  * replays count every kernel node). */

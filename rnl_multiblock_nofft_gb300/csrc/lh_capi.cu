@@ -57,6 +57,8 @@ struct lh_handle {
   int nlong, nshort;
   // statistics
   double *st_pl, *st_cd;
+  double *d_sp;              // spectra accumulators: U, V, W, UV, P, each [level][nlong] (allocated on first use)
+  double2 *d_slip, *d_slip_inst;  // slip statistics [2][4][ncol]: accumulated / instantaneous
   int st_ncl, st_dnx, st_dnz, st_ntx;
   long long istat;
   // triad-list nonlinear form
@@ -401,6 +403,8 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   // immersed boundaries
   h->ib = (cfg->ib_enable && cfg->dny > 0) ? 1 : 0;
   h->nib = 0; h->ncap = 0;
+  h->d_sp = nullptr;
+  h->d_slip = h->d_slip_inst = nullptr;
   h->d_lu = h->d_lv = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
   h->d_Au = h->d_Av = h->cap = h->duphys = nullptr;
   h->duib = nullptr;
@@ -520,7 +524,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     h->st_dnx = tiles ? g.G1 / cfg->ntilex : 0;
     h->st_dnz = tiles ? g.G2 / cfg->ntilez : 0;
     h->istat = 0;
-    ZA(h->st_pl, sizeof(double) * 9 * (size_t)nu);
+    ZA(h->st_pl, sizeof(double) * 11 * (size_t)nu);
     ZA(h->st_cd, sizeof(double) * 9 * (size_t)ncl * (tiles ? (size_t)h->st_dnx * h->st_dnz : 1));
   }
   int rc = set_smem_attrs_all(h);
@@ -588,7 +592,7 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->d_lu, h->d_lv, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
                   h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
-                  h->ysv, h->a3v, h->st_pl, h->st_cd};
+                  h->ysv, h->a3v, h->st_pl, h->st_cd, h->d_sp, h->d_slip, h->d_slip_inst};
   for (void *b : bufs)
     if (b) cudaFree(b);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -1067,10 +1071,51 @@ static int stats_launches(lh_handle *h) {
   return LH_OK;
 }
 
+// band 2's level counts of U, V, W, UV, P (jlim(1:2, grid, midband))
+static void spectra_levels(const lh_handle *h, int nl[5]) {
+  const int(*bq)[6] = h->g.bq;
+  nl[0] = nl[2] = nl[3] = bq[1][1] - bq[1][0] + 1;
+  nl[1] = bq[1][3] - bq[1][2] + 1;
+  nl[4] = bq[1][5] - bq[1][4] + 1;
+}
+static size_t spectra_size(const lh_handle *h) {
+  int nl[5];
+  spectra_levels(h, nl);
+  return (size_t)(nl[0] + nl[1] + nl[2] + nl[3] + nl[4]) * h->nlong;
+}
+// the accumulators of spectra and slip statistics, zeroed, on first use
+static int spectral_stats_buffers(lh_handle *h) {
+  if (h->d_sp) return LH_OK;
+  const size_t nsp = spectra_size(h), nsl = 8 * (size_t)h->g.ncolF;
+  CK(cudaMalloc(&h->d_sp, sizeof(double) * nsp));
+  CK(cudaMalloc(&h->d_slip, sizeof(double2) * nsl));
+  CK(cudaMalloc(&h->d_slip_inst, sizeof(double2) * nsl));
+  CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * nsp, h->st));
+  CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * nsl, h->st));
+  return LH_OK;
+}
+// the wall faces jlim(1, vgrid, 2), jlim(2, vgrid, 2) as v array indices
+static void slip_faces(const lh_handle *h, int &qb, int &qt) { qb = h->g.bq[1][2]; qt = h->g.bq[1][3]; }
+
+// stats() + spectra() + sl_stats() of the current state (FOU3D.f90:127-130, 298-373)
 extern "C" int lh_stats_accumulate(lh_handle *h) {
   if (!h) return LH_EINVAL;
-  const int rc = (h->prec == LH_PREC_FP64) ? stats_launches<double>(h) : stats_launches<float>(h);
+  int rc = (h->prec == LH_PREC_FP64) ? stats_launches<double>(h) : stats_launches<float>(h);
   if (rc) return rc;
+  if ((rc = spectral_stats_buffers(h))) return rc;
+  const Geo &g = h->g;
+  const int nhc = h->nviews > 1 ? h->gv[1].N1h : g.N1hF, n2c = h->nviews > 1 ? h->gv[1].N2 : g.N2F;
+  KL("k_wx_stats", k_wx_stats<<<g.nv, LH_STAT_THREADS, 0, h->st>>>(h->u2, h->u3, g, nhc, n2c, h->st_pl));
+  int nl[5];
+  spectra_levels(h, nl);
+  const size_t ne = (size_t)nl[0] * h->nlong;
+  KL("k_spectra", k_spectra<<<(unsigned)((ne + LH_STAT_THREADS - 1) / LH_STAT_THREADS), LH_STAT_THREADS, 0, h->st>>>(
+                      h->u1, h->u2, h->u3, h->p, g, h->d_bcols, h->nlong, h->cfg.gw_interp[1][0],
+                      h->cfg.gw_interp[1][1], h->d_sp));
+  int qb, qt;
+  slip_faces(h, qb, qt);
+  KL("k_slip", k_slip<<<(g.ncolF + LH_STAT_THREADS - 1) / LH_STAT_THREADS, LH_STAT_THREADS, 0, h->st>>>(
+                   h->u1, h->u3, g, qb, qt, h->d_slip, 1));
   h->istat += 1;
   return LH_OK;
 }
@@ -1078,8 +1123,12 @@ extern "C" int lh_stats_accumulate(lh_handle *h) {
 extern "C" int lh_stats_reset(lh_handle *h) {
   if (!h) return LH_EINVAL;
   const size_t ncd = 9 * (size_t)h->st_ncl * (h->st_dnx ? (size_t)h->st_dnx * h->st_dnz : 1);
-  CK(cudaMemsetAsync(h->st_pl, 0, sizeof(double) * 9 * (size_t)h->g.nu, h->st));
+  CK(cudaMemsetAsync(h->st_pl, 0, sizeof(double) * 11 * (size_t)h->g.nu, h->st));
   CK(cudaMemsetAsync(h->st_cd, 0, sizeof(double) * ncd, h->st));
+  if (h->d_sp) {
+    CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * spectra_size(h), h->st));
+    CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * 8 * (size_t)h->g.ncolF, h->st));
+  }
   h->istat = 0;
   return LH_OK;
 }
@@ -1094,12 +1143,69 @@ extern "C" int lh_stats_dims(lh_handle *h, int *ncl, int *dnx, int *dnz) {
 
 extern "C" int lh_stats_get(lh_handle *h, double *plane, double *cond, int64_t *istat) {
   if (!h) return LH_EINVAL;
-  if (plane) CK(cudaMemcpyAsync(plane, h->st_pl, sizeof(double) * 9 * (size_t)h->g.nu, cudaMemcpyDeviceToHost, h->st));
+  if (plane) CK(cudaMemcpyAsync(plane, h->st_pl, sizeof(double) * 11 * (size_t)h->g.nu, cudaMemcpyDeviceToHost, h->st));
   if (cond && h->st_dnx)
     CK(cudaMemcpyAsync(cond, h->st_cd, sizeof(double) * 9 * (size_t)h->st_ncl * h->st_dnx * h->st_dnz,
                        cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   if (istat) *istat = h->istat;
+  return LH_OK;
+}
+
+extern "C" int lh_spectra_dims(lh_handle *h, int *nlev, int *nlong) {
+  if (!h) return LH_EINVAL;
+  if (nlev) spectra_levels(h, nlev);
+  if (nlong) *nlong = h->nlong;
+  return LH_OK;
+}
+
+extern "C" int lh_spectra_get(lh_handle *h, double *sU, double *sV, double *sW, double *sUV, double *sP) {
+  if (!h) return LH_EINVAL;
+  int nl[5];
+  spectra_levels(h, nl);
+  double *dst[5] = {sU, sV, sW, sUV, sP};
+  const size_t nlg = h->nlong;
+  std::vector<double> buf;
+  size_t off = 0;
+  for (int q = 0; q < 5; ++q) {
+    const size_t n = (size_t)nl[q] * nlg;
+    if (dst[q]) {
+      if (!h->d_sp) {
+        memset(dst[q], 0, sizeof(double) * n);
+      } else {
+        buf.resize(n);
+        CK(cudaMemcpyAsync(buf.data(), h->d_sp + off, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        // device [level][column] -> sp(level, column), level fastest
+        for (size_t k = 0; k < nlg; ++k)
+          for (int l = 0; l < nl[q]; ++l) dst[q][k * nl[q] + l] = buf[(size_t)l * nlg + k];
+      }
+    }
+    off += n;
+  }
+  return LH_OK;
+}
+
+extern "C" int lh_slip_get(lh_handle *h, double *acc) {
+  if (!h) return LH_EINVAL;
+  const size_t n = 8 * (size_t)h->g.ncolF;
+  if (!acc) return LH_OK;
+  if (!h->d_sp) { memset(acc, 0, sizeof(double2) * n); return LH_OK; }
+  CK(cudaMemcpyAsync(acc, h->d_slip, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_slip_planes(lh_handle *h, double *out) {
+  if (!h || !out) return LH_EINVAL;
+  int rc = spectral_stats_buffers(h);
+  if (rc) return rc;
+  int qb, qt;
+  slip_faces(h, qb, qt);
+  KL("k_slip", k_slip<<<(h->g.ncolF + LH_STAT_THREADS - 1) / LH_STAT_THREADS, LH_STAT_THREADS, 0, h->st>>>(
+                   h->u1, h->u3, h->g, qb, qt, h->d_slip_inst, 0));
+  CK(cudaMemcpyAsync(out, h->d_slip_inst, sizeof(double2) * 8 * (size_t)h->g.ncolF, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return LH_OK;
 }
 

@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
 // flipped). u slots hold (u, v interpolated, w), v slots (u interpolated, v, w
 // interpolated). Sums: block reduction, one FP64 atomic per quantity and block; the
 // conditioned sums add the ntilex tiles of a row in registers first.
-// pl: [9][nu]; cd: [9][ncl][dnz][dnx].
+// pl: [11][nu] (quantities 0-8 here); cd: [9][ncl][dnz][dnx].
 // ============================================================================
 template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_xstats(const typename C2<T>::t *__restrict__ A, Geo g,
@@ -1195,6 +1195,143 @@ __global__ void k_err_from_bits(DevScalars *sc) {
 }
 
 // one band's host cfield [k][l] (staged) <-> device [lev0 + l][cols[k]]; put = 1 writes the device
+// ============================================================================
+// The other sums of the statistics step, formed from the spectral state (FP64 in both
+// forms; launched on request only, LH_STAT_THREADS threads per block).
+// ============================================================================
+#define LH_STAT_THREADS 256
+// omega_x = -der_z_N(v) + der_yv_h_wx(w) at every v level (FOU3D.f90:300-327), and its
+// plane sums over the N1 x N2 points of four_to_phys_N (stats.f90:56-63), by Parseval:
+// sum f = N1 N2 Re c(0,0); sum f^2 = N1 N2 [ sum over 0 < kx < N1/2 of 2 |c|^2, plus for
+// kx = 0 and N1/2 (whose Im the real transform drops) 1/2 |c(kz)|^2 + 1/2 Re c(kz) c(-kz) ].
+// One block per level; the level's plane class gives N1, N2 (wall bands: nhw, n2w; the
+// core band: nhc, n2c). pl: [11][nu], quantities 9 and 10.
+__device__ __forceinline__ double2 wx_mode(const double2 *__restrict__ u2, const double2 *__restrict__ u3,
+                                           const Geo &g, int q, int c, int fr, double fy) {
+  const double2 v = u2[(size_t)q * g.ncolF + c];
+  const double2 a = u3[(size_t)(q + 1) * g.ncolF + c], b = u3[(size_t)q * g.ncolF + c];
+  const double kz = g.k1z[fr];
+  // -(i kz v) + (a - b) fy
+  return make_double2(kz * v.y + (a.x - b.x) * fy, -kz * v.x + (a.y - b.y) * fy);
+}
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_wx_stats(const double2 *__restrict__ u2, const double2 *__restrict__ u3,
+                                                     Geo g, int nhc, int n2c, double *__restrict__ pl) {
+  __shared__ double red[LH_STAT_THREADS / 32][2];
+  const int q = blockIdx.x;
+  const int j = q - g.dny;
+  const bool fine = !g.mb || j <= g.N3[1] || j > g.N3[2];
+  const int nh = fine ? g.N1hF : nhc, n2 = fine ? g.N2F : n2c, n1 = 2 * (nh - 1);
+  const double fy = g.thv[q] * g.dd;
+  double s = 0.0, s2 = 0.0;
+  for (int e = threadIdx.x; e < nh * n2; e += blockDim.x) {
+    const int r = e / nh, kx = e - r * nh;
+    const int fr = r < n2 / 2 ? r : r + g.N2F - n2;
+    const double2 cv = wx_mode(u2, u3, g, q, fr * g.N1hF + kx, fr, fy);
+    const double m2 = cv.x * cv.x + cv.y * cv.y;
+    if (kx == 0 || kx == nh - 1) {
+      const int rm = (n2 - r) % n2;
+      const int frm = rm < n2 / 2 ? rm : rm + g.N2F - n2;
+      const double2 cm = wx_mode(u2, u3, g, q, frm * g.N1hF + kx, frm, fy);
+      s2 += 0.5 * m2 + 0.5 * (cv.x * cm.x - cv.y * cm.y);
+      if (e == 0) s = cv.x;
+    } else {
+      s2 += 2.0 * m2;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5][0] = s; red[threadIdx.x >> 5][1] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < LH_STAT_THREADS / 32; ++w) { a += red[w][0]; b += red[w][1]; }
+    const double nn = (double)n1 * (double)n2;
+    pl[9 * (size_t)g.nu + q] += nn * a;
+    pl[10 * (size_t)g.nu + q] += nn * b;
+  }
+}
+
+// spectra (spectra.f90:1-56): band 2's levels x the long columns (cols[0..nlong)),
+// sp(level, column) += |u|^2 (U, V, W, P) and Re u1 Re v + Im u1 Im v with v interpolated
+// to the centres (interp_v, FOU3D.f90:427-474; band 2's end levels extrapolated with
+// gridweighting_interp(2, 1:2) = gi0, gi1). sp: 5 arrays [level][nlong] at offsets off[].
+__device__ __forceinline__ double2 itp_v(const double2 *__restrict__ u2, const Geo &g, int q, int c) {
+  const double2 a = u2[(size_t)q * g.ncolF + c], b = u2[(size_t)(q - 1) * g.ncolF + c];
+  const double w0 = g.yu[q] - g.yv[q - 1], w1 = g.yv[q] - g.yu[q], d = g.yv[q] - g.yv[q - 1];
+  return make_double2((w0 * a.x + w1 * b.x) / d, (w0 * a.y + w1 * b.y) / d);
+}
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_spectra(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                    const double2 *__restrict__ u3, const double2 *__restrict__ p,
+                                                    Geo g, const int *__restrict__ cols, int nlong, double gi0,
+                                                    double gi1, double *__restrict__ sp) {
+  const int ulo = g.bq[1][0], uhi = g.bq[1][1], vlo = g.bq[1][2], vhi = g.bq[1][3];
+  const int plo = g.bq[1][4], phi = g.bq[1][5];
+  const int nlu = uhi - ulo + 1, nlv = vhi - vlo + 1, nlp = phi - plo + 1;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)nlu * nlong) return;
+  const int l = (int)(i / nlong), k = (int)(i - (size_t)l * nlong);
+  const int c = cols[k];
+  const size_t nc = g.ncolF;
+  double *sU = sp, *sV = sU + (size_t)nlu * nlong, *sW = sV + (size_t)nlv * nlong, *sUV = sW + (size_t)nlu * nlong;
+  double *sP = sUV + (size_t)nlu * nlong;
+  const int q = ulo + l;
+  const double2 a = u1[q * nc + c], w = u3[q * nc + c];
+  double2 v;
+  if (q > ulo && q < uhi) v = itp_v(u2, g, q, c);
+  else if (q == ulo) {
+    const double2 i1 = itp_v(u2, g, ulo + 1, c), b = u2[(size_t)vlo * nc + c];
+    v = make_double2(gi0 * (b.x - i1.x) + i1.x, gi0 * (b.y - i1.y) + i1.y);
+  } else {
+    const double2 i2 = itp_v(u2, g, uhi - 1, c), b = u2[(size_t)vhi * nc + c];
+    v = make_double2(gi1 * (b.x - i2.x) + i2.x, gi1 * (b.y - i2.y) + i2.y);
+  }
+  sU[i] = sU[i] + a.x * a.x + a.y * a.y;
+  sW[i] = sW[i] + w.x * w.x + w.y * w.y;
+  sUV[i] = sUV[i] + a.x * v.x + a.y * v.y;
+  if (l < nlv) {
+    const double2 b = u2[(size_t)(vlo + l) * nc + c];
+    sV[i] = sV[i] + b.x * b.x + b.y * b.y;
+  }
+  if (l < nlp) {
+    const double2 b = p[(size_t)(plo + l) * nc + c];
+    sP[i] = sP[i] + b.x * b.x + b.y * b.y;
+  }
+}
+
+// slip statistics (sl_stats2.f90:33-121, inst_sl_stats.f90:1-62) at the wall faces
+// jlim(1, vgrid, 2) and jlim(2, vgrid, 2) (v array indices qb, qt), every wall-grid column:
+// u1 and u3 interpolated to the face (interp_u) and (u(q+1) - u(q)) dthdyv ddthetavi,
+// negated at the top. out: [2][4][ncolF]; acc: add (sl_stats) or store (inst_sl_stats).
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_slip(const double2 *__restrict__ u1, const double2 *__restrict__ u3, Geo g,
+                                                 int qb, int qt, double2 *__restrict__ out, int acc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncolF) return;
+  const size_t nc = g.ncolF;
+  for (int w = 0; w < 2; ++w) {
+    const int q = w ? qt : qb;
+    const double sg = w ? -1.0 : 1.0;
+    const double fy = g.thv[q] * g.dd;
+    const double ya = g.yu[q], yb = g.yu[q + 1], yv = g.yv[q];
+    for (int f = 0; f < 2; ++f) {
+      const double2 *u = f ? u3 : u1;
+      const double2 hi = u[(size_t)(q + 1) * nc + c], lo = u[(size_t)q * nc + c];
+      const double2 it = make_double2(((yv - ya) * hi.x + (yb - yv) * lo.x) / (yb - ya),
+                                      ((yv - ya) * hi.y + (yb - yv) * lo.y) / (yb - ya));
+      const double2 dy = make_double2(sg * ((hi.x - lo.x) * fy), sg * ((hi.y - lo.y) * fy));
+      double2 *o0 = out + ((size_t)(w * 4 + 2 * f) * nc + c), *o1 = o0 + nc;
+      if (acc) {
+        *o0 = make_double2(o0->x + it.x, o0->y + it.y);
+        *o1 = make_double2(o1->x + dy.x, o1->y + dy.y);
+      } else {
+        *o0 = it;
+        *o1 = dy;
+      }
+    }
+  }
+}
+
 __global__ void k_band_io(double2 *__restrict__ dev, double2 *__restrict__ stage, const int *__restrict__ cols,
                           int ncb, int nlev, int lev0, int ncol, int put) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -18,7 +18,7 @@ _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
            "lh_upload_band", "lh_download_band", "lh_stats_accumulate", "lh_stats_reset", "lh_stats_dims",
-           "lh_stats_get",
+           "lh_stats_get", "lh_spectra_dims", "lh_spectra_get", "lh_slip_get", "lh_slip_planes",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
@@ -55,6 +55,10 @@ def load(path: str = _LIB_PATH):
     L.lh_stats_reset.argtypes = [vp]
     L.lh_stats_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.lh_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+    L.lh_spectra_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.lh_spectra_get.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.lh_slip_get.argtypes = [vp, dp]
+    L.lh_slip_planes.argtypes = [vp, dp]
     L.lh_download_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_set_scalars.argtypes = [vp, C.POINTER(LhScalars)]
     L.lh_get_scalars.argtypes = [vp, C.POINTER(LhScalars)]
@@ -159,18 +163,41 @@ class GpuChannel:
             out[b] = arrs
         return out
 
-    # ---- statistics (stats.f90) ----
+    # ---- statistics (stats.f90, spectra.f90, sl_stats2.f90) ----
     def stats_accumulate(self):
         self._check(self.L.lh_stats_accumulate(self.h))
 
     def stats_reset(self):
         self._check(self.L.lh_stats_reset(self.h))
 
+    def spectra(self) -> dict:
+        """Accumulated sp(level, long column) as {"U", "V", "W", "UV", "P"}: arrays
+        [long column][level of band 2]; see include/lh.h."""
+        nl = (C.c_int * 5)()
+        nlong = C.c_int()
+        self._check(self.L.lh_spectra_dims(self.h, nl, C.byref(nlong)))
+        keys = ("U", "V", "W", "UV", "P")
+        out = {k: np.zeros((nlong.value, nl[q])) for q, k in enumerate(keys)}
+        self._check(self.L.lh_spectra_get(self.h, *[_dptr(out[k]) for k in keys]))
+        return out
+
+    def slip(self) -> np.ndarray:
+        """Accumulated slip statistics: complex [face (bottom, top)][u1, du1dy, u3, du3dy][N2][N1/2+1]"""
+        out = np.zeros((2, 4, self.s.N2, self.s.N1 // 2 + 1), np.complex128)
+        self._check(self.L.lh_slip_get(self.h, _dptr(out.view(np.float64))))
+        return out
+
+    def slip_planes(self) -> np.ndarray:
+        """The slip planes of the current state, laid out as slip()"""
+        out = np.zeros((2, 4, self.s.N2, self.s.N1 // 2 + 1), np.complex128)
+        self._check(self.L.lh_slip_planes(self.h, _dptr(out.view(np.float64))))
+        return out
+
     def stats(self):
-        """(plane [9][nyu], cond [9][ncl][dnz][dnx] or None, istat); see include/lh.h."""
+        """(plane [11][nyu], cond [9][ncl][dnz][dnx] or None, istat); see include/lh.h."""
         ncl, dnx, dnz = C.c_int(), C.c_int(), C.c_int()
         self._check(self.L.lh_stats_dims(self.h, C.byref(ncl), C.byref(dnx), C.byref(dnz)))
-        plane = np.zeros((9, self.s.nyu))
+        plane = np.zeros((11, self.s.nyu))
         cond = np.zeros((9, ncl.value, dnz.value, dnx.value)) if dnx.value else None
         ist = C.c_int64()
         self._check(self.L.lh_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist)))

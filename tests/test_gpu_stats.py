@@ -1,6 +1,8 @@
-"""Statistics on the GPU (k_xstats, through the C ABI) vs the CPU oracle: plane sums
-and tile-conditioned sums of stats.f90 after accumulating twice around a step.
-Bar: FP64 form 1e-12 relative to the largest sum; mixed 1e-5."""
+"""Statistics on the GPU (k_xstats, k_wx_stats, k_spectra, k_slip, through the C ABI) vs the
+CPU oracle after accumulating twice around a step: plane sums and tile-conditioned sums of
+stats.f90 (omega_x by Parseval on the GPU, by the inverse transform in the oracle), the
+spectra of spectra.f90 and the wall slip statistics of sl_stats2.f90 / inst_sl_stats.f90.
+Bar: FP64 form 1e-12 relative to the largest sum of a kind; mixed 1e-5."""
 import numpy as np
 import pytest
 
@@ -30,7 +32,7 @@ def run(name, precision, seed):
         x.step()
         x.stats_accumulate()
     g.synchronize()
-    return o.stats(), g.stats()
+    return o, g
 
 
 def close(a, b, tol):
@@ -44,9 +46,28 @@ def close(a, b, tol):
 @pytest.mark.parametrize("name,precision,tol", [("SP", "fp64", 1e-12), ("MB", "fp64", 1e-12),
                                                 ("SP", "mixed", 1e-5)])
 def test_stats_match_oracle(cuda_ok, name, precision, tol):
-    (po, co, io), (pg, cg, ig) = run(name, precision, 51)
-    assert io == ig == 2
-    close(po, pg, tol)
+    o, g = run(name, precision, 51)
+    (po, co, io), (pg, cg, ig) = o.stats(), g.stats()
+    assert io == ig == 2 and pg.shape == po.shape == (11, o.s.nyu)
+    close(po[:9], pg[:9], tol)
+    close(po[9:], pg[9:], tol)                      # omega_x, on its own scale
     if co is not None:
         assert cg is not None and cg.shape == co.shape
         close(co.reshape(9, -1), cg.reshape(9, -1), tol)
+    so, sg = o.spectra(), g.spectra()
+    for k in so:
+        assert sg[k].shape == so[k].shape, k
+        close(so[k][None], sg[k][None], tol)
+    # slip statistics: the state agrees to the parity bar on the scale of the whole field, so
+    # that is their scale (the faces of a textured channel lie deep in the solid, where u is
+    # small); the derivatives scale with dthdyv ddthetavi at the faces
+    bands = o.get_bands() if o.s.multiblock else {2: o.get_state()}
+    umax = {f: max(np.abs(a[f]).max() for a in bands.values() if a[f].size) for f in (0, 2)}
+    q = o.s.band_levels(2, 1)
+    fy = max(abs(o.s.dthdyv[q[0]]), abs(o.s.dthdyv[q[1]])) * o.s.ddthetavi
+    lo, lg = o.slip(), g.slip()
+    io_, ig_ = o.slip_planes(), g.slip_planes()
+    for f in range(4):
+        sc = 2 * umax[f & 2] * (fy if f in (1, 3) else 1.0)
+        assert np.abs(lo[:, f] - lg[:, f]).max() <= tol * sc, f
+        assert np.abs(io_[:, f] - ig_[:, f]).max() <= tol * sc / 2, f
