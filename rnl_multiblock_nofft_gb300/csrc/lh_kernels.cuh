@@ -68,6 +68,28 @@ template <typename V> __host__ __device__ constexpr int kb_zfwd(int n) {
 // A layout: [(slot*3 + f)][l][kx], l = 0..G2-1, kx = 0..N1h-1.
 // Lines are interleaved in shared memory (element l of line kk at l*KB + kk).
 // ============================================================================
+// Levels loaded ahead in the y sweeps of the column solves (0: a plain loop). Without it
+// a sweep's loads wait for the previous level's stores (the compiler cannot separate the
+// addresses), one memory latency per level. Deeper prefetch costs registers, i.e. resident
+// warps; the depths below were the fastest of a sweep at 256x256x301 (mixed form).
+#ifndef LH_PF_PRESS
+#define LH_PF_PRESS 1
+#endif
+#ifndef LH_PF_HU
+#define LH_PF_HU 1
+#endif
+#ifndef LH_PF_HU_BACK
+#define LH_PF_HU_BACK 2
+#endif
+#ifndef LH_PF_HV
+#define LH_PF_HV 4
+#endif
+#ifndef LH_PF_HV_BACK
+#define LH_PF_HV_BACK 2
+#endif
+#ifndef LH_PRESS_MINB
+#define LH_PRESS_MINB 1
+#endif
 #ifndef LH_ZINV_THREADS
 #define LH_ZINV_THREADS 256
 #endif
@@ -675,6 +697,44 @@ __global__ void __launch_bounds__(NTHR) k_helm_v(double2 *__restrict__ u2, doubl
 __device__ __forceinline__ float2 f2d(double2 a) { return make_float2((float)a.x, (float)a.y); }
 __device__ __forceinline__ float2 f2sub(double2 a, double2 b) { return make_float2((float)(a.x - b.x), (float)(a.y - b.y)); }
 
+// Backward sweep of the mixed-form solves: x(q) = y(q) - a3'(q) x(q+1), u(q) += x(q) for
+// q = qhi-1 .. qlo, with ys(q) = (y(q), a3'(q)). The loads of level q are issued
+// D levels ahead, before the stores of the levels in between (D = 0: a plain loop).
+template <int D>
+__device__ __forceinline__ void back_sweep_mx(double *__restrict__ u, const float2 *__restrict__ ys, size_t lstride,
+                                              size_t ci, int qlo, int qhi, float x) {
+  if constexpr (D == 0) {
+#pragma unroll 4
+    for (int q = qhi - 1; q >= qlo; --q) {
+      const size_t e = (size_t)q * lstride + ci;
+      const float2 ya = ys[e];
+      x = ya.x - ya.y * x;
+      u[e] = u[e] + f2d_alu(x);
+    }
+    return;
+  } else {
+  float2 bys[D];
+  double bu[D];
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_) {
+    const int q = qhi - 1 - s_;
+    if (q >= qlo) { const size_t e = (size_t)q * lstride + ci; bys[s_] = ys[e]; bu[s_] = u[e]; }
+  }
+  for (int qb = qhi - 1; qb >= qlo; qb -= D) {
+#pragma unroll
+    for (int s_ = 0; s_ < D; ++s_) {
+      const int q = qb - s_;
+      if (q < qlo) break;
+      const float2 ya = bys[s_];
+      const double uq = bu[s_];
+      if (q - D >= qlo) { const size_t en = (size_t)(q - D) * lstride + ci; bys[s_] = ys[en]; bu[s_] = u[en]; }
+      x = ya.x - ya.y * x;
+      u[(size_t)q * lstride + ci] = uq + f2d_alu(x);
+    }
+  }
+  }
+}
+
 // ============================================================================
 // Mixed-form solves with one lane per (column, real/imaginary part): the matrix
 // is real, so the two parts are independent systems; each lane repeats the FP32
@@ -723,6 +783,69 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
   float flm = Fl[e0];
+  // the inputs of level q are loaded LH_PF_HU levels ahead of their use, before the
+  // stores of the levels in between (the sweep's own stores would otherwise order them)
+#if LH_PF_HU > 0
+  constexpr int D = LH_PF_HU;
+  double fu[D];
+  float ffl[D], fa[D], fb[D], fc[D], fsd[D], fth[D], fnu[D], fx[D];
+  int fib[D];
+  double2 fp[D];
+#define HU_FETCH(s_, qq_)                                                        \
+  {                                                                              \
+    const int q_ = (qq_);                                                        \
+    const size_t e_ = (size_t)q_ * lstride + ci;                                 \
+    fu[s_] = u[e_ + lstride];                                                    \
+    ffl[s_] = Fl[e_];                                                            \
+    fa[s_] = g.d2uf[q_]; fb[s_] = g.d2uf[nu + q_]; fc[s_] = g.d2uf[2 * nu + q_]; \
+    fsd[s_] = g.sdgu[q_]; fth[s_] = g.thuf[q_];                                  \
+    fib[s_] = ibslot_u ? ibslot_u[q_] : -1;                                      \
+    fp[s_] = p[(size_t)(q_ - 1) * nc + c];                                       \
+    fnu[s_] = Nu[e_]; fx[s_] = X[e_];                                            \
+  }
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_)
+    if (qlo + 1 + s_ <= qhi - 1) HU_FETCH(s_, qlo + 1 + s_)
+  for (int qb = qlo + 1; qb <= qhi - 1; qb += D) {
+#pragma unroll
+    for (int s_ = 0; s_ < D; ++s_) {
+      const int q = qb + s_;
+      if (q > qhi - 1) break;
+      const size_t e = (size_t)q * lstride + ci;
+      const double up1 = fu[s_];
+      const float flq = ffl[s_], a = fa[s_], b = fb[s_], cc = fc[s_], sdg = fsd[s_] + k2f, thq = fth[s_];
+      const float nuq = fnu[s_], xq = fx[s_];
+      const int ibs = fib[s_];
+      const double2 pj = fp[s_];
+      if (q + D <= qhi - 1) HU_FETCH(s_, q + D)
+      const double dp = up1 - u0;
+      const float L = a * d2f_alu(um - u0) + cc * d2f_alu(dp) + sdg * d2f_alu(u0);
+      float du;
+      if (ibs < 0) {
+        const float pt = part ? d2f_alu(pj.x) : -d2f_alu(pj.y);  // i*C3*p: (-C3 p.y, C3 p.x)
+        du = (C1 * L + C2 * nuq) + C3 * pt + mp;
+        const float n = xq + (flq - flm) * thq * dd;
+        Nu[e] = n;
+        du += G * n;
+      } else {
+        const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+        du = d2f_alu(part ? di.y : di.x);
+      }
+      const float rr = dtf * du + beta * L;
+      const float a1 = -beta * a;
+      const float a2 = 1.f - beta * (b + k2f);
+      const float a3p = a3raw * a2p;
+      ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+      a2p = 1.f / (a2 - a1 * a3p);
+      y = (rr - a1 * y) * a2p;
+      yprev = y;
+      a3raw = -beta * cc;
+      um = u0; u0 = up1;
+      flm = flq;
+    }
+  }
+#undef HU_FETCH
+#else
 #pragma unroll 4
   for (int q = qlo + 1; q <= qhi - 1; ++q) {
     const size_t e = (size_t)q * lstride + ci;
@@ -757,6 +880,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     um = u0; u0 = up1;
     flm = flq;
   }
+#endif
   {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1))
     const int q = qhi;
     const float a1 = (float)gw2;
@@ -767,14 +891,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     y = (rl - a1 * y) * a2p;
     u[(size_t)q * lstride + ci] = u0 + f2d_alu(y);
   }
-  float x = y;
-#pragma unroll 4
-  for (int q = qhi - 1; q >= qlo; --q) {
-    const size_t e = (size_t)q * lstride + ci;
-    const float2 ya = ys[e];
-    x = ya.x - ya.y * x;
-    u[e] = u[e] + f2d_alu(x);
-  }
+  back_sweep_mx<LH_PF_HU_BACK>(u, ys, lstride, ci, qlo, qhi, y);
 }
 
 __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, float *__restrict__ Nu2,
@@ -808,38 +925,61 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
   float vvq = vvc[e0 + lstride];
-#pragma unroll 4
-  for (int q = qlo + 1; q <= qhi - 1; ++q) {
-    const size_t e = (size_t)q * lstride + ci;
-    const double vp1 = u2[e + lstride];
-    const float vvp = vvc[e + lstride];
-    const float a = g.d2vf[q], b = g.d2vf[nv + q], cc = g.d2vf[2 * nv + q];
-    const float sdg = g.sdgv[q] + k2f;
-    const float L = a * d2f_alu(vm - v0) + cc * d2f_alu(vp1 - v0) + sdg * d2f_alu(v0);
-    float du;
-    const int ibs = ibslot_v ? ibslot_v[q] : -1;
-    if (ibs < 0) {
-      const float C3 = -dRf * dd * g.thvf[q];
-      const float pd = d2f_alu(p[e]) - d2f_alu(p[e - lstride]);
-      du = (C1 * L + C2 * Nu2[e]) + C3 * pd;
-      const float n = N2xz[e] + (vvp - vvq) * g.thvf[q] * dd;
-      Nu2[e] = n;
-      du += G * n;
-    } else {
-      const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
-      du = d2f_alu(part ? di.y : di.x);
-    }
-    const float rr = dtf * du + beta * L;
-    const float a1 = -beta * a;
-    const float a2 = 1.f - beta * (b + k2f);
-    const float a3p = a3raw * a2p;
-    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
-    a2p = 1.f / (a2 - a1 * a3p);
-    y = (rr - a1 * y) * a2p;
-    yprev = y;
-    a3raw = -beta * cc;
-    vm = v0; v0 = vp1; vvq = vvp;
+  constexpr int D = LH_PF_HV > 0 ? LH_PF_HV : 1;
+  double fv[D];
+  float fvv[D], fa[D], fb[D], fc[D], fsd[D], fth[D], fnu[D], fx[D], fpd[D];
+  int fib[D];
+#define HV_FETCH(s_, qq_)                                                        \
+  {                                                                              \
+    const int q_ = (qq_);                                                        \
+    const size_t e_ = (size_t)q_ * lstride + ci;                                 \
+    fv[s_] = u2[e_ + lstride];                                                   \
+    fvv[s_] = vvc[e_ + lstride];                                                 \
+    fa[s_] = g.d2vf[q_]; fb[s_] = g.d2vf[nv + q_]; fc[s_] = g.d2vf[2 * nv + q_]; \
+    fsd[s_] = g.sdgv[q_]; fth[s_] = g.thvf[q_];                                  \
+    fib[s_] = ibslot_v ? ibslot_v[q_] : -1;                                      \
+    fpd[s_] = d2f_alu(p[e_]) - d2f_alu(p[e_ - lstride]);                         \
+    fnu[s_] = Nu2[e_]; fx[s_] = N2xz[e_];                                        \
   }
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_)
+    if (qlo + 1 + s_ <= qhi - 1) HV_FETCH(s_, qlo + 1 + s_)
+  for (int qb = qlo + 1; qb <= qhi - 1; qb += D) {
+#pragma unroll
+    for (int s_ = 0; s_ < D; ++s_) {
+      const int q = qb + s_;
+      if (q > qhi - 1) break;
+      const size_t e = (size_t)q * lstride + ci;
+      const double vp1 = fv[s_];
+      const float vvp = fvv[s_], a = fa[s_], b = fb[s_], cc = fc[s_], sdg = fsd[s_] + k2f, thq = fth[s_];
+      const float nuq = fnu[s_], xq = fx[s_], pd = fpd[s_];
+      const int ibs = fib[s_];
+      if (q + D <= qhi - 1) HV_FETCH(s_, q + D)
+      const float L = a * d2f_alu(vm - v0) + cc * d2f_alu(vp1 - v0) + sdg * d2f_alu(v0);
+      float du;
+      if (ibs < 0) {
+        const float C3 = -dRf * dd * thq;
+        du = (C1 * L + C2 * nuq) + C3 * pd;
+        const float n = xq + (vvp - vvq) * thq * dd;
+        Nu2[e] = n;
+        du += G * n;
+      } else {
+        const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
+        du = d2f_alu(part ? di.y : di.x);
+      }
+      const float rr = dtf * du + beta * L;
+      const float a1 = -beta * a;
+      const float a2 = 1.f - beta * (b + k2f);
+      const float a3p = a3raw * a2p;
+      ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+      a2p = 1.f / (a2 - a1 * a3p);
+      y = (rr - a1 * y) * a2p;
+      yprev = y;
+      a3raw = -beta * cc;
+      vm = v0; v0 = vp1; vvq = vvp;
+    }
+  }
+#undef HV_FETCH
   {  // last row: d(n-1) = -v(n-1)
     const int q = qhi;
     const float a3p = a3raw * a2p;
@@ -847,14 +987,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     y = d2f_alu(-v0);
     u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
   }
-  float x = y;
-#pragma unroll 4
-  for (int q = qhi - 1; q >= qlo; --q) {
-    const size_t e = (size_t)q * lstride + ci;
-    const float2 ya = ys[e];
-    x = ya.x - ya.y * x;
-    u2[e] = u2[e] + f2d_alu(x);
-  }
+  back_sweep_mx<LH_PF_HV_BACK>(u2, ys, lstride, ci, qlo, qhi, y);
 }
 
 // ============================================================================
@@ -1054,14 +1187,14 @@ __global__ void __launch_bounds__(NTHR) k_build_dg(double *__restrict__ dg1, dou
 // (max |div|^2 -> errbits) when need_div: the reference recomputes div after
 // every v_corr but only reads it (error()) at the start of a step, so it is
 // formed in the third substep. p levels qp <-> u/v index q = qp + 1;
-// `psi` holds the forward-sweep values, then psi.
+// `psi` holds the forward-sweep values (psi itself stays in registers).
 // ============================================================================
 // One lane per (column, real/imaginary part): the pressure matrix is real, so the two
 // parts are independent systems; the i*k couplings of the divergence and of v_corr
 // exchange the other part through a shuffle within the lane pair. Two lanes per column
 // double the warps in flight (the solves are latency-bound at the 384x192 wall grid).
 // Scalar views: element (level, col, part) at (level*ncol + col)*2 + part.
-__global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double *__restrict__ u2,
+__global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restrict__ u1, double *__restrict__ u2,
                                                  double *__restrict__ u3, double *__restrict__ p,
                                                  double *__restrict__ psi, const double *__restrict__ dg1,
                                                  const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
@@ -1086,57 +1219,95 @@ __global__ void __launch_bounds__(NTHR) k_press2(double *__restrict__ u1, double
     const double dd = g.dd;
     const size_t ls = (size_t)nc * 2;
     const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
+    constexpr int D = LH_PF_PRESS > 0 ? LH_PF_PRESS : 1;
     double y = 0.0;
     double vm = u2[(size_t)plo * ls + ci];
-#pragma unroll 4
-    for (int qp = plo; qp <= phi; ++qp) {
-      const int q = qp + 1;
-      const size_t e = (size_t)q * ls;
-      const double ao = u1[e + co], wo = u3[e + co], v = u2[e + ci];
-      const double th = dd * g.thu[q];
-      const double dv = sgn * (kxv * ao + kzv * wo) + th * (v - vm);
-      vm = v;
-      double rhs = dtirk * dv;
-      if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
-      const double A1 = dg1[(size_t)qp * nc + c], a2p = dg2[(size_t)qp * nc + c];
-      y = (qp == plo) ? rhs * a2p : (rhs - A1 * y) * a2p;
-      psi[(size_t)qp * ls + ci] = y;
+    {  // forward sweep; the inputs of a level are loaded D levels ahead
+      double fa[D], fw[D], fv[D], f1[D], f2[D], ft[D];
+#define HP_FETCH(s_, qq_)                                              \
+  {                                                                    \
+    const int qp_ = (qq_);                                             \
+    const size_t e_ = (size_t)(qp_ + 1) * ls;                          \
+    fa[s_] = u1[e_ + co]; fw[s_] = u3[e_ + co]; fv[s_] = u2[e_ + ci];  \
+    f1[s_] = dg1[(size_t)qp_ * nc + c]; f2[s_] = dg2[(size_t)qp_ * nc + c]; \
+    ft[s_] = g.thu[qp_ + 1];                                           \
+  }
+#pragma unroll
+      for (int s_ = 0; s_ < D; ++s_)
+        if (plo + s_ <= phi) HP_FETCH(s_, plo + s_)
+      for (int qb = plo; qb <= phi; qb += D) {
+#pragma unroll
+        for (int s_ = 0; s_ < D; ++s_) {
+          const int qp = qb + s_;
+          if (qp > phi) break;
+          const double ao = fa[s_], wo = fw[s_], v = fv[s_], A1 = f1[s_], a2p = f2[s_];
+          const double th = dd * ft[s_];
+          if (qp + D <= phi) HP_FETCH(s_, qp + D)
+          const double dv = sgn * (kxv * ao + kzv * wo) + th * (v - vm);
+          vm = v;
+          double rhs = dtirk * dv;
+          if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
+          y = (qp == plo) ? rhs * a2p : (rhs - A1 * y) * a2p;
+          psi[(size_t)qp * ls + ci] = y;
+        }
+      }
+#undef HP_FETCH
     }
     const double dtrk = dt * aRb;
     const double dtrk2 = dtrk * dd;
     const double kxd = dtrk * kxv, kzd = dtrk * kzv;
     double xn = y;
     double vup = 0.0, aup_o = 0.0, wup_o = 0.0;
-#pragma unroll 4
-    for (int qp = phi; qp >= plo; --qp) {
-      const int q = qp + 1;
-      const size_t e = (size_t)q * ls;
-      double x;
-      if (qp == phi) x = xn;
-      else x = psi[(size_t)qp * ls + ci] - dg3[(size_t)qp * nc + c] * xn;
-      psi[(size_t)qp * ls + ci] = x;
-      p[(size_t)qp * ls + ci] += x;
-      // u -= dtrk i kx psi: the real part gains kxd*psi.y, the imaginary part loses kxd*psi.x
-      const double xo = __shfl_xor_sync(pm, x, 1);
-      const double a = u1[e + ci] - sgn * kxd * xo;
-      const double w = u3[e + ci] - sgn * kzd * xo;
-      u1[e + ci] = a;
-      u3[e + ci] = w;
-      double v = u2[e + ci];
-      if (q <= vhi - 1) {
-        v = v - dtrk2 * g.thv[q] * (xn - x);
-        u2[e + ci] = v;
+    {  // backward sweep, v_corr and the divergence of the corrected field; loads D levels ahead
+      double bs[D], b3[D], bp[D], bu[D], bw[D], bv[D], btv[D], btu[D];
+#define HB_FETCH(s_, qq_)                                                   \
+  {                                                                         \
+    const int qp_ = (qq_);                                                  \
+    const size_t e_ = (size_t)(qp_ + 1) * ls + ci;                          \
+    bs[s_] = psi[(size_t)qp_ * ls + ci]; b3[s_] = dg3[(size_t)qp_ * nc + c]; \
+    bp[s_] = p[(size_t)qp_ * ls + ci];                                      \
+    bu[s_] = u1[e_]; bw[s_] = u3[e_]; bv[s_] = u2[e_];                      \
+    btv[s_] = g.thv[qp_ + 1]; btu[s_] = g.thu[qp_ + 2];                     \
+  }
+#pragma unroll
+      for (int s_ = 0; s_ < D; ++s_)
+        if (phi - s_ >= plo) HB_FETCH(s_, phi - s_)
+      for (int qb = phi; qb >= plo; qb -= D) {
+#pragma unroll
+        for (int s_ = 0; s_ < D; ++s_) {
+          const int qp = qb - s_;
+          if (qp < plo) break;
+          const int q = qp + 1;
+          const size_t e = (size_t)q * ls;
+          const double ps = bs[s_], d3 = b3[s_], pq = bp[s_], uq = bu[s_], wq = bw[s_];
+          const double thv = btv[s_], thu1 = btu[s_];
+          double v = bv[s_];
+          if (qp - D >= plo) HB_FETCH(s_, qp - D)
+          const double x = (qp == phi) ? xn : ps - d3 * xn;
+          p[(size_t)qp * ls + ci] = pq + x;
+          // u -= dtrk i kx psi: the real part gains kxd*psi.y, the imaginary part loses kxd*psi.x
+          const double xo = __shfl_xor_sync(pm, x, 1);
+          const double a = uq - sgn * kxd * xo;
+          const double w = wq - sgn * kzd * xo;
+          u1[e + ci] = a;
+          u3[e + ci] = w;
+          if (q <= vhi - 1) {
+            v = v - dtrk2 * thv * (xn - x);
+            u2[e + ci] = v;
+          }
+          // divergence of the corrected field at the level above (p level qp + 1)
+          const double ao = __shfl_xor_sync(pm, a, 1), wo = __shfl_xor_sync(pm, w, 1);
+          if (need_div && qp < phi) {
+            const double th = dd * thu1;
+            const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - v);
+            const double d2 = dvp * dvp;
+            dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+          }
+          aup_o = ao; wup_o = wo; vup = v;
+          xn = x;
+        }
       }
-      // divergence of the corrected field at the level above (p level qp + 1)
-      const double ao = __shfl_xor_sync(pm, a, 1), wo = __shfl_xor_sync(pm, w, 1);
-      if (need_div && qp < phi) {
-        const double th = dd * g.thu[q + 1];
-        const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - v);
-        const double d2 = dvp * dvp;
-        dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
-      }
-      aup_o = ao; wup_o = wo; vup = v;
-      xn = x;
+#undef HB_FETCH
     }
     if (need_div) {
       const double th = dd * g.thu[plo + 1];
