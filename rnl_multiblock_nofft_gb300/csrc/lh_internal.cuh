@@ -210,7 +210,15 @@ __host__ __device__ __forceinline__ void dftR(V *v) {
 // l at l*N + e, threads over e); IL = true, interleaved (at e*NL + l, threads
 // over l first), which makes every stage's loads and stores bank-conflict free.
 // ---------------------------------------------------------------------------
-template <int R, bool INV, int N, int Ns, int NL, bool IL, typename V>
+// Intermediate buffers between two stages are XOR-swizzled, element i stored at
+// i ^ ((i >> 4) & 7) (a permutation within each aligned group of 8 elements, so any
+// multiple of 8 elements maps onto itself): a radix-8 stage stores the 8 outputs of a
+// butterfly 8 elements apart, and without the swizzle the lanes of a warp would all hit the
+// same banks (16-way for 8-byte elements). A stage's first input and last output are not
+// swizzled, so the buffers the kernels fill and read keep their plain layout.
+__device__ __forceinline__ int fft_swz(int i) { return i ^ ((i >> 4) & 7); }
+
+template <int R, bool INV, int N, int Ns, int NL, bool IL, bool SWI, bool SWO, typename V>
 __device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__restrict__ dst,
                                             const V *__restrict__ tw) {
   constexpr int nb = N / R;
@@ -223,7 +231,10 @@ __device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__rest
     const int k = j % Ns;
     V v[R];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = IL ? src[(j + t * nb) * NL + line] : src[line * N + j + t * nb];
+    for (int t = 0; t < R; ++t) {
+      const int i = IL ? (j + t * nb) * NL + line : line * N + j + t * nb;
+      v[t] = src[SWI ? fft_swz(i) : i];
+    }
 #pragma unroll
     for (int t = 1; t < R; ++t) {
       V w = tw[k * step * t];
@@ -234,20 +245,22 @@ __device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__rest
     const int base = (j / Ns) * Ns * R + k;
 #pragma unroll
     for (int t = 0; t < R; ++t) {
-      if (IL) dst[(base + t * Ns) * NL + line] = v[t];
-      else dst[line * N + base + t * Ns] = v[t];
+      const int i = IL ? (base + t * Ns) * NL + line : line * N + base + t * Ns;
+      dst[SWO ? fft_swz(i) : i] = v[t];
     }
   }
 }
 
 template <bool INV, int N, int Ns, int NL, bool IL, typename V>
 __device__ __forceinline__ V *fft_rec_c(V *a, V *b, const V *__restrict__ tw) {
+  static_assert(N % 8 == 0, "the stage swizzle permutes aligned groups of 8 elements");
   if constexpr (Ns >= N) {
     return a;
   } else {
     constexpr int rem = N / Ns;
     constexpr int R = (rem % 8 == 0) ? 8 : ((rem % 6 == 0) ? 6 : ((rem % 4 == 0) ? 4 : ((rem % 2 == 0) ? 2 : 3)));
-    fft_stage_c<R, INV, N, Ns, NL, IL>(a, b, tw);
+    constexpr bool first = (Ns == 1), last = (Ns * R >= N);
+    fft_stage_c<R, INV, N, Ns, NL, IL, !first, !last>(a, b, tw);
     __syncthreads();
     return fft_rec_c<INV, N, Ns * R, NL, IL>(b, a, tw);
   }

@@ -161,7 +161,9 @@ __global__ void __launch_bounds__(LH_ZINV_THREADS) k_zinv_nl(const double2 *__re
 // ============================================================================
 // T2: x pass. PB row pairs per block; each pair of rows (l, l+1) of a field is
 // carried by one complex line (row l in .x, row l+1 in .y after the transform).
-// B layout: [pslot][l][kx]; pslot = slot*4 + p (u levels), nuI*4 + (slot-nuI)*2 + p (v).
+// B layout: [pslot][l/2][kx][l%2] (the two rows of a pair interleaved, so that the z pass
+// reads a few columns of a row pair as one contiguous run); pslot = slot*4 + p (u levels),
+// nuI*4 + (slot-nuI)*2 + p (v).
 // capture (optional): physical velocities of selected levels, [cap][f][l][m].
 // ============================================================================
 // x pass: one row pair per block (FP32) in 4 warps: a Stockham pass over the few lines
@@ -273,10 +275,11 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
   // constant here and the index split needs no runtime division.
   constexpr int NH = G1 / 3 + 1;
   for (int idx = threadIdx.x; idx < nprod * PB * 2 * NH; idx += blockDim.x) {
-    const int k = idx % NH;
-    const int rest = idx / NH;
-    const int half = rest & 1;
-    const int pb = (rest >> 1) % PB, p = (rest >> 1) / PB;
+    const int half = idx & 1;
+    const int rest = idx >> 1;
+    const int k = rest % NH;
+    const int r2 = rest / NH;
+    const int pb = r2 % PB, p = r2 / PB;
     if (pb >= npairs) continue;
     const V *L = pres + (p * PB + pb) * G1;
     const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
     if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
     else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }  // -0.5 i (z - zc)
     if (k == 0) o.y = 0;
-    B[((size_t)(pbase + p) * G2 + l0 + 2 * pb + half) * N1h + k] = o;
+    B[(((size_t)(pbase + p) * (G2 / 2) + (l0 >> 1) + pb) * N1h + k) * 2 + half] = o;
   }
 }
 
@@ -405,13 +408,18 @@ __device__ __forceinline__ void zfwd_body(const typename C2<T>::t *__restrict__ 
   const int kx0 = blockIdx.x * KB;
   V *b0 = reinterpret_cast<V *>(smem_raw);
   V *b1 = b0 + 4 * KB * N;
-  // line = p*KB + kk; element l at l*NL + line
+  // line = p*KB + kk; element l at l*NL + line. B holds the rows of a pair next to each
+  // other ([product][l/2][kx][l%2]): the KB columns of a row pair are 2*KB contiguous values.
   for (int idx = threadIdx.x; idx < N * NL; idx += blockDim.x) {
-    const int l = idx / NL, line = idx - l * NL;
-    const int p = line / KB, kk = line - p * KB, kx = kx0 + kk;
+    const int h = idx & 1;
+    int rest = idx >> 1;
+    const int kk = rest % KB;
+    rest /= KB;
+    const int lp = rest % (N / 2), p = rest / (N / 2);
+    const int l = 2 * lp + h, kx = kx0 + kk;
     V z = czero<V>();
-    if (kx < N1h) z = B[((size_t)(pbase + p) * N + l) * N1h + kx];
-    b0[idx] = z;
+    if (kx < N1h) z = B[(((size_t)(pbase + p) * (N / 2) + lp) * N1h + kx) * 2 + h];
+    b0[l * NL + p * KB + kk] = z;
   }
   __syncthreads();
   V *res = line_fft<false, N, NL, true>(b0, b1, twz);
