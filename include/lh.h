@@ -130,6 +130,16 @@ const char *lh_last_error(lh_handle *h);
 int lh_upload_state(lh_handle *h, const double *u1, const double *u2,
                     const double *u3, const double *p);
 int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p);
+/* The same, queued without blocking: an upload takes effect before the steps queued after
+ * it, a download reads the state left by the steps queued before it. The host->device
+ * copy runs on a copy stream of its own (overlapping the steps already queued) and the
+ * device->host copy on another (overlapping the steps queued later). The host arrays must
+ * stay valid, and unread/unwritten by the host, until lh_synchronize; page-locked host
+ * memory makes the copies asynchronous. Two full-state staging buffers are allocated on
+ * first use. Single-resolution channels only. */
+int lh_upload_state_async(lh_handle *h, const double *u1, const double *u2,
+                          const double *u3, const double *p);
+int lh_download_state_async(lh_handle *h, double *u1, double *u2, double *u3, double *p);
 
 /* Per-band state, the reference's cfield of one band (u1(iband)%f etc.,
  * declaration.f90:137-139): band 1 (bottom wall band) and 3 (top) hold the short

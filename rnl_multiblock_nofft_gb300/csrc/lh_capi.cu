@@ -41,10 +41,17 @@ struct lh_handle {
   float *geo_poolf;
   DevScalars *sc;
   double2 *stage;  // staging for transposes
+  // asynchronous state I/O (allocated on first use): staged copies of the whole state in
+  // each direction, copy streams, and the events that order them against the main stream
+  double2 *stage_in, *stage_out;
+  cudaStream_t st_in, st_out;
+  cudaEvent_t ev_in_copied, ev_in_used, ev_out_ready, ev_out_copied;
   // immersed boundaries
   int ib, nib, ncap;
-  int *d_lu, *d_lv, *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
-  double *d_Au, *d_Av, *cap, *duphys;
+  int *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
+  double *cap;
+  IbRec *d_ibrec;   // forced points, sorted by (plane of du, row)
+  int *d_iboff;     // [3 nib G2 + 1] record ranges per (plane, row)
   double2 *duib;
   // plane views of the nonlinear launches: wall-band planes, then core planes
   // (multiblock); one view when single-resolution
@@ -179,6 +186,7 @@ static cudaError_t set_attrs_sized(int lim) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xfwd_phys<T, N>, A, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_ib_xforce<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec<T, N>, A, lim);
   return e;
 }
@@ -405,8 +413,13 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->nib = 0; h->ncap = 0;
   h->d_sp = nullptr;
   h->d_slip = h->d_slip_inst = nullptr;
-  h->d_lu = h->d_lv = h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
-  h->d_Au = h->d_Av = h->cap = h->duphys = nullptr;
+  h->stage_in = h->stage_out = nullptr;
+  h->st_in = h->st_out = nullptr;
+  h->ev_in_copied = h->ev_in_used = h->ev_out_ready = h->ev_out_copied = nullptr;
+  h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
+  h->cap = nullptr;
+  h->d_ibrec = nullptr;
+  h->d_iboff = nullptr;
   h->duib = nullptr;
   std::vector<int> lev2cap_u(nu, -1), lev2cap_v(nv, -1);  // captured physical planes of the IB forcing
   if (h->ib) {
@@ -445,16 +458,44 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
         int rc = fail(h, LH_EINVAL, "immersed-boundary v list index out of range"); lh_destroy(h); return rc;
       }
     }
-    std::vector<double> Au(cfg->A_ib_u, cfg->A_ib_u + cfg->nib_u), Av(cfg->A_ib_v, cfg->A_ib_v + cfg->nib_v);
-    h->d_lu = (int *)upload_vec(lu, ce); h->d_lv = (int *)upload_vec(lv, ce);
-    h->d_Au = (double *)upload_vec(Au, ce); h->d_Av = (double *)upload_vec(Av, ce);
+    // forced points as records of du's planes (slot s, field f) sorted by (plane, row), in
+    // list order within a row: a u-list point forces u1 and u3, a v-list point v. Points
+    // whose level is not an immersed level or whose reference level is not captured are
+    // skipped (the reference's lists never hold such points).
+    const size_t pp = (size_t)g.G1 * g.G2;
+    const size_t nrow = (size_t)3 * h->nib * g.G2;
+    std::vector<std::vector<IbRec>> rows(nrow);
+    auto add = [&](const int *L, double A, const std::vector<int> &slot, const std::vector<int> &l2c, int f) {
+      const int q = L[2] + d, q1 = L[5] + d;
+      const int s = slot[q], cs = l2c[q], cs1 = l2c[q1];
+      if (s < 0 || cs < 0 || cs1 < 0) return;
+      IbRec R;
+      R.i = L[0] - 1; R.k = L[1] - 1;
+      R.src = (long long)((size_t)(cs * 3 + f) * pp + (size_t)R.k * g.G1 + R.i);
+      R.ref = (long long)((size_t)(cs1 * 3 + f) * pp + (size_t)(L[4] - 1) * g.G1 + (L[3] - 1));
+      R.A = A;
+      rows[((size_t)s * 3 + f) * g.G2 + R.k].push_back(R);
+    };
+    for (size_t e = 0; e < lu.size() / 6; ++e) {
+      add(&lu[6 * e], cfg->A_ib_u[e], ibslot_u, lev2cap_u, 0);
+      add(&lu[6 * e], cfg->A_ib_u[e], ibslot_u, lev2cap_u, 2);
+    }
+    for (size_t e = 0; e < lv.size() / 6; ++e) add(&lv[6 * e], cfg->A_ib_v[e], ibslot_v, lev2cap_v, 1);
+    std::vector<IbRec> rec;
+    std::vector<int> off(nrow + 1, 0);
+    for (size_t r = 0; r < nrow; ++r) {
+      off[r] = (int)rec.size();
+      rec.insert(rec.end(), rows[r].begin(), rows[r].end());
+    }
+    off[nrow] = (int)rec.size();
+    if (rec.empty()) rec.push_back(IbRec{0, 0, 0, 0, 0.0});  // a valid pointer; no range refers to it
+    h->d_ibrec = (IbRec *)upload_vec(rec, ce);
+    if (ce == cudaSuccess) h->d_iboff = (int *)upload_vec(off, ce);
     h->d_ibslot_u = (int *)upload_vec(ibslot_u, ce); h->d_ibslot_v = (int *)upload_vec(ibslot_v, ce);
     h->d_iblev = (int *)upload_vec(iblev, ce);
     h->d_lev2cap_u = (int *)upload_vec(lev2cap_u, ce); h->d_lev2cap_v = (int *)upload_vec(lev2cap_v, ce);
     if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
-    const size_t pp = (size_t)g.G1 * g.G2;
     ZA(h->cap, sizeof(double) * (size_t)h->ncap * 3 * pp);
-    ZA(h->duphys, sizeof(double) * (size_t)h->nib * 3 * pp);
     ZA(h->duib, cz * (size_t)h->nib * 3 * nc);
   }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -589,12 +630,16 @@ extern "C" int lh_destroy(lh_handle *h) {
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
   void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
-                  h->d_lu, h->d_lv, h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
-                  h->d_lev2cap_v, h->d_Au, h->d_Av, h->cap, h->duphys, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
+                  h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
+                  h->d_lev2cap_v, h->d_ibrec, h->d_iboff, h->cap, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
                   h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
-                  h->ysv, h->a3v, h->st_pl, h->st_cd, h->d_sp, h->d_slip, h->d_slip_inst};
+                  h->ysv, h->a3v, h->st_pl, h->st_cd, h->d_sp, h->d_slip, h->d_slip_inst, h->stage_in, h->stage_out};
   for (void *b : bufs)
     if (b) cudaFree(b);
+  for (cudaEvent_t e : {h->ev_in_copied, h->ev_in_used, h->ev_out_ready, h->ev_out_copied})
+    if (e) cudaEventDestroy(e);
+  if (h->st_in) cudaStreamDestroy(h->st_in);
+  if (h->st_out) cudaStreamDestroy(h->st_out);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->st2) cudaStreamDestroy(h->st2);
@@ -649,11 +694,95 @@ extern "C" int lh_upload_state(lh_handle *h, const double *u1, const double *u2,
 extern "C" int lh_download_state(lh_handle *h, double *u1, double *u2, double *u3, double *p) {
   if (!h) return LH_EINVAL;
   if (h->g.mb) return fail(h, LH_EINVAL, "multiblock channel: use lh_download_band");
-  int rc;
-  if (u1) { if ((rc = get_field(h, h->u1, h->g.nu, u1))) return rc; CK(cudaStreamSynchronize(h->st)); }
-  if (u2) { if ((rc = get_field(h, h->u2, h->g.nv, u2))) return rc; CK(cudaStreamSynchronize(h->st)); }
-  if (u3) { if ((rc = get_field(h, h->u3, h->g.nu, u3))) return rc; CK(cudaStreamSynchronize(h->st)); }
-  if (p) { if ((rc = get_field(h, h->p, h->g.np, p))) return rc; CK(cudaStreamSynchronize(h->st)); }
+  int rc;  // stream order protects the staging buffer between the fields
+  if (u1 && (rc = get_field(h, h->u1, h->g.nu, u1))) return rc;
+  if (u2 && (rc = get_field(h, h->u2, h->g.nv, u2))) return rc;
+  if (u3 && (rc = get_field(h, h->u3, h->g.nu, u3))) return rc;
+  if (p && (rc = get_field(h, h->p, h->g.np, p))) return rc;
+  CK(cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+// ---- asynchronous state I/O ----
+// The host->device copy of an upload runs on its own stream as soon as the previous
+// upload's transposes have consumed the input staging; only its transposes into the
+// state wait for the work already queued (the previous step, the previous download's
+// transposes). A download's transposes follow the queued steps on the main stream and its
+// device->host copy runs on a second copy stream, overlapping the steps queued after it.
+static int async_io_init(lh_handle *h) {
+  if (h->stage_in) return LH_OK;
+  const size_t n = (size_t)(2 * h->g.nu + h->g.nv + h->g.np) * h->g.ncol;
+  CK(cudaMalloc(&h->stage_in, sizeof(double2) * n));
+  CK(cudaMalloc(&h->stage_out, sizeof(double2) * n));
+  CK(cudaStreamCreateWithFlags(&h->st_in, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking));
+  for (cudaEvent_t *e : {&h->ev_in_copied, &h->ev_in_used, &h->ev_out_ready, &h->ev_out_copied})
+    CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  CK(cudaEventRecord(h->ev_in_used, h->st));
+  CK(cudaEventRecord(h->ev_out_copied, h->st));
+  return LH_OK;
+}
+// field f of the state: device array, levels, offset in the staging
+static void state_field(lh_handle *h, int f, double2 *&dev, int &nlev, size_t &off) {
+  const size_t nc = h->g.ncol, nu = h->g.nu, nv = h->g.nv;
+  double2 *F[4] = {h->u1, h->u2, h->u3, h->p};
+  const int L[4] = {h->g.nu, h->g.nv, h->g.nu, h->g.np};
+  const size_t O[4] = {0, nu * nc, (nu + nv) * nc, (2 * nu + nv) * nc};
+  dev = F[f]; nlev = L[f]; off = O[f];
+}
+
+extern "C" int lh_upload_state_async(lh_handle *h, const double *u1, const double *u2, const double *u3,
+                                     const double *p) {
+  if (!h) return LH_EINVAL;
+  if (h->g.mb) return fail(h, LH_EINVAL, "multiblock channel: use lh_upload_band");
+  int rc = async_io_init(h);
+  if (rc) return rc;
+  const double *H[4] = {u1, u2, u3, p};
+  const int nc = h->g.ncol;
+  CK(cudaStreamWaitEvent(h->st_in, h->ev_in_used, 0));
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    double2 *dev; int nl; size_t off;
+    state_field(h, f, dev, nl, off);
+    CK(cudaMemcpyAsync(h->stage_in + off, H[f], sizeof(double2) * (size_t)nc * nl, cudaMemcpyHostToDevice, h->st_in));
+  }
+  CK(cudaEventRecord(h->ev_in_copied, h->st_in));
+  CK(cudaStreamWaitEvent(h->st, h->ev_in_copied, 0));
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    double2 *dev; int nl; size_t off;
+    state_field(h, f, dev, nl, off);
+    dim3 grid((nl + 31) / 32, (nc + 31) / 32), blk(32, 8);
+    KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(h->stage_in + off, dev, nc, nl));
+  }
+  CK(cudaEventRecord(h->ev_in_used, h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_download_state_async(lh_handle *h, double *u1, double *u2, double *u3, double *p) {
+  if (!h) return LH_EINVAL;
+  if (h->g.mb) return fail(h, LH_EINVAL, "multiblock channel: use lh_download_band");
+  int rc = async_io_init(h);
+  if (rc) return rc;
+  double *H[4] = {u1, u2, u3, p};
+  const int nc = h->g.ncol;
+  CK(cudaStreamWaitEvent(h->st, h->ev_out_copied, 0));
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    double2 *dev; int nl; size_t off;
+    state_field(h, f, dev, nl, off);
+    dim3 grid((nc + 31) / 32, (nl + 31) / 32), blk(32, 8);
+    KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(dev, h->stage_out + off, nl, nc));
+  }
+  CK(cudaEventRecord(h->ev_out_ready, h->st));
+  CK(cudaStreamWaitEvent(h->st_out, h->ev_out_ready, 0));
+  for (int f = 0; f < 4; ++f) {
+    if (!H[f]) continue;
+    double2 *dev; int nl; size_t off;
+    state_field(h, f, dev, nl, off);
+    CK(cudaMemcpyAsync(H[f], h->stage_out + off, sizeof(double2) * (size_t)nc * nl, cudaMemcpyDeviceToHost, h->st_out));
+  }
+  CK(cudaEventRecord(h->ev_out_copied, h->st_out));
   return LH_OK;
 }
 
@@ -847,6 +976,15 @@ static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int n
   return LH_OK;
 }
 
+template <typename T, int N>
+static int launch_ib_xforce(lh_handle *h, int npl) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  dim3 g2((h->g.G2 / 2 + PB - 1) / PB, npl);
+  KL("k_ib_xforce", k_ib_xforce<T, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>(
+                        (const V *)h->A, (V *)h->B, h->g, (const V *)h->twx, h->d_ibrec, h->d_iboff, h->cap, h->sc));
+  return LH_OK;
+}
 template <typename T>
 static int spec_to_phys(lh_handle *h, const double2 *spec, double *phys, int npl, void *Ascr, const void *twx,
                         const void *twz) {
@@ -910,15 +1048,15 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                          (const float2 *)h->vvc, (const float2 *)h->wvf, h->p, h->duib,
                                                          h->d_iblev, h->nib, g, h->sc, kRK));
     }
-    if ((rc = spec_to_phys<T>(h, h->duib, h->duphys, 3 * h->nib, h->A, h->twx, h->twz))) return rc;
-    int ibu = (h->cfg.nib_u + 255) / 256, ibv = (h->cfg.nib_v + 255) / 256;
-    if (h->cfg.nib_u > 0)
-      KL("k_ib_force", k_ib_force<<<ibu, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lu, h->d_Au, h->cfg.nib_u, 1,
-                                                          h->d_ibslot_u, h->d_lev2cap_u, g, h->sc));
-    if (h->cfg.nib_v > 0)
-      KL("k_ib_force", k_ib_force<<<ibv, 256, 0, h->st>>>(h->duphys, h->cap, h->d_lv, h->d_Av, h->cfg.nib_v, 0,
-                                                          h->d_ibslot_v, h->d_lev2cap_v, g, h->sc));
-    if ((rc = phys_to_spec<T>(h, h->duphys, h->duib, 3 * h->nib, h->B, h->twx, h->twz))) return rc;
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G2, rc = launch_spec_zinv<T, N>(h, h->duib, h->A, 3 * h->nib, h->twz));
+    if (rc) return rc;
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G1, rc = launch_ib_xforce<T, N>(h, 3 * h->nib));
+    if (rc) return rc;
+    rc = LH_EINVAL;
+    LH_DISPATCH(g.G2, rc = launch_zfwd_spec<T, N>(h, h->B, h->duib, 3 * h->nib, h->twz));
+    if (rc) return rc;
   }
   // The u/w and v solves are independent: v runs on the side stream while u/w and the
   // mean-flow correction (which follows u) run on the main stream; each solve has its
@@ -1212,6 +1350,8 @@ extern "C" int lh_slip_planes(lh_handle *h, double *out) {
 extern "C" int lh_synchronize(lh_handle *h) {
   if (!h) return LH_EINVAL;
   CK(cudaStreamSynchronize(h->st));
+  if (h->st_in) CK(cudaStreamSynchronize(h->st_in));
+  if (h->st_out) CK(cudaStreamSynchronize(h->st_out));
   int status = 0;
   CK(cudaMemcpy(&status, &h->sc->status, sizeof(int), cudaMemcpyDeviceToHost));
   if (status == LH_ENONFINITE) return fail(h, LH_ENONFINITE, "non-finite state (divergence or dt)");

@@ -1832,27 +1832,80 @@ __global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u
   }
 }
 
-// forcing at listed solid points: list entries (i,k,j,i1,k1,j1), 1-based i,k
-// duphys [ibslot][field][G2][G1]; cap [capslot][field][G2][G1] (physical u,v,w)
-__global__ void k_ib_force(double *__restrict__ duphys, const double *__restrict__ cap,
-                           const int *__restrict__ list, const double *__restrict__ A, int n, int grid_is_u,
-                           const int *__restrict__ lev2ib, const int *__restrict__ lev2cap, Geo g,
-                           const DevScalars *__restrict__ sc) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  const int *L = list + 6 * (size_t)e;
-  const int i = L[0] - 1, k = L[1] - 1, q = L[2] + g.dny, i1 = L[3] - 1, k1 = L[4] - 1, q1 = L[5] + g.dny;
-  const double Kibdt = g.Kib / sc->dt;
-  const size_t pp = (size_t)g.G1 * g.G2;
-  const int s = lev2ib[q];
-  const int cs = lev2cap[q], cs1 = lev2cap[q1];
-  if (s < 0 || cs < 0 || cs1 < 0) return;
-  const int nf = grid_is_u ? 2 : 1;
-  for (int t = 0; t < nf; ++t) {
-    const int f = grid_is_u ? (t ? 2 : 0) : 1;
-    const double V = A[e] * cap[((size_t)cs1 * 3 + f) * pp + (size_t)k1 * g.G1 + i1];
-    const double u = cap[((size_t)cs * 3 + f) * pp + (size_t)k * g.G1 + i];
-    duphys[((size_t)s * 3 + f) * pp + (size_t)k * g.G1 + i] = Kibdt * (V - u);
+// ============================================================================
+// Immersed-boundary forcing in one x pass (imm_bounds_u/v, FOU3D.f90:806-998): the rows
+// of du's planes (z pass done, A layout) go to physical space, the forced points of the
+// rows are overwritten with Kib/dt (A u(i1,k1,j1) - u(i,k,j)) from the captured physical
+// velocities, and the rows go back (B layout for the z pass). Forced points come as
+// records sorted by (plane, row): rec_off[plane * G2 + row] .. rec_off[... + 1];
+// cap [capslot][field][G2][G1] holds the physical u, v, w the x pass captured.
+// ============================================================================
+struct IbRec {
+  int i, k;        // 0-based point of the plane: x index, row
+  long long src;   // cap offset of u at the point
+  long long ref;   // cap offset of u at the reference point (i1, k1, j1)
+  double A;
+};
+template <typename T, int N>
+__global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__restrict__ A, typename C2<T>::t *__restrict__ B,
+                                                    Geo g, const typename C2<T>::t *__restrict__ twx,
+                                                    const IbRec *__restrict__ rec, const int *__restrict__ rec_off,
+                                                    const double *__restrict__ cap, const DevScalars *__restrict__ sc) {
+  typedef typename C2<T>::t V;
+  constexpr int PB = 4 * pb_xpass<V>(N);
+  constexpr int G1 = N, H = N / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G2 = g.G2, N1h = g.N1h;
+  V *b0 = reinterpret_cast<V *>(smem_raw);
+  V *b1 = b0 + PB * G1;
+  const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const V *Ap = A + (size_t)pl * G2 * N1h;
+  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
+    const int pb = idx / G1, m = idx - pb * G1;
+    V z = czero<V>();
+    if (pb < npairs) {
+      const int l = l0 + 2 * pb;
+      int k = m; bool cj = false;
+      if (m > H) { k = G1 - m; cj = true; }
+      if (k < N1h) {
+        V a = Ap[(size_t)l * N1h + k], b = Ap[(size_t)(l + 1) * N1h + k];
+        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
+        if (!cj) { z.x = a.x - b.y; z.y = a.y + b.x; } else { z.x = a.x + b.y; z.y = -a.y + b.x; }
+      }
+    }
+    b0[idx] = z;
+  }
+  __syncthreads();
+  V *res = line_fft<true, N, PB, false>(b0, b1, twx);
+  V *oth = (res == b0) ? b1 : b0;
+  {
+    const double Kibdt = g.Kib / sc->dt;
+    const int r0 = rec_off[(size_t)pl * G2 + l0], r1 = rec_off[(size_t)pl * G2 + l0 + 2 * npairs];
+    for (int e = r0 + threadIdx.x; e < r1; e += blockDim.x) {
+      const IbRec R = rec[e];
+      const double val = Kibdt * (R.A * cap[R.ref] - cap[R.src]);
+      const int rr = R.k - l0;
+      V *z = res + (rr >> 1) * G1 + R.i;
+      if (rr & 1) z->y = to_t<T>(val);
+      else z->x = to_t<T>(val);
+    }
+  }
+  __syncthreads();
+  V *fres = line_fft<false, N, PB, false>(res, oth, twx);
+  const T s1 = (T)1 / (T)G1;
+  for (int idx = threadIdx.x; idx < PB * 2 * N1h; idx += blockDim.x) {
+    const int k = idx % N1h, rest = idx / N1h;
+    const int half = rest & 1, pb = rest >> 1;
+    if (pb >= npairs) continue;
+    const V *L = fres + pb * G1;
+    const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
+    V o;
+    if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
+    else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }
+    if (k == 0) o.y = 0;
+    B[((size_t)pl * G2 + l0 + 2 * pb + half) * N1h + k] = o;
   }
 }
+
 

@@ -17,6 +17,7 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
 _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
+           "lh_upload_state_async", "lh_download_state_async",
            "lh_upload_band", "lh_download_band", "lh_stats_accumulate", "lh_stats_reset", "lh_stats_dims",
            "lh_stats_get", "lh_spectra_dims", "lh_spectra_get", "lh_slip_get", "lh_slip_planes",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
@@ -50,6 +51,8 @@ def load(path: str = _LIB_PATH):
     L.lh_last_error.restype = C.c_char_p
     L.lh_upload_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_download_state.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_upload_state_async.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_download_state_async.argtypes = [vp, dp, dp, dp, dp]
     L.lh_upload_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_stats_accumulate.argtypes = [vp]
     L.lh_stats_reset.argtypes = [vp]
@@ -110,6 +113,7 @@ class GpuChannel:
             raise LhError(rc, "lh_create failed: " + self.L.lh_last_error(None).decode())
         self.h = h
         self.shapes = cfield_shape(setup)
+        self._pending = []   # host arrays of queued asynchronous copies
 
     def _check(self, rc: int):
         if rc != LH_OK:
@@ -143,6 +147,25 @@ class GpuChannel:
             if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
                 raise ValueError("download buffers must be C-contiguous complex128 of the state shapes")
         self._check(self.L.lh_download_state(self.h, *[_dptr(a) for a in out]))
+        return out
+
+    def upload_state_async(self, u1, u2, u3, p):
+        """Queued upload (lh_upload_state_async): the arrays must be C-contiguous complex128 of
+        the state shapes, ideally page-locked; they are kept alive until synchronize()."""
+        arrs = (u1, u2, u3, p)
+        for a, sh in zip(arrs, self.shapes):
+            if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                raise ValueError("upload buffers must be C-contiguous complex128 of the state shapes")
+        self._pending.extend(arrs)
+        self._check(self.L.lh_upload_state_async(self.h, *[_dptr(a) for a in arrs]))
+
+    def download_state_async(self, out):
+        """Queued download into `out` (lh_download_state_async); valid after synchronize()."""
+        for a, sh in zip(out, self.shapes):
+            if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                raise ValueError("download buffers must be C-contiguous complex128 of the state shapes")
+        self._pending.extend(out)
+        self._check(self.L.lh_download_state_async(self.h, *[_dptr(a) for a in out]))
         return out
 
     def upload_bands(self, bands: dict):
@@ -224,6 +247,7 @@ class GpuChannel:
 
     def synchronize(self):
         self._check(self.L.lh_synchronize(self.h))
+        self._pending = []
 
     def kernel_launches(self) -> int:
         return int(self.L.lh_kernel_launches(self.h))
