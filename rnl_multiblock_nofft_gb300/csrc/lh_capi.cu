@@ -323,6 +323,9 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   size_t o_k1x = put(cfg->k1x, g.N1h), o_k2x = put(cfg->k2x, g.N1h), o_k1z = put(cfg->k1z, g.N2), o_k2z = put(cfg->k2z, g.N2);
   size_t o_iua = put(iua.data(), nu), o_iub = put(iub.data(), nu), o_iud = put(iud.data(), nu);
   size_t o_iva = put(iva.data(), nv), o_ivb = put(ivb.data(), nv), o_ivd = put(ivd.data(), nv);
+  std::vector<double> thud(nu);  // ddthetavi * dthdyu, the divergence's y factor
+  for (int q = 0; q < nu; ++q) thud[q] = cfg->ddthetavi * cfg->dthdyu[q];
+  size_t o_thud = put(thud.data(), nu);
   cudaError_t ce;
   h->geo_pool = (double *)upload_vec(pool, ce);
   if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
@@ -330,6 +333,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   g.yu = P + o_yu; g.yv = P + o_yv; g.thu = P + o_thu; g.thv = P + o_thv; g.d2u = P + o_d2u; g.d2v = P + o_d2v;
   g.k1x = P + o_k1x; g.k2x = P + o_k2x; g.k1z = P + o_k1z; g.k2z = P + o_k2z;
   g.iua = P + o_iua; g.iub = P + o_iub; g.iud = P + o_iud; g.iva = P + o_iva; g.ivb = P + o_ivb; g.ivd = P + o_ivd;
+  g.thud = P + o_thud;
   {  // FP32 copies for the mixed form
     std::vector<float> pf;
     auto putf = [&](const double *src, size_t n) { size_t o = pf.size(); for (size_t i = 0; i < n; ++i) pf.push_back((float)src[i]); return o; };

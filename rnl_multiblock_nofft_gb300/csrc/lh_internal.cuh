@@ -20,6 +20,7 @@ struct Geo {
   const double *iua, *iub, *iud;
   // v-level q (centre -> face): (iva*u[q+1] + ivb*u[q]) / ivd
   const double *iva, *ivb, *ivd;
+  const double *thud;  // dd * thu (the divergence's y factor)
   // FP32 copies for the mixed form (no conversion in the kernels): wavenumbers,
   // interpolation weights, metrics, difference coefficients and their row sums
   const float *k1xf, *k1zf, *iuaf, *iubf, *ivaf, *ivbf, *thuf, *thvf, *d2uf, *d2vf, *sdgu, *sdgv;
@@ -235,11 +236,13 @@ __device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__rest
       const int i = IL ? (j + t * nb) * NL + line : line * N + j + t * nb;
       v[t] = src[SWI ? fft_swz(i) : i];
     }
+    if constexpr (Ns > 1) {  // the first stage's twiddles are all 1
 #pragma unroll
-    for (int t = 1; t < R; ++t) {
-      V w = tw[k * step * t];
-      if (INV) w.y = -w.y;
-      v[t] = cmul(v[t], w);
+      for (int t = 1; t < R; ++t) {
+        V w = tw[k * step * t];
+        if (INV) w.y = -w.y;
+        v[t] = cmul(v[t], w);
+      }
     }
     dftR<R, INV>(v);
     const int base = (j / Ns) * Ns * R + k;

@@ -798,7 +798,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   double fu[D];
   float ffl[D], fa[D], fb[D], fc[D], fsd[D], fth[D], fnu[D], fx[D];
   int fib[D];
-  double2 fp[D];
+  double fp[D];                       // the other part of p: i*C3*p = (-C3 p.y, C3 p.x)
+  const double *pc = reinterpret_cast<const double *>(p);
 #define HU_FETCH(s_, qq_)                                                        \
   {                                                                              \
     const int q_ = (qq_);                                                        \
@@ -808,7 +809,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     fa[s_] = g.d2uf[q_]; fb[s_] = g.d2uf[nu + q_]; fc[s_] = g.d2uf[2 * nu + q_]; \
     fsd[s_] = g.sdgu[q_]; fth[s_] = g.thuf[q_];                                  \
     fib[s_] = ibslot_u ? ibslot_u[q_] : -1;                                      \
-    fp[s_] = p[(size_t)(q_ - 1) * nc + c];                                       \
+    fp[s_] = pc[((size_t)(q_ - 1) * nc + c) * 2 + (part ^ 1)];                   \
     fnu[s_] = Nu[e_]; fx[s_] = X[e_];                                            \
   }
 #pragma unroll
@@ -824,13 +825,13 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
       const float flq = ffl[s_], a = fa[s_], b = fb[s_], cc = fc[s_], sdg = fsd[s_] + k2f, thq = fth[s_];
       const float nuq = fnu[s_], xq = fx[s_];
       const int ibs = fib[s_];
-      const double2 pj = fp[s_];
+      const double po = fp[s_];
       if (q + D <= qhi - 1) HU_FETCH(s_, q + D)
       const double dp = up1 - u0;
       const float L = a * d2f_alu(um - u0) + cc * d2f_alu(dp) + sdg * d2f_alu(u0);
       float du;
       if (ibs < 0) {
-        const float pt = part ? d2f_alu(pj.x) : -d2f_alu(pj.y);  // i*C3*p: (-C3 p.y, C3 p.x)
+        const float pt = part ? d2f_alu(po) : -d2f_alu(po);
         du = (C1 * L + C2 * nuq) + C3 * pt + mp;
         const float n = xq + (flq - flm) * thq * dd;
         Nu[e] = n;
@@ -1221,6 +1222,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     const double kxv = g.k1x[kx], kzv = g.k1z[r];
     // i*k*z: real part -k*z.y, imaginary part k*z.x; lane `part` reads the other part
     const double sgn = part ? 1.0 : -1.0;
+    const double skx = sgn * kxv, skz = sgn * kzv;  // sgn*(a+b) = sgn*a + sgn*b exactly
     const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
     const double dtirk = sc->dti / aRb;
     const double dt = sc->dt;
@@ -1238,7 +1240,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     const size_t e_ = (size_t)(qp_ + 1) * ls;                          \
     fa[s_] = u1[e_ + co]; fw[s_] = u3[e_ + co]; fv[s_] = u2[e_ + ci];  \
     f1[s_] = dg1[(size_t)qp_ * nc + c]; f2[s_] = dg2[(size_t)qp_ * nc + c]; \
-    ft[s_] = g.thu[qp_ + 1];                                           \
+    ft[s_] = g.thud[qp_ + 1];                                          \
   }
 #pragma unroll
       for (int s_ = 0; s_ < D; ++s_)
@@ -1249,9 +1251,9 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
           const int qp = qb + s_;
           if (qp > phi) break;
           const double ao = fa[s_], wo = fw[s_], v = fv[s_], A1 = f1[s_], a2p = f2[s_];
-          const double th = dd * ft[s_];
+          const double th = ft[s_];
           if (qp + D <= phi) HP_FETCH(s_, qp + D)
-          const double dv = sgn * (kxv * ao + kzv * wo) + th * (v - vm);
+          const double dv = (skx * ao + skz * wo) + th * (v - vm);
           vm = v;
           double rhs = dtirk * dv;
           if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
@@ -1275,7 +1277,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     bs[s_] = psi[(size_t)qp_ * ls + ci]; b3[s_] = dg3[(size_t)qp_ * nc + c]; \
     bp[s_] = p[(size_t)qp_ * ls + ci];                                      \
     bu[s_] = u1[e_]; bw[s_] = u3[e_]; bv[s_] = u2[e_];                      \
-    btv[s_] = g.thv[qp_ + 1]; btu[s_] = g.thu[qp_ + 2];                     \
+    btv[s_] = g.thv[qp_ + 1]; btu[s_] = g.thud[qp_ + 2];                    \
   }
 #pragma unroll
       for (int s_ = 0; s_ < D; ++s_)
@@ -1306,8 +1308,8 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
           // divergence of the corrected field at the level above (p level qp + 1)
           const double ao = __shfl_xor_sync(pm, a, 1), wo = __shfl_xor_sync(pm, w, 1);
           if (need_div && qp < phi) {
-            const double th = dd * thu1;
-            const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - v);
+            const double th = thu1;
+            const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - v);
             const double d2 = dvp * dvp;
             dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
           }
@@ -1318,9 +1320,9 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
 #undef HB_FETCH
     }
     if (need_div) {
-      const double th = dd * g.thu[plo + 1];
+      const double th = g.thud[plo + 1];
       const double vb = u2[(size_t)plo * ls + ci];
-      const double dvp = sgn * (kxv * aup_o + kzv * wup_o) + th * (vup - vb);
+      const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
       const double d2 = dvp * dvp;
       dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
     }

@@ -54,10 +54,13 @@ def test_stats_match_oracle(cuda_ok, name, precision, tol):
     if co is not None:
         assert cg is not None and cg.shape == co.shape
         close(co.reshape(9, -1), cg.reshape(9, -1), tol)
+    # spectra are quadratic in a field whose mixed-form error is up to 1e-5 of its own
+    # scale: 3x the field bar (FP64: the same bar)
     so, sg = o.spectra(), g.spectra()
+    tq = tol if precision == "fp64" else 3 * tol
     for k in so:
         assert sg[k].shape == so[k].shape, k
-        close(so[k][None], sg[k][None], tol)
+        close(so[k][None], sg[k][None], tq)
     # slip statistics: the state agrees to the parity bar on the scale of the whole field, so
     # that is their scale (the faces of a textured channel lie deep in the solid, where u is
     # small); the derivatives scale with dthdyv ddthetavi at the faces
