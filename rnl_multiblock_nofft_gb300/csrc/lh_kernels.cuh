@@ -788,6 +788,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   const size_t e0 = (size_t)qlo * lstride + ci;
   double um = u[e0], u0 = u[e0 + lstride];
   float y = d2f_alu(-(um + gw1 * u0));  // first row
+  // um - u0 at level q is -(up1 - u0) of level q-1: one FP64 difference per level
+  float fdm = d2f_alu(um - u0);
   float yprev = y;
   float a3raw = (float)gw1, a2p = 1.f;
   float flm = Fl[e0];
@@ -827,8 +829,9 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
       const int ibs = fib[s_];
       const double po = fp[s_];
       if (q + D <= qhi - 1) HU_FETCH(s_, q + D)
-      const double dp = up1 - u0;
-      const float L = a * d2f_alu(um - u0) + cc * d2f_alu(dp) + sdg * d2f_alu(u0);
+      const float fdp = d2f_alu(up1 - u0);
+      const float L = a * fdm + cc * fdp + sdg * d2f_alu(u0);
+      fdm = -fdp;
       float du;
       if (ibs < 0) {
         const float pt = part ? d2f_alu(po) : -d2f_alu(po);
@@ -862,8 +865,9 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     const float flq = Fl[e];
     const float a = g.d2uf[q], b = g.d2uf[nu + q], cc = g.d2uf[2 * nu + q];
     const float sdg = g.sdgu[q] + k2f;
-    const double dp = up1 - u0;
-    const float L = a * d2f_alu(um - u0) + cc * d2f_alu(dp) + sdg * d2f_alu(u0);
+    const float fdp = d2f_alu(up1 - u0);
+    const float L = a * fdm + cc * fdp + sdg * d2f_alu(u0);
+    fdm = -fdp;
     float du;
     const int ibs = ibslot_u ? ibslot_u[q] : -1;
     if (ibs < 0) {
@@ -931,6 +935,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   double vm = u2[e0], v0 = u2[e0 + lstride];
   const float dRf = (float)dR;
   float y = d2f_alu(-vm);
+  float fdm = d2f_alu(vm - v0);  // carried as -(vp1 - v0) of the level below
   float yprev = y;
   float a3raw = 0.f, a2p = 1.f;
   float vvq = vvc[e0 + lstride];
@@ -964,7 +969,9 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
       const float nuq = fnu[s_], xq = fx[s_], pd = fpd[s_];
       const int ibs = fib[s_];
       if (q + D <= qhi - 1) HV_FETCH(s_, q + D)
-      const float L = a * d2f_alu(vm - v0) + cc * d2f_alu(vp1 - v0) + sdg * d2f_alu(v0);
+      const float fdp = d2f_alu(vp1 - v0);
+      const float L = a * fdm + cc * fdp + sdg * d2f_alu(v0);
+      fdm = -fdp;
       float du;
       if (ibs < 0) {
         const float C3 = -dRf * dd * thq;
