@@ -1100,7 +1100,8 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
-  KL("k_press", k_press2<<<nbp2, h->tb_p, 0, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
+  const size_t ptab = sizeof(double) * (size_t)(g.nu + g.nv);  // the kernel's per-level factor tables
+  KL("k_press", k_press2<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
                                                     (double *)h->p, (double *)h->psi, h->dg1, h->dg2, h->dg3, g,
                                                     h->sc, kRK, need_div));
   if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));

@@ -1220,6 +1220,16 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
   const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
   const int nc = g.ncol;
   double dmax = 0.0;
+  // per-level factors of this substep: dti/(a+b) dd thu (divergence -> right-hand side)
+  // and dt (a+b) dd thv (v_corr), so that the lanes spend no FP64 multiply on them
+  extern __shared__ double ptab[];
+  {
+    const double aRb0 = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dti0 = sc->dti / aRb0, dtk0 = sc->dt * aRb0 * g.dd;
+    for (int i = threadIdx.x; i < g.nu; i += blockDim.x) ptab[i] = dti0 * g.thud[i];
+    for (int i = threadIdx.x; i < g.nv; i += blockDim.x) ptab[g.nu + i] = dtk0 * g.thv[i];
+    __syncthreads();
+  }
   if (vc < g.nvc) {
     int c, bd;
     vcol_of(g, vc, c, bd);
@@ -1237,6 +1247,9 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     const size_t ls = (size_t)nc * 2;
     const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
     constexpr int D = LH_PF_PRESS > 0 ? LH_PF_PRESS : 1;
+    const double dskx = dtirk * skx, dskz = dtirk * skz;
+#define HP_TH(q_) ptab[q_]
+#define HP_TV(q_) ptab[g.nu + (q_)]
     double y = 0.0;
     double vm = u2[(size_t)plo * ls + ci];
     {  // forward sweep; the inputs of a level are loaded D levels ahead
@@ -1247,7 +1260,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     const size_t e_ = (size_t)(qp_ + 1) * ls;                          \
     fa[s_] = u1[e_ + co]; fw[s_] = u3[e_ + co]; fv[s_] = u2[e_ + ci];  \
     f1[s_] = dg1[(size_t)qp_ * nc + c]; f2[s_] = dg2[(size_t)qp_ * nc + c]; \
-    ft[s_] = g.thud[qp_ + 1];                                          \
+    ft[s_] = HP_TH(qp_ + 1);                                           \
   }
 #pragma unroll
       for (int s_ = 0; s_ < D; ++s_)
@@ -1260,9 +1273,8 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
           const double ao = fa[s_], wo = fw[s_], v = fv[s_], A1 = f1[s_], a2p = f2[s_];
           const double th = ft[s_];
           if (qp + D <= phi) HP_FETCH(s_, qp + D)
-          const double dv = (skx * ao + skz * wo) + th * (v - vm);
+          double rhs = (dskx * ao + dskz * wo) + th * (v - vm);
           vm = v;
-          double rhs = dtirk * dv;
           if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
           y = (qp == plo) ? rhs * a2p : (rhs - A1 * y) * a2p;
           psi[(size_t)qp * ls + ci] = y;
@@ -1271,7 +1283,6 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
 #undef HP_FETCH
     }
     const double dtrk = dt * aRb;
-    const double dtrk2 = dtrk * dd;
     const double kxd = dtrk * kxv, kzd = dtrk * kzv;
     double xn = y;
     double vup = 0.0, aup_o = 0.0, wup_o = 0.0;
@@ -1284,7 +1295,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     bs[s_] = psi[(size_t)qp_ * ls + ci]; b3[s_] = dg3[(size_t)qp_ * nc + c]; \
     bp[s_] = p[(size_t)qp_ * ls + ci];                                      \
     bu[s_] = u1[e_]; bw[s_] = u3[e_]; bv[s_] = u2[e_];                      \
-    btv[s_] = g.thv[qp_ + 1]; btu[s_] = g.thud[qp_ + 2];                    \
+    btv[s_] = HP_TV(qp_ + 1); btu[s_] = g.thud[qp_ + 2];                    \
   }
 #pragma unroll
       for (int s_ = 0; s_ < D; ++s_)
@@ -1309,7 +1320,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
           u1[e + ci] = a;
           u3[e + ci] = w;
           if (q <= vhi - 1) {
-            v = v - dtrk2 * thv * (xn - x);
+            v = v - thv * (xn - x);
             u2[e + ci] = v;
           }
           // divergence of the corrected field at the level above (p level qp + 1)
@@ -1325,6 +1336,8 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
         }
       }
 #undef HB_FETCH
+#undef HP_TH
+#undef HP_TV
     }
     if (need_div) {
       const double th = g.thud[plo + 1];
