@@ -1243,7 +1243,6 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
     const double dtirk = sc->dti / aRb;
     const double dt = sc->dt;
-    const double dd = g.dd;
     const size_t ls = (size_t)nc * 2;
     const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
     constexpr int D = LH_PF_PRESS > 0 ? LH_PF_PRESS : 1;
