@@ -210,6 +210,39 @@ def triad_terms(s, tl) -> int:
     return n
 
 
+def error_by_steps(s, tl, ic, sc0, mb, counts):
+    """Relative L2 error of the mixed form against the FP64 form, per field, after each of
+    `counts` steps from the same initial state (untimed)."""
+    import numpy as np
+    from rnl_multiblock_nofft_gb300.native import GpuChannel
+    ref, out = {}, {}
+    for form in ("fp64", "mixed"):
+        g = GpuChannel(s, form, triads=tl)
+        if mb:
+            g.upload_bands(ic)
+        else:
+            g.upload_state(*ic)
+        g.set_scalars(**sc0)
+        done = 0
+        for n in sorted(counts):
+            g.step(n - done)
+            done = n
+            g.synchronize()
+            st = [a for b in (1, 2, 3) for a in g.download_bands()[b]] if mb else g.download_state()
+            if form == "fp64":
+                ref[n] = st
+                continue
+            e = {}
+            for i, f in enumerate(("u1", "u2", "u3", "p")):
+                a = np.concatenate([x.ravel() for x in ref[n][i::4]])
+                b = np.concatenate([x.ravel() for x in st[i::4]])
+                e[f] = float(np.linalg.norm(b - a) / np.linalg.norm(a))
+            del ref[n]
+            out[str(n)] = e
+        g.close()
+    return out
+
+
 def oracle_initial_state(o, s):
     from rnl_multiblock_nofft_gb300.workloads import initial_field, initial_field_bands
     if s.multiblock:
@@ -351,6 +384,9 @@ def main():
     ap.add_argument("--form", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--nonlin", default="products", choices=["products", "triads"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--error-steps", default="1,10,100",
+                    help="mixed vs FP64 relative error after these step counts from the same start "
+                         "(untimed, rank 0, both forms; 'none' to skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local, pg = dist_init()
@@ -515,6 +551,9 @@ def main():
         line["triads"] = {"complex_macs_per_substep": nt,
                           "k_triad_ms_per_step": tk[1] if tk else None,
                           "gflops": (8 * nt * 3 / (tk[1] * 1e-3) / 1e9) if tk else None}
+    counts = [int(x) for x in args.error_steps.split(",") if x.strip().isdigit() and int(x) > 0]
+    if rank == 0 and counts and "fp64" in res and "mixed" in res:
+        line["mixed_rel_err_by_steps"] = error_by_steps(s, tl, icb if mb else ic, sc0, mb, counts)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, triads=tl)
     if rank == 0:
