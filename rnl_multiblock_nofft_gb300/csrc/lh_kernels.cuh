@@ -191,25 +191,30 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
   const int npairs = min(PB, (G2 - l0) / 2);
   const size_t fstride = (size_t)G2 * N1h;
   const V *Af = A + (size_t)slot * 3 * fstride;
-  // gather Hermitian-completed lines of the 3 fields: line f*PB + pb
-  for (int idx = threadIdx.x; idx < 3 * PB * G1; idx += blockDim.x) {
-    const int line = idx / G1, m = idx - line * G1;
+  // gather Hermitian-completed lines of the 3 fields: line f*PB + pb. One work item per
+  // retained x-mode k writes element k (a + i b) and element G1 - k (conj(a) + i conj(b));
+  // elements N1h .. G1 - N1h (the dealiasing band) are zero. N1 = 2 (Ngal1 / 3) (lh_create
+  // checks it), so N1h = G1 / 3 + 1 is a compile-time constant here.
+  constexpr int NK = G1 / 3 + 1, NZ = G1 - 2 * NK + 1;
+  static_assert(NK <= H, "retained x-modes below the Nyquist index");
+  for (int idx = threadIdx.x; idx < 3 * PB * NK; idx += blockDim.x) {
+    const int line = idx / NK, k = idx - line * NK;
     const int f = line / PB, pb = line - f * PB;
-    V z = czero<V>();
+    V zd = czero<V>(), zc = czero<V>();
     if (pb < npairs) {
       const int l = l0 + 2 * pb;
-      int k = m;
-      bool conjpart = false;
-      if (m > H) { k = G1 - m; conjpart = true; }
-      if (k < N1h) {
-        V a = Af[f * fstride + (size_t)l * N1h + k];
-        V b = Af[f * fstride + (size_t)(l + 1) * N1h + k];
-        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
-        if (!conjpart) { z.x = a.x - b.y; z.y = a.y + b.x; }      // a + i b
-        else { z.x = a.x + b.y; z.y = -a.y + b.x; }              // conj(a) + i conj(b)
-      }
+      V a = Af[f * fstride + (size_t)l * NK + k];
+      V b = Af[f * fstride + (size_t)(l + 1) * NK + k];
+      if (k == 0) { a.y = 0; b.y = 0; }
+      zd.x = a.x - b.y; zd.y = a.y + b.x;   // a + i b
+      zc.x = a.x + b.y; zc.y = -a.y + b.x;  // conj(a) + i conj(b)
     }
-    b0[idx] = z;
+    b0[line * G1 + k] = zd;
+    if (k > 0) b0[line * G1 + G1 - k] = zc;
+  }
+  for (int idx = threadIdx.x; idx < 3 * PB * NZ; idx += blockDim.x) {
+    const int line = idx / NZ, m = idx - line * NZ;
+    b0[line * G1 + NK + m] = czero<V>();
   }
   __syncthreads();
   V *res = line_fft<true, N, 3 * PB, false>(b0, b1, twx);
@@ -282,7 +287,7 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
     const int pb = r2 % PB, p = r2 / PB;
     if (pb >= npairs) continue;
     const V *L = pres + (p * PB + pb) * G1;
-    const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
+    const V z = L[k], zc = cconj(L[k == 0 ? 0 : G1 - k]);
     V o;
     if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
     else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }  // -0.5 i (z - zc)
@@ -1882,20 +1887,25 @@ __global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__r
   const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
   const int npairs = min(PB, (G2 - l0) / 2);
   const V *Ap = A + (size_t)pl * G2 * N1h;
-  for (int idx = threadIdx.x; idx < PB * G1; idx += blockDim.x) {
-    const int pb = idx / G1, m = idx - pb * G1;
-    V z = czero<V>();
+  // one work item per retained x-mode (N1h = G1 / 3 + 1), the dealiasing band zeroed
+  constexpr int NK = G1 / 3 + 1, NZ = G1 - 2 * NK + 1;
+  static_assert(NK <= H, "retained x-modes below the Nyquist index");
+  for (int idx = threadIdx.x; idx < PB * NK; idx += blockDim.x) {
+    const int pb = idx / NK, k = idx - pb * NK;
+    V zd = czero<V>(), zc = czero<V>();
     if (pb < npairs) {
       const int l = l0 + 2 * pb;
-      int k = m; bool cj = false;
-      if (m > H) { k = G1 - m; cj = true; }
-      if (k < N1h) {
-        V a = Ap[(size_t)l * N1h + k], b = Ap[(size_t)(l + 1) * N1h + k];
-        if (k == 0 || k == H) { a.y = 0; b.y = 0; }
-        if (!cj) { z.x = a.x - b.y; z.y = a.y + b.x; } else { z.x = a.x + b.y; z.y = -a.y + b.x; }
-      }
+      V a = Ap[(size_t)l * NK + k], b = Ap[(size_t)(l + 1) * NK + k];
+      if (k == 0) { a.y = 0; b.y = 0; }
+      zd.x = a.x - b.y; zd.y = a.y + b.x;
+      zc.x = a.x + b.y; zc.y = -a.y + b.x;
     }
-    b0[idx] = z;
+    b0[pb * G1 + k] = zd;
+    if (k > 0) b0[pb * G1 + G1 - k] = zc;
+  }
+  for (int idx = threadIdx.x; idx < PB * NZ; idx += blockDim.x) {
+    const int pb = idx / NZ, m = idx - pb * NZ;
+    b0[pb * G1 + NK + m] = czero<V>();
   }
   __syncthreads();
   V *res = line_fft<true, N, PB, false>(b0, b1, twx);
@@ -1920,7 +1930,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__r
     const int half = rest & 1, pb = rest >> 1;
     if (pb >= npairs) continue;
     const V *L = fres + pb * G1;
-    const V z = L[k], zc = cconj(L[(G1 - k) % G1]);
+    const V z = L[k], zc = cconj(L[k == 0 ? 0 : G1 - k]);
     V o;
     if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
     else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }
