@@ -114,16 +114,16 @@ def measured_peaks():
 
 
 def traffic_table():
-    """Per-launch DRAM bytes of each kernel from the committed ncu summary
-    (profiles/ncu_traffic_C1.txt: `kernel form bytes_per_launch` lines)."""
+    """Per-launch DRAM bytes of a kernel on a workload from the committed ncu summary
+    (profiles/ncu_traffic_C1.txt: `workload kernel form bytes_per_launch` lines)."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic_C1.txt")
     out = {}
     if os.path.exists(p):
         for line in open(p):
             f = line.split()
-            if len(f) >= 3 and not line.startswith("#"):
+            if len(f) >= 4 and not line.startswith("#"):
                 try:
-                    out[(f[0], f[1])] = float(f[2])
+                    out[(f[0], f[1], f[2])] = float(f[3])
                 except ValueError:
                     pass
     return out
@@ -154,10 +154,13 @@ def column_levels(s, grid: int) -> int:
     return tot
 
 
-def algorithmic_bytes(s, kernel: str, form: str) -> float:
+def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0) -> float:
     """Compulsory HBM bytes of one substep's launches of a kernel: every input and
     output element once. Spectral fields are complex128; the transform intermediates
-    are complex128 in the FP64 form and complex64 in the mixed form."""
+    are complex128 in the FP64 form and complex64 in the mixed form. The triad kernel
+    reads one 4-byte term per complex multiply-add (`nterms` per substep), the three
+    velocities of every interior plane and writes five (u planes) / three (v planes)
+    products in the transform precision."""
     vs = 16 if form == "fp64" else 8
     z = 16
     tot = 0.0
@@ -182,6 +185,10 @@ def algorithmic_bytes(s, kernel: str, form: str) -> float:
         return column_levels(s, 1) * z * 7
     if kernel == "k_press":
         return column_levels(s, 2) * z * 8
+    if kernel == "k_triad":
+        ncol = (s.N1 // 2 + 1) * s.N2
+        nu, nv = s.nyu - 2, s.nyv - 2
+        return nterms * 4 + (nu + nv) * 3 * ncol * z + (5 * nu + 3 * nv) * ncol * vs
     return float("nan")
 
 
@@ -517,14 +524,16 @@ def main():
     dom = max(kern.items(), key=lambda kv: kv[1][1])
     dname, (dlaunch, dms) = dom
     avg_ms = dms / dlaunch
-    alg_step = 3 * algorithmic_bytes(s, dname, head)   # the profiled step has 3 substeps
+    alg_step = 3 * algorithmic_bytes(s, dname, head, triad_terms(s, tl) if tl is not None else 0)
     alg = alg_step / dlaunch
     peak, peak_kind = measured_peaks()
     achieved = alg_step / (dms * 1e-3) / 1e9
-    tt = traffic_table().get((dname, head))
+    if not math.isfinite(achieved):  # a kernel without an algorithmic byte count
+        achieved = alg = None
+    tt = traffic_table().get((args.workload, dname, head))
     step_total = sum(v[1] for v in kern.values())
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": tt, "kernel": dname,
+                "frac": achieved / peak if achieved is not None else None, "traffic": tt, "kernel": dname,
                 "kernel_share": dms / step_total, "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": alg, "peak_source": peak_kind}
     line = {"metric": METRIC, "value": R["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,

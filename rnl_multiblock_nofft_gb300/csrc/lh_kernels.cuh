@@ -278,21 +278,27 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
   // separate the two rows of each pair, keep kx = 0..N1h-1; kx fastest (coalesced rows).
   // N1 = 2 (Ngal1 / 3) (lh_create checks it), so N1h = G1 / 3 + 1 is a compile-time
   // constant here and the index split needs no runtime division.
+  // One work item per x-mode k writes both rows of the pair, which sit next to each other
+  // in B (one 16-byte store in the mixed form).
   constexpr int NH = G1 / 3 + 1;
-  for (int idx = threadIdx.x; idx < nprod * PB * 2 * NH; idx += blockDim.x) {
-    const int half = idx & 1;
-    const int rest = idx >> 1;
-    const int k = rest % NH;
-    const int r2 = rest / NH;
+  for (int idx = threadIdx.x; idx < nprod * PB * NH; idx += blockDim.x) {
+    const int k = idx % NH;
+    const int r2 = idx / NH;
     const int pb = r2 % PB, p = r2 / PB;
     if (pb >= npairs) continue;
     const V *L = pres + (p * PB + pb) * G1;
     const V z = L[k], zc = cconj(L[k == 0 ? 0 : G1 - k]);
-    V o;
-    if (!half) { o.x = (T)0.5 * (z.x + zc.x) * s1; o.y = (T)0.5 * (z.y + zc.y) * s1; }
-    else { o.x = (T)0.5 * (z.y - zc.y) * s1; o.y = (T)-0.5 * (z.x - zc.x) * s1; }  // -0.5 i (z - zc)
-    if (k == 0) o.y = 0;
-    B[(((size_t)(pbase + p) * (G2 / 2) + (l0 >> 1) + pb) * N1h + k) * 2 + half] = o;
+    V o0, o1;
+    o0.x = (T)0.5 * (z.x + zc.x) * s1; o0.y = (T)0.5 * (z.y + zc.y) * s1;
+    o1.x = (T)0.5 * (z.y - zc.y) * s1; o1.y = (T)-0.5 * (z.x - zc.x) * s1;  // -0.5 i (z - zc)
+    if (k == 0) { o0.y = 0; o1.y = 0; }
+    V *dst = B + (((size_t)(pbase + p) * (G2 / 2) + (l0 >> 1) + pb) * N1h + k) * 2;
+    if constexpr (sizeof(T) == 4) {
+      *reinterpret_cast<float4 *>(dst) = make_float4(o0.x, o0.y, o1.x, o1.y);
+    } else {
+      dst[0] = o0;
+      dst[1] = o1;
+    }
   }
 }
 
