@@ -153,6 +153,12 @@ int lh_download_state_async(lh_handle *h, double *u1, double *u2, double *u3, do
 int lh_upload_band(lh_handle *h, int band, const double *u1, const double *u2,
                    const double *u3, const double *p);
 int lh_download_band(lh_handle *h, int band, double *u1, double *u2, double *u3, double *p);
+/* The same, queued without blocking (as lh_upload_state_async / lh_download_state_async):
+ * each band has its own staging region, so the copies of one band overlap the scatter of
+ * another and the steps queued around them. */
+int lh_upload_band_async(lh_handle *h, int band, const double *u1, const double *u2,
+                         const double *u3, const double *p);
+int lh_download_band_async(lh_handle *h, int band, double *u1, double *u2, double *u3, double *p);
 
 /* Scalars: lh_set_scalars also (re)computes Qx, and QxT when flag_ctpress == 0,
  * as getini does (start.f90:2170-2176), and the initial divergence. */

@@ -45,7 +45,8 @@ struct lh_handle {
   // each direction, copy streams, and the events that order them against the main stream
   double2 *stage_in, *stage_out;
   cudaStream_t st_in, st_out;
-  cudaEvent_t ev_in_copied, ev_in_used, ev_out_ready, ev_out_copied;
+  // per staging slot: 0 the whole state, 1..3 the bands (each band its own region)
+  cudaEvent_t ev_in_copied[4], ev_in_used[4], ev_out_ready[4], ev_out_copied[4];
   // immersed boundaries
   int ib, nib, ncap;
   int *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
@@ -419,7 +420,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->d_slip = h->d_slip_inst = nullptr;
   h->stage_in = h->stage_out = nullptr;
   h->st_in = h->st_out = nullptr;
-  h->ev_in_copied = h->ev_in_used = h->ev_out_ready = h->ev_out_copied = nullptr;
+  for (int i = 0; i < 4; ++i) h->ev_in_copied[i] = h->ev_in_used[i] = h->ev_out_ready[i] = h->ev_out_copied[i] = nullptr;
   h->d_ibslot_u = h->d_ibslot_v = h->d_iblev = h->d_lev2cap_u = h->d_lev2cap_v = nullptr;
   h->cap = nullptr;
   h->d_ibrec = nullptr;
@@ -640,8 +641,9 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->ysv, h->a3v, h->st_pl, h->st_cd, h->d_sp, h->d_slip, h->d_slip_inst, h->stage_in, h->stage_out};
   for (void *b : bufs)
     if (b) cudaFree(b);
-  for (cudaEvent_t e : {h->ev_in_copied, h->ev_in_used, h->ev_out_ready, h->ev_out_copied})
-    if (e) cudaEventDestroy(e);
+  for (int i = 0; i < 4; ++i)
+    for (cudaEvent_t e : {h->ev_in_copied[i], h->ev_in_used[i], h->ev_out_ready[i], h->ev_out_copied[i]})
+      if (e) cudaEventDestroy(e);
   if (h->st_in) cudaStreamDestroy(h->st_in);
   if (h->st_out) cudaStreamDestroy(h->st_out);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -720,10 +722,23 @@ static int async_io_init(lh_handle *h) {
   CK(cudaMalloc(&h->stage_out, sizeof(double2) * n));
   CK(cudaStreamCreateWithFlags(&h->st_in, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking));
-  for (cudaEvent_t *e : {&h->ev_in_copied, &h->ev_in_used, &h->ev_out_ready, &h->ev_out_copied})
-    CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-  CK(cudaEventRecord(h->ev_in_used, h->st));
-  CK(cudaEventRecord(h->ev_out_copied, h->st));
+  for (int i = 0; i < 4; ++i) {
+    for (cudaEvent_t *e : {&h->ev_in_copied[i], &h->ev_in_used[i], &h->ev_out_ready[i], &h->ev_out_copied[i]})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    CK(cudaEventRecord(h->ev_in_used[i], h->st));
+    CK(cudaEventRecord(h->ev_out_copied[i], h->st));
+  }
+  return LH_OK;
+}
+// a slot's staging may be refilled once its previous contents are consumed; the whole-state
+// slot overlaps every band slot
+static int wait_slot(lh_handle *h, cudaStream_t st, cudaEvent_t *ev, int slot) {
+  if (slot == 0) {
+    for (int i = 0; i < 4; ++i) CK(cudaStreamWaitEvent(st, ev[i], 0));
+  } else {
+    CK(cudaStreamWaitEvent(st, ev[slot], 0));
+    CK(cudaStreamWaitEvent(st, ev[0], 0));
+  }
   return LH_OK;
 }
 // field f of the state: device array, levels, offset in the staging
@@ -743,15 +758,15 @@ extern "C" int lh_upload_state_async(lh_handle *h, const double *u1, const doubl
   if (rc) return rc;
   const double *H[4] = {u1, u2, u3, p};
   const int nc = h->g.ncol;
-  CK(cudaStreamWaitEvent(h->st_in, h->ev_in_used, 0));
+  if ((rc = wait_slot(h, h->st_in, h->ev_in_used, 0))) return rc;
   for (int f = 0; f < 4; ++f) {
     if (!H[f]) continue;
     double2 *dev; int nl; size_t off;
     state_field(h, f, dev, nl, off);
     CK(cudaMemcpyAsync(h->stage_in + off, H[f], sizeof(double2) * (size_t)nc * nl, cudaMemcpyHostToDevice, h->st_in));
   }
-  CK(cudaEventRecord(h->ev_in_copied, h->st_in));
-  CK(cudaStreamWaitEvent(h->st, h->ev_in_copied, 0));
+  CK(cudaEventRecord(h->ev_in_copied[0], h->st_in));
+  CK(cudaStreamWaitEvent(h->st, h->ev_in_copied[0], 0));
   for (int f = 0; f < 4; ++f) {
     if (!H[f]) continue;
     double2 *dev; int nl; size_t off;
@@ -759,7 +774,7 @@ extern "C" int lh_upload_state_async(lh_handle *h, const double *u1, const doubl
     dim3 grid((nl + 31) / 32, (nc + 31) / 32), blk(32, 8);
     KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(h->stage_in + off, dev, nc, nl));
   }
-  CK(cudaEventRecord(h->ev_in_used, h->st));
+  CK(cudaEventRecord(h->ev_in_used[0], h->st));
   return LH_OK;
 }
 
@@ -770,7 +785,7 @@ extern "C" int lh_download_state_async(lh_handle *h, double *u1, double *u2, dou
   if (rc) return rc;
   double *H[4] = {u1, u2, u3, p};
   const int nc = h->g.ncol;
-  CK(cudaStreamWaitEvent(h->st, h->ev_out_copied, 0));
+  if ((rc = wait_slot(h, h->st, h->ev_out_copied, 0))) return rc;
   for (int f = 0; f < 4; ++f) {
     if (!H[f]) continue;
     double2 *dev; int nl; size_t off;
@@ -778,15 +793,15 @@ extern "C" int lh_download_state_async(lh_handle *h, double *u1, double *u2, dou
     dim3 grid((nc + 31) / 32, (nl + 31) / 32), blk(32, 8);
     KL("k_transpose", k_transpose<<<grid, blk, 0, h->st>>>(dev, h->stage_out + off, nl, nc));
   }
-  CK(cudaEventRecord(h->ev_out_ready, h->st));
-  CK(cudaStreamWaitEvent(h->st_out, h->ev_out_ready, 0));
+  CK(cudaEventRecord(h->ev_out_ready[0], h->st));
+  CK(cudaStreamWaitEvent(h->st_out, h->ev_out_ready[0], 0));
   for (int f = 0; f < 4; ++f) {
     if (!H[f]) continue;
     double2 *dev; int nl; size_t off;
     state_field(h, f, dev, nl, off);
     CK(cudaMemcpyAsync(H[f], h->stage_out + off, sizeof(double2) * (size_t)nc * nl, cudaMemcpyDeviceToHost, h->st_out));
   }
-  CK(cudaEventRecord(h->ev_out_copied, h->st_out));
+  CK(cudaEventRecord(h->ev_out_copied[0], h->st_out));
   return LH_OK;
 }
 
@@ -837,6 +852,92 @@ extern "C" int lh_download_band(lh_handle *h, int band, double *u1, double *u2, 
     int rc = band_field(h, band, f, F[f], nullptr, H[f]);
     if (rc) return rc;
   }
+  return LH_OK;
+}
+
+// ---- asynchronous band I/O: as the state calls above, one staging region per band ----
+// band b's field f: its columns, level range and size; regions laid out band after band
+static void band_geom(lh_handle *h, int band, int field, const int *&cols, int &ncb, int &lo, int &nl) {
+  const int b = band - 1;
+  ncb = (band == 2) ? h->nlong : h->nshort;
+  cols = h->d_bcols + ((band == 2) ? 0 : h->nlong);
+  lo = h->g.bq[b][field == 3 ? 4 : (field == 1 ? 2 : 0)];
+  const int hi = h->g.bq[b][field == 3 ? 5 : (field == 1 ? 3 : 1)];
+  nl = hi - lo + 1;
+}
+static size_t band_offset(lh_handle *h, int band, int field) {
+  size_t off = 0;
+  for (int b = 1; b <= 3; ++b)
+    for (int f = 0; f < 4; ++f) {
+      if (b == band && f == field) return off;
+      const int *cols; int ncb, lo, nl;
+      band_geom(h, b, f, cols, ncb, lo, nl);
+      off += (size_t)ncb * nl;
+    }
+  return off;
+}
+
+extern "C" int lh_upload_band_async(lh_handle *h, int band, const double *u1, const double *u2, const double *u3,
+                                    const double *p) {
+  if (!h) return LH_EINVAL;
+  if (band < 1 || band > 3) return fail(h, LH_EINVAL, "band must be 1, 2 or 3");
+  int rc = async_io_init(h);
+  if (rc) return rc;
+  if (band_offset(h, 4, 0) > (size_t)(2 * h->g.nu + h->g.nv + h->g.np) * h->g.ncol)
+    return fail(h, LH_EINVAL, "band layouts larger than the staging buffer");
+  double2 *F[4] = {h->u1, h->u2, h->u3, h->p};
+  const double *H[4] = {u1, u2, u3, p};
+  if ((rc = wait_slot(h, h->st_in, h->ev_in_used, band))) return rc;
+  for (int f = 0; f < 4; ++f) {
+    const int *cols; int ncb, lo, nl;
+    band_geom(h, band, f, cols, ncb, lo, nl);
+    if (!H[f] || (size_t)ncb * nl == 0) continue;
+    CK(cudaMemcpyAsync(h->stage_in + band_offset(h, band, f), H[f], sizeof(double2) * (size_t)ncb * nl,
+                       cudaMemcpyHostToDevice, h->st_in));
+  }
+  CK(cudaEventRecord(h->ev_in_copied[band], h->st_in));
+  CK(cudaStreamWaitEvent(h->st, h->ev_in_copied[band], 0));
+  for (int f = 0; f < 4; ++f) {
+    const int *cols; int ncb, lo, nl;
+    band_geom(h, band, f, cols, ncb, lo, nl);
+    const size_t n = (size_t)ncb * nl;
+    if (!H[f] || n == 0) continue;
+    const int nb = (int)((n + NTHR_H - 1) / NTHR_H);
+    KL("k_band_io", k_band_io<<<nb, NTHR_H, 0, h->st>>>(F[f], h->stage_in + band_offset(h, band, f), cols, ncb, nl, lo,
+                                                         h->g.ncol, 1));
+  }
+  CK(cudaEventRecord(h->ev_in_used[band], h->st));
+  return LH_OK;
+}
+
+extern "C" int lh_download_band_async(lh_handle *h, int band, double *u1, double *u2, double *u3, double *p) {
+  if (!h) return LH_EINVAL;
+  if (band < 1 || band > 3) return fail(h, LH_EINVAL, "band must be 1, 2 or 3");
+  int rc = async_io_init(h);
+  if (rc) return rc;
+  double2 *F[4] = {h->u1, h->u2, h->u3, h->p};
+  double *H[4] = {u1, u2, u3, p};
+  if ((rc = wait_slot(h, h->st, h->ev_out_copied, band))) return rc;
+  for (int f = 0; f < 4; ++f) {
+    const int *cols; int ncb, lo, nl;
+    band_geom(h, band, f, cols, ncb, lo, nl);
+    const size_t n = (size_t)ncb * nl;
+    if (!H[f] || n == 0) continue;
+    const int nb = (int)((n + NTHR_H - 1) / NTHR_H);
+    KL("k_band_io", k_band_io<<<nb, NTHR_H, 0, h->st>>>(F[f], h->stage_out + band_offset(h, band, f), cols, ncb, nl, lo,
+                                                         h->g.ncol, 0));
+  }
+  CK(cudaEventRecord(h->ev_out_ready[band], h->st));
+  CK(cudaStreamWaitEvent(h->st_out, h->ev_out_ready[band], 0));
+  for (int f = 0; f < 4; ++f) {
+    const int *cols; int ncb, lo, nl;
+    band_geom(h, band, f, cols, ncb, lo, nl);
+    const size_t n = (size_t)ncb * nl;
+    if (!H[f] || n == 0) continue;
+    CK(cudaMemcpyAsync(H[f], h->stage_out + band_offset(h, band, f), sizeof(double2) * n, cudaMemcpyDeviceToHost,
+                       h->st_out));
+  }
+  CK(cudaEventRecord(h->ev_out_copied[band], h->st_out));
   return LH_OK;
 }
 

@@ -17,7 +17,7 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
 _lib = None
 
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
-           "lh_upload_state_async", "lh_download_state_async",
+           "lh_upload_state_async", "lh_download_state_async", "lh_upload_band_async", "lh_download_band_async",
            "lh_upload_band", "lh_download_band", "lh_stats_accumulate", "lh_stats_reset", "lh_stats_dims",
            "lh_stats_get", "lh_spectra_dims", "lh_spectra_get", "lh_slip_get", "lh_slip_planes",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
@@ -52,6 +52,8 @@ def load(path: str = _LIB_PATH):
     L.lh_upload_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_download_state.argtypes = [vp, dp, dp, dp, dp]
     L.lh_upload_state_async.argtypes = [vp, dp, dp, dp, dp]
+    L.lh_upload_band_async.argtypes = [vp, C.c_int, dp, dp, dp, dp]
+    L.lh_download_band_async.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_download_state_async.argtypes = [vp, dp, dp, dp, dp]
     L.lh_upload_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_stats_accumulate.argtypes = [vp]
@@ -166,6 +168,25 @@ class GpuChannel:
                 raise ValueError("download buffers must be C-contiguous complex128 of the state shapes")
         self._pending.extend(out)
         self._check(self.L.lh_download_state_async(self.h, *[_dptr(a) for a in out]))
+        return out
+
+    def upload_bands_async(self, bands: dict):
+        """Queued per-band upload (lh_upload_band_async); arrays kept alive until synchronize()."""
+        for b, arrs in bands.items():
+            for a, sh in zip(arrs, self.s.band_shapes(b)):
+                if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                    raise ValueError(f"band {b}: C-contiguous complex128 of shape {sh} expected")
+            self._pending.extend(arrs)
+            self._check(self.L.lh_upload_band_async(self.h, b, *[_dptr(a) for a in arrs]))
+
+    def download_bands_async(self, out: dict):
+        """Queued per-band download into `out` ({band: (u1, u2, u3, p)}); valid after synchronize()."""
+        for b, arrs in out.items():
+            for a, sh in zip(arrs, self.s.band_shapes(b)):
+                if a.shape != sh or a.dtype != np.complex128 or not a.flags.c_contiguous:
+                    raise ValueError(f"band {b}: C-contiguous complex128 of shape {sh} expected")
+            self._pending.extend(arrs)
+            self._check(self.L.lh_download_band_async(self.h, b, *[_dptr(a) for a in arrs]))
         return out
 
     def upload_bands(self, bands: dict):
