@@ -13,10 +13,14 @@
 //   k_helm_uw   : RHS0_u1/u3 + der_yu_h + du += -gRK N + solveU_W, one thread per column
 //   k_helm_v    : RHS0_u2 + der_yv_h + du += -gRK N + solveV
 //   k_meanflow  : flowrate_corr on mode (0,0) (constant flow rate)
-//   k_press     : divergence + solveP (LUsolP with the stored factors, k_build_dg) + v_corr
+//   k_press2    : divergence + solveP (LUsolP with the stored factors, k_build_dg) + v_corr
 //                 + divergence of the corrected field in the third substep (max |div| -> err)
+//   k_ib_du(_mx), k_spec_zinv, k_ib_xforce, k_zfwd_spec : immersed-boundary forcing of du
+//                 (imm_bounds_u/v, FOU3D.f90:806-998) when the geometry has posts
 //   Mixed form (LH_PREC_MIXED): FP32 transforms, and k_helm_u_mx2 / k_helm_v_mx2 solve
 //   the Helmholtz systems for the increment in FP32 on top of the FP64 state.
+// On request: k_xstats, k_wx_stats, k_spectra, k_slip (statistics), k_band_io, k_transpose
+// (state I/O).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
