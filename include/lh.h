@@ -5,7 +5,7 @@
  * Fortran subroutines `program littleharsh` calls once per RK3 substep
  * (littleharsh.f90:174-217), with all shared data in `module declaration`
  * (declaration.f90). This header replaces that boundary with plain C entry points
- * that a Fortran host binds through ISO_C_BINDING and that
+ * that a Fortran host binds through an ISO_C_BINDING interface module and that
  * the Python package binds through ctypes.
  *
  * Conventions
