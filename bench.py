@@ -61,15 +61,23 @@ def barrier(pg):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """SM clock and clock-event (throttle) reasons sampled during the timed region: through
+    NVML (libnvidia-ml, read-only queries) every 10 ms from a thread when the library loads,
+    else nvidia-smi every 200 ms."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # clock-event reason bits of NVML
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+            "hw_power_brake_slowdown": 0x80}
 
     def __init__(self, gpu_index: int):
+        self.p = self.thread = None
+        self.samples, self.reason_bits, self.max_mhz = [], 0, None
+        if self._nvml_start(gpu_index):
+            return
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.p = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
@@ -77,7 +85,54 @@ class ClockSampler:
         except (OSError, FileNotFoundError):
             self.p = None
 
+    def _nvml_start(self, gpu_index: int) -> bool:
+        import ctypes
+        import threading
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return False
+            h = ctypes.c_void_p()
+            ok = False
+            try:  # the device this process uses, by PCI bus id (CUDA and NVML numbering may differ)
+                import torch
+                pr = torch.cuda.get_device_properties(gpu_index)
+                bus = b"%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+                ok = nv.nvmlDeviceGetHandleByPciBusId_v2(ctypes.c_char_p(bus), ctypes.byref(h)) == 0
+            except Exception:
+                ok = False
+            if not ok and nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu_index), ctypes.byref(h)) != 0:
+                return False
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        except (OSError, AttributeError):
+            return False
+        self.stop_flag = threading.Event()
+
+        def run():
+            clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+            while not self.stop_flag.is_set():
+                if nv.nvmlDeviceGetClockInfo(h, ctypes.c_int(1), ctypes.byref(clk)) == 0:
+                    self.samples.append(float(clk.value))
+                if reasons_fn(h, ctypes.byref(rs)) == 0:
+                    self.reason_bits |= rs.value
+                self.stop_flag.wait(0.01)
+
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+        return True
+
     def stop(self) -> dict:
+        if self.thread is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+            sm = sorted(self.samples)
+            reasons = sorted(n for n, b in self.BITS.items() if self.reason_bits & b)
+            return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                    "samples": len(sm), "source": "nvml"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.p.terminate()
@@ -101,7 +156,8 @@ class ClockSampler:
                 continue
         sm.sort()
         med = sm[len(sm) // 2] if sm else None
-        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi"}
 
 
 def measured_peaks():
