@@ -217,7 +217,7 @@ __host__ __device__ __forceinline__ void dftR(V *v) {
 // butterfly 8 elements apart, and without the swizzle the lanes of a warp would all hit the
 // same banks (16-way for 8-byte elements). A stage's first input and last output are not
 // swizzled, so the buffers the kernels fill and read keep their plain layout.
-__device__ __forceinline__ int fft_swz(int i) { return i ^ ((i >> 4) & 7); }
+__host__ __device__ __forceinline__ int fft_swz(int i) { return i ^ ((i >> 4) & 7); }
 
 template <int R, bool INV, int N, int Ns, int NL, bool IL, bool SWI, bool SWO, typename V>
 __device__ __forceinline__ void fft_stage_c(const V *__restrict__ src, V *__restrict__ dst,

@@ -1,0 +1,32 @@
+"""The shared-memory FFT's plan on the CPU (tests/fft_host_check.cu): every compiled length,
+both layouts, both directions, FP64 and FP32, against a direct DFT in long double."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LENGTHS = (24, 48, 72, 96, 144, 192, 288, 384, 576, 768, 1152)
+
+
+def nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if c and os.path.exists(c):
+            return c
+    return None
+
+
+def test_fft_plan_against_direct_dft(tmp_path):
+    cc = nvcc()
+    if cc is None:
+        pytest.skip("nvcc not found")
+    exe = str(tmp_path / "fft_host_check")
+    subprocess.run([cc, "-O2", "-std=c++17", "-x", "cu", os.path.join(HERE, "fft_host_check.cu"), "-o", exe],
+                   check=True, capture_output=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=600).stdout
+    rows = {int(r.split()[0]): [float(x) for x in r.split()[1:]] for r in out.strip().splitlines()}
+    assert sorted(rows) == list(LENGTHS)
+    for n, e in rows.items():
+        assert max(e[:4]) < 1e-14, (n, e[:4])   # FP64: IL0 fwd/inv, IL1 fwd/inv
+        assert max(e[4:]) < 2e-6, (n, e[4:])    # FP32
