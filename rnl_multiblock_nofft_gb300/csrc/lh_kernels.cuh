@@ -34,6 +34,10 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double 
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// max that keeps a NaN (fmax drops it): the CFL and divergence maxima must carry a
+// non-finite state to dt and err, where the blow-up guard sees it
+template <typename T>
+__device__ __forceinline__ T nmax(T a, T b) { return (b > a || b != b) ? b : a; }
 template <typename T>
 __device__ __forceinline__ T warp_max(T v) {
   for (int o = 16; o > 0; o >>= 1) {
@@ -255,8 +259,8 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
       oth[(2 * PB + pb) * G1 + m] = p2;
       oth[(3 * PB + pb) * G1 + m] = p3;
       if (valid && doCFL) {
-        m1 = fmax(m1, fmax(fabs(u.x), fabs(u.y)));
-        m3 = fmax(m3, fmax(fabs(w.x), fabs(w.y)));
+        m1 = nmax(m1, nmax(fabs(u.x), fabs(u.y)));
+        m3 = nmax(m3, nmax(fabs(w.x), fabs(w.y)));
       }
     } else {
       V p0, p1;
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
       p1.x = w.x * v.x; p1.y = w.y * v.y;
       oth[(0 * PB + pb) * G1 + m] = p0;
       oth[(1 * PB + pb) * G1 + m] = p1;
-      if (valid && doCFL) m2 = fmax(m2, fmax(fabs(v.x), fabs(v.y)) * thv);
+      if (valid && doCFL) m2 = nmax(m2, nmax(fabs(v.x), fabs(v.y)) * thv);
     }
   }
   if (doCFL) {
@@ -1343,7 +1347,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
             const double th = thu1;
             const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - v);
             const double d2 = dvp * dvp;
-            dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+            dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
           }
           aup_o = ao; wup_o = wo; vup = v;
           xn = x;
@@ -1358,7 +1362,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
       const double vb = u2[(size_t)plo * ls + ci];
       const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
       const double d2 = dvp * dvp;
-      dmax = fmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+      dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
     }
     if (bd <= 1) {
       u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
@@ -1397,7 +1401,7 @@ __global__ void __launch_bounds__(NTHR) k_divmax(const double2 *__restrict__ u1,
       double2 dv;
       dv.x = (-kxv * a.y + -kzv * w.y) + th * (v.x - vm.x);
       dv.y = (kxv * a.x + kzv * w.x) + th * (v.y - vm.y);
-      dmax = fmax(dmax, dv.x * dv.x + dv.y * dv.y);
+      dmax = nmax(dmax, dv.x * dv.x + dv.y * dv.y);
     }
   }
   dmax = warp_max(dmax);
