@@ -716,17 +716,19 @@ extern "C" int lh_download_state(lh_handle *h, double *u1, double *u2, double *u
 // transposes). A download's transposes follow the queued steps on the main stream and its
 // device->host copy runs on a second copy stream, overlapping the steps queued after it.
 static int async_io_init(lh_handle *h) {
-  if (h->stage_in) return LH_OK;
+  if (h->ev_out_copied[3]) return LH_OK;  // the last resource created below
   const size_t n = (size_t)(2 * h->g.nu + h->g.nv + h->g.np) * h->g.ncol;
-  CK(cudaMalloc(&h->stage_in, sizeof(double2) * n));
-  CK(cudaMalloc(&h->stage_out, sizeof(double2) * n));
-  CK(cudaStreamCreateWithFlags(&h->st_in, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking));
+  // each resource on its own, so that a failure part-way is completed by the next call
+  if (!h->stage_in) CK(cudaMalloc(&h->stage_in, sizeof(double2) * n));
+  if (!h->stage_out) CK(cudaMalloc(&h->stage_out, sizeof(double2) * n));
+  if (!h->st_in) CK(cudaStreamCreateWithFlags(&h->st_in, cudaStreamNonBlocking));
+  if (!h->st_out) CK(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking));
   for (int i = 0; i < 4; ++i) {
-    for (cudaEvent_t *e : {&h->ev_in_copied[i], &h->ev_in_used[i], &h->ev_out_ready[i], &h->ev_out_copied[i]})
+    for (cudaEvent_t *e : {&h->ev_in_copied[i], &h->ev_in_used[i], &h->ev_out_ready[i], &h->ev_out_copied[i]}) {
+      if (*e) continue;
       CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    CK(cudaEventRecord(h->ev_in_used[i], h->st));
-    CK(cudaEventRecord(h->ev_out_copied[i], h->st));
+      CK(cudaEventRecord(*e, h->st));  // completed once the work queued so far is done
+    }
   }
   return LH_OK;
 }
@@ -1329,13 +1331,18 @@ static size_t spectra_size(const lh_handle *h) {
 }
 // the accumulators of spectra and slip statistics, zeroed, on first use
 static int spectral_stats_buffers(lh_handle *h) {
-  if (h->d_sp) return LH_OK;
+  if (h->d_sp && h->d_slip && h->d_slip_inst) return LH_OK;
   const size_t nsp = spectra_size(h), nsl = 8 * (size_t)h->g.ncolF;
-  CK(cudaMalloc(&h->d_sp, sizeof(double) * nsp));
-  CK(cudaMalloc(&h->d_slip, sizeof(double2) * nsl));
-  CK(cudaMalloc(&h->d_slip_inst, sizeof(double2) * nsl));
-  CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * nsp, h->st));
-  CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * nsl, h->st));
+  // each buffer on its own, so that a failed allocation is retried by the next call
+  if (!h->d_sp) {
+    CK(cudaMalloc(&h->d_sp, sizeof(double) * nsp));
+    CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * nsp, h->st));
+  }
+  if (!h->d_slip) {
+    CK(cudaMalloc(&h->d_slip, sizeof(double2) * nsl));
+    CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * nsl, h->st));
+  }
+  if (!h->d_slip_inst) CK(cudaMalloc(&h->d_slip_inst, sizeof(double2) * nsl));
   return LH_OK;
 }
 // the wall faces jlim(1, vgrid, 2), jlim(2, vgrid, 2) as v array indices
