@@ -165,6 +165,21 @@ int lh_download_band_async(lh_handle *h, int band, double *u1, double *u2, doubl
 int lh_set_scalars(lh_handle *h, const lh_scalars *s);
 int lh_get_scalars(lh_handle *h, lh_scalars *s);
 
+/* One record of the history file (hist_*.dat), the scalar part of record_out
+ * (FOU3D.f90:3040-3070): with flag_ctpress == 0 the file record is
+ * flag_ctpress, iter, t, dtv, dtc, dt, err, Qx, QxT, mpgx, dgx, Umax, Uslip, and with
+ * flag_ctpress == 1 QxT and dgx are left out. */
+typedef struct lh_history {
+  int32_t flag_ctpress, iter;
+  double t, dtv, dtc, dt, err, Qx, QxT, mpgx, dgx, Umax, Uslip;
+} lh_history;
+/* Forms the record of the current state as record_out does at an output step: Qx by
+ * flowrateIm (which also refreshes the scalar Qx), Umax by maxvel (littleharsh.f90:511-527)
+ * and the slip velocity of mode (0,0); dgx is the last flowrate_corr correction. Called
+ * between steps, after lh_step n it is the record the reference writes at iteration n.
+ * Blocking. */
+int lh_history_record(lh_handle *h, lh_history *out);
+
 /* One RK3 substep kRK = 1..3: RHS0_u1/u2/u3, nonlinear, solveU_W, solveV,
  * [meanflow_ctU], solveP, v_corr (littleharsh.f90:176-215). Asynchronous on the
  * handle's stream; dt and err stay on the device. */
@@ -282,7 +297,9 @@ void *lh_batch_stream(lh_batch *b);
  * LH_EINVAL and *err (if not NULL) points to a static message. The first call on a device
  * does a one-time set-up for that device (looks up the array's device address and
  * sets the kernels' shared-memory limit); make that first call before any stream
- * capture. Every call shares the one array and overwrites what it needs, so calls
+ * capture. Host threads that make their first calls at the same time are serialised
+ * during the set-up, and it runs again after a cudaDeviceReset (which clears it).
+ * Every call shares the one array and overwrites what it needs, so calls
  * that overlap on the GPU (other streams, other host threads) race: serialise them. */
 #define LH_NOALLOC_SCRATCH_BYTES (32u << 20)
 int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, const void *spec, void *phys,

@@ -54,6 +54,16 @@ class LhScalars(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class LhHistory(C.Structure):
+    _fields_ = [("flag_ctpress", C.c_int32), ("iter", C.c_int32),
+                ("t", C.c_double), ("dtv", C.c_double), ("dtc", C.c_double), ("dt", C.c_double),
+                ("err", C.c_double), ("Qx", C.c_double), ("QxT", C.c_double), ("mpgx", C.c_double),
+                ("dgx", C.c_double), ("Umax", C.c_double), ("Uslip", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 def _ptr(a: np.ndarray, typ):
     return a.ctypes.data_as(typ)
 

@@ -1,6 +1,7 @@
 """Build recipe of the native library (nvcc, sm_103a, one translation unit)."""
 from __future__ import annotations
 
+import glob
 import os
 import shutil
 import subprocess
@@ -8,7 +9,6 @@ import subprocess
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 LIB = os.path.join(PKG, "liblh.so")
-SOURCES = ["lh_capi.cu", "lh_kernels.cuh", "lh_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -23,7 +23,9 @@ def stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.join(PKG, "..", "include", "lh.h")]
+    # every source of the translation unit: the .cu and each header it includes
+    deps = glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        [os.path.join(PKG, "..", "include", "lh.h")]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 

@@ -4,6 +4,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -378,6 +380,8 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   if (h->prec == LH_PREC_MIXED) { ZA(h->ysf, 2 * sizeof(float4) * nu * nc); ZA(h->ysv, 2 * sizeof(float2) * nv * nc); }
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
+  // a3s: the FP64 solves' upper factors; in the mixed form the previous nonlinear term of mode
+  // (0,0) in FP64 (k_helm00_pcr: 6 x nu doubles; nc >= 8 always)
   ZA(h->psi, cz * g.np * nc); ZA(h->a3s, sizeof(double) * nu * nc); ZA(h->a3v, sizeof(double) * nv * nc);
   ZA(h->mfw, sizeof(double) * 6 * (size_t)(g.nn + 3));
   h->Abytes = h->Bbytes = 0;
@@ -575,6 +579,10 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
+  if (cudaFuncSetAttribute((const void *)k_helm00_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(8 * sizeof(double) * (size_t)(std::max(nu, nv) + 1))) != cudaSuccess) {
+    rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_helm00_pcr)"); lh_destroy(h); return rc;
+  }
   if (cudaFuncSetAttribute((const void *)k_meanflow_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) !=
       cudaSuccess) {
     rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_meanflow_pcr)"); lh_destroy(h); return rc;
@@ -969,6 +977,20 @@ extern "C" int lh_get_scalars(lh_handle *h, lh_scalars *s) {
   return LH_OK;
 }
 
+extern "C" int lh_history_record(lh_handle *h, lh_history *out) {
+  if (!h || !out) return LH_EINVAL;
+  KL("k_history", k_history<<<1, 32, 0, h->st>>>(h->u1, h->g, h->sc));
+  DevScalars d;
+  CK(cudaMemcpyAsync(&d, h->sc, sizeof(d), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  out->flag_ctpress = h->g.flag_ctpress;
+  out->iter = (int32_t)d.iter;
+  out->t = d.t; out->dtv = h->g.dtv; out->dtc = d.dtc; out->dt = d.dt; out->err = d.err;
+  out->Qx = d.Qx; out->QxT = d.QxT; out->mpgx = d.mpgx; out->dgx = d.dgx;
+  out->Umax = d.Umax; out->Uslip = d.Uslip;
+  return LH_OK;
+}
+
 // ---------------------------------------------------------------------------
 // one substep
 // ---------------------------------------------------------------------------
@@ -1165,6 +1187,14 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     LH_DISPATCH(g.G2, rc = launch_zfwd_spec<T, N>(h, h->B, h->duib, 3 * h->nib, h->twz));
     if (rc) return rc;
   }
+  if (h->prec == LH_PREC_MIXED) {  // mode (0,0) in FP64, before the solves of the other columns
+    const size_t sm00 = 8 * sizeof(double) * (size_t)(std::max(g.nu, g.nv) + 1);
+    KL("k_helm00", k_helm00_pcr<<<6, 512, sm00, h->st>>>(
+                       (double *)h->u1, (double *)h->u3, (double *)h->u2, (const float *)h->N1xz, (const float *)h->N3xz,
+                       (const float *)h->N2xz, (const float *)h->uvf, (const float *)h->wvf, (const float *)h->vvc,
+                       (const double *)h->p, h->duib, h->ib ? h->d_ibslot_u : nullptr, h->ib ? h->d_ibslot_v : nullptr,
+                       g, h->sc, kRK, h->a3s));
+  }
   // The u/w and v solves are independent: v runs on the side stream while u/w and the
   // mean-flow correction (which follows u) run on the main stream; each solve has its
   // own scratch. (Sequential on the main stream while per-kernel times are profiled.)
@@ -1333,14 +1363,21 @@ static size_t spectra_size(const lh_handle *h) {
 static int spectral_stats_buffers(lh_handle *h) {
   if (h->d_sp && h->d_slip && h->d_slip_inst) return LH_OK;
   const size_t nsp = spectra_size(h), nsl = 8 * (size_t)h->g.ncolF;
-  // each buffer on its own, so that a failed allocation is retried by the next call
+  // each buffer on its own, allocated into a local and published only once it is zeroed:
+  // a failed allocation or memset leaves the member null, and the next call retries it
   if (!h->d_sp) {
-    CK(cudaMalloc(&h->d_sp, sizeof(double) * nsp));
-    CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * nsp, h->st));
+    double *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double) * nsp));
+    const cudaError_t e = cudaMemsetAsync(d, 0, sizeof(double) * nsp, h->st);
+    if (e != cudaSuccess) { cudaFree(d); return fail(h, LH_ECUDA, std::string("zeroing the spectra: ") + cudaGetErrorString(e)); }
+    h->d_sp = d;
   }
   if (!h->d_slip) {
-    CK(cudaMalloc(&h->d_slip, sizeof(double2) * nsl));
-    CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * nsl, h->st));
+    double2 *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(double2) * nsl));
+    const cudaError_t e = cudaMemsetAsync(d, 0, sizeof(double2) * nsl, h->st);
+    if (e != cudaSuccess) { cudaFree(d); return fail(h, LH_ECUDA, std::string("zeroing the slip sums: ") + cudaGetErrorString(e)); }
+    h->d_slip = d;
   }
   if (!h->d_slip_inst) CK(cudaMalloc(&h->d_slip_inst, sizeof(double2) * nsl));
   return LH_OK;
@@ -1376,10 +1413,8 @@ extern "C" int lh_stats_reset(lh_handle *h) {
   const size_t ncd = 9 * (size_t)h->st_ncl * (h->st_dnx ? (size_t)h->st_dnx * h->st_dnz : 1);
   CK(cudaMemsetAsync(h->st_pl, 0, sizeof(double) * 11 * (size_t)h->g.nu, h->st));
   CK(cudaMemsetAsync(h->st_cd, 0, sizeof(double) * ncd, h->st));
-  if (h->d_sp) {
-    CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * spectra_size(h), h->st));
-    CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * 8 * (size_t)h->g.ncolF, h->st));
-  }
+  if (h->d_sp) CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * spectra_size(h), h->st));
+  if (h->d_slip) CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * 8 * (size_t)h->g.ncolF, h->st));
   h->istat = 0;
   return LH_OK;
 }
@@ -1441,7 +1476,7 @@ extern "C" int lh_slip_get(lh_handle *h, double *acc) {
   if (!h) return LH_EINVAL;
   const size_t n = 8 * (size_t)h->g.ncolF;
   if (!acc) return LH_OK;
-  if (!h->d_sp) { memset(acc, 0, sizeof(double2) * n); return LH_OK; }
+  if (!h->d_slip) { memset(acc, 0, sizeof(double2) * n); return LH_OK; }
   CK(cudaMemcpyAsync(acc, h->d_slip, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   return LH_OK;
@@ -1648,40 +1683,60 @@ __global__ void k_noalloc_twiddles(double2 *twx, int n1, double2 *twz, int n2) {
 
 namespace {
 const int LH_NOALLOC_MAX_DEVICES = 256;
-unsigned char *g_noalloc_ptr[LH_NOALLOC_MAX_DEVICES];
-bool g_noalloc_ready[LH_NOALLOC_MAX_DEVICES];
+// per device: the scratch array's device address, published by the set-up under the lock
+std::mutex g_noalloc_mu;
+std::atomic<unsigned char *> g_noalloc_ptr[LH_NOALLOC_MAX_DEVICES];
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Set-up, once per device, with that device current: the device address of the
-// scratch array (a host-side name of a __device__ array is not a device address)
-// and the shared-memory limit of the two kernels.
+// the shared-memory limit both kernels need at every supported length (the largest
+// request, k_xinv_phys at Ngal1 = 1152 in FP64, is above the default 48 KB)
+int noalloc_smem_limit(int dev) {
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 49152;
+  return optin;
+}
+
+// true when the set-up of this device is still in force: a cudaDeviceReset reloads the
+// module and clears the kernels' shared-memory attribute, which is detected here
+bool noalloc_attr_set(int lim) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, (const void *)k_xinv_phys<double, 24>) != cudaSuccess) return false;
+  return fa.maxDynamicSharedSizeBytes >= lim;
+}
+
+// Set-up, once per device (again after a device reset), with that device current: the
+// device address of the scratch array (a host-side name of a __device__ array is not a
+// device address) and the shared-memory limit of the two kernels. Host threads making
+// their first call at the same time are serialised by the lock; later calls read the
+// published address without it.
 int noalloc_setup(int dev, unsigned char **ptr, const char **err) {
   if (dev < 0 || dev >= LH_NOALLOC_MAX_DEVICES) { if (err) *err = "device index out of range"; return LH_EINVAL; }
-  if (!g_noalloc_ready[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, lh_noalloc_scratch) != cudaSuccess || !p) {
-      if (err) *err = "cudaGetSymbolAddress of the scratch array failed";
-      return LH_ECUDA;
-    }
-    int optin = 0;
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) optin = 49152;
-    cudaError_t e = cudaSuccess;
-#define LH_NOALLOC_ATTR(n_)                                                                                   \
-    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<double, n_>,                    \
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);    \
-    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<double, n_>,                    \
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
-    LH_FOR_SIZES(LH_NOALLOC_ATTR)
-#undef LH_NOALLOC_ATTR
-    if (e != cudaSuccess) {
-      if (err) *err = "cudaFuncSetAttribute failed";
-      return LH_ECUDA;
-    }
-    g_noalloc_ptr[dev] = (unsigned char *)p;
-    g_noalloc_ready[dev] = true;
+  const int lim = noalloc_smem_limit(dev);
+  unsigned char *cur = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (cur && noalloc_attr_set(lim)) { *ptr = cur; return LH_OK; }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  cur = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (cur && noalloc_attr_set(lim)) { *ptr = cur; return LH_OK; }
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, lh_noalloc_scratch) != cudaSuccess || !p) {
+    if (err) *err = "cudaGetSymbolAddress of the scratch array failed";
+    return LH_ECUDA;
   }
-  *ptr = g_noalloc_ptr[dev];
+  cudaError_t e = cudaSuccess;
+#define LH_NOALLOC_ATTR(n_)                                                                                   \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<double, n_>,                      \
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, lim);          \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<double, n_>,                      \
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  LH_FOR_SIZES(LH_NOALLOC_ATTR)
+#undef LH_NOALLOC_ATTR
+  if (e != cudaSuccess) {
+    if (err) *err = "cudaFuncSetAttribute failed";
+    return LH_ECUDA;
+  }
+  g_noalloc_ptr[dev].store((unsigned char *)p, std::memory_order_release);
+  *ptr = (unsigned char *)p;
   return LH_OK;
 }
 }  // namespace
@@ -1712,6 +1767,7 @@ extern "C" int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, con
   int rc = noalloc_setup(dev, &base, err);
   if (rc != LH_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  (void)cudaGetLastError();  // an earlier, unrelated launch error is not this call's
   double2 *twx = (double2 *)base;
   double2 *twz = (double2 *)(base + align256(sizeof(double2) * (size_t)Ngal1));
   double2 *Ascr = (double2 *)(base + align256(sizeof(double2) * (size_t)Ngal1) + align256(sizeof(double2) * (size_t)Ngal2));
@@ -1732,7 +1788,7 @@ extern "C" int lh_four_to_phys_noalloc(int N1, int N2, int Ngal1, int Ngal2, con
       k_xinv_phys<double, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(double2), st>>>(Ascr, (double *)phys, g, twx);
     });
   }
-  cudaError_t e = cudaPeekAtLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { if (err) *err = "kernel launch failed"; return LH_ECUDA; }
   return LH_OK;
 }

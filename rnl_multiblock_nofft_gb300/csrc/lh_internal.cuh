@@ -65,6 +65,8 @@ __device__ __forceinline__ void vcol_of(const Geo &g, int vc, int &c, int &b) {
 // Scalars kept on the device (no host round trip inside a step).
 struct DevScalars {
   double t, dt, dti, dtc, err, mpgx, QxT, Qx;
+  double dgx;          // the last flow-rate correction g of flowrate_corr (the history's dpgx)
+  double Umax, Uslip;  // maxvel and the slip velocity of mode (0,0), formed by lh_history_record
   long long iter;
   unsigned long long u1m, u2m, u3m;  // bit patterns of non-negative doubles (atomicMax)
   unsigned long long errbits;

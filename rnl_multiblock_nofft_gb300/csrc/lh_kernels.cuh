@@ -502,13 +502,14 @@ __global__ void k_dt(Geo g, DevScalars *sc) {
   const double cv = 1.0 / (u2m * g.dthetavi);
   double d = fmin(a, b);
   d = fmin(d, cv);
-  if (a != a || b != b) d = a + b;  // propagate a NaN
+  if (a != a || b != b || cv != cv) d = a + b + cv;  // propagate a NaN of any of the three maxima
   sc->dtc = d;
   const double lim = 2.5 * g.dtv, cfl = g.CFL * d;
   const double dt = (cfl != cfl) ? cfl : fmin(lim, cfl);
   sc->dt = dt;
   sc->dti = 1.0 / dt;
   sc->t = sc->t + dt;
+  if (!(dt == dt)) sc->status = LH_ENONFINITE;  // the guard fires in the substep that forms dt
 }
 
 __global__ void k_reset_cfl(DevScalars *sc) {
@@ -763,6 +764,111 @@ __device__ __forceinline__ void back_sweep_mx(double *__restrict__ u, const floa
 }
 
 // ============================================================================
+// Mode (0,0) of the mixed form in FP64. The mean flow and its -dRK mpgx forcing live in
+// column 0, so its Helmholtz systems are solved in FP64 as the plain form solves them
+// (LUsolU_W / LUsolV, tridLU_3D.f90:55-189, right-hand sides of RHS0_u1/u2/u3,
+// littleharsh.f90:635-788): FP64 right-hand side, FP64 solve, the column's previous
+// nonlinear term kept in FP64. Only the transforms' products (X, Fl) are the form's FP32
+// values. k = 0, so there are no i*k couplings and the real and imaginary parts are six
+// independent real systems (u, w, v x 2 parts): one block each, rows built in parallel and
+// solved by parallel cyclic reduction (log2(levels) steps) so that the column costs a few
+// microseconds instead of a serial FP64 recurrence over the levels. The mixed solve
+// kernels skip column 0.
+// Scalar views as the mixed kernels': element (q, col, part) at (q*ncol + col)*2 + part.
+// nuo: the previous nonlinear term of the column, [u re, u im, w re, w im, v re, v im][nu].
+// Shared memory: 8 (nu + 1) doubles.
+// ============================================================================
+__device__ __forceinline__ int fw2f(int fw) { return fw == 0 ? 0 : (fw == 1 ? 2 : 1); }
+__global__ void __launch_bounds__(512) k_helm00_pcr(double *__restrict__ u1, double *__restrict__ u3,
+                                                    double *__restrict__ u2, const float *__restrict__ N1xz,
+                                                    const float *__restrict__ N3xz, const float *__restrict__ N2xz,
+                                                    const float *__restrict__ uvf, const float *__restrict__ wvf,
+                                                    const float *__restrict__ vvc, const double *__restrict__ p,
+                                                    const double2 *__restrict__ duib, const int *__restrict__ ibslot_u,
+                                                    const int *__restrict__ ibslot_v, Geo g,
+                                                    const DevScalars *__restrict__ sc, int kRK,
+                                                    double *__restrict__ nuo_all) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int fw = blockIdx.x >> 1, part = blockIdx.x & 1;  // fw 0: u, 1: w, 2: v
+  const bool isv = fw == 2;
+  const int qlo = isv ? g.bq[1][2] : g.bq[1][0], qhi = isv ? g.bq[1][3] : g.bq[1][1];
+  const int n = qhi - qlo + 1, ny = isv ? g.nv : g.nu;
+  double *A = reinterpret_cast<double *>(smem_raw), *B = A + n, *Cc = B + n, *D = Cc + n;
+  double *A2 = D + n, *B2 = A2 + n, *C2b = B2 + n, *D2 = C2b + n;
+  const size_t ls = (size_t)g.ncol * 2;
+  double *u = fw == 0 ? u1 : (fw == 1 ? u3 : u2);
+  const float *X = fw == 0 ? N1xz : (fw == 1 ? N3xz : N2xz);
+  const float *Fl = fw == 0 ? uvf : (fw == 1 ? wvf : vvc);
+  const int *ibslot = isv ? ibslot_v : ibslot_u;
+  double *nuo = nuo_all + (size_t)blockIdx.x * g.nu;
+  const double *d2 = isv ? g.d2v : g.d2u;
+  const double dt = sc->dt;
+  const double C1 = g.aRK[kRK - 1] / g.Re, C2 = -g.cRK[kRK - 1], dR = g.dRK[kRK - 1], G = -g.gRK[kRK - 1];
+  const double beta = g.bRK[kRK - 1] * dt / g.Re;
+  const double mp = (fw == 0 && part == 0) ? -dR * sc->mpgx : 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int q = qlo + i;
+    double a, b, c, d;
+    if (q == qlo || q == qhi) {  // boundary rows: [1, gw(b,1)] / [gw(b,2), 1] (u, w); v = 0 (v)
+      a = 0.0; b = 1.0; c = 0.0; d = 0.0;
+      if (!isv) { if (q == qlo) c = g.gw[1][0]; else a = g.gw[1][1]; }
+    } else {
+      const size_t e = q * ls + part;
+      const double um = u[e - ls], u0 = u[e], up = u[e + ls];
+      const double d0q = d2[q], d1q = d2[ny + q], d2q = d2[2 * ny + q];
+      const int ibs = ibslot ? ibslot[q] : -1;
+      double du;
+      if (ibs < 0) {
+        const double L = (d0q * um + d1q * u0) + d2q * up;
+        double nq, rest;
+        if (!isv) {
+          nq = (double)X[e] + ((double)Fl[e] - (double)Fl[e - ls]) * g.thu[q] * g.dd;
+          rest = mp;
+        } else {
+          nq = (double)X[e] + ((double)Fl[e + ls] - (double)Fl[e]) * g.thv[q] * g.dd;
+          rest = (-dR * g.dd * g.thv[q]) * (p[e] - p[e - ls]);
+        }
+        du = ((C1 * L + C2 * nuo[q]) + rest) + G * nq;
+        nuo[q] = nq;
+      } else {
+        const double2 di = duib[((size_t)ibs * 3 + fw2f(fw)) * g.ncol];
+        du = part ? di.y : di.x;
+      }
+      a = -beta * d0q; b = 1.0 - beta * d1q; c = -beta * d2q;
+      d = u0 + dt * du;
+    }
+    A[i] = a; B[i] = b; Cc[i] = c; D[i] = d;
+  }
+  __syncthreads();
+  for (int st = 1; st < n; st *= 2) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int im = i - st, ip = i + st;
+      double a = 0.0, b = B[i], c = 0.0, d = D[i];
+      if (im >= 0) {
+        const double al = -A[i] / B[im];
+        a = al * A[im];
+        b += al * Cc[im];
+        d += al * D[im];
+      }
+      if (ip < n) {
+        const double ga = -Cc[i] / B[ip];
+        c = ga * Cc[ip];
+        b += ga * A[ip];
+        d += ga * D[ip];
+      }
+      A2[i] = a; B2[i] = b; C2b[i] = c; D2[i] = d;
+    }
+    __syncthreads();
+    double *t;
+    t = A; A = A2; A2 = t;
+    t = B; B = B2; B2 = t;
+    t = Cc; Cc = C2b; C2b = t;
+    t = D; D = D2; D2 = t;
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) u[(qlo + i) * ls + part] = D[i] / B[i];
+}
+
+// ============================================================================
 // Mixed-form solves with one lane per (column, real/imaginary part): the matrix
 // is real, so the two parts are independent systems; each lane repeats the FP32
 // factorisation. Scalar views: element (q, col, part) at (q*ncol + col)*2 + part.
@@ -788,6 +894,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   float *Nu = fw ? Nu3 : Nu1;
   const float *X = fw ? N3xz : N1xz;
   const float *Fl = fw ? wvf : uvf;
+  if (c == 0) return;  // mode (0,0): k_helm00_pcr (FP64)
   float2 *ys = ys2 + (size_t)fw * g.nu * nc * 2;
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
@@ -798,7 +905,6 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
   const float dtf = (float)dt;
   const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
   const float C3 = (float)(-dR * (fw ? g.k1z[r] : g.k1x[kx]));
-  const float mp = (c == 0 && fw == 0 && part == 0) ? (float)(-dR * sc->mpgx) : 0.f;
   const float dd = (float)g.dd;
   const int nu = g.nu;
   const double gw1 = g.gw[bd][0], gw2 = g.gw[bd][1];
@@ -854,7 +960,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
       float du;
       if (ibs < 0) {
         const float pt = part ? d2f_alu(po) : -d2f_alu(po);
-        du = (C1 * L + C2 * nuq) + C3 * pt + mp;
+        du = (C1 * L + C2 * nuq) + C3 * pt;
         const float n = xq + (flq - flm) * thq * dd;
         Nu[e] = n;
         du += G * n;
@@ -892,7 +998,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
     if (ibs < 0) {
       const double2 pj = p[(size_t)(q - 1) * nc + c];
       const float pt = part ? d2f_alu(pj.x) : -d2f_alu(pj.y);  // i*C3*p: (-C3 p.y, C3 p.x)
-      du = (C1 * L + C2 * Nu[e]) + C3 * pt + mp;
+      du = (C1 * L + C2 * Nu[e]) + C3 * pt;
       const float n = X[e] + (flq - flm) * g.thuf[q] * dd;
       Nu[e] = n;
       du += G * n;
@@ -937,6 +1043,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
   if (vc >= g.nvc) return;
   int c, bd;
   vcol_of(g, vc, c, bd);
+  if (c == 0) return;  // mode (0,0): k_helm00_pcr (FP64)
   const int qlo = g.bq[bd][2], qhi = g.bq[bd][3];
   const int r = c / g.N1h, kx = c - r * g.N1h;
   const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
@@ -1069,6 +1176,7 @@ __global__ void k_meanflow(double2 *__restrict__ u1, Geo g, DevScalars *sc, int 
     for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + dy[j] * ur[j];
     const double gg = (sc->QxT - Qx0) / Qx1;
     sc->mpgx = sc->mpgx + gg;
+    sc->dgx = gg;
     gg_sh = gg;
   }
   __syncthreads();
@@ -1142,6 +1250,7 @@ __global__ void __launch_bounds__(512) k_meanflow_pcr(double2 *__restrict__ u1, 
     for (int j = 1; j <= nn + 1; ++j) Qx0 = Qx0 + dy[j] * ur[j];
     const double gg = (sc->QxT - Qx0) / Qx1;
     sc->mpgx = sc->mpgx + gg;
+    sc->dgx = gg;
     gg_sh = gg;
   }
   __syncthreads();
@@ -1156,6 +1265,22 @@ __global__ void k_flowrate(const double2 *__restrict__ u1, Geo g, DevScalars *sc
   for (int j = 1; j <= g.nn + 1; ++j) Q = Q + (g.yv[j + g.dny] - g.yv[j - 1 + g.dny]) * u1[(size_t)(j + g.dny) * g.ncol].x;
   sc->Qx = Q;
   if (setQxT) sc->QxT = Q;
+}
+
+// The scalar part of record_out (FOU3D.f90:3040-3070) from mode (0,0) of u1: Qx by flowrateIm,
+// Umax by maxvel (littleharsh.f90:511-527: the largest Re u(j), j = 0..nn+2, not below 0) and
+// the slip velocity Uslip, u(0,0) extrapolated linearly from levels 0 and 1 to y = -1.
+__global__ void k_history(const double2 *__restrict__ u1, Geo g, DevScalars *sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int dny = g.dny, nc = g.ncol;
+  double Q = 0.0, um = 0.0;
+  for (int j = 1; j <= g.nn + 1; ++j) Q = Q + (g.yv[j + dny] - g.yv[j - 1 + dny]) * u1[(size_t)(j + dny) * nc].x;
+  for (int j = 0; j <= g.nn + 2; ++j) um = fmax(um, u1[(size_t)(j + dny) * nc].x);
+  const double u0 = u1[(size_t)dny * nc].x, u1v = u1[(size_t)(1 + dny) * nc].x;
+  const double y0 = g.yu[dny], y1 = g.yu[1 + dny];
+  sc->Qx = Q;
+  sc->Umax = um;
+  sc->Uslip = (u1v * (-1.0 - y0) + u0 * (y1 + 1.0)) / (y1 - y0);
 }
 
 __global__ void k_step_end(DevScalars *sc) {

@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from .abi import LH_OK, LH_PREC_FP64, LH_PREC_MIXED, LhConfig, LhScalars, cfield_shape, make_config
+from .abi import LH_OK, LH_PREC_FP64, LH_PREC_MIXED, LhConfig, LhHistory, LhScalars, cfield_shape, make_config
 from .setup_grid import ChannelSetup
 
 _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "liblh.so")
@@ -23,7 +23,7 @@ EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_do
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
-           "lh_batch_synchronize", "lh_batch_destroy", "lh_batch_stream")
+           "lh_batch_synchronize", "lh_batch_destroy", "lh_batch_stream", "lh_history_record")
 
 
 class LhKernelTime(C.Structure):
@@ -67,6 +67,7 @@ def load(path: str = _LIB_PATH):
     L.lh_download_band.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.lh_set_scalars.argtypes = [vp, C.POINTER(LhScalars)]
     L.lh_get_scalars.argtypes = [vp, C.POINTER(LhScalars)]
+    L.lh_history_record.argtypes = [vp, C.POINTER(LhHistory)]
     L.lh_substep.argtypes = [vp, i]
     L.lh_step.argtypes = [vp]
     L.lh_synchronize.argtypes = [vp]
@@ -257,6 +258,12 @@ class GpuChannel:
         s = LhScalars()
         self._check(self.L.lh_get_scalars(self.h, C.byref(s)))
         return s.as_dict()
+
+    def history_record(self) -> dict:
+        """The history-file record of the current state (lh_history_record)."""
+        r = LhHistory()
+        self._check(self.L.lh_history_record(self.h, C.byref(r)))
+        return r.as_dict()
 
     # ---- time stepping ----
     def substep(self, kRK: int):

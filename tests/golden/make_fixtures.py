@@ -61,4 +61,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LH_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("usage: make_fixtures.py REFERENCE_CHECKOUT (or set LH_REFERENCE_DIR)")
+    main(ref)

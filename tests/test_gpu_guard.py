@@ -33,3 +33,20 @@ def test_finite_state_passes(cuda_ok):
     g.step(2)
     g.synchronize()
     assert np.isfinite(g.scalars()["err"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nonfinite_v_reaches_dt_in_the_first_substep(cuda_ok, precision):
+    # a NaN only in v reaches dt through the v maximum of the CFL limit; the guard fires
+    # after lh_substep(1) alone, before the divergence of the third substep is formed
+    s = workload_setup("S")
+    st = initial_field(s, 92)
+    st[1][4, 7] = np.nan
+    g = GpuChannel(s, precision)
+    g.upload_state(*st)
+    g.set_scalars(**initial_scalars(s))
+    g.substep(1)
+    with pytest.raises(LhError) as e:
+        g.synchronize()
+    assert e.value.code == LH_ENONFINITE
+    assert np.isnan(g.scalars()["dt"])

@@ -1,0 +1,152 @@
+"""GPU (CUDA, through the C ABI) vs the CPU oracle at the benchmarked sizes, where the
+transform kernels run at their largest compiled lengths:
+* the 256x256x301 textured channel (posts 8x8 points on a 16-point period, 41 immersed
+  levels; x/z transforms of length 384): FP64 form within 1e-12 relative per field after one
+  RK3 step, mixed form within 1e-5 on u, v, w and PRESS_MIXED on p;
+* the multiblock channel with wall bands 768x384 and a core band 384x192, ny 385, posts 12x12
+  on a 24-point period (transforms of lengths 1152 and 576 on the wall planes, 576 and 288 on
+  the core planes): FP64 within 1e-12 for every band's fields after one step;
+* the leaf transforms (four_to_phys / phys_to_four) at every compiled length, 24 ... 1152,
+  within 1e-13 of the oracle's.
+The oracle runs on all host cores."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import Oracle
+from rnl_multiblock_nofft_gb300.native import GpuChannel
+from rnl_multiblock_nofft_gb300.setup_grid import build_setup
+from rnl_multiblock_nofft_gb300.workloads import (initial_field, initial_field_bands, initial_scalars,
+                                                  re_tau_params, workload_setup)
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("u1", "u2", "u3", "p")
+TOL64 = 1e-12
+TOL_MIXED_VEL = 1e-5
+# The mixed form's pressure: p is the sum of the substeps' psi, each solved from the divergence
+# of the FP32-transformed nonlinear term; its relative L2 error after one step is bounded by
+# this (the velocities stay within TOL_MIXED_VEL).
+PRESS_MIXED = 1e-4
+THREADS = os.cpu_count() or 1
+
+
+def relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def c1_reference():
+    """The 256x256x301 textured channel: setup, initial state and the oracle's state after
+    one step."""
+    s = workload_setup("C1")
+    st = initial_field(s, 1001)
+    o = Oracle(s, threads=THREADS)
+    o.set_state(*st)
+    o.set_scalars(**initial_scalars(s))
+    o.step()
+    ref = o.get_state()
+    sc = o.scalars()
+    o.close()
+    return s, st, ref, sc
+
+
+def run_gpu(s, st, precision, steps=1):
+    g = GpuChannel(s, precision)
+    g.upload_state(*st)
+    g.set_scalars(**initial_scalars(s))
+    g.step(steps)
+    g.synchronize()
+    out = g.download_state(), g.scalars()
+    g.close()
+    return out
+
+
+def test_c1_fp64_one_step(cuda_ok, c1_reference):
+    s, st, ref, sc = c1_reference
+    assert s.G1 == 384 and s.G2 == 384 and s.dny > 0 and len(s.list_ib[2]) > 0
+    got, gsc = run_gpu(s, st, "fp64")
+    errs = {f: relerr(y, x) for f, x, y in zip(FIELDS, ref, got)}
+    for f, e in errs.items():
+        assert e < TOL64, (f, e)
+    assert gsc["dt"] == pytest.approx(sc["dt"], rel=1e-13)
+    assert gsc["t"] == pytest.approx(sc["t"], rel=1e-13)
+    # flowrate_corr's g = (QxT - Qx0) / Qx1 cancels about six digits: mpgx agrees to ~1e-10
+    assert gsc["mpgx"] == pytest.approx(sc["mpgx"], rel=1e-9)
+    assert gsc["err"] < 1e-12
+
+
+def test_c1_mixed_one_step(cuda_ok, c1_reference):
+    s, st, ref, sc = c1_reference
+    got, gsc = run_gpu(s, st, "mixed")
+    errs = {f: relerr(y, x) for f, x, y in zip(FIELDS, ref, got)}
+    for f in ("u1", "u2", "u3"):
+        assert errs[f] < TOL_MIXED_VEL, (f, errs[f])
+    assert errs["p"] < PRESS_MIXED, errs["p"]
+    # the mean flow (mode (0,0) of u) and the flux correction are solved in FP64; their inputs
+    # carry the FP32 products, and flowrate_corr's g = (QxT - Qx0) / Qx1 cancels about six
+    # digits, so mpgx agrees to ~1e-8 relative
+    assert gsc["mpgx"] == pytest.approx(sc["mpgx"], rel=1e-7)
+    assert relerr(got[0][0], ref[0][0]) < 1e-8
+
+
+def test_c4_multiblock_fp64_one_step(cuda_ok):
+    s = workload_setup("C4")
+    assert (s.G1, s.G2) == (1152, 576)
+    f = initial_field_bands(s, 1004)
+    o = Oracle(s, threads=THREADS)
+    o.set_bands(f)
+    o.set_scalars(**initial_scalars(s))
+    o.step()
+    ref = o.get_bands()
+    sc = o.scalars()
+    o.close()
+    g = GpuChannel(s, "fp64")
+    g.upload_bands(f)
+    g.set_scalars(**initial_scalars(s))
+    g.step()
+    g.synchronize()
+    got = g.download_bands()
+    gsc = g.scalars()
+    g.close()
+    for band in (1, 2, 3):
+        for name, x, y in zip(FIELDS, ref[band], got[band]):
+            e = relerr(y, x)
+            assert e < TOL64, (band, name, e)
+    assert gsc["t"] == pytest.approx(sc["t"], rel=1e-13)
+    assert gsc["err"] < 1e-12
+
+
+LENGTHS = (24, 48, 72, 96, 144, 192, 288, 384, 576, 768, 1152)
+
+
+@pytest.mark.parametrize("G", LENGTHS)
+def test_leaf_transforms_every_length(cuda_ok, G):
+    """x length G with z length Gz (the next length down, or 24), so each length runs once
+    as the real x transform and once as the complex z transform across the set."""
+    import torch
+    Gz = LENGTHS[max(LENGTHS.index(G) - 1, 0)]
+    N1, N2 = 2 * (G // 3), 2 * (Gz // 3)
+    p = re_tau_params(N1, 41, Nz=N2)
+    s = build_setup(p)
+    assert (s.G1, s.G2) == (G, Gz)
+    o = Oracle(s, threads=THREADS)
+    g = GpuChannel(s, "fp64")
+    rng = np.random.default_rng(G)
+    npl = 3
+    spec = rng.normal(size=(npl, s.N2, s.N1 // 2 + 1)) + 1j * rng.normal(size=(npl, s.N2, s.N1 // 2 + 1))
+    ref = o.four_to_phys(spec)
+    ds = torch.from_numpy(spec.view(np.float64).copy()).cuda()
+    dp = torch.zeros((npl, s.G2, s.G1), dtype=torch.float64, device="cuda")
+    g.four_to_phys(ds.data_ptr(), dp.data_ptr(), npl)
+    g.synchronize()
+    phys = dp.cpu().numpy()
+    assert np.abs(phys - ref).max() / np.abs(ref).max() < 1e-13
+    back_ref = o.phys_to_four(ref)
+    db = torch.zeros_like(ds)
+    g.phys_to_four(dp.data_ptr(), db.data_ptr(), npl)
+    g.synchronize()
+    back = db.cpu().numpy().view(np.complex128).reshape(back_ref.shape)
+    assert np.abs(back - back_ref).max() / np.abs(back_ref).max() < 1e-13
+    g.close()
+    o.close()
