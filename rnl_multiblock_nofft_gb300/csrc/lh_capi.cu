@@ -13,6 +13,7 @@
 
 #include "lh_kernels.cuh"
 #include "lh_triads.cuh"
+#include "lh_xpass2.cuh"
 
 namespace {
 const int NTHR_H = 256;
@@ -191,6 +192,12 @@ static cudaError_t set_attrs_sized(int lim) {
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xfwd_phys<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_ib_xforce<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec<T, N>, A, lim);
+  if constexpr (sizeof(T) == 4) {  // the two-stage mixed-form passes
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv2<N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd2<N>, A, lim);
+    if constexpr (N <= 384)
+      if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass2<N>, A, lim);
+  }
   return e;
 }
 
@@ -997,6 +1004,13 @@ extern "C" int lh_history_record(lh_handle *h, lh_history *out) {
 template <typename T, int N>
 static int launch_zinv(lh_handle *h, const Geo &g, int nslots, const void *twz) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4) {  // the two-stage register form of the mixed inverse z pass
+    using P = zp2<N>;
+    dim3 grid((g.N1h + P::KB - 1) / P::KB, nslots, 3);
+    KL("k_zinv_nl", k_zinv2<N><<<grid, P::NT, P::SMEM, h->st>>>(h->u1, h->u2, h->u3, (float2 *)h->A, g,
+                                                                (const float2 *)twz));
+    return LH_OK;
+  }
   constexpr int KB = kb_zinv<V>(N);
   dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
   KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, LH_ZINV_THREADS, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
@@ -1006,6 +1020,13 @@ static int launch_zinv(lh_handle *h, const Geo &g, int nslots, const void *twz) 
 template <typename T, int N>
 static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const int *capslot, const void *twx) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4 && N <= 384) {  // the two-stage register form of the mixed x pass
+    using P = xp2<N>;
+    dim3 grid((g.G2 / 2 + P::PB - 1) / P::PB, nslots);
+    KL("k_xpass_nl", k_xpass2<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
+                                                                  (const float2 *)twx, doCFL, h->sc, capslot, h->cap));
+    return LH_OK;
+  }
   constexpr int PB = pb_xpass<V>(N);
   dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
   KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, LH_XPASS_THREADS, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
@@ -1015,6 +1036,14 @@ static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const
 template <typename T, int N>
 static int launch_zfwd(lh_handle *h, const Geo &g, int nslots, const void *twz) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4) {  // the two-stage register form of the mixed forward z pass
+    using P = zf2<N>;
+    dim3 grid((g.N1h + P::KF - 1) / P::KF, nslots);
+    KL("k_zfwd_nl", k_zfwd2<N><<<grid, P::NTH, P::SMEM, h->st>>>(
+                        (const float2 *)h->B, g, (const float2 *)twz, (float2 *)h->N1xz, (float2 *)h->N2xz,
+                        (float2 *)h->N3xz, (float2 *)h->uvf, (float2 *)h->vvc, (float2 *)h->wvf));
+    return LH_OK;
+  }
   constexpr int KB = kb_zfwd<V>(N);
   dim3 grid((g.N1h + KB - 1) / KB, nslots);
   KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, LH_ZFWD_THREADS, 8 * (size_t)KB * N * sizeof(V), h->st>>>(

@@ -1,0 +1,437 @@
+// lh_xpass2.cuh — the x pass of the mixed form as a two-stage transform held in registers.
+//
+// Same work as k_xpass_nl (lh_kernels.cuh) for one level's plane: the inverse x transforms
+// (rft, iopt >= 0) of u, v, w row pairs, the physical products of ops_in_planes2
+// (FOU3D.f90:2090-2251), the CFL maxima (dtc_calc) and the forward x transforms (rft,
+// iopt < 0) of the products, with the same A input and B output layouts. Two rows l, l+1 of
+// a field travel as one complex line (row l in .x, row l+1 in .y).
+//
+// The length-N transform is split N = XA * XB with XB = 8 (Stockham, two stages):
+//   inverse stage 1: XB threads per line, each an XA-point DFT of elements jj + XB t, read
+//                    straight from A with the Hermitian completion (the gather) -> shared E1
+//   inverse stage 2 + products + forward stage 1 (fused, registers): XA threads per row pair,
+//                    thread jj holds physical points jj + XA t (t < 8) of u, v and w, forms the
+//                    products there and transforms them with the forward 8-point DFT -> E2
+//   forward stage 2: XB threads per product line, each an XA-point DFT; the thread holds
+//                    outputs jj + XB t, the conjugate-symmetric partner N - k of every output k
+//                    is in lane (XB - jj) mod XB of the same 8-lane group, fetched by shuffle,
+//                    and the two rows of the pair are separated and written to B.
+// So the block exchanges data through shared memory once per direction, and every element
+// address inside a stage is an immediate offset from the thread's base.
+#pragma once
+#include "lh_internal.cuh"
+#include "lh_regfft.cuh"
+
+// row pairs per block (one block: 48 * PB threads at N = 384)
+template <int N> struct xp2 {
+  static constexpr int XB = 8, XA = N / XB;
+  static constexpr int PB = XA >= 36 ? 2 : (XA >= 18 ? 4 : 8);
+  static constexpr int NT = (XA * PB + 31) / 32 * 32;  // whole warps (the fused stage's shuffles)
+  // padded shared-memory lines: E1 (stage-1 output e = jj XA + t at e + e / XA), E2
+  // (forward stage-1 output e = jj 8 + t at e + e / 8); line strides = 8 (mod 16) float2 so
+  // that the lanes of two lines fall on different banks
+  static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
+  static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB);
+  static constexpr int SMEM = (3 * LS1 > 4 * LS2 ? 3 * LS1 : 4 * LS2) * PB * 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(xp2<N>::NT) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+                                                        const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
+                                                        const int *__restrict__ capslot, double *__restrict__ cap) {
+  using P = xp2<N>;
+  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1, LS2 = P::LS2;
+  constexpr int NK = N / 3 + 1;  // retained x-modes 0..N1/2 (N1 = 2 (Ngal1 / 3), checked at create)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *E = reinterpret_cast<float2 *>(smem_raw);
+  const int G2 = g.G2, N1h = g.N1h;
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const int l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const size_t fstride = (size_t)G2 * N1h;
+  const int tid = threadIdx.x;
+
+  // ---- inverse stage 1: line (f, pb), thread jj < 8: XA-point DFT of elements jj + 8 t ----
+  if (tid < 3 * PB * XB) {
+    const int line = tid / XB, jj = tid - line * XB;
+    const int f = line / PB, pb = line - f * PB;
+    float2 v[XA];
+    if (pb < npairs) {
+      const float2 *ra = A + (size_t)(slot * 3 + f) * fstride + (size_t)(l0 + 2 * pb) * N1h;
+      const float2 *rb = ra + N1h;
+      regfft::static_for<0, XA>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        // element m = jj + 8 t: retained mode k = m (m < NK), conjugate of mode N - m (m > N - NK), else 0
+        constexpr int mlo = XB * t, mhi = XB * t + XB - 1;
+        constexpr bool direct = mlo < NK, conj = mhi > N - NK;  // possible for some lane
+        const int m = jj + mlo;
+        float2 z = make_float2(0.f, 0.f);
+        if (direct && m < NK) {
+          float2 a = __ldg(ra + m), b = __ldg(rb + m);
+          if (m == 0) { a.y = 0.f; b.y = 0.f; }
+          z = make_float2(a.x - b.y, a.y + b.x);  // a + i b
+        } else if (conj && m > N - NK) {
+          const float2 a = __ldg(ra + (N - m)), b = __ldg(rb + (N - m));
+          z = make_float2(a.x + b.y, -a.y + b.x);  // conj(a) + i conj(b)
+        }
+        v[t] = z;
+      });
+    } else {
+      regfft::static_for<0, XA>([&](auto t_) { v[decltype(t_)::value] = make_float2(0.f, 0.f); });
+    }
+    regfft::dft_reg<XA, true>(v);
+    float2 *e1 = E + line * LS1 + jj * (XA + 1);
+    regfft::static_for<0, XA>([&](auto t_) { e1[decltype(t_)::value] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+
+  // ---- fused: inverse stage 2 (8-point DFTs), products, CFL maxima, forward stage 1 ----
+  const int pb = tid / XA, jj = tid - pb * XA;
+  const bool act = pb < PB;  // the threads that round the block up to whole warps only take part in the shuffles
+  float2 ph[3][XB];
+  if (!act) {
+#pragma unroll
+    for (int f = 0; f < 3; ++f)
+#pragma unroll
+      for (int t = 0; t < XB; ++t) ph[f][t] = make_float2(0.f, 0.f);
+  } else {
+    float2 w[XB];  // exp(+2 pi i jj t / N): the inverse twiddles of stage 2
+    w[0] = make_float2(1.f, 0.f);
+    regfft::static_for<1, XB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = __ldg(tw + jj * t);
+      w[t] = make_float2(x.x, -x.y);
+    });
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const float2 *e1 = E + (f * PB + pb) * LS1 + jj;
+      regfft::static_for<0, XB>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        const float2 x = e1[t * (XA + 1)];
+        ph[f][t] = t == 0 ? x : make_float2(x.x * w[t].x - x.y * w[t].y, x.x * w[t].y + x.y * w[t].x);
+      });
+      regfft::dft_reg<XB, true>(ph[f]);
+    }
+  }
+  const bool valid = act && pb < npairs;
+  if (capslot && valid) {
+    const int cs = capslot[slot];
+    if (cs >= 0) {
+      const int l = l0 + 2 * pb;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + jj;
+        regfft::static_for<0, XB>([&](auto t_) {
+          constexpr int t = decltype(t_)::value;
+          cp[t * XA] = f2d_alu(ph[f][t].x);
+          cp[N + t * XA] = f2d_alu(ph[f][t].y);
+        });
+      }
+    }
+  }
+  if (doCFL) {
+    float m1 = 0.f, m2 = 0.f, m3 = 0.f;
+    if (valid) {
+      if (isU) {
+#pragma unroll
+        for (int t = 0; t < XB; ++t) {
+          m1 = nmax(m1, nmax(fabsf(ph[0][t].x), fabsf(ph[0][t].y)));
+          m3 = nmax(m3, nmax(fabsf(ph[2][t].x), fabsf(ph[2][t].y)));
+        }
+      } else {
+        const float thv = g.thvf[q];
+#pragma unroll
+        for (int t = 0; t < XB; ++t) m2 = nmax(m2, nmax(fabsf(ph[1][t].x), fabsf(ph[1][t].y)) * thv);
+      }
+    }
+    m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
+    if ((tid & 31) == 0) {
+      if (isU) { atomic_max_pos(&sc->u1m, f2d_alu(m1)); atomic_max_pos(&sc->u3m, f2d_alu(m3)); }
+      else atomic_max_pos(&sc->u2m, f2d_alu(m2));
+    }
+  }
+  __syncthreads();  // E1 is read: E2 reuses the shared memory
+  const int nprod = isU ? 4 : 2;
+  if (act) {
+    // u level: uu, uw, vv, ww; v level: uv, wv (per row of the pair); field indices are
+    // compile-time so that ph stays in registers
+    regfft::static_for<0, 4>([&](auto p_) {
+      constexpr int p = decltype(p_)::value;
+      constexpr int ua = p == 2 ? 1 : (p == 3 ? 2 : 0), ub = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 1 : 2));
+      constexpr int va = p == 0 ? 0 : 2, vb = 1;
+      if (p < 2 || isU) {
+        float2 pr[XB];
+#pragma unroll
+        for (int t = 0; t < XB; ++t) {
+          const float2 x0 = isU ? ph[ua][t] : ph[va][t], x1 = isU ? ph[ub][t] : ph[vb][t];
+          pr[t] = make_float2(x0.x * x1.x, x0.y * x1.y);
+        }
+        regfft::dft_reg<XB, false>(pr);
+        float2 *e2 = E + (p * PB + pb) * LS2 + jj * (XB + 1);
+#pragma unroll
+        for (int t = 0; t < XB; ++t) e2[t] = pr[t];
+      }
+    });
+  }
+  __syncthreads();
+
+  // ---- forward stage 2: line (p, pb), thread jj < 8: twiddles, XA-point DFT of jj + 8 t ----
+  if (tid < nprod * PB * XB) {
+    const int line = tid / XB, jj2 = tid - line * XB;
+    const int p = line / PB, pb2 = line - p * PB;
+    float2 v[XA];
+    const float2 *e2 = E + line * LS2 + jj2;
+    regfft::static_for<0, XA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e2[t * (XB + 1)];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj2 * t);
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+    regfft::dft_reg<XA, false>(v);
+    // outputs k = jj2 + 8 t; the partner N - k = (8 - jj2) + 8 (XA - 1 - t) sits in lane
+    // (8 - jj2) mod 8 of this 8-lane group (lane jj2 = 0: its own entry XA - t)
+    const int lane = tid & 31, src = (lane & ~(XB - 1)) | ((XB - jj2) & (XB - 1));
+    const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+    float2 *dst = B + (((size_t)(pbase + p) * (G2 / 2) + (l0 >> 1) + pb2) * N1h) * 2;
+    const float s1 = 1.f / (float)N;
+    const bool ok = pb2 < npairs;
+    regfft::static_for<0, (NK + XB - 1) / XB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      float2 zp;
+      zp.x = __shfl_sync(0xffffffffu, v[XA - 1 - t].x, src);
+      zp.y = __shfl_sync(0xffffffffu, v[XA - 1 - t].y, src);
+      if (jj2 == 0) zp = t == 0 ? v[0] : v[(XA - t) % XA];
+      const int k = jj2 + XB * t;
+      if (ok && k < NK) {
+        const float2 z = v[t];
+        float4 o;
+        o.x = 0.5f * (z.x + zp.x) * s1; o.y = 0.5f * (z.y - zp.y) * s1;   // (z + conj zp) / 2
+        o.z = 0.5f * (z.y + zp.y) * s1; o.w = -0.5f * (z.x - zp.x) * s1;  // -i (z - conj zp) / 2
+        if (k == 0) { o.y = 0.f; o.w = 0.f; }
+        *reinterpret_cast<float4 *>(dst + (size_t)k * 2) = o;
+      }
+    });
+  }
+}
+
+// ============================================================================
+// The inverse z pass of the mixed form as a two-stage transform (the work of k_zinv_nl:
+// stagger interpolation (interp_u/v, FOU3D.f90:427-474) and the inverse z transforms (cft,
+// iopt >= 0) of one field's kx columns at one level, written to A [slot*3 + f][l][kx]).
+// N = ZA * ZB; stage 1: ZB threads per line, each a ZA-point DFT of rows jj + ZB t, gathered
+// straight from the FP64 state (retained kz rows only; the dealiasing rows are zero and the
+// loads of the rows that are zero for every lane are left out at compile time); stage 2: ZA
+// threads per line, each a ZB-point DFT, writing rows jj + ZA t of A. KB kx lines per block,
+// kx the fastest thread index (coalesced state loads and A stores).
+// ============================================================================
+template <int N> struct zp2 {
+  static constexpr int ZA = N == 24 ? 4 : N == 48 ? 6 : N == 72 ? 8 : N == 96 ? 8 : N == 144 ? 12 : N == 192 ? 12
+                          : N == 288 ? 16 : N == 384 ? 16 : N == 576 ? 24 : N == 768 ? 24 : 32;
+  static constexpr int ZB = N / ZA;
+  static constexpr int KB = 8;
+  static constexpr int NT = ((ZA > ZB ? ZA : ZB) * KB + 31) / 32 * 32;
+  static constexpr int SMEM = (N + ZB) * KB * 8;  // float2, one pad element per ZA-block
+};
+
+template <int N>
+__global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                       const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
+                                                       const float2 *__restrict__ tw) {
+  using P = zp2<N>;
+  constexpr int ZA = P::ZA, ZB = P::ZB, KB = P::KB;
+  static_assert(ZA * ZB == N, "z plan");
+  constexpr int H = N / 3;  // N2 / 2 retained kz rows on each side (N2 = 2 (Ngal2 / 3), checked at create)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *E = reinterpret_cast<float2 *>(smem_raw);
+  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const size_t nc = g.ncolF;
+  const int tid = threadIdx.x;
+  if (tid < ZB * KB) {
+    const int jj = tid / KB, kk = tid - jj * KB, kx = kx0 + kk;
+    float2 v[ZA];
+    // field f at level q (interpolated to the level's grid), FP32
+    const double2 *s0, *s1 = nullptr;
+    float ca = 1.f, cb = 0.f;
+    size_t o0 = (size_t)q * nc, o1 = 0;
+    if (isU) {
+      if (f == 0) s0 = u1;
+      else if (f == 2) s0 = u3;
+      else { s0 = u2; s1 = u2; o1 = (size_t)(q - 1) * nc; ca = g.iuaf[q]; cb = g.iubf[q]; }  // v faces -> centre
+    } else {
+      if (f == 1) s0 = u2;
+      else { s0 = s1 = (f == 0) ? u1 : u3; o0 = (size_t)(q + 1) * nc; o1 = (size_t)q * nc; ca = g.ivaf[q]; cb = g.ivbf[q]; }
+    }
+    const bool ok = kx < g.N1h;
+    regfft::static_for<0, ZA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      constexpr int mlo = ZB * t, mhi = ZB * t + ZB - 1;
+      constexpr bool lo = mlo < H, hi = mhi >= N - H;  // possible for some lane
+      const int m = jj + mlo;
+      float2 z = make_float2(0.f, 0.f);
+      int r = -1;
+      if (lo && m < H) r = m;
+      else if (hi && m >= N - H) r = m - N + 2 * H;
+      if ((lo || hi) && ok && r >= 0) {
+        const int c = gcol(g, r, kx);
+        const double2 a = s0[o0 + c];
+        if (s1) {
+          const double2 b = s1[o1 + c];
+          z = make_float2(ca * d2f_alu(a.x) + cb * d2f_alu(b.x), ca * d2f_alu(a.y) + cb * d2f_alu(b.y));
+        } else {
+          z = make_float2(d2f_alu(a.x), d2f_alu(a.y));
+        }
+      }
+      v[t] = z;
+    });
+    regfft::dft_reg<ZA, true>(v);
+    float2 *e = E + jj * (ZA + 1) * KB + kk;
+    regfft::static_for<0, ZA>([&](auto t_) { e[decltype(t_)::value * KB] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+  if (tid < ZA * KB) {
+    const int jj = tid / KB, kk = tid - jj * KB, kx = kx0 + kk;
+    float2 v[ZB];
+    const float2 *e = E + jj * KB + kk;
+    regfft::static_for<0, ZB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e[t * (ZA + 1) * KB];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj * t);  // conj: the inverse direction
+        v[t] = make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);
+      }
+    });
+    regfft::dft_reg<ZB, true>(v);
+    if (kx < g.N1h) {
+      float2 *dst = A + (size_t)(slot * 3 + f) * N * g.N1h + kx;
+      regfft::static_for<0, ZB>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        dst[(size_t)(jj + ZA * t) * g.N1h] = v[t];
+      });
+    }
+  }
+}
+
+// ============================================================================
+// The forward z pass of the mixed form as a two-stage transform (the work of k_zfwd_nl:
+// forward z transforms (cft, iopt < 0) of the x pass's products and der_x / der_z,
+// FOU3D.f90:476-593, 2253-2272). Per block: KF kx columns of the NP products of one level
+// (u level: uu, uw, vv, ww -> N1xz, N3xz, vvc; v level: uv, wv -> N2xz, uvf, wvf).
+// Stage 1: ZA threads per line, each a ZB-point DFT of rows jj + ZA t read from B (the two
+// rows of a pair adjacent there); stage 2: ZB threads per line, each a ZA-point DFT; the
+// retained kz rows go to shared memory, where one thread per (row, kx) combines the products.
+// ============================================================================
+template <int N> struct zf2 {
+  using Z = zp2<N>;
+  static constexpr int ZA = Z::ZA, ZB = Z::ZB, KF = 4;
+  static constexpr int NTH = ((ZA > ZB ? ZA : ZB) * 4 * KF + 31) / 32 * 32;
+  // line stride of the stage-1 output (e = jj ZB + t at e + e / ZB), = 4 (mod 16) float2 so that
+  // the KF lines of a half-warp start 8 banks apart
+  static constexpr int LSE = (N + N / ZB) + ((4 - (N + N / ZB) % 16) + 16) % 16;
+  static constexpr int SMEM = 4 * KF * LSE * 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(zf2<N>::NTH) k_zfwd2(const float2 *__restrict__ B, Geo g, const float2 *__restrict__ tw,
+                                                        float2 *__restrict__ N1xz, float2 *__restrict__ N2xz,
+                                                        float2 *__restrict__ N3xz, float2 *__restrict__ uvf,
+                                                        float2 *__restrict__ vvc, float2 *__restrict__ wvf) {
+  using P = zf2<N>;
+  constexpr int ZA = P::ZA, ZB = P::ZB, KF = P::KF, LSE = P::LSE;
+  constexpr int H = N / 3;  // N2 / 2
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *E = reinterpret_cast<float2 *>(smem_raw);
+  const int slot = blockIdx.y, kx0 = blockIdx.x * KF;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const int NP = isU ? 4 : 2;
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  const int N1h = g.N1h;
+  const int tid = threadIdx.x;
+  // stage 1: thread (p, jj, kk), kk fastest
+  if (tid < NP * ZA * KF) {
+    const int kk = tid % KF, r1 = tid / KF, jj = r1 % ZA, p = r1 / ZA, kx = kx0 + kk;
+    float2 v[ZB];
+    const float2 *src = B + ((size_t)(pbase + p) * (N / 2) * N1h + kx) * 2;
+    const bool ok = kx < N1h;
+    regfft::static_for<0, ZB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int l = jj + ZA * t;
+      v[t] = ok ? src[(size_t)(l >> 1) * N1h * 2 + (l & 1)] : make_float2(0.f, 0.f);
+    });
+    regfft::dft_reg<ZB, false>(v);
+    float2 *e = E + (p * KF + kk) * LSE + jj * (ZB + 1);
+    regfft::static_for<0, ZB>([&](auto t_) { e[decltype(t_)::value] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+  // stage 2: thread (p, jj2, kk); the inputs are read before the block reuses E for the rows
+  const bool s2 = tid < NP * ZB * KF;
+  const int kk = tid % KF, r2 = tid / KF, jj2 = r2 % ZB, p = r2 / ZB;
+  float2 v[ZA];
+  if (s2) {
+    const float2 *e = E + (p * KF + kk) * LSE + jj2;
+    regfft::static_for<0, ZA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e[t * (ZB + 1)];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj2 * t);
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+  }
+  __syncthreads();
+  float2 *R = E;  // [p][r][kk], the 2H retained kz rows
+  if (s2) {
+    regfft::dft_reg<ZA, false>(v);
+    regfft::static_for<0, ZA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      constexpr int mlo = ZB * t, mhi = ZB * t + ZB - 1;
+      const int m = jj2 + mlo;
+      int r = -1;
+      if (mlo < H && m < H) r = m;
+      else if (mhi >= N - H && m >= N - H) r = m - N + 2 * H;
+      if (r >= 0) R[((size_t)p * 2 * H + r) * KF + kk] = v[t];
+    });
+  }
+  __syncthreads();
+  // der_x / der_z and the stores, one thread per (kz row, kx)
+  const float s = 1.f / (float)N;
+  const size_t off = (size_t)q * g.ncolF;
+  for (int idx = tid; idx < 2 * H * KF; idx += blockDim.x) {
+    const int r = idx / KF, k2 = idx - r * KF, kx = kx0 + k2;
+    if (kx >= N1h) continue;
+    const int c = gcol(g, r, kx), rg = grow(g, r);
+    const float kxv = g.k1xf[kx], kzv = g.k1zf[rg];
+    const bool zr = (r == H);  // der_x / der_z zero the kz = -N2/2 row
+    if (isU) {
+      const float2 uu = cscale(R[((size_t)0 * 2 * H + r) * KF + k2], s), uw = cscale(R[((size_t)1 * 2 * H + r) * KF + k2], s);
+      const float2 vv = cscale(R[((size_t)2 * 2 * H + r) * KF + k2], s), ww = cscale(R[((size_t)3 * 2 * H + r) * KF + k2], s);
+      float2 n1 = make_float2(0.f, 0.f), n3 = make_float2(0.f, 0.f);
+      if (!zr) {
+        n1 = cadd(cimul(kxv, uu), cimul(kzv, uw));
+        n3 = cadd(cimul(kxv, uw), cimul(kzv, ww));
+      }
+      N1xz[off + c] = n1;
+      N3xz[off + c] = n3;
+      vvc[off + c] = vv;
+    } else {
+      const float2 uv = cscale(R[((size_t)0 * 2 * H + r) * KF + k2], s), wv = cscale(R[((size_t)1 * 2 * H + r) * KF + k2], s);
+      float2 n2 = make_float2(0.f, 0.f);
+      if (!zr) n2 = cadd(cimul(kxv, uv), cimul(kzv, wv));
+      N2xz[off + c] = n2;
+      uvf[off + c] = uv;
+      wvf[off + c] = wv;
+    }
+  }
+}

