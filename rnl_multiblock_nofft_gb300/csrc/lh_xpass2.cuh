@@ -22,11 +22,13 @@
 #include "lh_internal.cuh"
 #include "lh_regfft.cuh"
 
-// row pairs per block (one block: 48 * PB threads at N = 384)
+// row pairs per block (one block: 96 threads at N = 384)
 template <int N> struct xp2 {
   static constexpr int XB = 8, XA = N / XB;
   static constexpr int PB = XA >= 36 ? 2 : (XA >= 18 ? 4 : 8);
-  static constexpr int NT = (XA * PB + 31) / 32 * 32;  // whole warps (the fused stage's shuffles)
+  // threads: enough for every stage (fused: XA PB; the first and last stages: 3 and 4 lines x
+  // PB pairs x XB), in whole warps (the shuffles of the fused and last stages)
+  static constexpr int NT = ((XA * PB > 4 * PB * XB ? XA * PB : 4 * PB * XB) + 31) / 32 * 32;
   // padded shared-memory lines: E1 (stage-1 output e = jj XA + t at e + e / XA), E2
   // (forward stage-1 output e = jj 8 + t at e + e / 8); line strides = 8 (mod 16) float2 so
   // that the lanes of two lines fall on different banks

@@ -58,6 +58,9 @@ WORKLOADS = {
                desc="mid textured channel N 64x64, ny 97, posts"),
     "P": dict(N=192, ny=201, posts=False, flpress=0,
               desc="profiling case: smooth channel N 192x192, ny 201 (state 0.27 GB, above L2)"),
+    "P384": dict(N=256, ny=97, posts=False, flpress=0,
+                 desc="profiling case at the 384-point transforms: smooth channel N 256x256, ny 97 "
+                      "(state 0.26 GB, above L2)"),
     "C4": dict(N=768, Nz=384, ny=385, re_tau=550.0, posts=True, post_period=24, post_points=12,
                post_height_plus=6.0, flpress=0, core=(384, 192),
                desc="multiblock channel: wall bands N 768x384, core band N 384x192, ny 385, Re_tau 550, "
