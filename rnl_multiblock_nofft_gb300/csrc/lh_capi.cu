@@ -18,6 +18,9 @@
 namespace {
 const int NTHR_H = 256;
 }
+#ifndef LH_PRESS_KAPPA32
+#define LH_PRESS_KAPPA32 5000.0
+#endif
 
 struct lh_handle {
   lh_config cfg;
@@ -34,6 +37,9 @@ struct lh_handle {
   double2 *u1, *u2, *u3, *p, *psi;
   void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
   double *dg1, *dg2, *dg3;  // factorised pressure matrices (constant)
+  float *dgf;               // mixed form: FP32 copies of dg1, dg2, dg3 (3 x np x ncol)
+  float *psif;              // mixed form: forward-sweep scratch of the FP32 pressure columns
+  double k2low;             // mixed form: columns with k^2 below this solve the pressure in FP64
   void *ysf, *ysv;  // FP32 scratch of the mixed-form solves (u and w; v)
   void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
   double *a3s, *a3v, *mfw;
@@ -276,6 +282,14 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   for (int b = 0; b < 3; ++b) { g.gw[b][0] = cfg->gw[b][0]; g.gw[b][1] = cfg->gw[b][1]; }
   g.gwbc1 = cfg->gw_bc_u1; g.gwbc3 = cfg->gw_bc_u3;
+  {  // mixed form: the wavenumber below which a pressure column is solved in FP64. The column's
+     // matrix D G - k^2 has a condition number ~ 1 + 2 max|diag(D G)| / k^2; FP32 is used where
+     // that is at most LH_PRESS_KAPPA32 (an FP32 solve error of ~ kappa * 6e-8 at worst)
+    double dmax = 0.0;
+    for (int q = 1; q + 1 < cfg->nyu; ++q)
+      dmax = std::max(dmax, cfg->ddthetavi * cfg->ddthetavi * cfg->dthdyu[q] * (cfg->dthdyv[q - 1] + cfg->dthdyv[q]));
+    h->k2low = 2.0 * dmax / (LH_PRESS_KAPPA32 - 1.0);
+  }
   // multiblock description: wall-band grid, band level ranges (jlim, start.f90:1675-1709)
   g.mb = mb;
   g.N1hF = g.N1h; g.N2F = g.N2; g.ncolF = g.ncol;
@@ -384,6 +398,8 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
   ZA(h->Nu1, vs * nu * nc); ZA(h->Nu3, vs * nu * nc); ZA(h->Nu2, vs * nv * nc);
   ZA(h->dg1, sizeof(double) * g.np * nc); ZA(h->dg2, sizeof(double) * g.np * nc); ZA(h->dg3, sizeof(double) * g.np * nc);
+  h->dgf = nullptr; h->psif = nullptr;
+  if (h->prec == LH_PREC_MIXED) { ZA(h->dgf, 3 * sizeof(float) * g.np * nc); ZA(h->psif, 2 * sizeof(float) * g.np * nc); }
   if (h->prec == LH_PREC_MIXED) { ZA(h->ysf, 2 * sizeof(float4) * nu * nc); ZA(h->ysv, 2 * sizeof(float2) * nv * nc); }
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
@@ -626,6 +642,12 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   {  // pressure factors, once (start.f90:656-658)
     const int nb = (g.nvc + NTHR_H - 1) / NTHR_H;
     k_build_dg<<<nb, NTHR_H, 0, h->st>>>(h->dg1, h->dg2, h->dg3, g);
+    if (h->prec == LH_PREC_MIXED) {
+      const size_t n1 = (size_t)g.np * nc;
+      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg1, h->dgf, n1);
+      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg2, h->dgf + n1, n1);
+      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg3, h->dgf + 2 * n1, n1);
+    }
     cudaError_t e = cudaStreamSynchronize(h->st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("k_build_dg: ") + cudaGetErrorString(e)); lh_destroy(h); return rc; }
@@ -648,7 +670,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
 extern "C" int lh_destroy(lh_handle *h) {
   if (!h) return LH_EINVAL;
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
-  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
+  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->dgf, h->psif, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_ibrec, h->d_iboff, h->cap, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
@@ -1263,9 +1285,17 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
   const size_t ptab = sizeof(double) * (size_t)(g.nu + g.nv);  // the kernel's per-level factor tables
-  KL("k_press", k_press2<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
-                                                    (double *)h->p, (double *)h->psi, h->dg1, h->dg2, h->dg3, g,
-                                                    h->sc, kRK, need_div));
+  if (h->prec == LH_PREC_FP64) {
+    KL("k_press", k_press2<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
+                                                      (double *)h->p, (double *)h->psi, h->dg1, h->dg2, h->dg3, g,
+                                                      h->sc, kRK, need_div));
+  } else {
+    const size_t n1 = (size_t)g.np * g.ncol;
+    KL("k_press", k_press_mx<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
+                                                        (double *)h->p, (double *)h->psi, h->psif, h->dg1, h->dg2,
+                                                        h->dg3, h->dgf, h->dgf + n1, h->dgf + 2 * n1, g, h->sc, kRK,
+                                                        need_div, h->k2low));
+  }
   if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
 }

@@ -148,7 +148,8 @@ def test_c4_multiblock_mixed_one_step(cuda_ok, c4_reference):
         for name, x, y in zip(FIELDS, ref[band], got[band]):
             e = relerr(y, x)
             assert e < (PRESS_MIXED if name == "p" else TOL_MIXED_VEL), (band, name, e)
-    assert gsc["t"] == pytest.approx(sc["t"], rel=1e-12)
+    # dt comes from the CFL maxima of the FP32 physical velocities
+    assert gsc["t"] == pytest.approx(sc["t"], rel=1e-6)
 
 
 LENGTHS = (24, 48, 72, 96, 144, 192, 288, 384, 576, 768, 1152)
