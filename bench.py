@@ -209,7 +209,7 @@ def column_levels(s, grid: int) -> int:
     return tot
 
 
-def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0) -> float:
+def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0, ib: bool = True) -> float:
     """Compulsory HBM bytes of one substep's launches of a kernel: every input and
     output element once. Spectral fields are complex128; the transform intermediates
     are complex128 in the FP64 form and complex64 in the mixed form. The triad kernel
@@ -228,7 +228,7 @@ def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0) -> float:
             tot += A + B
         elif kernel == "k_zfwd_nl":
             tot += B + (nuI + nvI) * 3 * ncv * z
-    if kernel == "k_xpass_nl" and s.dny > 0 and s.p.ib_enable and s.p.geometry_type == 2:
+    if kernel == "k_xpass_nl" and ib and s.dny > 0 and s.p.ib_enable and s.p.geometry_type == 2:
         # physical planes of the immersed-boundary levels (and the two tip levels) captured
         # for the forcing: 3 fields, FP64
         tot += (4 * s.dny + 2) * 3 * s.G1 * s.G2 * 8
@@ -436,6 +436,92 @@ def run_ensemble(args, ws, rank, pg, torch, np):
         print(json.dumps(line), flush=True)
 
 
+def e2e_run(s, form, tl, ic, icb, sc0, steps, ws, pg, torch, np):
+    """The metric through the C ABI: every step's state copied in from pinned host memory and
+    the result copied back (queued lh_upload_state_async / lh_download_state_async, per band
+    for multiblock channels), timed on the host clock around the whole chain."""
+    from rnl_multiblock_nofft_gb300.native import GpuChannel
+    mb = icb is not None
+    g = GpuChannel(s, form, triads=tl)
+    shapes = [sh for b in (1, 2, 3) for sh in s.band_shapes(b)] if mb else list(g.shapes)
+    pin = lambda sh: torch.empty(tuple(sh) + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+    pinned = [pin(sh) for sh in shapes]
+    for dst, src in zip(pinned, ic):
+        dst[...] = src
+    pinned_out = [pin(sh) for sh in shapes]
+    if mb:
+        g.upload_bands({b: pinned[4 * (b - 1):4 * b] for b in (1, 2, 3)})
+    else:
+        g.upload_state(*pinned)
+    g.set_scalars(**sc0)
+    g.step(1)
+    g.synchronize()
+    barrier(pg)
+    nb = sum(a.nbytes for a in pinned)
+    t0 = time.perf_counter()
+    if mb:
+        bin_ = {b: pinned[4 * (b - 1):4 * b] for b in (1, 2, 3)}
+        bout = {b: pinned_out[4 * (b - 1):4 * b] for b in (1, 2, 3)}
+        for _ in range(steps):
+            g.upload_bands_async(bin_)
+            g.step(1)
+            g.download_bands_async(bout)
+    else:
+        for _ in range(steps):
+            g.upload_state_async(*pinned)
+            g.step(1)
+            g.download_state_async(pinned_out)
+    g.synchronize()
+    e2e_s = reduce_max(pg, time.perf_counter() - t0)
+    g.close()
+    return {"value": ws * s.mode_points() * 3 * steps / e2e_s / 1e6, "unit": UNIT,
+            "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
+
+
+def kernel_roofline(s, kern, form, tl, peak, peak_kind, workload):
+    """Roofline of the kernel with the largest share of the step (live per-kernel CUDA-event
+    times of one eager step): algorithmic bytes per launch / average launch time."""
+    dom = max(kern.items(), key=lambda kv: kv[1][1])
+    dname, (dlaunch, dms) = dom
+    alg_step = 3 * algorithmic_bytes(s, dname, form, triad_terms(s, tl) if tl is not None else 0)
+    achieved = alg_step / (dms * 1e-3) / 1e9
+    alg = alg_step / dlaunch
+    if not math.isfinite(achieved):  # a kernel without an algorithmic byte count
+        achieved = alg = None
+    step_total = sum(v[1] for v in kern.values())
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak if achieved is not None else None,
+           "traffic": traffic_table().get((workload, dname, form)), "kernel": dname,
+           "kernel_share": dms / step_total, "avg_launch_ms": dms / dlaunch,
+           "algorithmic_bytes_per_launch": alg, "peak_source": peak_kind}
+    if dname == "k_xpass_nl":  # the same without the captured physical planes of the immersed levels
+        ab = 3 * algorithmic_bytes(s, dname, form, ib=False) / (dms * 1e-3) / 1e9
+        out["frac_A_B_only"] = ab / peak
+    return out
+
+
+def step_roofline(s, form, ms_per_step, peak, peak_kind):
+    """The whole step against the HBM roofline with fixed algorithmic bytes per mode-point and
+    substep: 960 B (FP64 form) / 736 B (mixed form), plus 210 B x (immersed levels / ny) with
+    posts."""
+    b = 960.0 if form == "fp64" else 736.0
+    ib = 210.0 * (2 * s.dny) / s.p.ny if (s.dny > 0 and s.p.geometry_type == 2) else 0.0
+    per_s = s.mode_points() * 3 / (ms_per_step * 1e-3)
+    ach = (b + ib) * per_s / 1e9
+    return {"bytes_per_mode_point": b, "ib_bytes_per_mode_point": ib, "achieved": ach, "peak": peak,
+            "unit": "GB/s", "frac": ach / peak, "frac_without_ib": b * per_s / 1e9 / peak, "peak_source": peak_kind}
+
+
+def fp64_rate(s, ms_per_step):
+    """FP64 flop rate of the FP64 form: 12 transforms of 2.5 log2(Ngal1 Ngal2) flops per physical
+    point (2.25 physical points per mode-point) + ~150 flops of solves per mode-point and
+    substep, against the nominal FP64 rate of the part (1.25 TFLOP/s, not measured here)."""
+    per_pt = 12 * 2.5 * math.log2(s.G1 * s.G2) * (s.G1 * s.G2) / (s.N1 * s.N2) + 150.0
+    gf = per_pt * s.mode_points() * 3 / (ms_per_step * 1e-3) / 1e9
+    return {"flops_per_mode_point": per_pt, "achieved_gflops": gf, "nominal_gflops": 1250.0,
+            "frac_of_nominal": gf / 1250.0}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -523,71 +609,17 @@ def main():
         head = forms[0]
     R = res[head]
 
-    # e2e through the C ABI: pinned host state in, step, state out, every step (queued
-    # lh_upload_state_async / lh_download_state_async, per band for multiblock channels)
-    g = GpuChannel(s, head, triads=tl)
-    shapes = [sh for b in (1, 2, 3) for sh in s.band_shapes(b)] if mb else list(g.shapes)
-    pin = lambda sh: torch.empty(tuple(sh) + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
-    pinned = [pin(sh) for sh in shapes]
-    for dst, src in zip(pinned, ic):
-        dst[...] = src
-    pinned_out = [pin(sh) for sh in shapes]
-
-    def put(arrs):
-        if mb:
-            g.upload_bands({b: arrs[4 * (b - 1):4 * b] for b in (1, 2, 3)})
-        else:
-            g.upload_state(*arrs)
-
-    put(pinned)
-    g.set_scalars(**sc0)
-    g.step(1)
-    g.synchronize()
-    barrier(pg)
-    nb = sum(a.nbytes for a in pinned)
-    t0 = time.perf_counter()
-    # queued I/O: every step's input copied in and its result copied out on copy streams
-    # that overlap the neighbouring steps' kernels
-    if mb:
-        bin_ = {b: pinned[4 * (b - 1):4 * b] for b in (1, 2, 3)}
-        bout = {b: pinned_out[4 * (b - 1):4 * b] for b in (1, 2, 3)}
-        for _ in range(args.steps):
-            g.upload_bands_async(bin_)
-            g.step(1)
-            g.download_bands_async(bout)
-    else:
-        for _ in range(args.steps):
-            g.upload_state_async(*pinned)
-            g.step(1)
-            g.download_state_async(pinned_out)
-    g.synchronize()
-    e2e_s = reduce_max(pg, time.perf_counter() - t0)
-    g.close()
-    e2e = {"value": ws * pts * 3 * args.steps / e2e_s / 1e6, "unit": UNIT,
-           "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
-    del pinned_out
-
-    # roofline of the dominant kernel (largest share of the step)
-    kern = R["kernels"]
-    dom = max(kern.items(), key=lambda kv: kv[1][1])
-    dname, (dlaunch, dms) = dom
-    avg_ms = dms / dlaunch
-    alg_step = 3 * algorithmic_bytes(s, dname, head, triad_terms(s, tl) if tl is not None else 0)
-    alg = alg_step / dlaunch
     peak, peak_kind = measured_peaks()
-    achieved = alg_step / (dms * 1e-3) / 1e9
-    if not math.isfinite(achieved):  # a kernel without an algorithmic byte count
-        achieved = alg = None
-    tt = traffic_table().get((args.workload, dname, head))
-    step_total = sum(v[1] for v in kern.values())
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved is not None else None, "traffic": tt, "kernel": dname,
-                "kernel_share": dms / step_total, "avg_launch_ms": avg_ms,
-                "algorithmic_bytes_per_launch": alg, "peak_source": peak_kind}
+    for form, r in res.items():
+        r["e2e"] = e2e_run(s, form, tl, ic, icb if mb else None, sc0, args.steps, ws, pg, torch, np)
+        r["roofline"] = kernel_roofline(s, r["kernels"], form, tl, peak, peak_kind, args.workload)
+        r["step_roofline"] = step_roofline(s, form, r["ms"] / args.steps, peak, peak_kind)
+        if form == "fp64":
+            r["fp64_rate"] = fp64_rate(s, r["ms"] / args.steps)
     line = {"metric": METRIC, "value": R["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": R["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if head == "fp64" else "f32 transforms/products, f64 state and solves",
+            "dtype": "f64" if head == "fp64" else "f32 transforms/products/solves, f64 state, (0,0) mode and low-k pressure",
             "data": "synthetic (seeded perturbed laminar channel, see rnl_multiblock_nofft_gb300/workloads.py)",
             "config": {"workload": f"{args.workload}: {workload_desc(args.workload)}", "form": head,
                        "mode_points_per_substep": pts, "N1": s.N1, "N2": s.N2, "ny": s.p.ny,
@@ -595,8 +627,11 @@ def main():
                        "ny_with_immersed_region": s.nyv, "Ngal": [s.G1, s.G2],
                        "l2": "inputs larger than L2 (state ~%.0f MB)" % (sum(a.nbytes for a in ic) / 1e6),
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
-            "roofline": roofline, "gpu_launches": R["launches"], "clocks": R["clocks"], "e2e": e2e,
+            "roofline": R["roofline"], "step_roofline": R["step_roofline"], "gpu_launches": R["launches"],
+            "clocks": R["clocks"], "e2e": R["e2e"],
             "forms": {f: {"value": r["value"], "ms_per_step": r["ms"] / args.steps, "scalars": r["scalars"],
+                          "roofline": r["roofline"], "step_roofline": r["step_roofline"], "e2e": r["e2e"],
+                          **({"fp64_rate": r["fp64_rate"]} if "fp64_rate" in r else {}),
                           "kernel_ms_per_step": {k: v[1] for k, v in r["kernels"].items()}}
                       for f, r in res.items()},
             "mixed_rel_err_vs_fp64": relerr}

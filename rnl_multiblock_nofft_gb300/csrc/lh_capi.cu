@@ -18,9 +18,7 @@
 namespace {
 const int NTHR_H = 256;
 }
-#ifndef LH_PRESS_KAPPA32
-#define LH_PRESS_KAPPA32 5000.0
-#endif
+
 
 struct lh_handle {
   lh_config cfg;
@@ -37,9 +35,6 @@ struct lh_handle {
   double2 *u1, *u2, *u3, *p, *psi;
   void *Nu1, *Nu2, *Nu3;  // nonlinear term of the last substep, transform precision
   double *dg1, *dg2, *dg3;  // factorised pressure matrices (constant)
-  float *dgf;               // mixed form: FP32 copies of dg1, dg2, dg3 (3 x np x ncol)
-  float *psif;              // mixed form: forward-sweep scratch of the FP32 pressure columns
-  double k2low;             // mixed form: columns with k^2 below this solve the pressure in FP64
   void *ysf, *ysv;  // FP32 scratch of the mixed-form solves (u and w; v)
   void *N1xz, *N2xz, *N3xz, *uvf, *vvc, *wvf;  // transform outputs, transform precision
   double *a3s, *a3v, *mfw;
@@ -91,6 +86,7 @@ struct lh_handle {
   bool graph_ready;
   long long launches;
   int tb_uw, tb_v, tb_p;  // threads per block of the one-thread-per-column kernels (lh_autotune)
+  int pf_p;               // levels the pressure kernel stages ahead through shared memory (lh_autotune)
   std::string err;
   // per-kernel timing (lh_profile_steps): events around each launch
   bool prof;
@@ -265,6 +261,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->graph_ready = false;
   h->launches = 0;
   h->tb_uw = h->tb_v = h->tb_p = 128;
+  h->pf_p = 4;
   if (!size_supported(cfg->Ngal1) || !size_supported(cfg->Ngal2)) {
     int rc = fail(h, LH_EINVAL, "Ngal must be one of 24 48 72 96 144 192 288 384 576 768 1152");
     delete h;
@@ -282,14 +279,6 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   for (int b = 0; b < 3; ++b) { g.gw[b][0] = cfg->gw[b][0]; g.gw[b][1] = cfg->gw[b][1]; }
   g.gwbc1 = cfg->gw_bc_u1; g.gwbc3 = cfg->gw_bc_u3;
-  {  // mixed form: the wavenumber below which a pressure column is solved in FP64. The column's
-     // matrix D G - k^2 has a condition number ~ 1 + 2 max|diag(D G)| / k^2; FP32 is used where
-     // that is at most LH_PRESS_KAPPA32 (an FP32 solve error of ~ kappa * 6e-8 at worst)
-    double dmax = 0.0;
-    for (int q = 1; q + 1 < cfg->nyu; ++q)
-      dmax = std::max(dmax, cfg->ddthetavi * cfg->ddthetavi * cfg->dthdyu[q] * (cfg->dthdyv[q - 1] + cfg->dthdyv[q]));
-    h->k2low = 2.0 * dmax / (LH_PRESS_KAPPA32 - 1.0);
-  }
   // multiblock description: wall-band grid, band level ranges (jlim, start.f90:1675-1709)
   g.mb = mb;
   g.N1hF = g.N1h; g.N2F = g.N2; g.ncolF = g.ncol;
@@ -398,8 +387,6 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   ZA(h->u1, cz * nu * nc); ZA(h->u3, cz * nu * nc); ZA(h->u2, cz * nv * nc); ZA(h->p, cz * g.np * nc);
   ZA(h->Nu1, vs * nu * nc); ZA(h->Nu3, vs * nu * nc); ZA(h->Nu2, vs * nv * nc);
   ZA(h->dg1, sizeof(double) * g.np * nc); ZA(h->dg2, sizeof(double) * g.np * nc); ZA(h->dg3, sizeof(double) * g.np * nc);
-  h->dgf = nullptr; h->psif = nullptr;
-  if (h->prec == LH_PREC_MIXED) { ZA(h->dgf, 3 * sizeof(float) * g.np * nc); ZA(h->psif, 2 * sizeof(float) * g.np * nc); }
   if (h->prec == LH_PREC_MIXED) { ZA(h->ysf, 2 * sizeof(float4) * nu * nc); ZA(h->ysv, 2 * sizeof(float2) * nv * nc); }
   ZA(h->N1xz, vs * nu * nc); ZA(h->N3xz, vs * nu * nc); ZA(h->vvc, vs * nu * nc);
   ZA(h->N2xz, vs * nv * nc); ZA(h->uvf, vs * nv * nc); ZA(h->wvf, vs * nv * nc);
@@ -602,6 +589,14 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
+  {
+    int lim = 0;
+    if (smem_optin(&lim) || cudaFuncSetAttribute((const void *)k_press3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_press3<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_press3<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+      rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_press3)"); lh_destroy(h); return rc;
+    }
+  }
   if (cudaFuncSetAttribute((const void *)k_helm00_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(8 * sizeof(double) * (size_t)(std::max(nu, nv) + 1))) != cudaSuccess) {
     rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_helm00_pcr)"); lh_destroy(h); return rc;
@@ -642,12 +637,6 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   {  // pressure factors, once (start.f90:656-658)
     const int nb = (g.nvc + NTHR_H - 1) / NTHR_H;
     k_build_dg<<<nb, NTHR_H, 0, h->st>>>(h->dg1, h->dg2, h->dg3, g);
-    if (h->prec == LH_PREC_MIXED) {
-      const size_t n1 = (size_t)g.np * nc;
-      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg1, h->dgf, n1);
-      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg2, h->dgf + n1, n1);
-      k_dg_to_f32<<<1024, 256, 0, h->st>>>(h->dg3, h->dgf + 2 * n1, n1);
-    }
     cudaError_t e = cudaStreamSynchronize(h->st);
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("k_build_dg: ") + cudaGetErrorString(e)); lh_destroy(h); return rc; }
@@ -670,7 +659,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
 extern "C" int lh_destroy(lh_handle *h) {
   if (!h) return LH_EINVAL;
   if (h->graph_ready) { cudaGraphExecDestroy(h->gexec); cudaGraphDestroy(h->graph); }
-  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->dgf, h->psif, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
+  void *bufs[] = {h->u1, h->u2, h->u3, h->p, h->Nu1, h->Nu2, h->Nu3, h->dg1, h->dg2, h->dg3, h->ysf, h->N1xz, h->N2xz, h->N3xz, h->uvf, h->vvc,
                   h->wvf, h->psi, h->a3s, h->mfw, h->A, h->B, h->twx, h->twz, h->twx64, h->twz64, h->geo_pool, h->geo_poolf, h->sc, h->stage,
                   h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_ibrec, h->d_iboff, h->cap, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
@@ -1285,16 +1274,16 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
   const size_t ptab = sizeof(double) * (size_t)(g.nu + g.nv);  // the kernel's per-level factor tables
-  if (h->prec == LH_PREC_FP64) {
-    KL("k_press", k_press2<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
-                                                      (double *)h->p, (double *)h->psi, h->dg1, h->dg2, h->dg3, g,
-                                                      h->sc, kRK, need_div));
-  } else {
-    const size_t n1 = (size_t)g.np * g.ncol;
-    KL("k_press", k_press_mx<<<nbp2, h->tb_p, ptab, h->st>>>((double *)h->u1, (double *)h->u2, (double *)h->u3,
-                                                        (double *)h->p, (double *)h->psi, h->psif, h->dg1, h->dg2,
-                                                        h->dg3, h->dgf, h->dgf + n1, h->dgf + 2 * n1, g, h->sc, kRK,
-                                                        need_div, h->k2low));
+  {  // the pressure step with its y-columns staged pf_p levels ahead (k_press3)
+    const size_t sm = sizeof(double) * (((size_t)g.nu + g.nv + 1) & ~(size_t)1) +
+                      sizeof(double) * 6 * (size_t)(h->pf_p + 1) * h->tb_p;
+    double *U1 = (double *)h->u1, *U2 = (double *)h->u2, *U3 = (double *)h->u3, *P = (double *)h->p;
+    double *PS = (double *)h->psi;
+    switch (h->pf_p) {
+      case 2: KL("k_press", k_press3<2><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
+      case 8: KL("k_press", k_press3<8><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
+      default: KL("k_press", k_press3<4><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
+    }
   }
   if (need_div) KL("k_err_from_bits", k_err_from_bits<<<1, 32, 0, h->st>>>(h->sc));
   return LH_OK;
@@ -1609,23 +1598,35 @@ extern "C" int lh_autotune(lh_handle *h) {
   };
   cudaError_t e = copy_all(true);
   if (e != cudaSuccess) { cudaFree(save); return fail(h, LH_ECUDA, cudaGetErrorString(e)); }
-  const int cand[] = {64, 128, 256};
+  // trials: every block size with every staging depth of the pressure kernel; each kernel
+  // keeps the configuration of its fastest trial (the Helmholtz kernels depend on the block
+  // size only)
+  const int cand[] = {64, 128, 256}, cpf[] = {2, 4, 8};
   double best[3] = {1e30, 1e30, 1e30};
-  int pick[3] = {h->tb_uw, h->tb_v, h->tb_p};
+  int pick[3] = {h->tb_uw, h->tb_v, h->tb_p}, pick_pf = h->pf_p;
   const char *names[3] = {"k_helm_uw", "k_helm_v", "k_press"};
   lh_kernel_time kt[64];
   int rc = LH_OK;
-  for (int ci = 0; ci < 3 && rc == LH_OK; ++ci) {
-    h->tb_uw = h->tb_v = h->tb_p = cand[ci];
+  int optin = 0;
+  if (smem_optin(&optin)) optin = 49152;
+  for (int ti = 0; ti < 9 && rc == LH_OK; ++ti) {
+    const int tb = cand[ti % 3], pf = cpf[ti / 3];
+    if (sizeof(double) * (((size_t)g.nu + g.nv + 1 + 6 * (size_t)(pf + 1) * tb)) > (size_t)optin) continue;
+    h->tb_uw = h->tb_v = h->tb_p = tb;
+    h->pf_p = pf;
     int n = 0;
     rc = lh_profile_steps(h, 1, kt, 64, &n);
     for (int k = 0; k < 3 && rc == LH_OK; ++k)
       for (int i = 0; i < n; ++i)
-        if (strncmp(kt[i].name, names[k], 32) == 0 && kt[i].total_ms < best[k]) { best[k] = kt[i].total_ms; pick[k] = cand[ci]; }
+        if (strncmp(kt[i].name, names[k], 32) == 0 && kt[i].total_ms < best[k]) {
+          best[k] = kt[i].total_ms;
+          pick[k] = tb;
+          if (k == 2) pick_pf = pf;
+        }
     if (copy_all(false) != cudaSuccess) rc = fail(h, LH_ECUDA, "state restore failed");
   }
   cudaFree(save);
-  h->tb_uw = pick[0]; h->tb_v = pick[1]; h->tb_p = pick[2];
+  h->tb_uw = pick[0]; h->tb_v = pick[1]; h->tb_p = pick[2]; h->pf_p = pick_pf;
   if (h->graph_ready) {  // recapture with the chosen configuration
     cudaGraphExecDestroy(h->gexec);
     cudaGraphDestroy(h->graph);

@@ -1506,90 +1506,124 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
 }
 
 // ============================================================================
-// Mixed form of the pressure step. The right-hand side, dti/(a+b) div u, is the residual of
-// the zero guess and is formed in FP64 from the FP64 state; the correction psi is solved
-// with FP32 factors and FP32 sweeps, and every update of the state (p += psi, v_corr) is
-// FP64. The FP32 solve's relative error grows with the condition number of the column's
-// matrix (~1 + 4 / (k^2 h_min^2)), so the gauge column (0,0) and the columns with
-// k^2 < k2low (the lowest wavenumbers) take the FP64 path instead: the same sweeps with the
-// FP64 factors (tridLU_3D.f90:192-226). press_lane<S> is one lane's work (column c, band bd,
-// real or imaginary part), S the solve precision; dga/dgb/dgc the factors and ps the
-// forward-sweep scratch in S. As k_press2 otherwise.
+// The pressure step of k_press2 with the y-columns staged through shared memory: every lane
+// keeps a ring of D + 1 levels of its inputs, filled by cp.async copies issued D levels ahead
+// of the sweep (into the slot not being read), so that D memory latencies overlap without
+// holding the prefetched values in registers (the solves have few warps per SM: one lane per
+// column and part). Same arithmetic as k_press2, so the same results bit for bit. Shared
+// memory: the per-level factor tables (nu + nv doubles) and the ring, 6 (D + 1) doubles per
+// thread.
 // ============================================================================
-// conversions between the solve precision and FP64 (FP32: on the integer pipe, see d2f_alu)
-__device__ __forceinline__ double s2d(double x) { return x; }
-__device__ __forceinline__ double s2d(float x) { return f2d_alu(x); }
-template <typename S> __device__ __forceinline__ S d2s(double x) { return to_t<S>(x); }
+__device__ __forceinline__ void cpa8(double *dst, const double *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <typename S>
-__device__ __forceinline__ void press_lane(double *__restrict__ u1, double *__restrict__ u2, double *__restrict__ u3,
-                                           double *__restrict__ p, S *__restrict__ ps, const S *__restrict__ dga,
-                                           const S *__restrict__ dgb, const S *__restrict__ dgc, const Geo &g,
-                                           const double *__restrict__ ptab, int c, int bd, int part, unsigned pm,
-                                           double dti, double dt, double aRb, int need_div, double &dmax) {
+template <int D>
+__global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double *__restrict__ u2,
+                                                 double *__restrict__ u3, double *__restrict__ p,
+                                                 double *__restrict__ psi, const double *__restrict__ dg1,
+                                                 const double *__restrict__ dg2, const double *__restrict__ dg3, Geo g,
+                                                 DevScalars *sc, int kRK, int need_div) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = tid >> 1, part = tid & 1;
+  const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
   const int nc = g.ncol;
-  const int plo = g.bq[bd][4], phi = g.bq[bd][5];
-  const int ulo = g.bq[bd][0], uhi = g.bq[bd][1], vlo = g.bq[bd][2], vhi = g.bq[bd][3];
-  const int r = c / g.N1h, kx = c - r * g.N1h;
-  const double kxv = g.k1x[kx], kzv = g.k1z[r];
-  const double sgn = part ? 1.0 : -1.0;
-  const double skx = sgn * kxv, skz = sgn * kzv;
-  const double dtirk = dti / aRb;
-  const size_t ls = (size_t)nc * 2;
-  const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
-  const double dskx = dtirk * skx, dskz = dtirk * skz;
-  S y = 0;
-  double vm = u2[(size_t)plo * ls + ci];
-  {  // forward sweep: the FP64 divergence as right-hand side, S elimination; inputs one level ahead
-    double fa = u1[(size_t)(plo + 1) * ls + co], fw = u3[(size_t)(plo + 1) * ls + co], fv = u2[(size_t)(plo + 1) * ls + ci];
-    S f1 = dga[(size_t)plo * nc + c], f2 = dgb[(size_t)plo * nc + c];
+  double dmax = 0.0;
+  extern __shared__ double ptab[];
+  const int nt = blockDim.x;
+  double *ring = ptab + ((g.nu + g.nv + 1) & ~1);  // [D + 1][6][nt]
+  constexpr int NS = D + 1;
+  {
+    const double aRb0 = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dti0 = sc->dti / aRb0, dtk0 = sc->dt * aRb0 * g.dd;
+    for (int i = threadIdx.x; i < g.nu; i += blockDim.x) ptab[i] = dti0 * g.thud[i];
+    for (int i = threadIdx.x; i < g.nv; i += blockDim.x) ptab[g.nu + i] = dtk0 * g.thv[i];
+    __syncthreads();
+  }
+#define RS(s_, f_) ring[((s_) * 6 + (f_)) * nt + threadIdx.x]
+  if (vc < g.nvc) {
+    int c, bd;
+    vcol_of(g, vc, c, bd);
+    const int plo = g.bq[bd][4], phi = g.bq[bd][5];
+    const int ulo = g.bq[bd][0], uhi = g.bq[bd][1], vlo = g.bq[bd][2], vhi = g.bq[bd][3];
+    const int r = c / g.N1h, kx = c - r * g.N1h;
+    const double kxv = g.k1x[kx], kzv = g.k1z[r];
+    const double sgn = part ? 1.0 : -1.0;
+    const double skx = sgn * kxv, skz = sgn * kzv;
+    const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
+    const double dtirk = sc->dti / aRb;
+    const double dt = sc->dt;
+    const size_t ls = (size_t)nc * 2;
+    const size_t ci = (size_t)c * 2 + part, co = (size_t)c * 2 + (part ^ 1);
+    const double dskx = dtirk * skx, dskz = dtirk * skz;
+    double y = 0.0;
+    double vm = u2[(size_t)plo * ls + ci];
+    // forward sweep: level qp's inputs (u1, u3 of the other part, v, dg1, dg2) in ring slot qp % D
+    auto fetch_f = [&](int qp) {
+      const int s_ = (qp - plo) % NS;
+      const size_t e_ = (size_t)(qp + 1) * ls;
+      cpa8(&RS(s_, 0), u1 + e_ + co); cpa8(&RS(s_, 1), u3 + e_ + co); cpa8(&RS(s_, 2), u2 + e_ + ci);
+      cpa8(&RS(s_, 3), dg1 + (size_t)qp * nc + c); cpa8(&RS(s_, 4), dg2 + (size_t)qp * nc + c);
+    };
+#pragma unroll
+    for (int s_ = 0; s_ < D; ++s_) {
+      if (plo + s_ <= phi) fetch_f(plo + s_);
+      cpa_commit();
+    }
     for (int qp = plo; qp <= phi; ++qp) {
-      const double ao = fa, wo = fw, v = fv;
-      const S A1 = f1, a2p = f2;
+      cpa_wait<D - 1>();
+      const int s_ = (qp - plo) % NS;
+      const double ao = RS(s_, 0), wo = RS(s_, 1), v = RS(s_, 2), A1 = RS(s_, 3), a2p = RS(s_, 4);
       const double th = ptab[qp + 1];
-      if (qp + 1 <= phi) {
-        const size_t e_ = (size_t)(qp + 2) * ls;
-        fa = u1[e_ + co]; fw = u3[e_ + co]; fv = u2[e_ + ci];
-        f1 = dga[(size_t)(qp + 1) * nc + c]; f2 = dgb[(size_t)(qp + 1) * nc + c];
-      }
+      if (qp + D <= phi) fetch_f(qp + D);
+      cpa_commit();
       double rhs = (dskx * ao + dskz * wo) + th * (v - vm);
       vm = v;
       if (qp == plo && c == 0 && bd == 1) rhs = 0.0;
-      const S rs = d2s<S>(rhs);
-      y = (qp == plo) ? rs * a2p : (rs - A1 * y) * a2p;
-      ps[(size_t)qp * ls + ci] = y;
+      y = (qp == plo) ? rhs * a2p : (rhs - A1 * y) * a2p;
+      psi[(size_t)qp * ls + ci] = y;
     }
-  }
-  const double dtrk = dt * aRb;
-  const double kxd = dtrk * kxv, kzd = dtrk * kzv;
-  S xn = y;
-  double vup = 0.0, aup_o = 0.0, wup_o = 0.0;
-  {  // backward sweep in S, the state updates (p, v_corr) and the corrected divergence in FP64
-    S bs = ps[(size_t)phi * ls + ci], b3 = dgc[(size_t)phi * nc + c];
-    double bp = p[(size_t)phi * ls + ci];
-    double bu = u1[(size_t)(phi + 1) * ls + ci], bw = u3[(size_t)(phi + 1) * ls + ci], bv = u2[(size_t)(phi + 1) * ls + ci];
+    cpa_wait<0>();
+    __threadfence_block();  // the backward sweep's copies read psi written above by this thread
+    const double dtrk = dt * aRb;
+    const double kxd = dtrk * kxv, kzd = dtrk * kzv;
+    double xn = y;
+    double vup = 0.0, aup_o = 0.0, wup_o = 0.0;
+    // backward sweep: level qp's inputs (psi, dg3, p, u1, u3, v of this part) in slot (phi - qp) % D
+    auto fetch_b = [&](int qp) {
+      const int s_ = (phi - qp) % NS;
+      const size_t e_ = (size_t)(qp + 1) * ls + ci;
+      cpa8(&RS(s_, 0), psi + (size_t)qp * ls + ci); cpa8(&RS(s_, 1), dg3 + (size_t)qp * nc + c);
+      cpa8(&RS(s_, 2), p + (size_t)qp * ls + ci);
+      cpa8(&RS(s_, 3), u1 + e_); cpa8(&RS(s_, 4), u3 + e_); cpa8(&RS(s_, 5), u2 + e_);
+    };
+#pragma unroll
+    for (int s_ = 0; s_ < D; ++s_) {
+      if (phi - s_ >= plo) fetch_b(phi - s_);
+      cpa_commit();
+    }
     for (int qp = phi; qp >= plo; --qp) {
+      cpa_wait<D - 1>();
+      const int s_ = (phi - qp) % NS;
       const int q = qp + 1;
       const size_t e = (size_t)q * ls;
-      const S sps = bs, d3 = b3;
-      const double pq = bp, uq = bu, wq = bw;
-      double v = bv;
+      const double ps = RS(s_, 0), d3 = RS(s_, 1), pq = RS(s_, 2), uq = RS(s_, 3), wq = RS(s_, 4);
+      double v = RS(s_, 5);
       const double thv = ptab[g.nu + q], thu1 = g.thud[qp + 2];
-      if (qp - 1 >= plo) {
-        const size_t e_ = (size_t)qp * ls + ci;
-        bs = ps[(size_t)(qp - 1) * ls + ci]; b3 = dgc[(size_t)(qp - 1) * nc + c];
-        bp = p[(size_t)(qp - 1) * ls + ci];
-        bu = u1[e_]; bw = u3[e_]; bv = u2[e_];
-      }
-      const S x = (qp == phi) ? xn : sps - d3 * xn;
-      p[(size_t)qp * ls + ci] = pq + s2d(x);
-      const double xo = s2d(__shfl_xor_sync(pm, x, 1));
+      if (qp - D >= plo) fetch_b(qp - D);
+      cpa_commit();
+      const double x = (qp == phi) ? xn : ps - d3 * xn;
+      p[(size_t)qp * ls + ci] = pq + x;
+      const double xo = __shfl_xor_sync(pm, x, 1);
       const double a = uq - sgn * kxd * xo;
       const double w = wq - sgn * kzd * xo;
       u1[e + ci] = a;
       u3[e + ci] = w;
       if (q <= vhi - 1) {
-        v = v - thv * s2d(xn - x);
+        v = v - thv * (xn - x);
         u2[e + ci] = v;
       }
       const double ao = __shfl_xor_sync(pm, a, 1), wo = __shfl_xor_sync(pm, w, 1);
@@ -1601,63 +1635,28 @@ __device__ __forceinline__ void press_lane(double *__restrict__ u1, double *__re
       aup_o = ao; wup_o = wo; vup = v;
       xn = x;
     }
+    cpa_wait<0>();
+    if (need_div) {
+      const double th = g.thud[plo + 1];
+      const double vb = u2[(size_t)plo * ls + ci];
+      const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
+      const double d2 = dvp * dvp;
+      dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+    }
+    if (bd <= 1) {
+      u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
+      u3[(size_t)ulo * ls + ci] = g.gwbc3 * u3[(size_t)(ulo + 1) * ls + ci];
+    }
+    if (bd >= 1) {
+      u1[(size_t)uhi * ls + ci] = g.gwbc1 * u1[(size_t)(uhi - 1) * ls + ci];
+      u3[(size_t)uhi * ls + ci] = g.gwbc3 * u3[(size_t)(uhi - 1) * ls + ci];
+    }
+    u2[(size_t)vlo * ls + ci] = 0.0;
+    u2[(size_t)vhi * ls + ci] = 0.0;
   }
-  if (need_div) {
-    const double th = g.thud[plo + 1];
-    const double vb = u2[(size_t)plo * ls + ci];
-    const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
-    const double d2 = dvp * dvp;
-    dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
-  }
-  if (bd <= 1) {
-    u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
-    u3[(size_t)ulo * ls + ci] = g.gwbc3 * u3[(size_t)(ulo + 1) * ls + ci];
-  }
-  if (bd >= 1) {
-    u1[(size_t)uhi * ls + ci] = g.gwbc1 * u1[(size_t)(uhi - 1) * ls + ci];
-    u3[(size_t)uhi * ls + ci] = g.gwbc3 * u3[(size_t)(uhi - 1) * ls + ci];
-  }
-  u2[(size_t)vlo * ls + ci] = 0.0;
-  u2[(size_t)vhi * ls + ci] = 0.0;
-}
-
-__global__ void __launch_bounds__(NTHR) k_press_mx(double *__restrict__ u1, double *__restrict__ u2,
-                                                   double *__restrict__ u3, double *__restrict__ p,
-                                                   double *__restrict__ psi, float *__restrict__ psif,
-                                                   const double *__restrict__ dg1, const double *__restrict__ dg2,
-                                                   const double *__restrict__ dg3, const float *__restrict__ dg1f,
-                                                   const float *__restrict__ dg2f, const float *__restrict__ dg3f,
-                                                   Geo g, DevScalars *sc, int kRK, int need_div, double k2low) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int vc = tid >> 1, part = tid & 1;
-  const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
-  double dmax = 0.0;
-  extern __shared__ double ptab[];
-  const double aRb = g.aRK[kRK - 1] + g.bRK[kRK - 1];
-  {
-    const double dti0 = sc->dti / aRb, dtk0 = sc->dt * aRb * g.dd;
-    for (int i = threadIdx.x; i < g.nu; i += blockDim.x) ptab[i] = dti0 * g.thud[i];
-    for (int i = threadIdx.x; i < g.nv; i += blockDim.x) ptab[g.nu + i] = dtk0 * g.thv[i];
-    __syncthreads();
-  }
-  if (vc < g.nvc) {
-    int c, bd;
-    vcol_of(g, vc, c, bd);
-    const int r = c / g.N1h, kx = c - r * g.N1h;
-    const bool low = -(g.k2x[kx] + g.k2z[r]) < k2low;  // k2F are -k^2
-    if (low) press_lane<double>(u1, u2, u3, p, psi, dg1, dg2, dg3, g, ptab, c, bd, part, pm, sc->dti, sc->dt, aRb,
-                                need_div, dmax);
-    else press_lane<float>(u1, u2, u3, p, psif, dg1f, dg2f, dg3f, g, ptab, c, bd, part, pm, sc->dti, sc->dt, aRb,
-                           need_div, dmax);
-  }
+#undef RS
   dmax = warp_max(dmax);
   if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
-}
-
-// FP32 copies of the pressure factors (the mixed form's solve)
-__global__ void k_dg_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n) {
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
 }
 
 __global__ void k_reset_err(DevScalars *sc) {
