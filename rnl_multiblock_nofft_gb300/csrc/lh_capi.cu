@@ -1273,7 +1273,6 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
-  const size_t ptab = sizeof(double) * (size_t)(g.nu + g.nv);  // the kernel's per-level factor tables
   {  // the pressure step with its y-columns staged pf_p levels ahead (k_press3)
     const size_t sm = sizeof(double) * (((size_t)g.nu + g.nv + 1) & ~(size_t)1) +
                       sizeof(double) * 6 * (size_t)(h->pf_p + 1) * h->tb_p;
