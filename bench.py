@@ -574,6 +574,7 @@ def main():
             g.upload_state(*ic)
         g.set_scalars(**sc0)
         g.autotune()
+        tuning = g.tuning()
         g.step(args.warmup)
         g.synchronize()
         barrier(pg)
@@ -582,7 +583,7 @@ def main():
         clocks = clk.stop()
         barrier(pg)
         ms = reduce_max(pg, ms)
-        res[form] = {"ms": ms, "launches": launches, "clocks": clocks,
+        res[form] = {"ms": ms, "launches": launches, "clocks": clocks, "tuning": tuning,
                      "value": ws * pts * 3 * args.steps / (ms * 1e-3) / 1e6}
         states[form] = ([a for b in (1, 2, 3) for a in g.download_bands()[b]] if mb else g.download_state())
         sc = g.scalars()
@@ -631,6 +632,7 @@ def main():
             "clocks": R["clocks"], "e2e": R["e2e"],
             "forms": {f: {"value": r["value"], "ms_per_step": r["ms"] / args.steps, "scalars": r["scalars"],
                           "roofline": r["roofline"], "step_roofline": r["step_roofline"], "e2e": r["e2e"],
+                          "autotuned": r["tuning"],
                           **({"fp64_rate": r["fp64_rate"]} if "fp64_rate" in r else {}),
                           "kernel_ms_per_step": {k: v[1] for k, v in r["kernels"].items()}}
                       for f, r in res.items()},

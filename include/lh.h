@@ -269,6 +269,12 @@ int lh_profile_steps(lh_handle *h, int nsteps, lh_kernel_time *out, int nmax, in
  * state. Call before the first lh_step (or it recaptures the step graph). */
 int lh_autotune(lh_handle *h);
 
+/* The configuration lh_autotune chose (or the defaults): threads per block of the u/w
+ * Helmholtz, v Helmholtz and pressure kernels, then the levels each stages ahead through shared
+ * memory (0: the variant that prefetches into registers). cfg: [6]. No counterpart in the
+ * reference. */
+int lh_get_tuning(lh_handle *h, int32_t *cfg);
+
 /* Batches (the ensemble form; no counterpart in the reference): one RK3 step of
  * each of `n` independent channels, of any sizes, captured once into a single
  * CUDA graph in which every channel is a branch on its own stream, and replayed

@@ -86,7 +86,9 @@ struct lh_handle {
   bool graph_ready;
   long long launches;
   int tb_uw, tb_v, tb_p;  // threads per block of the one-thread-per-column kernels (lh_autotune)
-  int pf_p;               // levels the pressure kernel stages ahead through shared memory (lh_autotune)
+  // levels the solve kernels stage ahead through shared memory (0: the kernels that prefetch into
+  // registers instead), per kernel: u/w, v (mixed form) and pressure (lh_autotune)
+  int pf_uw, pf_v, pf_p;
   std::string err;
   // per-kernel timing (lh_profile_steps): events around each launch
   bool prof;
@@ -261,7 +263,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
   h->graph_ready = false;
   h->launches = 0;
   h->tb_uw = h->tb_v = h->tb_p = 128;
-  h->pf_p = 4;
+  h->pf_uw = h->pf_v = h->pf_p = 4;
   if (!size_supported(cfg->Ngal1) || !size_supported(cfg->Ngal2)) {
     int rc = fail(h, LH_EINVAL, "Ngal must be one of 24 48 72 96 144 192 288 384 576 768 1152");
     delete h;
@@ -593,7 +595,13 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     int lim = 0;
     if (smem_optin(&lim) || cudaFuncSetAttribute((const void *)k_press3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
         cudaFuncSetAttribute((const void *)k_press3<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
-        cudaFuncSetAttribute((const void *)k_press3<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+        cudaFuncSetAttribute((const void *)k_press3<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_u_mx3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_u_mx3<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_u_mx3<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_v_mx3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_v_mx3<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_helm_v_mx3<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
       rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_press3)"); lh_destroy(h); return rc;
     }
   }
@@ -1194,6 +1202,15 @@ static int meanflow(lh_handle *h, int kRK) {
   return LH_OK;
 }
 
+// shared memory of the staged mixed solves (k_helm_u_mx3 / k_helm_v_mx3): six per-level tables
+// and a ring of 28 bytes per thread and slot (D + 1 slots)
+static size_t staged_smem(int nlev, int pf, int tb) {
+  return pf == 0 ? 0 : (((size_t)6 * nlev * 4 + 15) & ~(size_t)15) + (size_t)28 * (pf + 1) * tb;
+}
+static size_t press_smem(const Geo &g, int pf, int tb) {
+  return sizeof(double) * (((size_t)g.nu + g.nv + 1) & ~(size_t)1) + sizeof(double) * 6 * (size_t)(pf + 1) * tb;
+}
+
 template <typename T>
 static int substep_launches_t(lh_handle *h, int kRK) {
   typedef typename C2<T>::t V;
@@ -1250,9 +1267,19 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                          h->a3v, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib);
   } else {
     const int nb2v = (2 * g.nvc + h->tb_v - 1) / h->tb_v;
-    k_helm_v_mx2<<<nb2v, h->tb_v, 0, sv>>>((double *)h->u2, (float *)h->Nu2, (const float *)h->N2xz,
-                                           (const float *)h->vvc, (const double *)h->p, (float2 *)h->ysv, g, h->sc,
-                                           kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib);
+    const size_t sm = staged_smem(g.nv, h->pf_v, h->tb_v);
+    const int *ibv = h->ib ? h->d_ibslot_v : nullptr;
+    double *V = (double *)h->u2;
+    float *NV = (float *)h->Nu2;
+    const float *XV = (const float *)h->N2xz, *VV = (const float *)h->vvc;
+    const double *PP = (const double *)h->p;
+    float2 *YS = (float2 *)h->ysv;
+    switch (h->pf_v) {
+      case 0: k_helm_v_mx2<<<nb2v, h->tb_v, 0, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
+      case 2: k_helm_v_mx3<2><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
+      case 8: k_helm_v_mx3<8><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
+      default: k_helm_v_mx3<4><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
+    }
   }
   if ((rc = count_launch(h))) return rc;
   if (fork) CK(cudaEventRecord(h->ev_join, h->st2));
@@ -1263,10 +1290,20 @@ static int substep_launches_t(lh_handle *h, int kRK) {
                                                            h->ib ? h->d_ibslot_u : nullptr, h->duib));
   } else {
     const int nb2u = (2 * g.nvc + h->tb_uw - 1) / h->tb_uw;
-    KL("k_helm_uw", k_helm_u_mx2<<<dim3(nb2u, 2), h->tb_uw, 0, h->st>>>(
-                        (double *)h->u1, (double *)h->u3, (float *)h->Nu1, (float *)h->Nu3, (const float *)h->N1xz,
-                        (const float *)h->N3xz, (const float *)h->uvf, (const float *)h->wvf, h->p, (float2 *)h->ysf, g,
-                        h->sc, kRK, h->ib ? h->d_ibslot_u : nullptr, h->duib));
+    const size_t sm = staged_smem(g.nu, h->pf_uw, h->tb_uw);
+    const dim3 gr(nb2u, 2);
+    double *U1 = (double *)h->u1, *U3 = (double *)h->u3;
+    float *N1 = (float *)h->Nu1, *N3 = (float *)h->Nu3;
+    const float *X1 = (const float *)h->N1xz, *X3 = (const float *)h->N3xz, *F1 = (const float *)h->uvf,
+                *F3 = (const float *)h->wvf;
+    const int *ibu = h->ib ? h->d_ibslot_u : nullptr;
+    float2 *YS = (float2 *)h->ysf;
+    switch (h->pf_uw) {
+      case 0: KL("k_helm_uw", k_helm_u_mx2<<<gr, h->tb_uw, 0, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
+      case 2: KL("k_helm_uw", k_helm_u_mx3<2><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
+      case 8: KL("k_helm_uw", k_helm_u_mx3<8><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
+      default: KL("k_helm_uw", k_helm_u_mx3<4><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
+    }
   }
   if ((rc = meanflow(h, kRK))) return rc;
   if (fork) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
@@ -1274,11 +1311,11 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
   {  // the pressure step with its y-columns staged pf_p levels ahead (k_press3)
-    const size_t sm = sizeof(double) * (((size_t)g.nu + g.nv + 1) & ~(size_t)1) +
-                      sizeof(double) * 6 * (size_t)(h->pf_p + 1) * h->tb_p;
+    const size_t sm = press_smem(g, h->pf_p, h->tb_p);
     double *U1 = (double *)h->u1, *U2 = (double *)h->u2, *U3 = (double *)h->u3, *P = (double *)h->p;
     double *PS = (double *)h->psi;
     switch (h->pf_p) {
+      case 0: KL("k_press", k_press2<<<nbp2, h->tb_p, sizeof(double) * ((size_t)g.nu + g.nv), h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
       case 2: KL("k_press", k_press3<2><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
       case 8: KL("k_press", k_press3<8><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
       default: KL("k_press", k_press3<4><<<nbp2, h->tb_p, sm, h->st>>>(U1, U2, U3, P, PS, h->dg1, h->dg2, h->dg3, g, h->sc, kRK, need_div)); break;
@@ -1597,22 +1634,22 @@ extern "C" int lh_autotune(lh_handle *h) {
   };
   cudaError_t e = copy_all(true);
   if (e != cudaSuccess) { cudaFree(save); return fail(h, LH_ECUDA, cudaGetErrorString(e)); }
-  // trials: every block size with every staging depth of the pressure kernel; each kernel
-  // keeps the configuration of its fastest trial (the Helmholtz kernels depend on the block
-  // size only)
-  const int cand[] = {64, 128, 256}, cpf[] = {2, 4, 8};
+  // trials: every block size with every staging depth (0: the register-prefetch kernels); each
+  // solve kernel keeps the configuration of its fastest trial. The FP64 form's Helmholtz kernels
+  // depend on the block size only.
+  const int cand[] = {64, 128, 256}, cpf[] = {0, 2, 4, 8};
   double best[3] = {1e30, 1e30, 1e30};
-  int pick[3] = {h->tb_uw, h->tb_v, h->tb_p}, pick_pf = h->pf_p;
+  int pick[3] = {h->tb_uw, h->tb_v, h->tb_p}, pickpf[3] = {h->pf_uw, h->pf_v, h->pf_p};
   const char *names[3] = {"k_helm_uw", "k_helm_v", "k_press"};
   lh_kernel_time kt[64];
   int rc = LH_OK;
   int optin = 0;
   if (smem_optin(&optin)) optin = 49152;
-  for (int ti = 0; ti < 9 && rc == LH_OK; ++ti) {
+  for (int ti = 0; ti < 12 && rc == LH_OK; ++ti) {
     const int tb = cand[ti % 3], pf = cpf[ti / 3];
-    if (sizeof(double) * (((size_t)g.nu + g.nv + 1 + 6 * (size_t)(pf + 1) * tb)) > (size_t)optin) continue;
+    if (press_smem(g, pf, tb) > (size_t)optin || staged_smem(g.nu, pf, tb) > (size_t)optin) continue;
     h->tb_uw = h->tb_v = h->tb_p = tb;
-    h->pf_p = pf;
+    h->pf_uw = h->pf_v = h->pf_p = pf;
     int n = 0;
     rc = lh_profile_steps(h, 1, kt, 64, &n);
     for (int k = 0; k < 3 && rc == LH_OK; ++k)
@@ -1620,18 +1657,26 @@ extern "C" int lh_autotune(lh_handle *h) {
         if (strncmp(kt[i].name, names[k], 32) == 0 && kt[i].total_ms < best[k]) {
           best[k] = kt[i].total_ms;
           pick[k] = tb;
-          if (k == 2) pick_pf = pf;
+          pickpf[k] = pf;
         }
     if (copy_all(false) != cudaSuccess) rc = fail(h, LH_ECUDA, "state restore failed");
   }
   cudaFree(save);
-  h->tb_uw = pick[0]; h->tb_v = pick[1]; h->tb_p = pick[2]; h->pf_p = pick_pf;
+  h->tb_uw = pick[0]; h->tb_v = pick[1]; h->tb_p = pick[2];
+  h->pf_uw = pickpf[0]; h->pf_v = pickpf[1]; h->pf_p = pickpf[2];
   if (h->graph_ready) {  // recapture with the chosen configuration
     cudaGraphExecDestroy(h->gexec);
     cudaGraphDestroy(h->graph);
     h->graph_ready = false;
   }
   return rc;
+}
+
+extern "C" int lh_get_tuning(lh_handle *h, int32_t *cfg) {
+  if (!h || !cfg) return LH_EINVAL;
+  cfg[0] = h->tb_uw; cfg[1] = h->tb_v; cfg[2] = h->tb_p;
+  cfg[3] = h->pf_uw; cfg[4] = h->pf_v; cfg[5] = h->pf_p;
+  return LH_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -868,6 +868,18 @@ __global__ void __launch_bounds__(512) k_helm00_pcr(double *__restrict__ u1, dou
   for (int i = threadIdx.x; i < n; i += blockDim.x) u[(qlo + i) * ls + part] = D[i] / B[i];
 }
 
+// cp.async copies from global to shared memory (8 and 4 bytes), their commit groups and waits
+__device__ __forceinline__ void cpa8(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa4(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // ============================================================================
 // Mixed-form solves with one lane per (column, real/imaginary part): the matrix
 // is real, so the two parts are independent systems; each lane repeats the FP32
@@ -1130,6 +1142,280 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
     u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
   }
   back_sweep_mx<LH_PF_HV_BACK>(u2, ys, lstride, ci, qlo, qhi, y);
+}
+
+// ============================================================================
+// The mixed-form solves with their y-columns staged through shared memory (the arithmetic of
+// k_helm_u_mx2 / k_helm_v_mx2, so the same results bit for bit): every lane keeps a ring of
+// D + 1 levels of its inputs, filled by cp.async copies D levels ahead (into the slot not being
+// read), and the per-level coefficient tables sit in shared memory; the backward sweep stages
+// (y, upper factor) and the state the same way. Shared memory: 6 nu tables + the ring,
+// 24 (D + 1) bytes per thread.
+// ============================================================================
+template <int D>
+__device__ __forceinline__ void back_sweep_staged(double *__restrict__ u, const float2 *__restrict__ ys, size_t lstride,
+                                                  size_t ci, int qlo, int qhi, float x, unsigned char *ring, int nt) {
+  constexpr int NS = D + 1;
+  float2 *ry = reinterpret_cast<float2 *>(ring);          // [NS][nt]
+  double *ru = reinterpret_cast<double *>(ring) + NS * nt;  // [NS][nt]
+  auto fetch = [&](int q) {
+    const int s_ = (qhi - 1 - q) % NS;
+    const size_t e = (size_t)q * lstride + ci;
+    cpa8(&ry[s_ * nt + threadIdx.x], ys + e);
+    cpa8(&ru[s_ * nt + threadIdx.x], u + e);
+  };
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_) {
+    if (qhi - 1 - s_ >= qlo) fetch(qhi - 1 - s_);
+    cpa_commit();
+  }
+  for (int q = qhi - 1; q >= qlo; --q) {
+    cpa_wait<D - 1>();
+    const int s_ = (qhi - 1 - q) % NS;
+    const float2 ya = ry[s_ * nt + threadIdx.x];
+    const double uq = ru[s_ * nt + threadIdx.x];
+    if (q - D >= qlo) fetch(q - D);
+    cpa_commit();
+    x = ya.x - ya.y * x;
+    u[(size_t)q * lstride + ci] = uq + f2d_alu(x);
+  }
+  cpa_wait<0>();
+}
+
+template <int D>
+__global__ void __launch_bounds__(NTHR) k_helm_u_mx3(double *__restrict__ u1, double *__restrict__ u3,
+                                                     float *__restrict__ Nu1, float *__restrict__ Nu3,
+                                                     const float *__restrict__ N1xz, const float *__restrict__ N3xz,
+                                                     const float *__restrict__ uvf, const float *__restrict__ wvf,
+                                                     const double2 *__restrict__ p, float2 *__restrict__ ys2, Geo g,
+                                                     const DevScalars *__restrict__ sc, int kRK,
+                                                     const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
+  constexpr int NS = D + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nu = g.nu, nt = blockDim.x;
+  float *ta = reinterpret_cast<float *>(smem_raw), *tb = ta + nu, *tc = tb + nu, *tsd = tc + nu, *tth = tsd + nu;
+  int *tib = reinterpret_cast<int *>(tth + nu);
+  unsigned char *ring = smem_raw + (((size_t)6 * nu * 4 + 15) & ~(size_t)15);
+  for (int i = threadIdx.x; i < nu; i += nt) {
+    ta[i] = g.d2uf[i]; tb[i] = g.d2uf[nu + i]; tc[i] = g.d2uf[2 * nu + i]; tsd[i] = g.sdgu[i]; tth[i] = g.thuf[i];
+    tib[i] = ibslot_u ? ibslot_u[i] : -1;
+  }
+  __syncthreads();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = tid >> 1, part = tid & 1;
+  const int nc = g.ncol;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  if (c == 0) return;  // mode (0,0): k_helm00_pcr (FP64)
+  const int qlo = g.bq[bd][0], qhi = g.bq[bd][1];
+  const int fw = blockIdx.y;  // 0: u, 1: w
+  double *u = fw ? u3 : u1;
+  float *Nu = fw ? Nu3 : Nu1;
+  const float *X = fw ? N3xz : N1xz;
+  const float *Fl = fw ? wvf : uvf;
+  float2 *ys = ys2 + (size_t)fw * g.nu * nc * 2;
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
+  const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
+  const double dR = g.dRK[kRK - 1];
+  const float G = (float)(-g.gRK[kRK - 1]);
+  const double dt = sc->dt;
+  const float dtf = (float)dt;
+  const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
+  const float C3 = (float)(-dR * (fw ? g.k1z[r] : g.k1x[kx]));
+  const float dd = (float)g.dd;
+  const double gw1 = g.gw[bd][0], gw2 = g.gw[bd][1];
+  const size_t lstride = (size_t)nc * 2;
+  const size_t ci = (size_t)c * 2 + part;
+  const size_t e0 = (size_t)qlo * lstride + ci;
+  const double *pc = reinterpret_cast<const double *>(p);
+  double um = u[e0], u0 = u[e0 + lstride];
+  float y = d2f_alu(-(um + gw1 * u0));  // first row
+  float fdm = d2f_alu(um - u0);
+  float yprev = y;
+  float a3raw = (float)gw1, a2p = 1.f;
+  float flm = Fl[e0];
+  // ring: doubles [NS][2][nt] (u of the level above, p of the other part), floats [NS][3][nt] (Fl, Nu, X)
+  double *rd = reinterpret_cast<double *>(ring);
+  float *rf = reinterpret_cast<float *>(rd + 2 * NS * nt);
+  auto fetch = [&](int q) {
+    const int s_ = (q - qlo - 1) % NS;
+    const size_t e = (size_t)q * lstride + ci;
+    cpa8(&rd[(s_ * 2 + 0) * nt + threadIdx.x], u + e + lstride);
+    cpa8(&rd[(s_ * 2 + 1) * nt + threadIdx.x], pc + ((size_t)(q - 1) * nc + c) * 2 + (part ^ 1));
+    cpa4(&rf[(s_ * 3 + 0) * nt + threadIdx.x], Fl + e);
+    cpa4(&rf[(s_ * 3 + 1) * nt + threadIdx.x], Nu + e);
+    cpa4(&rf[(s_ * 3 + 2) * nt + threadIdx.x], X + e);
+  };
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_) {
+    if (qlo + 1 + s_ <= qhi - 1) fetch(qlo + 1 + s_);
+    cpa_commit();
+  }
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
+    cpa_wait<D - 1>();
+    const int s_ = (q - qlo - 1) % NS;
+    const size_t e = (size_t)q * lstride + ci;
+    const double up1 = rd[(s_ * 2 + 0) * nt + threadIdx.x], po = rd[(s_ * 2 + 1) * nt + threadIdx.x];
+    const float flq = rf[(s_ * 3 + 0) * nt + threadIdx.x], nuq = rf[(s_ * 3 + 1) * nt + threadIdx.x],
+                xq = rf[(s_ * 3 + 2) * nt + threadIdx.x];
+    if (q + D <= qhi - 1) fetch(q + D);
+    cpa_commit();
+    const float a = ta[q], b = tb[q], cc = tc[q], sdg = tsd[q] + k2f, thq = tth[q];
+    const int ibs = tib[q];
+    const float fdp = d2f_alu(up1 - u0);
+    const float L = a * fdm + cc * fdp + sdg * d2f_alu(u0);
+    fdm = -fdp;
+    float du;
+    if (ibs < 0) {
+      const float pt = part ? d2f_alu(po) : -d2f_alu(po);
+      du = (C1 * L + C2 * nuq) + C3 * pt;
+      const float n = xq + (flq - flm) * thq * dd;
+      Nu[e] = n;
+      du += G * n;
+    } else {
+      const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+      du = d2f_alu(part ? di.y : di.x);
+    }
+    const float rr = dtf * du + beta * L;
+    const float a1 = -beta * a;
+    const float a2 = 1.f - beta * (b + k2f);
+    const float a3p = a3raw * a2p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+    a2p = 1.f / (a2 - a1 * a3p);
+    y = (rr - a1 * y) * a2p;
+    yprev = y;
+    a3raw = -beta * cc;
+    um = u0; u0 = up1;
+    flm = flq;
+  }
+  cpa_wait<0>();
+  {  // last row: gw2 d(n-2) + d(n-1) = -(gw2 u(n-2) + u(n-1))
+    const int q = qhi;
+    const float a1 = (float)gw2;
+    const float rl = d2f_alu(-(gw2 * um + u0));
+    const float a3p = a3raw * a2p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+    a2p = 1.f / (1.f - a1 * a3p);
+    y = (rl - a1 * y) * a2p;
+    u[(size_t)q * lstride + ci] = u0 + f2d_alu(y);
+  }
+  __threadfence_block();  // the backward sweep's copies read ys written above by this thread
+  back_sweep_staged<D>(u, ys, lstride, ci, qlo, qhi, y, ring, nt);
+}
+
+template <int D>
+__global__ void __launch_bounds__(NTHR) k_helm_v_mx3(double *__restrict__ u2, float *__restrict__ Nu2,
+                                                     const float *__restrict__ N2xz, const float *__restrict__ vvc,
+                                                     const double *__restrict__ p, float2 *__restrict__ ys, Geo g,
+                                                     const DevScalars *__restrict__ sc, int kRK,
+                                                     const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
+  constexpr int NS = D + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nv = g.nv, nt = blockDim.x;
+  float *ta = reinterpret_cast<float *>(smem_raw), *tb = ta + nv, *tc = tb + nv, *tsd = tc + nv, *tth = tsd + nv;
+  int *tib = reinterpret_cast<int *>(tth + nv);
+  unsigned char *ring = smem_raw + (((size_t)6 * nv * 4 + 15) & ~(size_t)15);
+  for (int i = threadIdx.x; i < nv; i += nt) {
+    ta[i] = g.d2vf[i]; tb[i] = g.d2vf[nv + i]; tc[i] = g.d2vf[2 * nv + i]; tsd[i] = g.sdgv[i]; tth[i] = g.thvf[i];
+    tib[i] = ibslot_v ? ibslot_v[i] : -1;
+  }
+  __syncthreads();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int vc = tid >> 1, part = tid & 1;
+  const int nc = g.ncol;
+  if (vc >= g.nvc) return;
+  int c, bd;
+  vcol_of(g, vc, c, bd);
+  if (c == 0) return;  // mode (0,0): k_helm00_pcr (FP64)
+  const int qlo = g.bq[bd][2], qhi = g.bq[bd][3];
+  const int r = c / g.N1h, kx = c - r * g.N1h;
+  const float k2f = (float)(g.k2x[kx] + g.k2z[r]);
+  const float C1 = (float)(g.aRK[kRK - 1] / g.Re), C2 = (float)(-g.cRK[kRK - 1]);
+  const double dR = g.dRK[kRK - 1];
+  const float G = (float)(-g.gRK[kRK - 1]);
+  const double dt = sc->dt;
+  const float dtf = (float)dt;
+  const float beta = (float)(g.bRK[kRK - 1] * dt / g.Re);
+  const float dd = (float)g.dd;
+  const size_t ci = (size_t)c * 2 + part;
+  const size_t lstride = (size_t)nc * 2;
+  const size_t e0 = (size_t)qlo * lstride + ci;
+  double vm = u2[e0], v0 = u2[e0 + lstride];
+  const float dRf = (float)dR;
+  float y = d2f_alu(-vm);
+  float fdm = d2f_alu(vm - v0);
+  float yprev = y;
+  float a3raw = 0.f, a2p = 1.f;
+  float vvq = vvc[e0 + lstride];
+  float pprev = d2f_alu(p[e0]);  // p of the level below (the pressure difference of level q)
+  // ring: doubles [NS][2][nt] (v of the level above, p), floats [NS][3][nt] (vv above, Nu, X)
+  double *rd = reinterpret_cast<double *>(ring);
+  float *rf = reinterpret_cast<float *>(rd + 2 * NS * nt);
+  auto fetch = [&](int q) {
+    const int s_ = (q - qlo - 1) % NS;
+    const size_t e = (size_t)q * lstride + ci;
+    cpa8(&rd[(s_ * 2 + 0) * nt + threadIdx.x], u2 + e + lstride);
+    cpa8(&rd[(s_ * 2 + 1) * nt + threadIdx.x], p + e);
+    cpa4(&rf[(s_ * 3 + 0) * nt + threadIdx.x], vvc + e + lstride);
+    cpa4(&rf[(s_ * 3 + 1) * nt + threadIdx.x], Nu2 + e);
+    cpa4(&rf[(s_ * 3 + 2) * nt + threadIdx.x], N2xz + e);
+  };
+#pragma unroll
+  for (int s_ = 0; s_ < D; ++s_) {
+    if (qlo + 1 + s_ <= qhi - 1) fetch(qlo + 1 + s_);
+    cpa_commit();
+  }
+  for (int q = qlo + 1; q <= qhi - 1; ++q) {
+    cpa_wait<D - 1>();
+    const int s_ = (q - qlo - 1) % NS;
+    const size_t e = (size_t)q * lstride + ci;
+    const double vp1 = rd[(s_ * 2 + 0) * nt + threadIdx.x];
+    const float pq = d2f_alu(rd[(s_ * 2 + 1) * nt + threadIdx.x]);
+    const float vvp = rf[(s_ * 3 + 0) * nt + threadIdx.x], nuq = rf[(s_ * 3 + 1) * nt + threadIdx.x],
+                xq = rf[(s_ * 3 + 2) * nt + threadIdx.x];
+    if (q + D <= qhi - 1) fetch(q + D);
+    cpa_commit();
+    const float a = ta[q], b = tb[q], cc = tc[q], sdg = tsd[q] + k2f, thq = tth[q];
+    const int ibs = tib[q];
+    const float pd = pq - pprev;
+    pprev = pq;
+    const float fdp = d2f_alu(vp1 - v0);
+    const float L = a * fdm + cc * fdp + sdg * d2f_alu(v0);
+    fdm = -fdp;
+    float du;
+    if (ibs < 0) {
+      const float C3 = -dRf * dd * thq;
+      du = (C1 * L + C2 * nuq) + C3 * pd;
+      const float n = xq + (vvp - vvq) * thq * dd;
+      Nu2[e] = n;
+      du += G * n;
+    } else {
+      const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
+      du = d2f_alu(part ? di.y : di.x);
+    }
+    const float rr = dtf * du + beta * L;
+    const float a1 = -beta * a;
+    const float a2 = 1.f - beta * (b + k2f);
+    const float a3p = a3raw * a2p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+    a2p = 1.f / (a2 - a1 * a3p);
+    y = (rr - a1 * y) * a2p;
+    yprev = y;
+    a3raw = -beta * cc;
+    vm = v0; v0 = vp1; vvq = vvp;
+  }
+  cpa_wait<0>();
+  {  // last row: d(n-1) = -v(n-1)
+    const int q = qhi;
+    const float a3p = a3raw * a2p;
+    ys[(size_t)(q - 1) * lstride + ci] = make_float2(yprev, a3p);
+    y = d2f_alu(-v0);
+    u2[(size_t)q * lstride + ci] = v0 + f2d_alu(y);
+  }
+  __threadfence_block();
+  back_sweep_staged<D>(u2, ys, lstride, ci, qlo, qhi, y, ring, nt);
 }
 
 // ============================================================================
@@ -1514,12 +1800,6 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
 // memory: the per-level factor tables (nu + nv doubles) and the ring, 6 (D + 1) doubles per
 // thread.
 // ============================================================================
-__device__ __forceinline__ void cpa8(double *dst, const double *src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cpa_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 template <int D>
 __global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double *__restrict__ u2,

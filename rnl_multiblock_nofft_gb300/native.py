@@ -23,7 +23,7 @@ EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_do
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
-           "lh_batch_synchronize", "lh_batch_destroy", "lh_batch_stream", "lh_history_record")
+           "lh_batch_synchronize", "lh_batch_destroy", "lh_batch_stream", "lh_history_record", "lh_get_tuning")
 
 
 class LhKernelTime(C.Structure):
@@ -81,6 +81,7 @@ def load(path: str = _LIB_PATH):
     L.lh_profile_steps.argtypes = [vp, i, C.POINTER(LhKernelTime), i, C.POINTER(i)]
     L.lh_four_to_phys_noalloc.argtypes = [i, i, i, i, vp, vp, i, vp, C.POINTER(C.c_char_p)]
     L.lh_autotune.argtypes = [vp]
+    L.lh_get_tuning.argtypes = [vp, C.POINTER(C.c_int32)]
     L.lh_batch_create.argtypes = [C.POINTER(vp), i, C.POINTER(vp)]
     L.lh_batch_step.argtypes = [vp]
     L.lh_batch_synchronize.argtypes = [vp]
@@ -279,6 +280,12 @@ class GpuChannel:
 
     def kernel_launches(self) -> int:
         return int(self.L.lh_kernel_launches(self.h))
+
+    def tuning(self) -> dict:
+        """Block sizes and staging depths of the solve kernels (lh_get_tuning)."""
+        a = (C.c_int32 * 6)()
+        self._check(self.L.lh_get_tuning(self.h, a))
+        return dict(threads_uw=a[0], threads_v=a[1], threads_p=a[2], stage_uw=a[3], stage_v=a[4], stage_p=a[5])
 
     def autotune(self):
         """Pick the block sizes of the column kernels for this channel (state restored)."""
