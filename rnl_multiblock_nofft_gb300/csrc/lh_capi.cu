@@ -199,6 +199,10 @@ static cudaError_t set_attrs_sized(int lim) {
   if constexpr (sizeof(T) == 4) {  // the two-stage mixed-form passes
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv2<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd2<N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv2<N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec2<N>, A, lim);
+    if constexpr (N <= 384)
+      if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_ib_xforce2<N>, A, lim);
     if constexpr (N <= 384)
       if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass2<N>, A, lim);
   }
@@ -1123,6 +1127,12 @@ static int triad_nonlinear(lh_handle *h, int kRK) {
 template <typename T, int N>
 static int launch_spec_zinv(lh_handle *h, const double2 *spec, void *Ascr, int npl, const void *twz) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4) {  // the two-stage register form (immersed boundaries, mixed form)
+    using P = zp2<N>;
+    dim3 g1((h->g.N1h + P::KB - 1) / P::KB, npl);
+    KL("k_spec_zinv", k_spec_zinv2<N><<<g1, P::NT, P::SMEM, h->st>>>(spec, (float2 *)Ascr, h->g, (const float2 *)twz));
+    return LH_OK;
+  }
   constexpr int KB = kb_zinv<V>(N);
   dim3 g1((h->g.N1h + KB - 1) / KB, npl);
   KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(spec, (V *)Ascr, h->g, (const V *)twz));
@@ -1147,6 +1157,12 @@ static int launch_xfwd_phys(lh_handle *h, const double *phys, void *Bscr, int np
 template <typename T, int N>
 static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int npl, const void *twz) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4) {  // the two-stage register form (immersed boundaries, mixed form)
+    using P = zp2<N>;
+    dim3 g2((h->g.N1h + P::KB - 1) / P::KB, npl);
+    KL("k_zfwd_spec", k_zfwd_spec2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)Bscr, spec, h->g, (const float2 *)twz));
+    return LH_OK;
+  }
   constexpr int KB = kb_zinv<V>(N);
   dim3 g2((h->g.N1h + KB - 1) / KB, npl);
   KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, spec, h->g, (const V *)twz));
@@ -1156,6 +1172,14 @@ static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int n
 template <typename T, int N>
 static int launch_ib_xforce(lh_handle *h, int npl) {
   typedef typename C2<T>::t V;
+  if constexpr (sizeof(T) == 4 && N <= 384) {  // the two-stage register form (mixed form)
+    using P = ibx2<N>;
+    dim3 g2((h->g.G2 / 2 + P::PB - 1) / P::PB, npl);
+    KL("k_ib_xforce", k_ib_xforce2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, h->g,
+                                                                     (const float2 *)h->twx, h->d_ibrec, h->d_iboff,
+                                                                     h->cap, h->sc));
+    return LH_OK;
+  }
   constexpr int PB = 4 * pb_xpass<V>(N);
   dim3 g2((h->g.G2 / 2 + PB - 1) / PB, npl);
   KL("k_ib_xforce", k_ib_xforce<T, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>(

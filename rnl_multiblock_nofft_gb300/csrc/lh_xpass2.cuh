@@ -241,37 +241,22 @@ template <int N> struct zp2 {
   static constexpr int SMEM = (N + ZB) * KB * 8;  // float2, one pad element per ZA-block
 };
 
-template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
-                                                       const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
-                                                       const float2 *__restrict__ tw) {
+// The two stages of the inverse z pass for one block of KB kx columns: gather(r, kx) gives
+// spectral row r (0..N2-1) of column kx in FP32; the physical rows l go to dst[l * N1h + kx].
+template <int N, typename Gather>
+__device__ __forceinline__ void zinv2_body(Gather &&gather, float2 *__restrict__ dst, int N1h, int kx0,
+                                           const float2 *__restrict__ tw) {
   using P = zp2<N>;
   constexpr int ZA = P::ZA, ZB = P::ZB, KB = P::KB;
   static_assert(ZA * ZB == N, "z plan");
   constexpr int H = N / 3;  // N2 / 2 retained kz rows on each side (N2 = 2 (Ngal2 / 3), checked at create)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *E = reinterpret_cast<float2 *>(smem_raw);
-  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
-  const bool isU = slot < g.nuI;
-  const int q = slot_level(g, slot, isU);
-  const size_t nc = g.ncolF;
   const int tid = threadIdx.x;
   if (tid < ZB * KB) {
     const int jj = tid / KB, kk = tid - jj * KB, kx = kx0 + kk;
     float2 v[ZA];
-    // field f at level q (interpolated to the level's grid), FP32
-    const double2 *s0, *s1 = nullptr;
-    float ca = 1.f, cb = 0.f;
-    size_t o0 = (size_t)q * nc, o1 = 0;
-    if (isU) {
-      if (f == 0) s0 = u1;
-      else if (f == 2) s0 = u3;
-      else { s0 = u2; s1 = u2; o1 = (size_t)(q - 1) * nc; ca = g.iuaf[q]; cb = g.iubf[q]; }  // v faces -> centre
-    } else {
-      if (f == 1) s0 = u2;
-      else { s0 = s1 = (f == 0) ? u1 : u3; o0 = (size_t)(q + 1) * nc; o1 = (size_t)q * nc; ca = g.ivaf[q]; cb = g.ivbf[q]; }
-    }
-    const bool ok = kx < g.N1h;
+    const bool ok = kx < N1h;
     regfft::static_for<0, ZA>([&](auto t_) {
       constexpr int t = decltype(t_)::value;
       constexpr int mlo = ZB * t, mhi = ZB * t + ZB - 1;
@@ -281,16 +266,7 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict_
       int r = -1;
       if (lo && m < H) r = m;
       else if (hi && m >= N - H) r = m - N + 2 * H;
-      if ((lo || hi) && ok && r >= 0) {
-        const int c = gcol(g, r, kx);
-        const double2 a = s0[o0 + c];
-        if (s1) {
-          const double2 b = s1[o1 + c];
-          z = make_float2(ca * d2f_alu(a.x) + cb * d2f_alu(b.x), ca * d2f_alu(a.y) + cb * d2f_alu(b.y));
-        } else {
-          z = make_float2(d2f_alu(a.x), d2f_alu(a.y));
-        }
-      }
+      if ((lo || hi) && ok && r >= 0) z = gather(r, kx);
       v[t] = z;
     });
     regfft::dft_reg<ZA, true>(v);
@@ -313,14 +289,60 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict_
       }
     });
     regfft::dft_reg<ZB, true>(v);
-    if (kx < g.N1h) {
-      float2 *dst = A + (size_t)(slot * 3 + f) * N * g.N1h + kx;
+    if (kx < N1h) {
       regfft::static_for<0, ZB>([&](auto t_) {
         constexpr int t = decltype(t_)::value;
-        dst[(size_t)(jj + ZA * t) * g.N1h] = v[t];
+        dst[(size_t)(jj + ZA * t) * N1h + kx] = v[t];
       });
     }
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+                                                       const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
+                                                       const float2 *__restrict__ tw) {
+  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * zp2<N>::KB;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const size_t nc = g.ncolF;
+  // field f at level q (interpolated to the level's grid), FP32
+  const double2 *s0, *s1 = nullptr;
+  float ca = 1.f, cb = 0.f;
+  size_t o0 = (size_t)q * nc, o1 = 0;
+  if (isU) {
+    if (f == 0) s0 = u1;
+    else if (f == 2) s0 = u3;
+    else { s0 = u2; s1 = u2; o1 = (size_t)(q - 1) * nc; ca = g.iuaf[q]; cb = g.iubf[q]; }  // v faces -> centre
+  } else {
+    if (f == 1) s0 = u2;
+    else { s0 = s1 = (f == 0) ? u1 : u3; o0 = (size_t)(q + 1) * nc; o1 = (size_t)q * nc; ca = g.ivaf[q]; cb = g.ivbf[q]; }
+  }
+  auto gather = [&](int r, int kx) {
+    const int c = gcol(g, r, kx);
+    const double2 a = s0[o0 + c];
+    if (s1) {
+      const double2 b = s1[o1 + c];
+      return make_float2(ca * d2f_alu(a.x) + cb * d2f_alu(b.x), ca * d2f_alu(a.y) + cb * d2f_alu(b.y));
+    }
+    return make_float2(d2f_alu(a.x), d2f_alu(a.y));
+  };
+  zinv2_body<N>(gather, A + (size_t)(slot * 3 + f) * N * g.N1h, g.N1h, kx0, tw);
+}
+
+// The inverse z transforms of spectral planes [pl][N2][N1h] complex128 (the immersed-boundary
+// du planes) into A [pl][l][kx] in FP32, as k_spec_zinv<float, N>.
+template <int N>
+__global__ void __launch_bounds__(zp2<N>::NT) k_spec_zinv2(const double2 *__restrict__ spec, float2 *__restrict__ A,
+                                                            Geo g, const float2 *__restrict__ tw) {
+  const int pl = blockIdx.y, kx0 = blockIdx.x * zp2<N>::KB;
+  const double2 *S = spec + (size_t)pl * g.ncol;
+  const int N1h = g.N1h;
+  auto gather = [&](int r, int kx) {
+    const double2 a = S[(size_t)r * N1h + kx];
+    return make_float2(d2f_alu(a.x), d2f_alu(a.y));
+  };
+  zinv2_body<N>(gather, A + (size_t)pl * N * N1h, N1h, kx0, tw);
 }
 
 // ============================================================================
@@ -434,6 +456,216 @@ __global__ void __launch_bounds__(zf2<N>::NTH) k_zfwd2(const float2 *__restrict_
       N2xz[off + c] = n2;
       uvf[off + c] = uv;
       wvf[off + c] = wv;
+    }
+  }
+}
+
+// ============================================================================
+// Immersed-boundary forcing in one two-stage x pass (the work of k_ib_xforce: imm_bounds_u/v,
+// FOU3D.f90:806-998): the rows of the du planes (A [pl][l][kx], after the inverse z pass) go
+// to physical space with the first inverse stage reading A directly (Hermitian completion), the
+// second stage leaves every row pair's physical line in shared memory, the forced points of the
+// rows are overwritten with Kib/dt (A u(i1,k1,j1) - u(i,k,j)) from the captured physical
+// velocities (records sorted by (plane, row)), and the lines come back with the forward stages;
+// the two rows of a pair are separated by warp shuffles into B [pl][l][kx].
+// ============================================================================
+template <int N> struct ibx2 {
+  static constexpr int XB = 8, XA = N / XB;
+  static constexpr int PB = XA >= 36 ? 4 : (XA >= 18 ? 8 : 16);
+  static constexpr int NT = ((XA * PB > PB * XB ? XA * PB : PB * XB) + 31) / 32 * 32;
+  static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
+  static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB), LSP = pad16(N);
+  static constexpr int SMEM = (LS1 > LS2 ? LS1 : LS2) * PB * 8 + LSP * PB * 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(ibx2<N>::NT) k_ib_xforce2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+                                                             const float2 *__restrict__ tw, const IbRec *__restrict__ rec,
+                                                             const int *__restrict__ rec_off,
+                                                             const double *__restrict__ cap,
+                                                             const DevScalars *__restrict__ sc) {
+  using P = ibx2<N>;
+  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1, LS2 = P::LS2, LSP = P::LSP;
+  constexpr int NK = N / 3 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *E = reinterpret_cast<float2 *>(smem_raw);
+  float2 *Ph = E + (LS1 > LS2 ? LS1 : LS2) * PB;  // physical lines [pb][LSP]
+  const int G2 = g.G2, N1h = g.N1h;
+  const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
+  const int npairs = min(PB, (G2 - l0) / 2);
+  const int tid = threadIdx.x;
+  // inverse stage 1: line pb, thread jj < 8
+  if (tid < PB * XB) {
+    const int pb = tid / XB, jj = tid - pb * XB;
+    float2 v[XA];
+    if (pb < npairs) {
+      const float2 *ra = A + (size_t)pl * G2 * N1h + (size_t)(l0 + 2 * pb) * N1h;
+      const float2 *rb = ra + N1h;
+      regfft::static_for<0, XA>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        constexpr int mlo = XB * t, mhi = XB * t + XB - 1;
+        constexpr bool direct = mlo < NK, conj = mhi > N - NK;
+        const int m = jj + mlo;
+        float2 z = make_float2(0.f, 0.f);
+        if (direct && m < NK) {
+          float2 a = __ldg(ra + m), b = __ldg(rb + m);
+          if (m == 0) { a.y = 0.f; b.y = 0.f; }
+          z = make_float2(a.x - b.y, a.y + b.x);
+        } else if (conj && m > N - NK) {
+          const float2 a = __ldg(ra + (N - m)), b = __ldg(rb + (N - m));
+          z = make_float2(a.x + b.y, -a.y + b.x);
+        }
+        v[t] = z;
+      });
+    } else {
+      regfft::static_for<0, XA>([&](auto t_) { v[decltype(t_)::value] = make_float2(0.f, 0.f); });
+    }
+    regfft::dft_reg<XA, true>(v);
+    float2 *e1 = E + pb * LS1 + jj * (XA + 1);
+    regfft::static_for<0, XA>([&](auto t_) { e1[decltype(t_)::value] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+  // inverse stage 2: thread (pb, jj < XA) -> physical points jj + XA t of the pair, to Ph
+  const int pb = tid / XA, jj = tid - pb * XA;
+  const bool act = pb < PB;
+  if (act) {
+    float2 ph[XB];
+    const float2 *e1 = E + pb * LS1 + jj;
+    regfft::static_for<0, XB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e1[t * (XA + 1)];
+      if constexpr (t == 0) {
+        ph[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj * t);
+        ph[t] = make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);
+      }
+    });
+    regfft::dft_reg<XB, true>(ph);
+#pragma unroll
+    for (int t = 0; t < XB; ++t) Ph[pb * LSP + jj + XA * t] = ph[t];
+  }
+  __syncthreads();
+  {  // the forced points of the block's rows
+    const float Kibdt = (float)(g.Kib / sc->dt);
+    const int r0 = rec_off[(size_t)pl * G2 + l0], r1 = rec_off[(size_t)pl * G2 + l0 + 2 * npairs];
+    for (int e = r0 + tid; e < r1; e += blockDim.x) {
+      const IbRec R = rec[e];
+      const float val = Kibdt * d2f_alu(R.A * cap[R.ref] - cap[R.src]);
+      const int rr = R.k - l0;
+      float2 *z = Ph + (rr >> 1) * LSP + R.i;
+      if (rr & 1) z->y = val;
+      else z->x = val;
+    }
+  }
+  __syncthreads();
+  // forward stage 1: thread (pb, jj) transforms its points jj + XA t with the 8-point DFT -> E2
+  if (act) {
+    float2 pr[XB];
+#pragma unroll
+    for (int t = 0; t < XB; ++t) pr[t] = Ph[pb * LSP + jj + XA * t];
+    regfft::dft_reg<XB, false>(pr);
+    float2 *e2 = E + pb * LS2 + jj * (XB + 1);
+#pragma unroll
+    for (int t = 0; t < XB; ++t) e2[t] = pr[t];
+  }
+  __syncthreads();
+  // forward stage 2: line pb, thread jj2 < 8; outputs k = jj2 + 8 t, partner N - k by shuffle
+  if (tid < PB * XB) {
+    const int pb2 = tid / XB, jj2 = tid - pb2 * XB;
+    float2 v[XA];
+    const float2 *e2 = E + pb2 * LS2 + jj2;
+    regfft::static_for<0, XA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e2[t * (XB + 1)];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj2 * t);
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+    regfft::dft_reg<XA, false>(v);
+    const int lane = tid & 31, src = (lane & ~(XB - 1)) | ((XB - jj2) & (XB - 1));
+    const float s1 = 1.f / (float)N;
+    const bool ok = pb2 < npairs;
+    float2 *d0 = B + ((size_t)pl * G2 + l0 + 2 * pb2) * N1h, *d1 = d0 + N1h;
+    regfft::static_for<0, (NK + XB - 1) / XB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      float2 zp;
+      zp.x = __shfl_sync(0xffffffffu, v[XA - 1 - t].x, src);
+      zp.y = __shfl_sync(0xffffffffu, v[XA - 1 - t].y, src);
+      if (jj2 == 0) zp = t == 0 ? v[0] : v[(XA - t) % XA];
+      const int k = jj2 + XB * t;
+      if (ok && k < NK) {
+        const float2 z = v[t];
+        float2 o0 = make_float2(0.5f * (z.x + zp.x) * s1, 0.5f * (z.y - zp.y) * s1);
+        float2 o1 = make_float2(0.5f * (z.y + zp.y) * s1, -0.5f * (z.x - zp.x) * s1);
+        if (k == 0) { o0.y = 0.f; o1.y = 0.f; }
+        d0[k] = o0;
+        d1[k] = o1;
+      }
+    });
+  }
+}
+
+// ============================================================================
+// The forward z transforms of physical-x planes B [pl][l][kx] (FP32) into spectral planes
+// [pl][N2][N1h] complex128, x 1/N, the retained kz rows only (as k_zfwd_spec<float, N>).
+// ============================================================================
+template <int N>
+__global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restrict__ Bp, double2 *__restrict__ spec,
+                                                            Geo g, const float2 *__restrict__ tw) {
+  using P = zp2<N>;
+  // the inverse pass's plan read backwards: stage 1 ZA threads per line (ZB-point DFTs of rows
+  // jj + ZA t), stage 2 ZB threads per line (ZA-point DFTs), KB kx lines per block
+  constexpr int ZA = P::ZA, ZB = P::ZB, KB = P::KB;
+  constexpr int H = N / 3;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *E = reinterpret_cast<float2 *>(smem_raw);
+  const int pl = blockIdx.y, kx0 = blockIdx.x * KB, N1h = g.N1h;
+  const float2 *src = Bp + (size_t)pl * N * N1h;
+  const int tid = threadIdx.x;
+  if (tid < ZA * KB) {
+    const int jj = tid / KB, kk = tid - jj * KB, kx = kx0 + kk;
+    float2 v[ZB];
+    const bool ok = kx < N1h;
+    regfft::static_for<0, ZB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      v[t] = ok ? src[(size_t)(jj + ZA * t) * N1h + kx] : make_float2(0.f, 0.f);
+    });
+    regfft::dft_reg<ZB, false>(v);
+    float2 *e = E + jj * (ZB + 1) * KB + kk;  // e = jj ZB + t at e + e / ZB
+    regfft::static_for<0, ZB>([&](auto t_) { e[decltype(t_)::value * KB] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+  if (tid < ZB * KB) {
+    const int jj2 = tid / KB, kk = tid - jj2 * KB, kx = kx0 + kk;
+    float2 v[ZA];
+    const float2 *e = E + jj2 * KB + kk;
+    regfft::static_for<0, ZA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = e[t * (ZB + 1) * KB];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + jj2 * t);
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+    regfft::dft_reg<ZA, false>(v);
+    if (kx < N1h) {
+      const float s = 1.f / (float)N;
+      double2 *dst = spec + (size_t)pl * g.ncol + kx;
+      regfft::static_for<0, ZA>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        constexpr int mlo = ZB * t, mhi = ZB * t + ZB - 1;
+        const int m = jj2 + mlo;
+        int r = -1;
+        if (mlo < H && m < H) r = m;
+        else if (mhi >= N - H && m >= N - H) r = m - N + 2 * H;
+        if (r >= 0) dst[(size_t)r * N1h] = make_double2(f2d_alu(v[t].x * s), f2d_alu(v[t].y * s));
+      });
     }
   }
 }
