@@ -620,7 +620,7 @@ def main():
     line = {"metric": METRIC, "value": R["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": R["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if head == "fp64" else "f32 transforms/products/solves, f64 state, (0,0) mode and low-k pressure",
+            "dtype": "f64" if head == "fp64" else "f32 transforms/products and Helmholtz solves; f64 state, (0,0) mode, pressure and flux correction",
             "data": "synthetic (seeded perturbed laminar channel, see rnl_multiblock_nofft_gb300/workloads.py)",
             "config": {"workload": f"{args.workload}: {workload_desc(args.workload)}", "form": head,
                        "mode_points_per_substep": pts, "N1": s.N1, "N2": s.N2, "ny": s.p.ny,
