@@ -22,6 +22,19 @@
 #include "lh_internal.cuh"
 #include "lh_regfft.cuh"
 
+// Blocks per SM the compiler must leave registers for (the second __launch_bounds__ argument)
+// of the x pass, the inverse z pass and the forward z pass; 1 lets it use as many as it likes.
+// Build-time knobs for occupancy sweeps.
+#ifndef LH_XPASS2_MINB
+#define LH_XPASS2_MINB 1
+#endif
+#ifndef LH_ZINV2_MINB
+#define LH_ZINV2_MINB 1
+#endif
+#ifndef LH_ZFWD2_MINB
+#define LH_ZFWD2_MINB 1
+#endif
+
 // row pairs per block (one block: 96 threads at N = 384)
 template <int N> struct xp2 {
   static constexpr int XB = 8, XA = N / XB;
@@ -38,7 +51,7 @@ template <int N> struct xp2 {
 };
 
 template <int N>
-__global__ void __launch_bounds__(xp2<N>::NT) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+__global__ void __launch_bounds__(xp2<N>::NT, LH_XPASS2_MINB) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
                                                         const int *__restrict__ capslot, double *__restrict__ cap) {
   using P = xp2<N>;
@@ -299,7 +312,7 @@ __device__ __forceinline__ void zinv2_body(Gather &&gather, float2 *__restrict__
 }
 
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+__global__ void __launch_bounds__(zp2<N>::NT, LH_ZINV2_MINB) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                        const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
                                                        const float2 *__restrict__ tw) {
   const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * zp2<N>::KB;
@@ -365,7 +378,7 @@ template <int N> struct zf2 {
 };
 
 template <int N>
-__global__ void __launch_bounds__(zf2<N>::NTH) k_zfwd2(const float2 *__restrict__ B, Geo g, const float2 *__restrict__ tw,
+__global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const float2 *__restrict__ B, Geo g, const float2 *__restrict__ tw,
                                                         float2 *__restrict__ N1xz, float2 *__restrict__ N2xz,
                                                         float2 *__restrict__ N3xz, float2 *__restrict__ uvf,
                                                         float2 *__restrict__ vvc, float2 *__restrict__ wvf) {
@@ -470,9 +483,11 @@ __global__ void __launch_bounds__(zf2<N>::NTH) k_zfwd2(const float2 *__restrict_
 // the two rows of a pair are separated by warp shuffles into B [pl][l][kx].
 // ============================================================================
 template <int N> struct ibx2 {
+  // 16 row pairs per block: the first and last stages (8 threads per pair, XA-point DFTs) get
+  // 128 threads; the middle stages loop over their XA * PB work items with the block's 256
   static constexpr int XB = 8, XA = N / XB;
-  static constexpr int PB = XA >= 36 ? 4 : (XA >= 18 ? 8 : 16);
-  static constexpr int NT = ((XA * PB > PB * XB ? XA * PB : PB * XB) + 31) / 32 * 32;
+  static constexpr int PB = 16;
+  static constexpr int NT = 256;
   static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
   static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB), LSP = pad16(N);
   static constexpr int SMEM = (LS1 > LS2 ? LS1 : LS2) * PB * 8 + LSP * PB * 8;
@@ -485,7 +500,7 @@ __global__ void __launch_bounds__(ibx2<N>::NT) k_ib_xforce2(const float2 *__rest
                                                              const double *__restrict__ cap,
                                                              const DevScalars *__restrict__ sc) {
   using P = ibx2<N>;
-  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1, LS2 = P::LS2, LSP = P::LSP;
+  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, NT = P::NT, LS1 = P::LS1, LS2 = P::LS2, LSP = P::LSP;
   constexpr int NK = N / 3 + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *E = reinterpret_cast<float2 *>(smem_raw);
@@ -525,10 +540,9 @@ __global__ void __launch_bounds__(ibx2<N>::NT) k_ib_xforce2(const float2 *__rest
     regfft::static_for<0, XA>([&](auto t_) { e1[decltype(t_)::value] = v[decltype(t_)::value]; });
   }
   __syncthreads();
-  // inverse stage 2: thread (pb, jj < XA) -> physical points jj + XA t of the pair, to Ph
-  const int pb = tid / XA, jj = tid - pb * XA;
-  const bool act = pb < PB;
-  if (act) {
+  // inverse stage 2: item (pb, jj < XA) -> physical points jj + XA t of the pair, to Ph
+  for (int item = tid; item < XA * PB; item += NT) {
+    const int pb = item / XA, jj = item - pb * XA;
     float2 ph[XB];
     const float2 *e1 = E + pb * LS1 + jj;
     regfft::static_for<0, XB>([&](auto t_) {
@@ -559,8 +573,9 @@ __global__ void __launch_bounds__(ibx2<N>::NT) k_ib_xforce2(const float2 *__rest
     }
   }
   __syncthreads();
-  // forward stage 1: thread (pb, jj) transforms its points jj + XA t with the 8-point DFT -> E2
-  if (act) {
+  // forward stage 1: item (pb, jj) transforms its points jj + XA t with the 8-point DFT -> E2
+  for (int item = tid; item < XA * PB; item += NT) {
+    const int pb = item / XA, jj = item - pb * XA;
     float2 pr[XB];
 #pragma unroll
     for (int t = 0; t < XB; ++t) pr[t] = Ph[pb * LSP + jj + XA * t];
