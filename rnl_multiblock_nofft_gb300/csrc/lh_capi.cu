@@ -202,8 +202,6 @@ static cudaError_t set_attrs_sized(int lim) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv2<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec2<N>, A, lim);
     if constexpr (N <= 384)
-      if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_ib_xforce2<N>, A, lim);
-    if constexpr (N <= 384)
       if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass2<N>, A, lim);
   }
   return e;
@@ -1172,14 +1170,6 @@ static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int n
 template <typename T, int N>
 static int launch_ib_xforce(lh_handle *h, int npl) {
   typedef typename C2<T>::t V;
-  if constexpr (sizeof(T) == 4 && N <= 384) {  // the two-stage register form (mixed form)
-    using P = ibx2<N>;
-    dim3 g2((h->g.G2 / 2 + P::PB - 1) / P::PB, npl);
-    KL("k_ib_xforce", k_ib_xforce2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, h->g,
-                                                                     (const float2 *)h->twx, h->d_ibrec, h->d_iboff,
-                                                                     h->cap, h->sc));
-    return LH_OK;
-  }
   constexpr int PB = 4 * pb_xpass<V>(N);
   dim3 g2((h->g.G2 / 2 + PB - 1) / PB, npl);
   KL("k_ib_xforce", k_ib_xforce<T, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>(

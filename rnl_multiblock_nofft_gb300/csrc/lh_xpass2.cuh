@@ -29,7 +29,7 @@
 #define LH_XPASS2_MINB 1
 #endif
 #ifndef LH_ZINV2_MINB
-#define LH_ZINV2_MINB 1
+#define LH_ZINV2_MINB 6  // 56 registers: the state gather's latency wants the warps (fastest of a sweep at C1)
 #endif
 #ifndef LH_ZFWD2_MINB
 #define LH_ZFWD2_MINB 1
@@ -470,157 +470,6 @@ __global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const floa
       uvf[off + c] = uv;
       wvf[off + c] = wv;
     }
-  }
-}
-
-// ============================================================================
-// Immersed-boundary forcing in one two-stage x pass (the work of k_ib_xforce: imm_bounds_u/v,
-// FOU3D.f90:806-998): the rows of the du planes (A [pl][l][kx], after the inverse z pass) go
-// to physical space with the first inverse stage reading A directly (Hermitian completion), the
-// second stage leaves every row pair's physical line in shared memory, the forced points of the
-// rows are overwritten with Kib/dt (A u(i1,k1,j1) - u(i,k,j)) from the captured physical
-// velocities (records sorted by (plane, row)), and the lines come back with the forward stages;
-// the two rows of a pair are separated by warp shuffles into B [pl][l][kx].
-// ============================================================================
-template <int N> struct ibx2 {
-  // 16 row pairs per block: the first and last stages (8 threads per pair, XA-point DFTs) get
-  // 128 threads; the middle stages loop over their XA * PB work items with the block's 256
-  static constexpr int XB = 8, XA = N / XB;
-  static constexpr int PB = 16;
-  static constexpr int NT = 256;
-  static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
-  static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB), LSP = pad16(N);
-  static constexpr int SMEM = (LS1 > LS2 ? LS1 : LS2) * PB * 8 + LSP * PB * 8;
-};
-
-template <int N>
-__global__ void __launch_bounds__(ibx2<N>::NT) k_ib_xforce2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
-                                                             const float2 *__restrict__ tw, const IbRec *__restrict__ rec,
-                                                             const int *__restrict__ rec_off,
-                                                             const double *__restrict__ cap,
-                                                             const DevScalars *__restrict__ sc) {
-  using P = ibx2<N>;
-  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, NT = P::NT, LS1 = P::LS1, LS2 = P::LS2, LSP = P::LSP;
-  constexpr int NK = N / 3 + 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2 *E = reinterpret_cast<float2 *>(smem_raw);
-  float2 *Ph = E + (LS1 > LS2 ? LS1 : LS2) * PB;  // physical lines [pb][LSP]
-  const int G2 = g.G2, N1h = g.N1h;
-  const int pl = blockIdx.y, l0 = blockIdx.x * PB * 2;
-  const int npairs = min(PB, (G2 - l0) / 2);
-  const int tid = threadIdx.x;
-  // inverse stage 1: line pb, thread jj < 8
-  if (tid < PB * XB) {
-    const int pb = tid / XB, jj = tid - pb * XB;
-    float2 v[XA];
-    if (pb < npairs) {
-      const float2 *ra = A + (size_t)pl * G2 * N1h + (size_t)(l0 + 2 * pb) * N1h;
-      const float2 *rb = ra + N1h;
-      regfft::static_for<0, XA>([&](auto t_) {
-        constexpr int t = decltype(t_)::value;
-        constexpr int mlo = XB * t, mhi = XB * t + XB - 1;
-        constexpr bool direct = mlo < NK, conj = mhi > N - NK;
-        const int m = jj + mlo;
-        float2 z = make_float2(0.f, 0.f);
-        if (direct && m < NK) {
-          float2 a = __ldg(ra + m), b = __ldg(rb + m);
-          if (m == 0) { a.y = 0.f; b.y = 0.f; }
-          z = make_float2(a.x - b.y, a.y + b.x);
-        } else if (conj && m > N - NK) {
-          const float2 a = __ldg(ra + (N - m)), b = __ldg(rb + (N - m));
-          z = make_float2(a.x + b.y, -a.y + b.x);
-        }
-        v[t] = z;
-      });
-    } else {
-      regfft::static_for<0, XA>([&](auto t_) { v[decltype(t_)::value] = make_float2(0.f, 0.f); });
-    }
-    regfft::dft_reg<XA, true>(v);
-    float2 *e1 = E + pb * LS1 + jj * (XA + 1);
-    regfft::static_for<0, XA>([&](auto t_) { e1[decltype(t_)::value] = v[decltype(t_)::value]; });
-  }
-  __syncthreads();
-  // inverse stage 2: item (pb, jj < XA) -> physical points jj + XA t of the pair, to Ph
-  for (int item = tid; item < XA * PB; item += NT) {
-    const int pb = item / XA, jj = item - pb * XA;
-    float2 ph[XB];
-    const float2 *e1 = E + pb * LS1 + jj;
-    regfft::static_for<0, XB>([&](auto t_) {
-      constexpr int t = decltype(t_)::value;
-      const float2 x = e1[t * (XA + 1)];
-      if constexpr (t == 0) {
-        ph[0] = x;
-      } else {
-        const float2 w = __ldg(tw + jj * t);
-        ph[t] = make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);
-      }
-    });
-    regfft::dft_reg<XB, true>(ph);
-#pragma unroll
-    for (int t = 0; t < XB; ++t) Ph[pb * LSP + jj + XA * t] = ph[t];
-  }
-  __syncthreads();
-  {  // the forced points of the block's rows
-    const float Kibdt = (float)(g.Kib / sc->dt);
-    const int r0 = rec_off[(size_t)pl * G2 + l0], r1 = rec_off[(size_t)pl * G2 + l0 + 2 * npairs];
-    for (int e = r0 + tid; e < r1; e += blockDim.x) {
-      const IbRec R = rec[e];
-      const float val = Kibdt * d2f_alu(R.A * cap[R.ref] - cap[R.src]);
-      const int rr = R.k - l0;
-      float2 *z = Ph + (rr >> 1) * LSP + R.i;
-      if (rr & 1) z->y = val;
-      else z->x = val;
-    }
-  }
-  __syncthreads();
-  // forward stage 1: item (pb, jj) transforms its points jj + XA t with the 8-point DFT -> E2
-  for (int item = tid; item < XA * PB; item += NT) {
-    const int pb = item / XA, jj = item - pb * XA;
-    float2 pr[XB];
-#pragma unroll
-    for (int t = 0; t < XB; ++t) pr[t] = Ph[pb * LSP + jj + XA * t];
-    regfft::dft_reg<XB, false>(pr);
-    float2 *e2 = E + pb * LS2 + jj * (XB + 1);
-#pragma unroll
-    for (int t = 0; t < XB; ++t) e2[t] = pr[t];
-  }
-  __syncthreads();
-  // forward stage 2: line pb, thread jj2 < 8; outputs k = jj2 + 8 t, partner N - k by shuffle
-  if (tid < PB * XB) {
-    const int pb2 = tid / XB, jj2 = tid - pb2 * XB;
-    float2 v[XA];
-    const float2 *e2 = E + pb2 * LS2 + jj2;
-    regfft::static_for<0, XA>([&](auto t_) {
-      constexpr int t = decltype(t_)::value;
-      const float2 x = e2[t * (XB + 1)];
-      if constexpr (t == 0) {
-        v[0] = x;
-      } else {
-        const float2 w = __ldg(tw + jj2 * t);
-        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
-      }
-    });
-    regfft::dft_reg<XA, false>(v);
-    const int lane = tid & 31, src = (lane & ~(XB - 1)) | ((XB - jj2) & (XB - 1));
-    const float s1 = 1.f / (float)N;
-    const bool ok = pb2 < npairs;
-    float2 *d0 = B + ((size_t)pl * G2 + l0 + 2 * pb2) * N1h, *d1 = d0 + N1h;
-    regfft::static_for<0, (NK + XB - 1) / XB>([&](auto t_) {
-      constexpr int t = decltype(t_)::value;
-      float2 zp;
-      zp.x = __shfl_sync(0xffffffffu, v[XA - 1 - t].x, src);
-      zp.y = __shfl_sync(0xffffffffu, v[XA - 1 - t].y, src);
-      if (jj2 == 0) zp = t == 0 ? v[0] : v[(XA - t) % XA];
-      const int k = jj2 + XB * t;
-      if (ok && k < NK) {
-        const float2 z = v[t];
-        float2 o0 = make_float2(0.5f * (z.x + zp.x) * s1, 0.5f * (z.y - zp.y) * s1);
-        float2 o1 = make_float2(0.5f * (z.y + zp.y) * s1, -0.5f * (z.x - zp.x) * s1);
-        if (k == 0) { o0.y = 0.f; o1.y = 0.f; }
-        d0[k] = o0;
-        d1[k] = o1;
-      }
-    });
   }
 }
 
