@@ -141,7 +141,7 @@ static void prof_begin(lh_handle *h, const char *name) {
 static int count_launch(lh_handle *h) {
   h->launches++;
   if (h->prof && !h->prof_ev.empty()) cudaEventRecord(h->prof_ev.back().second.second, h->st);
-  cudaError_t e = cudaPeekAtLastError();
+  cudaError_t e = cudaGetLastError();  // this launch's error (and clears it)
   if (e != cudaSuccess) return fail(h, LH_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
   return LH_OK;
 }
@@ -1699,46 +1699,75 @@ extern "C" int lh_get_tuning(lh_handle *h, int32_t *cfg) {
 // ---------------------------------------------------------------------------
 struct lh_batch {
   std::vector<lh_handle *> hs;
-  cudaStream_t root;
-  cudaEvent_t ev0;
+  cudaStream_t root = nullptr;
+  cudaEvent_t ev0 = nullptr;
   std::vector<cudaEvent_t> evs;
-  cudaGraph_t graph;
-  cudaGraphExec_t gexec;
-  long long nodes;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  long long nodes = 0;
   std::string err;
 };
+extern "C" int lh_batch_destroy(lh_batch *b);
+
+// failure of a batch call: the message goes to lh_last_error(NULL)
+static int batch_fail(lh_batch *b, int code, const std::string &msg) {
+  t_last_err = msg;
+  if (b) b->err = msg;
+  return code;
+}
 
 extern "C" int lh_batch_create(lh_handle *const *handles, int n, lh_batch **out) {
-  if (!handles || n <= 0 || !out) return LH_EINVAL;
+  if (!handles || n <= 0 || !out) return batch_fail(nullptr, LH_EINVAL, "lh_batch_create: no handles");
   *out = nullptr;
   lh_batch *b = new lh_batch();
   b->hs.assign(handles, handles + n);
   for (lh_handle *h : b->hs)
-    if (!h) { delete b; return LH_EINVAL; }
-  if (cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev0, cudaEventDisableTiming) != cudaSuccess) { delete b; return LH_ECUDA; }
+    if (!h) { delete b; return batch_fail(nullptr, LH_EINVAL, "lh_batch_create: a null handle"); }
+  cudaError_t e = cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev0, cudaEventDisableTiming);
   b->evs.resize(n);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->evs[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    lh_batch_destroy(b);
+    return batch_fail(nullptr, LH_ECUDA, std::string("lh_batch_create: streams/events: ") + cudaGetErrorString(e));
+  }
   for (int i = 0; i < n; ++i)
-    if (cudaEventCreateWithFlags(&b->evs[i], cudaEventDisableTiming) != cudaSuccess) { delete b; return LH_ECUDA; }
-  for (lh_handle *h : b->hs)
-    if (cudaStreamSynchronize(h->st) != cudaSuccess) { delete b; return LH_ECUDA; }
-  if (cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { delete b; return LH_ECUDA; }
+    if ((e = cudaStreamSynchronize(b->hs[i]->st)) != cudaSuccess) {
+      lh_batch_destroy(b);
+      return batch_fail(nullptr, LH_ECUDA, "lh_batch_create: channel " + std::to_string(i) + " has a failed launch: " +
+                                               cudaGetErrorString(e));
+    }
+  if ((e = cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+    lh_batch_destroy(b);
+    return batch_fail(nullptr, LH_ECUDA, std::string("lh_batch_create: begin capture: ") + cudaGetErrorString(e));
+  }
   cudaEventRecord(b->ev0, b->root);
   int rc = LH_OK;
+  std::string why;
   for (int i = 0; i < n && rc == LH_OK; ++i) {
     lh_handle *h = b->hs[i];
     cudaStreamWaitEvent(h->st, b->ev0, 0);
     long long before = h->launches;
     rc = step_launches(h);
     h->launches = before;
+    if (rc != LH_OK) why = "channel " + std::to_string(i) + ": " + h->err;
     cudaEventRecord(b->evs[i], h->st);
     cudaStreamWaitEvent(b->root, b->evs[i], 0);
   }
-  cudaGraph_t gr;
-  cudaError_t e = cudaStreamEndCapture(b->root, &gr);
-  if (rc != LH_OK || e != cudaSuccess) { delete b; return rc != LH_OK ? rc : LH_ECUDA; }
+  cudaGraph_t gr = nullptr;
+  e = cudaStreamEndCapture(b->root, &gr);
+  if (rc != LH_OK || e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    lh_batch_destroy(b);
+    return rc != LH_OK ? batch_fail(nullptr, rc, "lh_batch_create: " + why)
+                       : batch_fail(nullptr, LH_ECUDA, std::string("lh_batch_create: end capture: ") + cudaGetErrorString(e));
+  }
   e = cudaGraphInstantiate(&b->gexec, gr, 0);
-  if (e != cudaSuccess) { cudaGraphDestroy(gr); delete b; return LH_ECUDA; }
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(gr);
+    lh_batch_destroy(b);
+    return batch_fail(nullptr, LH_ECUDA, std::string("lh_batch_create: graph instantiate: ") + cudaGetErrorString(e));
+  }
   b->graph = gr;
   size_t nn = 0;
   cudaGraphGetNodes(gr, nullptr, &nn);

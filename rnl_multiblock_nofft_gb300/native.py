@@ -326,7 +326,7 @@ class GpuBatch:
         b = C.c_void_p()
         rc = self.L.lh_batch_create(arr, len(self.channels), C.byref(b))
         if rc != LH_OK:
-            raise LhError(rc, "lh_batch_create failed")
+            raise LhError(rc, (self.L.lh_last_error(None) or b"lh_batch_create failed").decode())
         self.b = b
 
     def step(self, n: int = 1):
