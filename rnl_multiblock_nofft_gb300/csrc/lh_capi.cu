@@ -607,9 +607,14 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
       rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_press3)"); lh_destroy(h); return rc;
     }
   }
-  if (cudaFuncSetAttribute((const void *)k_helm00_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(8 * sizeof(double) * (size_t)(std::max(nu, nv) + 1))) != cudaSuccess) {
-    rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_helm00_pcr)"); lh_destroy(h); return rc;
+  {  // function attributes are per process, not per handle: the device's limit serves every channel
+    int lim = 0;
+    if (smem_optin(&lim) || (size_t)lim < 8 * sizeof(double) * (size_t)(std::max(nu, nv) + 1)) {
+      rc = fail(h, LH_EINVAL, "too many levels for the (0,0) solve's shared memory"); lh_destroy(h); return rc;
+    }
+    if (cudaFuncSetAttribute((const void *)k_helm00_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
+      rc = fail(h, LH_ECUDA, "cudaFuncSetAttribute(k_helm00_pcr)"); lh_destroy(h); return rc;
+    }
   }
   if (cudaFuncSetAttribute((const void *)k_meanflow_pcr, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) !=
       cudaSuccess) {
@@ -639,9 +644,10 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     if (smem_optin(&lim) || h->tri_smem > (size_t)lim) {
       rc = fail(h, LH_EINVAL, "plane too large for the triad form (shared memory)"); lh_destroy(h); return rc;
     }
+    // the device's limit, not this channel's need: the attribute is shared by every handle
     cudaError_t ea = (h->prec == LH_PREC_FP64)
-                         ? cudaFuncSetAttribute(k_triad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->tri_smem)
-                         : cudaFuncSetAttribute(k_triad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->tri_smem);
+                         ? cudaFuncSetAttribute(k_triad<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim)
+                         : cudaFuncSetAttribute(k_triad<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (ea != cudaSuccess) { rc = fail(h, LH_ECUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(ea)); lh_destroy(h); return rc; }
   }
   {  // pressure factors, once (start.f90:656-658)

@@ -57,3 +57,27 @@ def test_autotune_keeps_state_and_parity(cuda_ok):
     g.synchronize()
     for x, y in zip(o.get_state(), g.download_state()):
         assert rel(y, x) < 2 * 1e-12
+
+
+def test_mixed_batch_matches_channels_stepped_alone(cuda_ok):
+    """The mixed form in a batch: every channel's state after two batched steps equals (bit for bit)
+    the same channel stepped on its own. The channels are created largest first, so a kernel
+    attribute that one handle set for its own sizes could not serve an earlier, larger one."""
+    setups = sorted(ensemble_setups(6, seed=91), key=lambda s: -s.nyu * s.ncols)
+    alone, batched = [], []
+    for i, s in enumerate(setups):
+        st = initial_field(s, 500 + i)
+        for lst in (alone, batched):
+            g = GpuChannel(s, "mixed")
+            g.upload_state(*st)
+            g.set_scalars(**initial_scalars(s))
+            lst.append(g)
+    b = GpuBatch(batched)
+    b.step(2)
+    b.synchronize()
+    for g in alone:
+        g.step(2)
+        g.synchronize()
+    for ga, gb in zip(alone, batched):
+        for x, y in zip(ga.download_state(), gb.download_state()):
+            assert np.array_equal(x, y)
