@@ -427,7 +427,8 @@ def run_ensemble(args, ws, rank, pg, torch, np):
     head = "mixed" if "mixed" in res else forms[0]
     line = {"metric": METRIC, "value": res[head]["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res[head]["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32 transforms, f64 state",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if head == "fp64" else "f32 transforms/products and Helmholtz solves; f64 state, (0,0) mode, pressure and flux correction",
             "data": "synthetic ensemble (seeded grids, Re_tau, textures and fields)",
             "config": {"workload": "C3: 64 channels, N in {32,48,64,96}, ny in {97,129,153}, Re_tau 120-300, posts",
                        "form": head, "mode_points_per_substep": pts, "launch": "one CUDA graph per step"},

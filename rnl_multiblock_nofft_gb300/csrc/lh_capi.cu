@@ -200,6 +200,8 @@ static cudaError_t set_attrs_sized(int lim) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv2<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd2<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv2<N>, A, lim);
+    if constexpr (N == 576 || N == 768 || N == 1152)
+      if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass3<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec2<N>, A, lim);
     if constexpr (N <= 384)
       if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass2<N>, A, lim);
@@ -1051,6 +1053,12 @@ static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const
     using P = xp2<N>;
     dim3 grid((g.G2 / 2 + P::PB - 1) / P::PB, nslots);
     KL("k_xpass_nl", k_xpass2<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
+                                                                  (const float2 *)twx, doCFL, h->sc, capslot, h->cap));
+    return LH_OK;
+  } else if constexpr (sizeof(T) == 4 && (N == 576 || N == 768 || N == 1152)) {  // three-stage register form
+    using P = xp3<N>;
+    dim3 grid(g.G2 / 2, nslots);
+    KL("k_xpass_nl", k_xpass3<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
                                                                   (const float2 *)twx, doCFL, h->sc, capslot, h->cap));
     return LH_OK;
   }

@@ -533,3 +533,236 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restr
     }
   }
 }
+
+// ============================================================================
+// The x pass of the mixed form at the long lengths (576, 768, 1152) as a three-stage register
+// transform, N = XA * XM * 8, one row pair per block (the work of k_xpass_nl, same A and B
+// layouts). Stages, each a register DFT between padded shared-memory lines:
+//   inverse: XA-point DFTs gathered straight from A (Hermitian completion) -> XM-point DFTs ->
+//            8-point DFTs fused with the products, the CFL maxima and the forward 8-point DFTs
+//   forward: -> XM-point DFTs -> XA-point DFTs -> natural order, from where the two rows of the
+//            pair are separated (output k with its partner N - k) into B.
+// The element e of a stage's output sits at e + e / D in its line (D the stage's contiguous
+// block), so the lanes of one store or load fall on different banks.
+// ============================================================================
+template <int N> struct xp3 {
+  static constexpr int XA = N == 576 ? 12 : 16, XM = N / (8 * XA), XB = 8;
+  static constexpr int L1 = N / XA, LM = N / XM, LB = N / XB;  // threads per line of the stages
+  static constexpr int NT = 256;
+  static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
+  static constexpr int LS = pad16(N + N / 8 + 1);            // line stride (float2), >= every padded size
+  static constexpr int SMEM = 2 * 4 * LS * 8;                // two buffers of 4 lines
+};
+
+template <int N>
+__global__ void __launch_bounds__(xp3<N>::NT) k_xpass3(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+                                                        const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
+                                                        const int *__restrict__ capslot, double *__restrict__ cap) {
+  using P = xp3<N>;
+  constexpr int XA = P::XA, XM = P::XM, XB = P::XB, L1 = P::L1, LM = P::LM, LB = P::LB, NT = P::NT, LS = P::LS;
+  static_assert(XA * XM * XB == N, "x plan");
+  constexpr int NK = N / 3 + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *BA = reinterpret_cast<float2 *>(smem_raw), *BB = BA + 4 * LS;  // the two buffers [line][LS]
+  const int G2 = g.G2, N1h = g.N1h;
+  const int slot = blockIdx.y;
+  const bool isU = slot < g.nuI;
+  const int q = slot_level(g, slot, isU);
+  const int l = blockIdx.x * 2;  // the row pair (l, l + 1)
+  const size_t fstride = (size_t)G2 * N1h;
+  const int tid = threadIdx.x;
+  // ---- inverse stage 1 (XA-point, Ns = 1): line f, thread j < L1, elements j + L1 t -> BA at e + e / XA ----
+  for (int it = tid; it < 3 * L1; it += NT) {
+    const int f = it / L1, j = it - f * L1;
+    const float2 *ra = A + (size_t)(slot * 3 + f) * fstride + (size_t)l * N1h, *rb = ra + N1h;
+    float2 v[XA];
+    regfft::static_for<0, XA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      constexpr int mlo = L1 * t, mhi = L1 * t + L1 - 1;
+      constexpr bool direct = mlo < NK, conj = mhi > N - NK;
+      const int m = j + mlo;
+      float2 z = make_float2(0.f, 0.f);
+      if (direct && m < NK) {
+        float2 a = __ldg(ra + m), b = __ldg(rb + m);
+        if (m == 0) { a.y = 0.f; b.y = 0.f; }
+        z = make_float2(a.x - b.y, a.y + b.x);
+      } else if (conj && m > N - NK) {
+        const float2 a = __ldg(ra + (N - m)), b = __ldg(rb + (N - m));
+        z = make_float2(a.x + b.y, -a.y + b.x);
+      }
+      v[t] = z;
+    });
+    regfft::dft_reg<XA, true>(v);
+    float2 *o = BA + f * LS + j * (XA + 1);  // e = j XA + t
+    regfft::static_for<0, XA>([&](auto t_) { o[decltype(t_)::value] = v[decltype(t_)::value]; });
+  }
+  __syncthreads();
+  // ---- inverse stage 2 (XM-point, Ns = XA): thread j < LM, k = j % XA, elements j + LM t ----
+  for (int it = tid; it < 3 * LM; it += NT) {
+    const int f = it / LM, j = it - f * LM, k = j % XA;
+    float2 v[XM];
+    const float2 *in = BA + f * LS;
+    regfft::static_for<0, XM>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int e = j + LM * t;
+      const float2 x = in[e + e / XA];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + k * t * XB);  // exp(+2 pi i k t / (XA XM)): conj of the table
+        v[t] = make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);
+      }
+    });
+    regfft::dft_reg<XM, true>(v);
+    float2 *o = BB + f * LS;
+    const int base = (j / XA) * XA * XM + k;
+    regfft::static_for<0, XM>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int e = base + XA * t;
+      o[e + e / (XA * XM)] = v[t];
+    });
+  }
+  __syncthreads();
+  // ---- fused: inverse stage 3 (8-point, Ns = LB), products, CFL, forward stage 1 -> BA at e + e / 8 ----
+  const int nprod = isU ? 4 : 2;
+  float m1 = 0.f, m2 = 0.f, m3 = 0.f;
+  for (int j = tid; j < LB; j += NT) {
+    float2 ph[3][XB];
+    float2 w[XB];
+    w[0] = make_float2(1.f, 0.f);
+    regfft::static_for<1, XB>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const float2 x = __ldg(tw + j * t);
+      w[t] = make_float2(x.x, -x.y);
+    });
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const float2 *in = BB + f * LS;
+      regfft::static_for<0, XB>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        const int e = j + LB * t;
+        const float2 x = in[e + e / (XA * XM)];
+        ph[f][t] = t == 0 ? x : make_float2(x.x * w[t].x - x.y * w[t].y, x.x * w[t].y + x.y * w[t].x);
+      });
+      regfft::dft_reg<XB, true>(ph[f]);
+    }
+    if (capslot) {
+      const int cs = capslot[slot];
+      if (cs >= 0) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + j;
+          regfft::static_for<0, XB>([&](auto t_) {
+            constexpr int t = decltype(t_)::value;
+            cp[t * LB] = f2d_alu(ph[f][t].x);
+            cp[N + t * LB] = f2d_alu(ph[f][t].y);
+          });
+        }
+      }
+    }
+    if (doCFL) {
+      if (isU) {
+#pragma unroll
+        for (int t = 0; t < XB; ++t) {
+          m1 = nmax(m1, nmax(fabsf(ph[0][t].x), fabsf(ph[0][t].y)));
+          m3 = nmax(m3, nmax(fabsf(ph[2][t].x), fabsf(ph[2][t].y)));
+        }
+      } else {
+        const float thv = g.thvf[q];
+#pragma unroll
+        for (int t = 0; t < XB; ++t) m2 = nmax(m2, nmax(fabsf(ph[1][t].x), fabsf(ph[1][t].y)) * thv);
+      }
+    }
+    regfft::static_for<0, 4>([&](auto p_) {
+      constexpr int p = decltype(p_)::value;
+      constexpr int ua = p == 2 ? 1 : (p == 3 ? 2 : 0), ub = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 1 : 2));
+      constexpr int va = p == 0 ? 0 : 2, vb = 1;
+      if (p < 2 || isU) {
+        float2 pr[XB];
+#pragma unroll
+        for (int t = 0; t < XB; ++t) {
+          const float2 x0 = isU ? ph[ua][t] : ph[va][t], x1 = isU ? ph[ub][t] : ph[vb][t];
+          pr[t] = make_float2(x0.x * x1.x, x0.y * x1.y);
+        }
+        regfft::dft_reg<XB, false>(pr);
+        float2 *o = BA + p * LS + j * (XB + 1);  // e = j 8 + t
+#pragma unroll
+        for (int t = 0; t < XB; ++t) o[t] = pr[t];
+      }
+    });
+  }
+  if (doCFL) {
+    m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
+    if ((tid & 31) == 0) {
+      if (isU) { atomic_max_pos(&sc->u1m, f2d_alu(m1)); atomic_max_pos(&sc->u3m, f2d_alu(m3)); }
+      else atomic_max_pos(&sc->u2m, f2d_alu(m2));
+    }
+  }
+  __syncthreads();
+  // ---- forward stage 2 (XM-point, Ns = 8): thread j < LM, k = j % 8, elements j + LM t -> BB at e + e / (8 XM) ----
+  for (int it = tid; it < nprod * LM; it += NT) {
+    const int p = it / LM, j = it - p * LM, k = j % XB;
+    float2 v[XM];
+    const float2 *in = BA + p * LS;
+    regfft::static_for<0, XM>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int e = j + LM * t;
+      const float2 x = in[e + e / XB];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + k * t * XA);  // exp(-2 pi i k t / (8 XM))
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+    regfft::dft_reg<XM, false>(v);
+    float2 *o = BB + p * LS;
+    const int base = (j / XB) * XB * XM + k;
+    regfft::static_for<0, XM>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int e = base + XB * t;
+      o[e + e / (XB * XM)] = v[t];
+    });
+  }
+  __syncthreads();
+  // ---- forward stage 3 (XA-point, Ns = 8 XM = L1): thread j < L1, elements j + L1 t -> BA natural (k + k / 32) ----
+  for (int it = tid; it < nprod * L1; it += NT) {
+    const int p = it / L1, j = it - p * L1;
+    float2 v[XA];
+    const float2 *in = BB + p * LS;
+    regfft::static_for<0, XA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int e = j + L1 * t;
+      const float2 x = in[e + e / (XB * XM)];
+      if constexpr (t == 0) {
+        v[0] = x;
+      } else {
+        const float2 w = __ldg(tw + j * t);
+        v[t] = make_float2(x.x * w.x - x.y * w.y, x.x * w.y + x.y * w.x);
+      }
+    });
+    regfft::dft_reg<XA, false>(v);
+    float2 *o = BA + p * LS;
+    regfft::static_for<0, XA>([&](auto t_) {
+      constexpr int t = decltype(t_)::value;
+      const int k = j + L1 * t;
+      o[k + k / 32] = v[t];
+    });
+  }
+  __syncthreads();
+  // ---- the two rows of the pair: output k with its partner N - k, written to B ----
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  const float s1 = 1.f / (float)N;
+  for (int it = tid; it < nprod * NK; it += NT) {
+    const int p = it / NK, k = it - p * NK;
+    const float2 *L = BA + p * LS;
+    const int kp = k == 0 ? 0 : N - k;
+    const float2 z = L[k + k / 32], zp = L[kp + kp / 32];
+    float4 o;
+    o.x = 0.5f * (z.x + zp.x) * s1; o.y = 0.5f * (z.y - zp.y) * s1;
+    o.z = 0.5f * (z.y + zp.y) * s1; o.w = -0.5f * (z.x - zp.x) * s1;
+    if (k == 0) { o.y = 0.f; o.w = 0.f; }
+    float2 *dst = B + (((size_t)(pbase + p) * (G2 / 2) + (l >> 1)) * N1h + k) * 2;
+    *reinterpret_cast<float4 *>(dst) = o;
+  }
+}
