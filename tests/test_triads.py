@@ -143,3 +143,35 @@ def test_triad_fields_closer_to_golden(triad_run5, it):
         rel = np.linalg.norm(a - b) / np.linalg.norm(b)
         assert rel < 1.25 * TRIAD_GAP[it][f], (f, rel)
         assert rel < PRODUCT_GAP[it][f], (f, rel)
+
+
+# the same gaps restricted to the planes whose list files are the reference's own (files y01-y09:
+# planes 1-9 and their mirror planes 144-152) against the other planes, after 1 and 5 steps
+# (measured, 25 % headroom): w is 9x closer there, p 3.8x (the pressure solve couples every level,
+# so the missing lists above plane 9 still reach it), u and v ~20 % closer
+TRIAD_GAP_OWN = {1: {"u1": 7.7e-5, "u2": 5.3e-4, "u3": 3.9e-4, "p": 5.6e-2},
+                 5: {"u1": 3.5e-4, "u2": 2.3e-3, "u3": 2.2e-3, "p": 7.5e-2}}
+
+
+@pytest.mark.parametrize("it", [1, 5])
+def test_triad_gap_on_the_planes_with_the_references_lists(triad_run5, it):
+    states, _ = triad_run5
+    s = build_setup(ChannelParams())
+    fu, fv = plane_files(s)
+    g = np.load(os.path.join(GOLD, f"golden_it{it}.npz"))
+    for f, a in zip(FIELDS, states[it - 1]):
+        b = g[f].astype(np.complex128)
+        files = np.asarray(fv if f == "u2" else fu)
+        if f == "p":
+            files = files[1:-1]
+        own, other = (files >= 1) & (files <= 9), files > 9
+        r_own = np.linalg.norm((a - b)[:, own]) / np.linalg.norm(b[:, own])
+        r_other = np.linalg.norm((a - b)[:, other]) / np.linalg.norm(b[:, other])
+        assert r_own < TRIAD_GAP_OWN[it][f], (f, r_own)
+        assert r_own < r_other, (f, r_own, r_other)
+    e = lambda f: states[it - 1][FIELDS.index(f)]
+    files = np.asarray(fu)
+    own, other = (files >= 1) & (files <= 9), files > 9
+    w = g["u3"].astype(np.complex128)
+    assert (np.linalg.norm((e("u3") - w)[:, own]) / np.linalg.norm(w[:, own])) * 5 < \
+        np.linalg.norm((e("u3") - w)[:, other]) / np.linalg.norm(w[:, other])
