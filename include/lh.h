@@ -220,11 +220,22 @@ int lh_phys_to_four(lh_handle *h, const void *phys, void *spec, int nplanes);
  * stats.f90:109-250): wall-band planes only, indexed by the distance j1 = 1.. from the
  * wall, the top band mirrored onto the bottom with the sign of V flipped. Sums 0-8 are in
  * FP64 from planes in the form's transform precision; 9-10 from the FP64 state. The
- * pressure sums are not formed: the reference's come from ppPL, which holds the spectral
- * packing of p (FOU3D.f90:156-157), not a physical field. */
+ * pressure sums and the tile-conditioned omega_x sums are accumulated by the same call and
+ * read with lh_stats_get_pw. */
 int lh_stats_accumulate(lh_handle *h);
 /* zeroes every accumulator (plane, conditioned, spectra, slip) and istat */
 int lh_stats_reset(lh_handle *h);
+/* Pressure plane sums P, P^2 (stats.f90:43-50) and the tile-conditioned P, P^2, omega_x,
+ * omega_x^2 (PmC, P2mC, wxmC, wx2mC: stats.f90:91-92, 100-101), from the FP64 state. The
+ * reference sums ppPL, which holds the spectral packing of p left by record_out
+ * (FOU3D.f90:156-157), and conditions wx, allocated (N1+2) x N2, through an igal x kgal dummy;
+ * here p is transformed the way the velocities are (the plane's dealiased grid; the p planes
+ * of the wall bands are N(4,0)+1 .. N(4,1)-1 and N(4,2)+2 .. N(4,3), the others core planes)
+ * and omega_x of the wall-band v planes N(3,0) .. N(3,1), N(3,2)+1 .. N(3,3)+1 on the same
+ * dealiased grid, conditioned like the velocities with xsign 1.
+ * pplane: [2][nyu - 2] (p level index); cond4: [4][ncl + 1][dnz][dnx], level j1 = 0 .. ncl
+ * (0: the first plane from the wall, the file's level 0); NULL skips one. Blocking. */
+int lh_stats_get_pw(lh_handle *h, double *pplane, double *cond4);
 /* ncl: conditioned levels; dnx, dnz: tile size in physical points (0 without tiles) */
 int lh_stats_dims(lh_handle *h, int *ncl, int *dnx, int *dnz);
 /* plane: [11][nyu] (u-level quantities at u index j+dny, v-level ones at v index j+dny);

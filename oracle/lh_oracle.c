@@ -145,8 +145,9 @@ struct orc {
   fftplan pxc, pzc;
   unsigned char *lng;
   int bj[3][3][2]; /* [band 0..2][grid: 0 u, 1 v, 2 p][lo, hi], reference j */
-  /* statistics (stats.f90): plane sums [11][nu], tile-conditioned sums [9][ncl][dnz][dnx] */
-  double *st_pl, *st_cd;
+  /* statistics (stats.f90): plane sums [11][nu], tile-conditioned sums [9][ncl][dnz][dnx];
+   * pressure plane sums [2][np] and the conditioned P, omega_x sums [4][ncl + 1][dnz][dnx] */
+  double *st_pl, *st_cd, *st_pp, *st_cd4;
   int st_ncl, st_dnx, st_dnz;
   int64_t istat;
   /* spectra (spectra.f90): sp(level, long column) of U, V, W, UV, P, level fastest */
@@ -352,7 +353,7 @@ void orc_destroy(orc *O) {
                   O->Au, O->Av, O->lu, O->lv, O->u1, O->u2, O->u3, O->p, O->Nu1, O->Nu2, O->Nu3,
                   O->du1, O->du2, O->du3, O->psi, O->div, O->u1i, O->u2i, O->u3i, O->uvf, O->wvf,
                   O->vvc, O->N1xz, O->N2xz, O->N3xz, O->DG, O->phys_u1, O->phys_u3, O->phys_u2,
-                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng, O->st_pl, O->st_cd,
+                  O->tdata, O->toff, O->tlen, O->tsu, O->tsv, O->lng, O->st_pl, O->st_cd, O->st_pp, O->st_cd4,
                   O->sp[0], O->sp[1], O->sp[2], O->sp[3], O->sp[4], O->slip};
   for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
   plan_free(&O->px); plan_free(&O->pz); plan_free(&O->pxc); plan_free(&O->pzc);
@@ -1193,6 +1194,8 @@ static void stats_alloc(orc *O) {
   O->st_dnz = (tx > 0 && tz > 0) ? O->G2 / tz : 0;
   O->st_pl = (double *)calloc((size_t)11 * O->nu, sizeof(double));
   O->st_cd = (double *)calloc((size_t)9 * ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1), sizeof(double));
+  O->st_pp = (double *)calloc((size_t)2 * O->np, sizeof(double));
+  O->st_cd4 = (double *)calloc((size_t)4 * (ncl + 1) * (O->st_dnx ? O->st_dnx * O->st_dnz : 1), sizeof(double));
   O->istat = 0;
   O->nlong = 0;
   for (int c = 0; c < O->ncol; ++c) O->nlong += (!O->mb || O->lng[c]);
@@ -1305,6 +1308,75 @@ static void wx_plane(orc *O, int j, double *phys, pwork *w, double *ps, double *
   *ps2 = s2;
 }
 
+/* p plane j of the wall bands: N(4,0)+1 .. N(4,1)-1 and N(4,2)+2 .. N(4,3), the pgrid
+ * plane ranges of the bottom and top bands (start.f90:1995-2049); the others are core-band
+ * planes */
+static inline int fine_p(const orc *O, int j) { return !O->mb || j <= O->c.N4[1] - 1 || j >= O->c.N4[2] + 2; }
+
+/* conddown1 / condup1 with xsign 1 (stats.f90:109-138, 178-210) of one physical plane on
+ * the G1 x G2 grid: tile position (i mod dnx, l mod dnz), level j1 (0 = the first plane of
+ * the band, the file's level 0), into the pair qa, qa + 1 of st_cd4 */
+static void cond_plane(orc *O, int qa, int j1, const double *f, int G1, int G2) {
+  const int dnx = O->st_dnx, dnz = O->st_dnz, ncl1 = O->st_ncl + 1;
+  double *m = O->st_cd4 + ((size_t)qa * ncl1 + j1) * dnz * dnx;
+  double *m2 = O->st_cd4 + ((size_t)(qa + 1) * ncl1 + j1) * dnz * dnx;
+  for (int l = 0; l < G2; ++l)
+    for (int i = 0; i < G1; ++i) {
+      const double x = f[(size_t)l * G1 + i];
+      const size_t e = (size_t)(l % dnz) * dnx + (i % dnx);
+      m[e] += x;
+      m2[e] += x * x;
+    }
+}
+
+/* Pressure statistics (stats.f90:43-50 and the PmC / wxmC calls, stats.f90:91-92, 100-101). The
+ * reference sums ppPL, which holds the spectral packing of p left by record_out
+ * (FOU3D.f90:156-157); here the physical pressure is formed the way the velocities are
+ * (four_to_phys on the plane's dealiased grid) and summed over its points: every p plane
+ * for P, P^2 (st_pp [2][np]), the wall-band planes for the conditioned sums (st_cd4 pairs
+ * 0, 1). omega_x (FOU3D.f90:300-327) of the wall-band v planes j = N(3,0) .. N(3,1) and
+ * N(3,2)+1 .. N(3,3)+1 is transformed on the same dealiased grid (its spectrum padded like
+ * the velocities') and conditioned into pairs 2, 3. */
+static void pressure_wx_stats(orc *O, double *f, pwork *w) {
+  const int *N3 = O->c.N3, *N4 = O->c.N4;
+  for (int j = N4[0] + 1; j <= N4[3]; ++j) {
+    pview v;
+    const int fine = fine_p(O, j);
+    view_of(O, fine, &v);
+    four_to_phys_plane(O, &v, PL(O->p, PIDX(j)), f, w);
+    const size_t pp = (size_t)v.G1 * v.G2;
+    double s = 0, s2 = 0;
+    for (size_t e = 0; e < pp; ++e) {
+      s += f[e];
+      s2 += f[e] * f[e];
+    }
+    O->st_pp[PIDX(j)] += s;
+    O->st_pp[(size_t)O->np + PIDX(j)] += s2;
+    if (!O->st_dnx || !fine) continue;
+    if (j <= N4[1] - 1) cond_plane(O, 0, j - N4[0] - 1, f, v.G1, v.G2);
+    else if (j >= N4[2] + 2) cond_plane(O, 0, N4[3] - j, f, v.G1, v.G2);
+  }
+  if (!O->st_dnx) return;
+  cplx *ws = zalloc((size_t)O->ncol);
+  pview v;
+  view_of(O, 1, &v);
+  for (int j = N3[0]; j <= N3[3] + 1; ++j) {
+    int j1;
+    if (j <= N3[1]) j1 = j - N3[0];
+    else if (j > N3[2]) j1 = N3[3] + 1 - j;
+    else continue;
+    const int q = UIDX(j);
+    const double fy = O->thv[q] * O->c.ddthetavi;
+    for (int c = 0; c < O->ncol; ++c) {
+      const cplx dz = (I * O->k1z[c / O->N1h]) * PL(O->u2, q)[c];
+      ws[c] = -dz + (PL(O->u3, q + 1)[c] - PL(O->u3, q)[c]) * fy;
+    }
+    four_to_phys_plane(O, &v, ws, f, w);
+    cond_plane(O, 2, j1, f, v.G1, v.G2);
+  }
+  free(ws);
+}
+
 /* spectra (spectra.f90:1-56): buildsp / buildspUV over band 2's columns (the long
  * columns, in the order of columns_long_list) and levels, sp(j, column) += |u|^2,
  * spUV += Re u1 Re u2_itp + Im u1 Im u2_itp (u2_itp: v interpolated to the centres) */
@@ -1386,6 +1458,7 @@ int orc_stats_accumulate(orc *O) {
     O->st_pl[9 * (size_t)O->nu + UIDX(j)] += s;
     O->st_pl[10 * (size_t)O->nu + UIDX(j)] += s2;
   }
+  pressure_wx_stats(O, f1, &w);
   pwork_free(&w);
   free(f1); free(f2); free(f3);
   spectra_accumulate(O);
@@ -1401,6 +1474,16 @@ int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims
   if (cond && O->st_dnx) memcpy(cond, O->st_cd, sizeof(double) * nc);
   if (istat) *istat = O->istat;
   if (dims) { dims[0] = O->st_ncl; dims[1] = O->st_dnx; dims[2] = O->st_dnz; }
+  return 0;
+}
+
+/* pressure plane sums [2][np] and conditioned P, P^2, omega_x, omega_x^2 [4][ncl + 1][dnz][dnx]
+ * (NULL skips one; cond only with tiles) */
+int orc_stats_get_pw(orc *O, double *pplane, double *cond4) {
+  if (!O->st_pl) stats_alloc(O);
+  if (pplane) memcpy(pplane, O->st_pp, sizeof(double) * 2 * (size_t)O->np);
+  if (cond4 && O->st_dnx)
+    memcpy(cond4, O->st_cd4, sizeof(double) * 4 * (size_t)(O->st_ncl + 1) * O->st_dnx * O->st_dnz);
   return 0;
 }
 
@@ -1434,6 +1517,8 @@ int orc_stats_reset(orc *O) {
   if (!O->st_pl) stats_alloc(O);
   memset(O->st_pl, 0, sizeof(double) * 11 * (size_t)O->nu);
   memset(O->st_cd, 0, sizeof(double) * 9 * (size_t)O->st_ncl * (O->st_dnx ? O->st_dnx * O->st_dnz : 1));
+  memset(O->st_pp, 0, sizeof(double) * 2 * (size_t)O->np);
+  memset(O->st_cd4, 0, sizeof(double) * 4 * (size_t)(O->st_ncl + 1) * (O->st_dnx ? O->st_dnx * O->st_dnz : 1));
   for (int q = 0; q < 5; ++q) memset(O->sp[q], 0, sizeof(double) * (size_t)O->sp_nl[q] * O->nlong);
   memset(O->slip, 0, sizeof(cplx) * 8 * (size_t)O->ncol);
   O->istat = 0;

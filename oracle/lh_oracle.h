@@ -23,6 +23,8 @@ int orc_stats_accumulate(orc *O);
 /* plane: [11][nu]; dims: ncl, dnx, dnz */
 int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims);
 int orc_stats_reset(orc *O);
+/* pplane: [2][np] (P, P^2); cond4: [4][ncl + 1][dnz][dnx] (P, P^2, omega_x, omega_x^2) */
+int orc_stats_get_pw(orc *O, double *pplane, double *cond4);
 int orc_spectra_get(orc *O, double *sU, double *sV, double *sW, double *sUV, double *sP, int *nl, int *nlong);
 int orc_slip_get(orc *O, double *acc);
 int orc_slip_planes(orc *O, double *out);

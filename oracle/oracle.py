@@ -50,6 +50,7 @@ def lib():
         L.orc_stats_accumulate.argtypes = [vp]
         L.orc_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
         L.orc_stats_reset.argtypes = [vp]
+        L.orc_stats_get_pw.argtypes = [vp, dp, dp]
         L.orc_spectra_get.argtypes = [vp] + [dp] * 5 + [C.POINTER(C.c_int)] * 2
         L.orc_slip_get.argtypes = [vp, dp]
         L.orc_slip_planes.argtypes = [vp, dp]
@@ -180,6 +181,17 @@ class Oracle:
         ist = C.c_int64()
         lib().orc_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist), dims)
         return plane, cond, ist.value
+
+    def stats_pw(self):
+        """(pressure plane sums [2][nyu - 2], conditioned P, P^2, omega_x, omega_x^2
+        [4][ncl + 1][dnz][dnx] or None)"""
+        dims = (C.c_int * 3)()
+        lib().orc_stats_get(self.h, None, None, None, dims)
+        ncl, dnx, dnz = dims[0], dims[1], dims[2]
+        pplane = np.zeros((2, self.s.nyu - 2))
+        cond = np.zeros((4, ncl + 1, dnz, dnx)) if dnx else None
+        lib().orc_stats_get_pw(self.h, _dptr(pplane), _dptr(cond))
+        return pplane, cond
 
     def four_to_phys(self, spec: np.ndarray) -> np.ndarray:
         spec = np.ascontiguousarray(spec, np.complex128)

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "lh_internal.cuh"
@@ -69,6 +70,11 @@ struct lh_handle {
   int nlong, nshort;
   // statistics
   double *st_pl, *st_cd;
+  double *st_pp, *st_cd4;    // pressure plane sums [2][np]; conditioned P, omega_x [4][ncl + 1][dnz][dnx]
+  int4 *d_cond_list;         // planes of the conditioned P, omega_x sums: (kind, level, j1) (first use)
+  int n_cond;
+  void *d_cond_scr;          // their spectral and physical planes, one chunk of cond_chunk planes
+  int cond_chunk;
   double *d_sp;              // spectra accumulators: U, V, W, UV, P, each [level][nlong] (allocated on first use)
   double2 *d_slip, *d_slip_inst;  // slip statistics [2][4][ncol]: accumulated / instantaneous
   int st_ncl, st_dnx, st_dnz, st_ntx;
@@ -592,6 +598,8 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     h->istat = 0;
     ZA(h->st_pl, sizeof(double) * 11 * (size_t)nu);
     ZA(h->st_cd, sizeof(double) * 9 * (size_t)ncl * (tiles ? (size_t)h->st_dnx * h->st_dnz : 1));
+    ZA(h->st_pp, sizeof(double) * 2 * (size_t)(nu - 2));
+    ZA(h->st_cd4, sizeof(double) * 4 * (size_t)(ncl + 1) * (tiles ? (size_t)h->st_dnx * h->st_dnz : 1));
   }
   int rc = set_smem_attrs_all(h);
   if (rc != LH_OK) { lh_destroy(h); return rc; }
@@ -682,7 +690,7 @@ extern "C" int lh_destroy(lh_handle *h) {
                   h->d_ibslot_u, h->d_ibslot_v, h->d_iblev, h->d_lev2cap_u,
                   h->d_lev2cap_v, h->d_ibrec, h->d_iboff, h->cap, h->duib, h->d_terms, h->d_wb, h->d_lid, h->d_tmap,
                   h->d_slotq, h->d_capv, h->d_vcol, h->d_bcols, h->twv[1][0], h->twv[1][1],
-                  h->ysv, h->a3v, h->st_pl, h->st_cd, h->d_sp, h->d_slip, h->d_slip_inst, h->stage_in, h->stage_out};
+                  h->ysv, h->a3v, h->st_pl, h->st_cd, h->st_pp, h->st_cd4, h->d_cond_list, h->d_cond_scr, h->d_sp, h->d_slip, h->d_slip_inst, h->stage_in, h->stage_out};
   for (void *b : bufs)
     if (b) cudaFree(b);
   for (int i = 0; i < 4; ++i)
@@ -1497,6 +1505,71 @@ static int spectral_stats_buffers(lh_handle *h) {
 // the wall faces jlim(1, vgrid, 2), jlim(2, vgrid, 2) as v array indices
 static void slip_faces(const lh_handle *h, int &qb, int &qt) { qb = h->g.bq[1][2]; qt = h->g.bq[1][3]; }
 
+// the planes of the tile-conditioned P and omega_x sums, and a scratch chunk for their
+// spectral and physical forms (first use): p levels of the wall bands (N(4,0)+1 .. N(4,1)-1,
+// j1 = j - N(4,0) - 1; N(4,2)+2 .. N(4,3), j1 = N(4,3) - j) and the v levels of omega_x
+// (N(3,0) .. N(3,1), j1 = j - N(3,0); N(3,2)+1 .. N(3,3)+1, j1 = N(3,3) + 1 - j)
+static int cond_planes(lh_handle *h) {
+  if (h->d_cond_list) return LH_OK;
+  const Geo &g = h->g;
+  const int *N3 = g.N3, *N4 = g.N4;
+  std::vector<int4> L;
+  for (int j = N4[0] + 1; j <= N4[3]; ++j) {
+    if (j <= N4[1] - 1) L.push_back(make_int4(0, j + g.dny - 1, j - N4[0] - 1, 0));
+    else if (j >= N4[2] + 2) L.push_back(make_int4(0, j + g.dny - 1, N4[3] - j, 0));
+  }
+  for (int j = N3[0]; j <= N3[3] + 1; ++j) {
+    if (j <= N3[1]) L.push_back(make_int4(1, j + g.dny, j - N3[0], 0));
+    else if (j > N3[2]) L.push_back(make_int4(1, j + g.dny, N3[3] + 1 - j, 0));
+  }
+  for (const int4 &d : L)
+    if (d.z < 0 || d.z > h->st_ncl || d.y < 0 || d.y >= (d.x ? g.nv : g.np))
+      return fail(h, LH_EINVAL, "conditioned statistics: plane outside the grid");
+  const size_t per = sizeof(double2) * (size_t)g.G2 * g.N1h;  // z-transformed plane in the A scratch
+  const int chunk = (int)std::min<size_t>({(size_t)32, L.size(), h->Abytes / per});
+  if (chunk < 1) return fail(h, LH_EINVAL, "conditioned statistics: scratch too small");
+  void *scr = nullptr;
+  int4 *dl = nullptr;
+  CK(cudaMalloc(&scr, (size_t)chunk * (sizeof(double2) * g.ncolF + sizeof(double) * (size_t)g.G1 * g.G2)));
+  cudaError_t e = cudaMalloc(&dl, sizeof(int4) * L.size());
+  if (e == cudaSuccess) e = cudaMemcpy(dl, L.data(), sizeof(int4) * L.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(scr);
+    if (dl) cudaFree(dl);
+    return fail(h, LH_ECUDA, std::string("conditioned statistics: ") + cudaGetErrorString(e));
+  }
+  h->d_cond_scr = scr;
+  h->cond_chunk = chunk;
+  h->n_cond = (int)L.size();
+  h->d_cond_list = dl;
+  return LH_OK;
+}
+
+// pressure plane sums (every p level, Parseval) and the tile-conditioned P and omega_x sums
+// (wall-band planes transformed to the dealiased grid in FP64, then summed per tile position)
+static int pressure_wx_stats(lh_handle *h, int nhc, int n2c) {
+  const Geo &g = h->g;
+  const double Gf = (double)g.G1 * g.G2;
+  const double Gc = h->nviews > 1 ? (double)h->gv[1].G1 * h->gv[1].G2 : Gf;
+  KL("k_p_stats", k_p_stats<<<g.np, LH_STAT_THREADS, 0, h->st>>>(h->p, g, nhc, n2c, Gf, Gc, h->st_pp));
+  if (!h->st_dnx) return LH_OK;
+  int rc = cond_planes(h);
+  if (rc) return rc;
+  double2 *spec = (double2 *)h->d_cond_scr;
+  double *phys = (double *)(spec + (size_t)h->cond_chunk * g.ncolF);
+  const int cells = h->st_dnx * h->st_dnz;
+  for (int b0 = 0; b0 < h->n_cond; b0 += h->cond_chunk) {
+    const int nb = std::min(h->cond_chunk, h->n_cond - b0);
+    KL("k_cond_spec", k_cond_spec<<<dim3((g.ncolF + LH_STAT_THREADS - 1) / LH_STAT_THREADS, nb), LH_STAT_THREADS, 0,
+                                     h->st>>>(h->u2, h->u3, h->p, g, h->d_cond_list + b0, spec));
+    if ((rc = spec_to_phys<double>(h, spec, phys, nb, h->A, fp64_tw(h, true), fp64_tw(h, false)))) return rc;
+    KL("k_cond_phys", k_cond_phys<<<dim3((cells + LH_STAT_THREADS - 1) / LH_STAT_THREADS, nb), LH_STAT_THREADS, 0,
+                                     h->st>>>(phys, h->d_cond_list + b0, g.G1, g.G2, h->st_dnx, h->st_dnz,
+                                              h->st_ncl + 1, h->st_cd4));
+  }
+  return LH_OK;
+}
+
 // stats() + spectra() + sl_stats() of the current state (FOU3D.f90:127-130, 298-373)
 extern "C" int lh_stats_accumulate(lh_handle *h) {
   if (!h) return LH_EINVAL;
@@ -1506,6 +1579,7 @@ extern "C" int lh_stats_accumulate(lh_handle *h) {
   const Geo &g = h->g;
   const int nhc = h->nviews > 1 ? h->gv[1].N1h : g.N1hF, n2c = h->nviews > 1 ? h->gv[1].N2 : g.N2F;
   KL("k_wx_stats", k_wx_stats<<<g.nv, LH_STAT_THREADS, 0, h->st>>>(h->u2, h->u3, g, nhc, n2c, h->st_pl));
+  if ((rc = pressure_wx_stats(h, nhc, n2c))) return rc;
   int nl[5];
   spectra_levels(h, nl);
   const size_t ne = (size_t)nl[0] * h->nlong;
@@ -1525,6 +1599,8 @@ extern "C" int lh_stats_reset(lh_handle *h) {
   const size_t ncd = 9 * (size_t)h->st_ncl * (h->st_dnx ? (size_t)h->st_dnx * h->st_dnz : 1);
   CK(cudaMemsetAsync(h->st_pl, 0, sizeof(double) * 11 * (size_t)h->g.nu, h->st));
   CK(cudaMemsetAsync(h->st_cd, 0, sizeof(double) * ncd, h->st));
+  CK(cudaMemsetAsync(h->st_pp, 0, sizeof(double) * 2 * (size_t)h->g.np, h->st));
+  CK(cudaMemsetAsync(h->st_cd4, 0, sizeof(double) * 4 * (size_t)(h->st_ncl + 1) * (h->st_dnx ? (size_t)h->st_dnx * h->st_dnz : 1), h->st));
   if (h->d_sp) CK(cudaMemsetAsync(h->d_sp, 0, sizeof(double) * spectra_size(h), h->st));
   if (h->d_slip) CK(cudaMemsetAsync(h->d_slip, 0, sizeof(double2) * 8 * (size_t)h->g.ncolF, h->st));
   h->istat = 0;
@@ -1547,6 +1623,16 @@ extern "C" int lh_stats_get(lh_handle *h, double *plane, double *cond, int64_t *
                        cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   if (istat) *istat = h->istat;
+  return LH_OK;
+}
+
+extern "C" int lh_stats_get_pw(lh_handle *h, double *pplane, double *cond4) {
+  if (!h) return LH_EINVAL;
+  if (pplane) CK(cudaMemcpyAsync(pplane, h->st_pp, sizeof(double) * 2 * (size_t)h->g.np, cudaMemcpyDeviceToHost, h->st));
+  if (cond4 && h->st_dnx)
+    CK(cudaMemcpyAsync(cond4, h->st_cd4, sizeof(double) * 4 * (size_t)(h->st_ncl + 1) * h->st_dnx * h->st_dnz,
+                       cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
   return LH_OK;
 }
 

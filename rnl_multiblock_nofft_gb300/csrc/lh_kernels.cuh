@@ -2031,6 +2031,95 @@ __global__ void __launch_bounds__(LH_STAT_THREADS) k_wx_stats(const double2 *__r
   }
 }
 
+// Pressure plane sums (stats.f90:43-50 over the physical pressure): one block per p level q
+// (reference level j = q + 1 - dny). Wall-band planes (j <= N(4,1)-1, j >= N(4,2)+2, the
+// pgrid plane ranges of the outer bands) hold every mode of the wall-band grid, on the
+// Gf = G1 x G2 dealiased points; core planes the long columns (nhc x n2c) on Gc points.
+// Parseval on the padded grid: sum p = G p(0,0); sum p^2 = G (sum over kx >= 1 of 2|p|^2,
+// kx = N1/2 included, + the kx = 0 column's Hermitian part, whose row -N2/2 has no mirror).
+// pp: [2][np].
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_p_stats(const double2 *__restrict__ p, Geo g, int nhc, int n2c,
+                                                    double Gf, double Gc, double *__restrict__ pp) {
+  __shared__ double red[LH_STAT_THREADS / 32][2];
+  const int q = blockIdx.x;
+  const int j = q + 1 - g.dny;
+  const bool fine = !g.mb || j <= g.N4[1] - 1 || j >= g.N4[2] + 2;
+  const int nh = fine ? g.N1hF : nhc, n2 = fine ? g.N2F : n2c;
+  const double2 *P = p + (size_t)q * g.ncolF;
+  double s = 0.0, s2 = 0.0;
+  for (int e = threadIdx.x; e < nh * n2; e += blockDim.x) {
+    const int r = e / nh, kx = e - r * nh;
+    const int fr = r < n2 / 2 ? r : r + g.N2F - n2;
+    const double2 a = P[fr * g.N1hF + kx];
+    const double m2 = a.x * a.x + a.y * a.y;
+    if (kx > 0) {
+      s2 += 2.0 * m2;
+    } else if (r == n2 / 2) {
+      s2 += 0.5 * m2;
+    } else {
+      const int rm = (n2 - r) % n2;
+      const int frm = rm < n2 / 2 ? rm : rm + g.N2F - n2;
+      const double2 b = P[frm * g.N1hF];
+      s2 += 0.5 * m2 + 0.5 * (a.x * b.x - a.y * b.y);
+      if (r == 0) s = a.x;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5][0] = s; red[threadIdx.x >> 5][1] = s2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < LH_STAT_THREADS / 32; ++w) { a += red[w][0]; b += red[w][1]; }
+    const double G = fine ? Gf : Gc;
+    pp[q] += G * a;
+    pp[(size_t)g.np + q] += G * b;
+  }
+}
+
+// Spectral planes of the tile-conditioned P and omega_x sums: plane b of the chunk is
+// list[b] = (kind, level, j1): kind 0 copies p level `level`; kind 1 forms omega_x at v level
+// `level` (-i kz v + (w(q+1) - w(q)) dthdyv ddthetavi, FOU3D.f90:300-327). spec: [nb][ncolF].
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_cond_spec(const double2 *__restrict__ u2, const double2 *__restrict__ u3,
+                                                      const double2 *__restrict__ p, Geo g,
+                                                      const int4 *__restrict__ list, double2 *__restrict__ spec) {
+  const int4 d = list[blockIdx.y];
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (size_t)g.ncolF) return;
+  double2 *o = spec + (size_t)blockIdx.y * g.ncolF + c;
+  if (d.x == 0) {
+    *o = p[(size_t)d.y * g.ncolF + c];
+  } else {
+    *o = wx_mode(u2, u3, g, d.y, (int)c, (int)(c / g.N1hF), g.thv[d.y] * g.dd);
+  }
+}
+
+// conddown1 / condup1 with xsign 1 (stats.f90:109-138, 178-210) of the chunk's physical
+// planes (phys [nb][G2][G1]): one thread per tile position (i, k), summing the value and
+// its square over the ntx x ntz tiles into the pair 2 kind, 2 kind + 1 of
+// cd4 [4][ncl1][dnz][dnx] at level j1 (bottom and top planes of a level add into one cell).
+__global__ void __launch_bounds__(LH_STAT_THREADS) k_cond_phys(const double *__restrict__ phys, const int4 *__restrict__ list,
+                                                      int G1, int G2, int dnx, int dnz, int ncl1,
+                                                      double *__restrict__ cd4) {
+  const int4 d = list[blockIdx.y];
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= dnx * dnz) return;
+  const int k = cell / dnx, i = cell - k * dnx;
+  const double *f = phys + (size_t)blockIdx.y * G1 * G2;
+  double s = 0.0, s2 = 0.0;
+  for (int l = k; l < G2; l += dnz)
+    for (int m = i; m < G1; m += dnx) {
+      const double x = f[(size_t)l * G1 + m];
+      s += x;
+      s2 += x * x;
+    }
+  const size_t lv = (size_t)dnz * dnx;
+  atomicAdd(&cd4[((size_t)(2 * d.x) * ncl1 + d.z) * lv + cell], s);
+  atomicAdd(&cd4[((size_t)(2 * d.x + 1) * ncl1 + d.z) * lv + cell], s2);
+}
+
 // spectra (spectra.f90:1-56): band 2's levels x the long columns (cols[0..nlong)),
 // sp(level, column) += |u|^2 (U, V, W, P) and Re u1 Re v + Im u1 Im v with v interpolated
 // to the centres (interp_v, FOU3D.f90:427-474; band 2's end levels extrapolated with

@@ -19,7 +19,7 @@ _lib = None
 EXPORTS = ("lh_create", "lh_destroy", "lh_last_error", "lh_upload_state", "lh_download_state",
            "lh_upload_state_async", "lh_download_state_async", "lh_upload_band_async", "lh_download_band_async",
            "lh_upload_band", "lh_download_band", "lh_stats_accumulate", "lh_stats_reset", "lh_stats_dims",
-           "lh_stats_get", "lh_spectra_dims", "lh_spectra_get", "lh_slip_get", "lh_slip_planes",
+           "lh_stats_get", "lh_stats_get_pw", "lh_spectra_dims", "lh_spectra_get", "lh_slip_get", "lh_slip_planes",
            "lh_set_scalars", "lh_get_scalars", "lh_substep", "lh_step", "lh_synchronize",
            "lh_device_state", "lh_stream", "lh_four_to_phys", "lh_phys_to_four", "lh_kernel_launches",
            "lh_profile_steps", "lh_four_to_phys_noalloc", "lh_autotune", "lh_batch_create", "lh_batch_step",
@@ -60,6 +60,7 @@ def load(path: str = _LIB_PATH):
     L.lh_stats_reset.argtypes = [vp]
     L.lh_stats_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.lh_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+    L.lh_stats_get_pw.argtypes = [vp, dp, dp]
     L.lh_spectra_dims.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.lh_spectra_get.argtypes = [vp, dp, dp, dp, dp, dp]
     L.lh_slip_get.argtypes = [vp, dp]
@@ -248,6 +249,16 @@ class GpuChannel:
         ist = C.c_int64()
         self._check(self.L.lh_stats_get(self.h, _dptr(plane), _dptr(cond), C.byref(ist)))
         return plane, cond, ist.value
+
+    def stats_pw(self):
+        """(pressure plane sums [2][nyu - 2], conditioned P, P^2, omega_x, omega_x^2
+        [4][ncl + 1][dnz][dnx] or None); see include/lh.h."""
+        ncl, dnx, dnz = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.lh_stats_dims(self.h, C.byref(ncl), C.byref(dnx), C.byref(dnz)))
+        pplane = np.zeros((2, self.s.nyu - 2))
+        cond = np.zeros((4, ncl.value + 1, dnz.value, dnx.value)) if dnx.value else None
+        self._check(self.L.lh_stats_get_pw(self.h, _dptr(pplane), _dptr(cond)))
+        return pplane, cond
 
     def set_scalars(self, **kw):
         s = LhScalars()
