@@ -15,12 +15,14 @@ rank 0 does when it writes (``flagwr``):
   ``write_slip_inst_file`` (inst_sl_stats.f90:1-82): Fortran unformatted sequential records,
   4-byte little-endian markers, like the plane files.
 
-Quantities the reference writes but this build does not form are written as zeros:
-P and P^2 (stats.f90 sums ``ppPL``, which holds the spectral packing of p from the last
-record_out, FOU3D.f90:156-157, not a physical field), the tile-conditioned P and omega_x
-sums (conddown1 reads ``wx``, allocated (N1+2) x N2 per plane, through an igal x kgal
-dummy, stats.f90:96-97) and the values on the wall and ghost planes of the velocity
-statistics (the reference sums the untransformed spectral packing there).
+The pressure sums P, P^2 and the tile-conditioned P and omega_x sums come from
+``lh_stats_get_pw`` (argument ``pw`` of ``write_stats_file``): the reference sums ``ppPL``,
+which holds the spectral packing of p from the last record_out (FOU3D.f90:156-157), and
+conditions ``wx``, allocated (N1+2) x N2 per plane, through an igal x kgal dummy
+(stats.f90:91-92, 100-101); these are the physical pressure and omega_x on the dealiased
+grid instead. Without ``pw`` those records are zeros. The values on the wall and ghost planes
+of the velocity statistics are zeros (the reference sums the untransformed spectral packing
+there).
 """
 from __future__ import annotations
 
@@ -81,13 +83,15 @@ def write_spectra_file(path: str, s: ChannelSetup, sp: np.ndarray, istat: int, t
 
 
 def write_stats_file(path: str, s: ChannelSetup, plane: np.ndarray, cond, istat: int, t: float, mpgx: float,
-                     it: int) -> None:
-    """plane [11][nyu] and cond [9][ncl][dnz][dnx] (or None) as lh_stats_get returns them."""
+                     it: int, pw=None) -> None:
+    """plane [11][nyu] and cond [9][ncl][dnz][dnx] (or None) as lh_stats_get returns them;
+    pw = (pplane [2][nyu - 2], cond4 [4][ncl + 1][dnz][dnx] or None) as lh_stats_get_pw
+    returns them, or None (P records zero)."""
     nu, nv, npl = s.nyu, s.nyv, s.nyu - 2
     q = {k: plane[i] for i, k in enumerate(PLANE_QTY)}
-    zu, zv, zp = np.zeros(nu), np.zeros(nv), np.zeros(npl)
-    recs = [q["U"][:nu], q["U2"][:nu], q["V"][:nv], q["V2"][:nv], q["W"][:nu], q["W2"][:nu], zp, zp,
-            q["UV"][:nu], q["UW"][:nu], q["VW"][:nv], q["wx"][:nv], q["wx2"][:nv]]
+    pp, c4 = pw if pw is not None else (np.zeros((2, npl)), None)
+    recs = [q["U"][:nu], q["U2"][:nu], q["V"][:nv], q["V2"][:nv], q["W"][:nu], q["W2"][:nu], pp[0][:npl],
+            pp[1][:npl], q["UV"][:nu], q["UW"][:nu], q["VW"][:nv], q["wx"][:nv], q["wx2"][:nv]]
     out = [_header(s, t, mpgx, it), _rec(_i4(s.Ngal))] + _grids(s)
     out.append(_rec(struct.pack("<i", int(istat))))
     out += [_rec(_f8(r)) for r in recs]
@@ -104,10 +108,17 @@ def write_stats_file(path: str, s: ChannelSetup, plane: np.ndarray, cond, istat:
             o[1:1 + m] = a[:m]
             return o
 
-        zc = lambda n: np.zeros((n, dnz, dnx))
+        def lv0(qty, n):
+            # conditioned P / omega_x: level j1 = 0 .. n - 1 from the wall, level 0 included
+            o = np.zeros((n, dnz, dnx))
+            if c4 is not None:
+                m = min(n, c4.shape[1])
+                o[:m] = c4[qty, :m]
+            return o
+
         crecs = [lv(c["U"], ncu), lv(c["U2"], ncu), lv(c["V"], ncv), lv(c["V2"], ncv), lv(c["W"], ncu),
-                 lv(c["W2"], ncu), zc(ncp), zc(ncp), lv(c["UV"], ncu), lv(c["UW"], ncu), lv(c["VW"], ncv),
-                 zc(ncv), zc(ncv)]
+                 lv(c["W2"], ncu), lv0(0, ncp), lv0(1, ncp), lv(c["UV"], ncu), lv(c["UW"], ncu), lv(c["VW"], ncv),
+                 lv0(2, ncv), lv0(3, ncv)]
         out += [_rec(np.ascontiguousarray(r, "<f8").tobytes()) for r in crecs]
     with open(path, "wb") as f:
         f.write(b"".join(out))

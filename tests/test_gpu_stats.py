@@ -1,6 +1,7 @@
-"""Statistics on the GPU (k_xstats, k_wx_stats, k_spectra, k_slip, through the C ABI) vs the
-CPU oracle after accumulating twice around a step: plane sums and tile-conditioned sums of
-stats.f90 (omega_x by Parseval on the GPU, by the inverse transform in the oracle), the
+"""Statistics on the GPU (k_xstats, k_wx_stats, k_p_stats, k_cond_spec + k_cond_phys, k_spectra,
+k_slip, through the C ABI) vs the CPU oracle after accumulating twice around a step: plane sums
+and tile-conditioned sums of stats.f90 (omega_x and P by Parseval on the GPU, by the inverse
+transform in the oracle; the conditioned P and omega_x from FP64 physical planes), the
 spectra of spectra.f90 and the wall slip statistics of sl_stats2.f90 / inst_sl_stats.f90.
 Bar: FP64 form 1e-12 relative to the largest sum of a kind; mixed 1e-5."""
 import numpy as np
@@ -44,7 +45,7 @@ def close(a, b, tol):
 
 
 @pytest.mark.parametrize("name,precision,tol", [("SP", "fp64", 1e-12), ("MB", "fp64", 1e-12),
-                                                ("SP", "mixed", 1e-5)])
+                                                ("MBP", "fp64", 1e-12), ("SP", "mixed", 1e-5)])
 def test_stats_match_oracle(cuda_ok, name, precision, tol):
     o, g = run(name, precision, 51)
     (po, co, io), (pg, cg, ig) = o.stats(), g.stats()
@@ -54,6 +55,16 @@ def test_stats_match_oracle(cuda_ok, name, precision, tol):
     if co is not None:
         assert cg is not None and cg.shape == co.shape
         close(co.reshape(9, -1), cg.reshape(9, -1), tol)
+    # pressure sums (Parseval on the GPU, transform + point sums in the oracle) and the
+    # conditioned P, omega_x sums; the mixed form's pressure is within 1e-4 of the oracle's
+    (ppo, c4o), (ppg, c4g) = o.stats_pw(), g.stats_pw()
+    tp = tol if precision == "fp64" else 3e-4
+    assert ppg.shape == ppo.shape == (2, o.s.nyu - 2)
+    close(ppo, ppg, tp)
+    if c4o is not None:
+        assert c4g is not None and c4g.shape == c4o.shape
+        close(c4o[:2].reshape(2, -1), c4g[:2].reshape(2, -1), tp)
+        close(c4o[2:].reshape(2, -1), c4g[2:].reshape(2, -1), tol)
     # spectra are quadratic in a field whose mixed-form error is up to 1e-5 of its own
     # scale: 3x the field bar (FP64: the same bar)
     so, sg = o.spectra(), g.spectra()

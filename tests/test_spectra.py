@@ -142,6 +142,17 @@ def test_files_roundtrip(tmp_path):
     assert len(r) == 5 + 13 + (13 if cd is not None else 0)
     assert np.array_equal(np.frombuffer(r[5], "<f8"), pl[0, : s.nyu])
     assert np.array_equal(np.frombuffer(r[16], "<f8"), pl[9, : s.nyv])
+    assert not np.frombuffer(r[11], "<f8").any()                       # P without pw
+    pp, c4 = o.stats_pw()
+    write_stats_file(p, s, pl, cd, ist, 0.5, -3e-3, 7, pw=(pp, c4))
+    r = read_records(p)
+    assert np.array_equal(np.frombuffer(r[11], "<f8"), pp[0]) and np.array_equal(np.frombuffer(r[12], "<f8"), pp[1])
+    if cd is not None:
+        dnz, dnx = cd.shape[2:]
+        n4, n3 = s.N[3], s.N[2]
+        ncp, ncv = int(n4[1] - n4[0]) - 1, int(n3[1] - n3[0]) + 1
+        assert np.array_equal(np.frombuffer(r[24], "<f8").reshape(ncp, dnz, dnx), c4[0, :ncp])
+        assert np.array_equal(np.frombuffer(r[29], "<f8").reshape(ncv, dnz, dnx), c4[2, :ncv])
     p = str(tmp_path / "sl.dat")
     acc = o.slip()
     write_slip_file(p, s, acc, ist, 0.5, -3e-3, 7)
