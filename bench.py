@@ -230,8 +230,8 @@ def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0, ib: bool = Tru
             tot += B + (nuI + nvI) * 3 * ncv * z
     if kernel == "k_xpass_nl" and ib and s.dny > 0 and s.p.ib_enable and s.p.geometry_type == 2:
         # physical planes of the immersed-boundary levels (and the two tip levels) captured
-        # for the forcing: 3 fields, FP64
-        tot += (4 * s.dny + 2) * 3 * s.G1 * s.G2 * 8
+        # for the forcing: 3 fields, in the transform precision
+        tot += (4 * s.dny + 2) * 3 * s.G1 * s.G2 * (8 if form == "fp64" else 4)
     if kernel in ("k_zinv_nl", "k_xpass_nl", "k_zfwd_nl"):
         return tot
     if kernel == "k_helm_uw":
@@ -455,23 +455,28 @@ def e2e_run(s, form, tl, ic, icb, sc0, steps, ws, pg, torch, np):
     else:
         g.upload_state(*pinned)
     g.set_scalars(**sc0)
-    g.step(1)
+    bin_ = {b: pinned[4 * (b - 1):4 * b] for b in (1, 2, 3)} if mb else None
+    bout = {b: pinned_out[4 * (b - 1):4 * b] for b in (1, 2, 3)} if mb else None
+
+    def io_step():
+        if mb:
+            g.upload_bands_async(bin_)
+            g.step(1)
+            g.download_bands_async(bout)
+        else:
+            g.upload_state_async(*pinned)
+            g.step(1)
+            g.download_state_async(pinned_out)
+
+    # warm-up: the first queued copy creates the staging buffers, streams and events
+    for _ in range(2):
+        io_step()
     g.synchronize()
     barrier(pg)
     nb = sum(a.nbytes for a in pinned)
     t0 = time.perf_counter()
-    if mb:
-        bin_ = {b: pinned[4 * (b - 1):4 * b] for b in (1, 2, 3)}
-        bout = {b: pinned_out[4 * (b - 1):4 * b] for b in (1, 2, 3)}
-        for _ in range(steps):
-            g.upload_bands_async(bin_)
-            g.step(1)
-            g.download_bands_async(bout)
-    else:
-        for _ in range(steps):
-            g.upload_state_async(*pinned)
-            g.step(1)
-            g.download_state_async(pinned_out)
+    for _ in range(steps):
+        io_step()
     g.synchronize()
     e2e_s = reduce_max(pg, time.perf_counter() - t0)
     g.close()

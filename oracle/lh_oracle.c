@@ -125,10 +125,31 @@ static void fft_rec(const fftplan *P, const cplx *in, cplx *out, int len, int st
 }
 
 /* in-place complex transform of x[0..n) with element stride 1 */
+/* Test hook: uniform noise of amplitude eps x (the line's largest modulus) added to every
+ * transform output, standing in for the rounding of a transform less accurate than FP64
+ * (orc_set_transform_noise; 0 = off). The noise is a hash of the value, so runs repeat. */
+static double g_transform_noise = 0.0;
+static inline double noise_unit(double v) {
+  uint64_t b;
+  memcpy(&b, &v, 8);
+  b ^= b >> 33; b *= 0xff51afd7ed558ccdULL; b ^= b >> 33; b *= 0xc4ceb9fe1a85ec53ULL; b ^= b >> 33;
+  return (double)(b >> 11) / 4503599627370496.0 - 1.0;  /* [-1, 1) */
+}
+int orc_set_transform_noise(double eps) { g_transform_noise = eps; return 0; }
+
 static void fft_inplace(const fftplan *P, cplx *x, int sgn, cplx *tmp) {
   cplx scr[64];
   memcpy(tmp, x, sizeof(cplx) * (size_t)P->n);
   fft_rec(P, tmp, x, P->n, 1, 0, sgn, scr);
+  if (g_transform_noise != 0.0) {
+    double mx = 0.0;
+    for (int i = 0; i < P->n; ++i) if (cabs(x[i]) > mx) mx = cabs(x[i]);
+    const double a = g_transform_noise * mx;
+    for (int i = 0; i < P->n; ++i) {
+      const double re = creal(x[i]), im = cimag(x[i]);
+      x[i] = (re + a * noise_unit(re)) + I * (im + a * noise_unit(im));
+    }
+  }
 }
 
 /* ------------------------------------------------------------------------- */

@@ -19,6 +19,8 @@ int orc_step(orc *O);
 int orc_four_to_phys(orc *O, const double *spec, double *phys, int nplanes);
 int orc_phys_to_four(orc *O, const double *phys, double *spec, int nplanes);
 int orc_set_threads(int n);
+/* test hook: noise eps x max|line| on every transform output (0: off), process-wide */
+int orc_set_transform_noise(double eps);
 int orc_stats_accumulate(orc *O);
 /* plane: [11][nu]; dims: ncl, dnx, dnz */
 int orc_stats_get(orc *O, double *plane, double *cond, int64_t *istat, int *dims);

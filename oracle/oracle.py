@@ -47,6 +47,7 @@ def lib():
         L.orc_four_to_phys.argtypes = [vp, dp, dp, C.c_int]
         L.orc_phys_to_four.argtypes = [vp, dp, dp, C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_transform_noise.argtypes = [C.c_double]
         L.orc_stats_accumulate.argtypes = [vp]
         L.orc_stats_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
         L.orc_stats_reset.argtypes = [vp]
@@ -56,6 +57,12 @@ def lib():
         L.orc_slip_planes.argtypes = [vp, dp]
         _lib = L
     return _lib
+
+
+def set_transform_noise(eps: float) -> None:
+    """Test hook of the oracle: noise of amplitude eps x (the line's largest modulus) on every
+    transform output, process-wide (0 turns it off)."""
+    lib().orc_set_transform_noise(float(eps))
 
 
 def _dptr(a):

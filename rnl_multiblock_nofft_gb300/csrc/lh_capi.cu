@@ -55,7 +55,7 @@ struct lh_handle {
   // immersed boundaries
   int ib, nib, ncap;
   int *d_ibslot_u, *d_ibslot_v, *d_iblev, *d_lev2cap_u, *d_lev2cap_v;
-  double *cap;
+  void *cap;  // captured physical planes of the immersed levels, in the transform precision
   IbRec *d_ibrec;   // forced points, sorted by (plane of du, row)
   int *d_iboff;     // [3 nib G2 + 1] record ranges per (plane, row)
   double2 *duib;
@@ -526,7 +526,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     h->d_iblev = (int *)upload_vec(iblev, ce);
     h->d_lev2cap_u = (int *)upload_vec(lev2cap_u, ce); h->d_lev2cap_v = (int *)upload_vec(lev2cap_v, ce);
     if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
-    ZA(h->cap, sizeof(double) * (size_t)h->ncap * 3 * pp);
+    ZA(h->cap, h->vsz / 2 * (size_t)h->ncap * 3 * pp);
     ZA(h->duib, cz * (size_t)h->nib * 3 * nc);
   }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1061,19 +1061,19 @@ static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const
     using P = xp2<N>;
     dim3 grid((g.G2 / 2 + P::PB - 1) / P::PB, nslots);
     KL("k_xpass_nl", k_xpass2<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
-                                                                  (const float2 *)twx, doCFL, h->sc, capslot, h->cap));
+                                                                  (const float2 *)twx, doCFL, h->sc, capslot, (float *)h->cap));
     return LH_OK;
   } else if constexpr (sizeof(T) == 4 && (N == 576 || N == 768 || N == 1152)) {  // three-stage register form
     using P = xp3<N>;
     dim3 grid(g.G2 / 2, nslots);
     KL("k_xpass_nl", k_xpass3<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
-                                                                  (const float2 *)twx, doCFL, h->sc, capslot, h->cap));
+                                                                  (const float2 *)twx, doCFL, h->sc, capslot, (float *)h->cap));
     return LH_OK;
   }
   constexpr int PB = pb_xpass<V>(N);
   dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
   KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, LH_XPASS_THREADS, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
-                       (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, h->cap));
+                       (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, (T *)h->cap));
   return LH_OK;
 }
 template <typename T, int N>
@@ -1195,7 +1195,7 @@ static int launch_ib_xforce(lh_handle *h, int npl) {
   constexpr int PB = 4 * pb_xpass<V>(N);
   dim3 g2((h->g.G2 / 2 + PB - 1) / PB, npl);
   KL("k_ib_xforce", k_ib_xforce<T, N><<<g2, NTHR_H, 2 * (size_t)PB * N * sizeof(V), h->st>>>(
-                        (const V *)h->A, (V *)h->B, h->g, (const V *)h->twx, h->d_ibrec, h->d_iboff, h->cap, h->sc));
+                        (const V *)h->A, (V *)h->B, h->g, (const V *)h->twx, h->d_ibrec, h->d_iboff, (const T *)h->cap, h->sc));
   return LH_OK;
 }
 template <typename T>

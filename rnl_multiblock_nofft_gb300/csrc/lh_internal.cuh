@@ -83,17 +83,17 @@ struct DevScalars {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float d2f_alu(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned int hi = (unsigned int)(b >> 32), lo = (unsigned int)b;
-  const unsigned int sign = hi & 0x80000000u;
-  const int ed = (int)((hi >> 20) & 0x7ffu);
-  const int e = ed - 1023 + 127;
-  const unsigned int m = ((hi & 0x000fffffu) << 3) | (lo >> 29);
-  const unsigned int rest = lo & 0x1fffffffu;
-  unsigned int f = ((unsigned int)e << 23) | m;
-  f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
-  if (e <= 0) f = 0u;
-  if (e >= 255) f = (ed == 0x7ff && (((hi & 0x000fffffu) | lo) != 0u)) ? 0x7fc00000u : 0x7f800000u;
-  return __uint_as_float(sign | f);
+  const unsigned int hi = (unsigned int)(b >> 32);
+  const unsigned int ed = (hi >> 20) & 0x7ffu;  // biased double exponent
+  // round to nearest even on the 29 dropped mantissa bits (adding half an ulp minus one, plus
+  // the kept lowest bit; a carry runs into the exponent), then drop them; bits 23-31 of the
+  // shifted word hold the low 9 exponent bits, and subtracting 896 << 23 (mod 2^32) rebiases
+  // them for every exponent of the normal float range
+  const unsigned long long r = b + 0x0fffffffull + ((b >> 29) & 1ull);
+  unsigned int f = (unsigned int)(r >> 29) - 0xc0000000u;
+  if (ed - 897u > 253u)  // below 2^-126: zero; above the float range: inf, or NaN for a NaN
+    f = ed < 897u ? 0u : ((ed == 0x7ffu && (b << 12) != 0ull) ? 0x7fc00000u : 0x7f800000u);
+  return __uint_as_float((hi & 0x80000000u) | f);
 }
 __device__ __forceinline__ double f2d_alu(float x) {
   const unsigned int u = __float_as_uint(x);

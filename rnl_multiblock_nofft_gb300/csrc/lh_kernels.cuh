@@ -38,6 +38,20 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double 
 // non-finite state to dt and err, where the blow-up guard sees it
 template <typename T>
 __device__ __forceinline__ T nmax(T a, T b) { return (b > a || b != b) ? b : a; }
+// running maximum of non-negative doubles (or NaN) kept as their bit patterns: the integer
+// order of those patterns is the order of the values, a NaN above every number, so the
+// comparisons stay off the FP64 pipe; warp_max_bits reduces it over the warp
+__device__ __forceinline__ void bits_max(unsigned long long &m, double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  m = b > m ? b : m;
+}
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long m) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, m, o);
+    m = w > m ? w : m;
+  }
+  return m;
+}
 template <typename T>
 __device__ __forceinline__ T warp_max(T v) {
   for (int o = 16; o > 0; o >>= 1) {
@@ -184,7 +198,7 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
                                                    typename C2<T>::t *__restrict__ B, Geo g,
                                                    const typename C2<T>::t *__restrict__ twx, int doCFL,
                                                    DevScalars *sc, const int *__restrict__ capslot,
-                                                   double *__restrict__ cap) {
+                                                   T *__restrict__ cap) {
   typedef typename C2<T>::t V;
   constexpr int PB = pb_xpass<V>(N);
   constexpr int G1 = N, H = N / 2;
@@ -235,10 +249,10 @@ __global__ void __launch_bounds__(LH_XPASS_THREADS) k_xpass_nl(const typename C2
         const int f = line / PB, pb = line - f * PB;
         if (pb >= npairs) continue;
         const int l = l0 + 2 * pb;
-        double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * G1;
+        T *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * G1;
         const V z = res[idx];
-        cp[(size_t)l * G1 + m] = to_d(z.x);
-        cp[(size_t)(l + 1) * G1 + m] = to_d(z.y);
+        cp[(size_t)l * G1 + m] = z.x;
+        cp[(size_t)(l + 1) * G1 + m] = z.y;
       }
     }
   }
@@ -1649,7 +1663,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
   const int vc = tid >> 1, part = tid & 1;
   const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
   const int nc = g.ncol;
-  double dmax = 0.0;
+  unsigned long long dmax = 0ull;  // max |div|^2 as bits
   // per-level factors of this substep: dti/(a+b) dd thu (divergence -> right-hand side)
   // and dt (a+b) dd thv (v_corr), so that the lanes spend no FP64 multiply on them
   extern __shared__ double ptab[];
@@ -1758,7 +1772,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
             const double th = thu1;
             const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - v);
             const double d2 = dvp * dvp;
-            dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+            bits_max(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
           }
           aup_o = ao; wup_o = wo; vup = v;
           xn = x;
@@ -1773,7 +1787,7 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
       const double vb = u2[(size_t)plo * ls + ci];
       const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
       const double d2 = dvp * dvp;
-      dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+      bits_max(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
     }
     if (bd <= 1) {
       u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
@@ -1787,8 +1801,8 @@ __global__ void __launch_bounds__(NTHR, LH_PRESS_MINB) k_press2(double *__restri
     u2[(size_t)vhi * ls + ci] = 0.0;
   }
   // |div|^2 = re^2 + im^2 per level, summed over the lane pair above
-  dmax = warp_max(dmax);
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
+  dmax = warp_max_bits(dmax);
+  if ((threadIdx.x & 31) == 0) atomicMax(&sc->errbits, dmax);
 }
 
 // ============================================================================
@@ -1811,7 +1825,7 @@ __global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double
   const int vc = tid >> 1, part = tid & 1;
   const unsigned pm = 3u << ((threadIdx.x & 31) & ~1);  // the lane pair
   const int nc = g.ncol;
-  double dmax = 0.0;
+  unsigned long long dmax = 0ull;  // max |div|^2 as bits
   extern __shared__ double ptab[];
   const int nt = blockDim.x;
   double *ring = ptab + ((g.nu + g.nv + 1) & ~1);  // [D + 1][6][nt]
@@ -1910,7 +1924,7 @@ __global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double
       if (need_div && qp < phi) {
         const double dvp = (skx * aup_o + skz * wup_o) + thu1 * (vup - v);
         const double d2 = dvp * dvp;
-        dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+        bits_max(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
       }
       aup_o = ao; wup_o = wo; vup = v;
       xn = x;
@@ -1921,7 +1935,7 @@ __global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double
       const double vb = u2[(size_t)plo * ls + ci];
       const double dvp = (skx * aup_o + skz * wup_o) + th * (vup - vb);
       const double d2 = dvp * dvp;
-      dmax = nmax(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
+      bits_max(dmax, d2 + __shfl_xor_sync(pm, d2, 1));
     }
     if (bd <= 1) {
       u1[(size_t)ulo * ls + ci] = g.gwbc1 * u1[(size_t)(ulo + 1) * ls + ci];
@@ -1935,8 +1949,8 @@ __global__ void __launch_bounds__(NTHR) k_press3(double *__restrict__ u1, double
     u2[(size_t)vhi * ls + ci] = 0.0;
   }
 #undef RS
-  dmax = warp_max(dmax);
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&sc->errbits, dmax);
+  dmax = warp_max_bits(dmax);
+  if ((threadIdx.x & 31) == 0) atomicMax(&sc->errbits, dmax);
 }
 
 __global__ void k_reset_err(DevScalars *sc) {
@@ -2526,7 +2540,8 @@ __global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u
 // rows are overwritten with Kib/dt (A u(i1,k1,j1) - u(i,k,j)) from the captured physical
 // velocities, and the rows go back (B layout for the z pass). Forced points come as
 // records sorted by (plane, row): rec_off[plane * G2 + row] .. rec_off[... + 1];
-// cap [capslot][field][G2][G1] holds the physical u, v, w the x pass captured.
+// cap [capslot][field][G2][G1] holds the physical u, v, w the x pass captured, in the
+// transform precision (FP32 in the mixed form: the values are FP32 there).
 // ============================================================================
 struct IbRec {
   int i, k;        // 0-based point of the plane: x index, row
@@ -2538,7 +2553,7 @@ template <typename T, int N>
 __global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__restrict__ A, typename C2<T>::t *__restrict__ B,
                                                     Geo g, const typename C2<T>::t *__restrict__ twx,
                                                     const IbRec *__restrict__ rec, const int *__restrict__ rec_off,
-                                                    const double *__restrict__ cap, const DevScalars *__restrict__ sc) {
+                                                    const T *__restrict__ cap, const DevScalars *__restrict__ sc) {
   typedef typename C2<T>::t V;
   constexpr int PB = 4 * pb_xpass<V>(N);
   constexpr int G1 = N, H = N / 2;
@@ -2577,7 +2592,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__r
     const int r0 = rec_off[(size_t)pl * G2 + l0], r1 = rec_off[(size_t)pl * G2 + l0 + 2 * npairs];
     for (int e = r0 + threadIdx.x; e < r1; e += blockDim.x) {
       const IbRec R = rec[e];
-      const double val = Kibdt * (R.A * cap[R.ref] - cap[R.src]);
+      const double val = Kibdt * (R.A * to_d(cap[R.ref]) - to_d(cap[R.src]));
       const int rr = R.k - l0;
       V *z = res + (rr >> 1) * G1 + R.i;
       if (rr & 1) z->y = to_t<T>(val);

@@ -53,7 +53,7 @@ template <int N> struct xp2 {
 template <int N>
 __global__ void __launch_bounds__(xp2<N>::NT, LH_XPASS2_MINB) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
-                                                        const int *__restrict__ capslot, double *__restrict__ cap) {
+                                                        const int *__restrict__ capslot, float *__restrict__ cap) {
   using P = xp2<N>;
   constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1, LS2 = P::LS2;
   constexpr int NK = N / 3 + 1;  // retained x-modes 0..N1/2 (N1 = 2 (Ngal1 / 3), checked at create)
@@ -137,11 +137,11 @@ __global__ void __launch_bounds__(xp2<N>::NT, LH_XPASS2_MINB) k_xpass2(const flo
       const int l = l0 + 2 * pb;
 #pragma unroll
       for (int f = 0; f < 3; ++f) {
-        double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + jj;
+        float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + jj;
         regfft::static_for<0, XB>([&](auto t_) {
           constexpr int t = decltype(t_)::value;
-          cp[t * XA] = f2d_alu(ph[f][t].x);
-          cp[N + t * XA] = f2d_alu(ph[f][t].y);
+          cp[t * XA] = ph[f][t].x;
+          cp[N + t * XA] = ph[f][t].y;
         });
       }
     }
@@ -387,16 +387,20 @@ __global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const floa
   constexpr int H = N / 3;  // N2 / 2
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *E = reinterpret_cast<float2 *>(smem_raw);
-  const int slot = blockIdx.y, kx0 = blockIdx.x * KF;
+  const int slot = blockIdx.y;
   const bool isU = slot < g.nuI;
-  const int q = slot_level(g, slot, isU);
-  const int NP = isU ? 4 : 2;
-  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
+  // a v level has two products: its blocks take twice the kx lines (the grid's second half
+  // of v-level blocks has none and returns), so that every level fills the block
+  const int NP = isU ? 4 : 2, KE = isU ? KF : 2 * KF;
+  const int kx0 = blockIdx.x * KE;
   const int N1h = g.N1h;
+  if (kx0 >= N1h) return;
+  const int q = slot_level(g, slot, isU);
+  const int pbase = isU ? slot * 4 : g.nuI * 4 + (slot - g.nuI) * 2;
   const int tid = threadIdx.x;
   // stage 1: thread (p, jj, kk), kk fastest
-  if (tid < NP * ZA * KF) {
-    const int kk = tid % KF, r1 = tid / KF, jj = r1 % ZA, p = r1 / ZA, kx = kx0 + kk;
+  if (tid < NP * ZA * KE) {
+    const int kk = tid % KE, r1 = tid / KE, jj = r1 % ZA, p = r1 / ZA, kx = kx0 + kk;
     float2 v[ZB];
     const float2 *src = B + ((size_t)(pbase + p) * (N / 2) * N1h + kx) * 2;
     const bool ok = kx < N1h;
@@ -406,16 +410,16 @@ __global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const floa
       v[t] = ok ? src[(size_t)(l >> 1) * N1h * 2 + (l & 1)] : make_float2(0.f, 0.f);
     });
     regfft::dft_reg<ZB, false>(v);
-    float2 *e = E + (p * KF + kk) * LSE + jj * (ZB + 1);
+    float2 *e = E + (p * KE + kk) * LSE + jj * (ZB + 1);
     regfft::static_for<0, ZB>([&](auto t_) { e[decltype(t_)::value] = v[decltype(t_)::value]; });
   }
   __syncthreads();
   // stage 2: thread (p, jj2, kk); the inputs are read before the block reuses E for the rows
-  const bool s2 = tid < NP * ZB * KF;
-  const int kk = tid % KF, r2 = tid / KF, jj2 = r2 % ZB, p = r2 / ZB;
+  const bool s2 = tid < NP * ZB * KE;
+  const int kk = tid % KE, r2 = tid / KE, jj2 = r2 % ZB, p = r2 / ZB;
   float2 v[ZA];
   if (s2) {
-    const float2 *e = E + (p * KF + kk) * LSE + jj2;
+    const float2 *e = E + (p * KE + kk) * LSE + jj2;
     regfft::static_for<0, ZA>([&](auto t_) {
       constexpr int t = decltype(t_)::value;
       const float2 x = e[t * (ZB + 1)];
@@ -438,22 +442,22 @@ __global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const floa
       int r = -1;
       if (mlo < H && m < H) r = m;
       else if (mhi >= N - H && m >= N - H) r = m - N + 2 * H;
-      if (r >= 0) R[((size_t)p * 2 * H + r) * KF + kk] = v[t];
+      if (r >= 0) R[((size_t)p * 2 * H + r) * KE + kk] = v[t];
     });
   }
   __syncthreads();
   // der_x / der_z and the stores, one thread per (kz row, kx)
   const float s = 1.f / (float)N;
   const size_t off = (size_t)q * g.ncolF;
-  for (int idx = tid; idx < 2 * H * KF; idx += blockDim.x) {
-    const int r = idx / KF, k2 = idx - r * KF, kx = kx0 + k2;
+  for (int idx = tid; idx < 2 * H * KE; idx += blockDim.x) {
+    const int r = idx / KE, k2 = idx - r * KE, kx = kx0 + k2;
     if (kx >= N1h) continue;
     const int c = gcol(g, r, kx), rg = grow(g, r);
     const float kxv = g.k1xf[kx], kzv = g.k1zf[rg];
     const bool zr = (r == H);  // der_x / der_z zero the kz = -N2/2 row
     if (isU) {
-      const float2 uu = cscale(R[((size_t)0 * 2 * H + r) * KF + k2], s), uw = cscale(R[((size_t)1 * 2 * H + r) * KF + k2], s);
-      const float2 vv = cscale(R[((size_t)2 * 2 * H + r) * KF + k2], s), ww = cscale(R[((size_t)3 * 2 * H + r) * KF + k2], s);
+      const float2 uu = cscale(R[((size_t)0 * 2 * H + r) * KE + k2], s), uw = cscale(R[((size_t)1 * 2 * H + r) * KE + k2], s);
+      const float2 vv = cscale(R[((size_t)2 * 2 * H + r) * KE + k2], s), ww = cscale(R[((size_t)3 * 2 * H + r) * KE + k2], s);
       float2 n1 = make_float2(0.f, 0.f), n3 = make_float2(0.f, 0.f);
       if (!zr) {
         n1 = cadd(cimul(kxv, uu), cimul(kzv, uw));
@@ -463,7 +467,7 @@ __global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const floa
       N3xz[off + c] = n3;
       vvc[off + c] = vv;
     } else {
-      const float2 uv = cscale(R[((size_t)0 * 2 * H + r) * KF + k2], s), wv = cscale(R[((size_t)1 * 2 * H + r) * KF + k2], s);
+      const float2 uv = cscale(R[((size_t)0 * 2 * H + r) * KE + k2], s), wv = cscale(R[((size_t)1 * 2 * H + r) * KE + k2], s);
       float2 n2 = make_float2(0.f, 0.f);
       if (!zr) n2 = cadd(cimul(kxv, uv), cimul(kzv, wv));
       N2xz[off + c] = n2;
@@ -557,7 +561,7 @@ template <int N> struct xp3 {
 template <int N>
 __global__ void __launch_bounds__(xp3<N>::NT) k_xpass3(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
-                                                        const int *__restrict__ capslot, double *__restrict__ cap) {
+                                                        const int *__restrict__ capslot, float *__restrict__ cap) {
   using P = xp3<N>;
   constexpr int XA = P::XA, XM = P::XM, XB = P::XB, L1 = P::L1, LM = P::LM, LB = P::LB, NT = P::NT, LS = P::LS;
   static_assert(XA * XM * XB == N, "x plan");
@@ -651,11 +655,11 @@ __global__ void __launch_bounds__(xp3<N>::NT) k_xpass3(const float2 *__restrict_
       if (cs >= 0) {
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-          double *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + j;
+          float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + j;
           regfft::static_for<0, XB>([&](auto t_) {
             constexpr int t = decltype(t_)::value;
-            cp[t * LB] = f2d_alu(ph[f][t].x);
-            cp[N + t * LB] = f2d_alu(ph[f][t].y);
+            cp[t * LB] = ph[f][t].x;
+            cp[N + t * LB] = ph[f][t].y;
           });
         }
       }

@@ -9,7 +9,9 @@ transform kernels run at their largest compiled lengths:
   the core planes): FP64 within 1e-12 for every band's fields after one step, the mixed form
   within 1e-5 (velocities) and PRESS_MIXED (pressure);
 * the leaf transforms (four_to_phys / phys_to_four) at every compiled length, 24 ... 1152,
-  within 1e-13 of the oracle's.
+  within 1e-13 of the oracle's;
+* one mixed-form step of textured channels whose x transforms have the lengths 192, 288 and
+  384 (the two-stage register x pass), against the oracle.
 The oracle runs on all host cores."""
 import os
 
@@ -185,3 +187,23 @@ def test_leaf_transforms_every_length(cuda_ok, G):
     assert np.abs(back - back_ref).max() / np.abs(back_ref).max() < 1e-13
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("G", (192, 288, 384))
+def test_mixed_step_at_x_lengths(cuda_ok, G):
+    """x length G (z length 96), posts on a 16-point period: one RK3 step of the mixed form
+    within TOL_MIXED_VEL (velocities) and PRESS_MIXED (pressure) of the oracle"""
+    p = re_tau_params(2 * (G // 3), 61, posts=True, Nz=64)
+    s = build_setup(p)
+    assert (s.G1, s.G2) == (G, 96) and s.dny > 0
+    st = initial_field(s, 7 + G)
+    o = Oracle(s, threads=THREADS)
+    o.set_state(*st)
+    o.set_scalars(**initial_scalars(s))
+    o.step()
+    ref = o.get_state()
+    o.close()
+    got, _ = run_gpu(s, st, "mixed")
+    for f, x, y in zip(FIELDS, ref, got):
+        e = relerr(y, x)
+        assert e < (PRESS_MIXED if f == "p" else TOL_MIXED_VEL), (f, e)

@@ -63,7 +63,10 @@ def test_stats_match_oracle(cuda_ok, name, precision, tol):
     close(ppo, ppg, tp)
     if c4o is not None:
         assert c4g is not None and c4g.shape == c4o.shape
-        close(c4o[:2].reshape(2, -1), c4g[:2].reshape(2, -1), tp)
+        # the conditioned P sums cover the wall planes, where the posts are: the FP64 pressure
+        # there agrees to ~5e-12 (the parity tests at size), and the tile sums of a field with
+        # a near-zero mean keep that absolute error (measured 8.3e-12 of the largest sum)
+        close(c4o[:2].reshape(2, -1), c4g[:2].reshape(2, -1), max(tp, 5e-11))
         close(c4o[2:].reshape(2, -1), c4g[2:].reshape(2, -1), tol)
     # spectra are quadratic in a field whose mixed-form error is up to 1e-5 of its own
     # scale: 3x the field bar (FP64: the same bar)
