@@ -56,6 +56,16 @@ def test_multiblock_mixed_within_1e5(cuda_ok):
                 assert v < 1e-5, (band, f, v)
 
 
+def test_multiblock_posts_mixed_three_steps(cuda_ok):
+    """the wall bands' short columns and the immersed levels through three mixed steps: every
+    band within the mixed bar, the divergence at round-off"""
+    _, g, errs = run_pair("MBP", 47, "mixed", 3)
+    for e in errs:
+        for (band, f), v in e.items():
+            assert v < (1e-4 if f == "p" else 1e-5), (band, f, v)
+    assert g.scalars()["err"] < 1e-12
+
+
 def test_band_upload_of_a_single_resolution_channel(cuda_ok):
     s = workload_setup("S")
     st = initial_field(s, 44)
