@@ -23,17 +23,15 @@
 #include "lh_regfft.cuh"
 
 // Blocks per SM the compiler must leave registers for (the second __launch_bounds__ argument)
-// of the x pass, the inverse z pass and the forward z pass; 1 lets it use as many as it likes.
-// Build-time knobs for occupancy sweeps.
-#ifndef LH_XPASS2_MINB
-#define LH_XPASS2_MINB 1
-#endif
-#ifndef LH_ZINV2_MINB
-#define LH_ZINV2_MINB 6  // 56 registers: the state gather's latency wants the warps (fastest of a sweep at C1)
-#endif
-#ifndef LH_ZFWD2_MINB
-#define LH_ZFWD2_MINB 1
-#endif
+// of the x pass, the inverse z pass and the forward z pass: as many blocks as a register budget
+// per thread allows (x pass 128; z passes 56, none from 768 on, whose 24- to 36-point register
+// DFTs need more), capped (5 / 6 / 3). At 384 (the fastest of a sweep at 256²×301 with posts):
+// x pass 5 blocks of 96 threads, inverse z pass 6 of 192, forward z pass 3 of 384.
+// LH_*_MINB override them for sweeps.
+__host__ __device__ constexpr int lh_minb(int threads, int regs, int cap) {
+  const int b = 65536 / (regs * threads);
+  return b < 1 ? 1 : (b > cap ? cap : b);
+}
 
 // row pairs per block (one block: 96 threads at N = 384)
 template <int N> struct xp2 {
@@ -48,10 +46,15 @@ template <int N> struct xp2 {
   static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
   static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB);
   static constexpr int SMEM = (3 * LS1 > 4 * LS2 ? 3 * LS1 : 4 * LS2) * PB * 8;
+#ifdef LH_XPASS2_MINB
+  static constexpr int MINB = LH_XPASS2_MINB;
+#else
+  static constexpr int MINB = lh_minb(NT, 128, 5);
+#endif
 };
 
 template <int N>
-__global__ void __launch_bounds__(xp2<N>::NT, LH_XPASS2_MINB) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+__global__ void __launch_bounds__(xp2<N>::NT, xp2<N>::MINB) k_xpass2(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
                                                         const int *__restrict__ capslot, float *__restrict__ cap) {
   using P = xp2<N>;
@@ -252,6 +255,11 @@ template <int N> struct zp2 {
   static constexpr int KB = 8;
   static constexpr int NT = ((ZA > ZB ? ZA : ZB) * KB + 31) / 32 * 32;
   static constexpr int SMEM = (N + ZB) * KB * 8;  // float2, one pad element per ZA-block
+#ifdef LH_ZINV2_MINB
+  static constexpr int MINB = LH_ZINV2_MINB;
+#else
+  static constexpr int MINB = lh_minb(NT, N >= 768 ? 255 : 56, 6);
+#endif
 };
 
 // The two stages of the inverse z pass for one block of KB kx columns: gather(r, kx) gives
@@ -312,7 +320,7 @@ __device__ __forceinline__ void zinv2_body(Gather &&gather, float2 *__restrict__
 }
 
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT, LH_ZINV2_MINB) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+__global__ void __launch_bounds__(zp2<N>::NT, zp2<N>::MINB) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                        const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
                                                        const float2 *__restrict__ tw) {
   const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * zp2<N>::KB;
@@ -375,10 +383,15 @@ template <int N> struct zf2 {
   // the KF lines of a half-warp start 8 banks apart
   static constexpr int LSE = (N + N / ZB) + ((4 - (N + N / ZB) % 16) + 16) % 16;
   static constexpr int SMEM = 4 * KF * LSE * 8;
+#ifdef LH_ZFWD2_MINB
+  static constexpr int MINB = LH_ZFWD2_MINB;
+#else
+  static constexpr int MINB = lh_minb(NTH, N >= 768 ? 255 : 56, 3);
+#endif
 };
 
 template <int N>
-__global__ void __launch_bounds__(zf2<N>::NTH, LH_ZFWD2_MINB) k_zfwd2(const float2 *__restrict__ B, Geo g, const float2 *__restrict__ tw,
+__global__ void __launch_bounds__(zf2<N>::NTH, zf2<N>::MINB) k_zfwd2(const float2 *__restrict__ B, Geo g, const float2 *__restrict__ tw,
                                                         float2 *__restrict__ N1xz, float2 *__restrict__ N2xz,
                                                         float2 *__restrict__ N3xz, float2 *__restrict__ uvf,
                                                         float2 *__restrict__ vvc, float2 *__restrict__ wvf) {
@@ -556,10 +569,15 @@ template <int N> struct xp3 {
   static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
   static constexpr int LS = pad16(N + N / 8 + 1);            // line stride (float2), >= every padded size
   static constexpr int SMEM = 2 * 4 * LS * 8;                // two buffers of 4 lines
+#ifdef LH_XPASS3_MINB
+  static constexpr int MINB = LH_XPASS3_MINB;
+#else
+  static constexpr int MINB = 1;
+#endif
 };
 
 template <int N>
-__global__ void __launch_bounds__(xp3<N>::NT) k_xpass3(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
+__global__ void __launch_bounds__(xp3<N>::NT, xp3<N>::MINB) k_xpass3(const float2 *__restrict__ A, float2 *__restrict__ B, Geo g,
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
                                                         const int *__restrict__ capslot, float *__restrict__ cap) {
   using P = xp3<N>;
