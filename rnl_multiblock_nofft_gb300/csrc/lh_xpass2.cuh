@@ -565,14 +565,14 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restr
 template <int N> struct xp3 {
   static constexpr int XA = N == 576 ? 12 : 16, XM = N / (8 * XA), XB = 8;
   static constexpr int L1 = N / XA, LM = N / XM, LB = N / XB;  // threads per line of the stages
-  static constexpr int NT = 256;
+  static constexpr int NT = 288;  // the fused stage's 2 LB work items in one round at 1152
   static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
   static constexpr int LS = pad16(N + N / 8 + 1);            // line stride (float2), >= every padded size
   static constexpr int SMEM = 2 * 4 * LS * 8;                // two buffers of 4 lines
 #ifdef LH_XPASS3_MINB
   static constexpr int MINB = LH_XPASS3_MINB;
 #else
-  static constexpr int MINB = 1;
+  static constexpr int MINB = 3;  // 72 registers, no spills (1 block per SM unconstrained: 105 registers, 1.8x slower)
 #endif
 };
 
@@ -646,10 +646,13 @@ __global__ void __launch_bounds__(xp3<N>::NT, xp3<N>::MINB) k_xpass3(const float
   }
   __syncthreads();
   // ---- fused: inverse stage 3 (8-point, Ns = LB), products, CFL, forward stage 1 -> BA at e + e / 8 ----
+  // two work items per point set j, each holding at most two fields: u level: (u, w -> uu, uw,
+  // ww) and (v -> vv); v level: (u, v -> uv) and (w, v -> wv), v transformed by both
   const int nprod = isU ? 4 : 2;
+  const int cs = capslot ? capslot[slot] : -1;
   float m1 = 0.f, m2 = 0.f, m3 = 0.f;
-  for (int j = tid; j < LB; j += NT) {
-    float2 ph[3][XB];
+  for (int it = tid; it < 2 * LB; it += NT) {
+    const int grp = it / LB, j = it - grp * LB;
     float2 w[XB];
     w[0] = make_float2(1.f, 0.f);
     regfft::static_for<1, XB>([&](auto t_) {
@@ -657,61 +660,65 @@ __global__ void __launch_bounds__(xp3<N>::NT, xp3<N>::MINB) k_xpass3(const float
       const float2 x = __ldg(tw + j * t);
       w[t] = make_float2(x.x, -x.y);
     });
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
+    // inverse stage 3 of field f -> physical points j + LB t (captured for the forcing if asked)
+    auto field = [&](int f, float2 *ph, bool capture) {
       const float2 *in = BB + f * LS;
       regfft::static_for<0, XB>([&](auto t_) {
         constexpr int t = decltype(t_)::value;
         const int e = j + LB * t;
         const float2 x = in[e + e / (XA * XM)];
-        ph[f][t] = t == 0 ? x : make_float2(x.x * w[t].x - x.y * w[t].y, x.x * w[t].y + x.y * w[t].x);
+        ph[t] = t == 0 ? x : make_float2(x.x * w[t].x - x.y * w[t].y, x.x * w[t].y + x.y * w[t].x);
       });
-      regfft::dft_reg<XB, true>(ph[f]);
-    }
-    if (capslot) {
-      const int cs = capslot[slot];
-      if (cs >= 0) {
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-          float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + j;
-          regfft::static_for<0, XB>([&](auto t_) {
-            constexpr int t = decltype(t_)::value;
-            cp[t * LB] = ph[f][t].x;
-            cp[N + t * LB] = ph[f][t].y;
-          });
-        }
+      regfft::dft_reg<XB, true>(ph);
+      if (capture && cs >= 0) {
+        float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + j;
+        regfft::static_for<0, XB>([&](auto t_) {
+          constexpr int t = decltype(t_)::value;
+          cp[t * LB] = ph[t].x;
+          cp[N + t * LB] = ph[t].y;
+        });
       }
-    }
-    if (doCFL) {
-      if (isU) {
+    };
+    // product of two fields (row l in .x, row l + 1 in .y), forward 8-point DFT -> BA line p
+    auto product = [&](const float2 *x0, const float2 *x1, int p) {
+      float2 pr[XB];
 #pragma unroll
-        for (int t = 0; t < XB; ++t) {
-          m1 = nmax(m1, nmax(fabsf(ph[0][t].x), fabsf(ph[0][t].y)));
-          m3 = nmax(m3, nmax(fabsf(ph[2][t].x), fabsf(ph[2][t].y)));
-        }
+      for (int t = 0; t < XB; ++t) pr[t] = make_float2(x0[t].x * x1[t].x, x0[t].y * x1[t].y);
+      regfft::dft_reg<XB, false>(pr);
+      float2 *o = BA + p * LS + j * (XB + 1);  // e = j 8 + t
+#pragma unroll
+      for (int t = 0; t < XB; ++t) o[t] = pr[t];
+    };
+    auto amax = [](const float2 *x) {
+      float m = 0.f;
+#pragma unroll
+      for (int t = 0; t < XB; ++t) m = nmax(m, nmax(fabsf(x[t].x), fabsf(x[t].y)));
+      return m;
+    };
+    float2 pa[XB], pc[XB];
+    if (isU) {
+      if (grp == 0) {
+        field(0, pa, true);
+        field(2, pc, true);
+        if (doCFL) { m1 = nmax(m1, amax(pa)); m3 = nmax(m3, amax(pc)); }
+        product(pa, pa, 0);
+        product(pa, pc, 1);
+        product(pc, pc, 3);
       } else {
-        const float thv = g.thvf[q];
-#pragma unroll
-        for (int t = 0; t < XB; ++t) m2 = nmax(m2, nmax(fabsf(ph[1][t].x), fabsf(ph[1][t].y)) * thv);
+        field(1, pa, true);
+        product(pa, pa, 2);
+      }
+    } else {
+      field(1, pc, grp == 0);
+      if (grp == 0) {
+        if (doCFL) m2 = nmax(m2, amax(pc) * g.thvf[q]);
+        field(0, pa, true);
+        product(pa, pc, 0);
+      } else {
+        field(2, pa, true);
+        product(pa, pc, 1);
       }
     }
-    regfft::static_for<0, 4>([&](auto p_) {
-      constexpr int p = decltype(p_)::value;
-      constexpr int ua = p == 2 ? 1 : (p == 3 ? 2 : 0), ub = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 1 : 2));
-      constexpr int va = p == 0 ? 0 : 2, vb = 1;
-      if (p < 2 || isU) {
-        float2 pr[XB];
-#pragma unroll
-        for (int t = 0; t < XB; ++t) {
-          const float2 x0 = isU ? ph[ua][t] : ph[va][t], x1 = isU ? ph[ub][t] : ph[vb][t];
-          pr[t] = make_float2(x0.x * x1.x, x0.y * x1.y);
-        }
-        regfft::dft_reg<XB, false>(pr);
-        float2 *o = BA + p * LS + j * (XB + 1);  // e = j 8 + t
-#pragma unroll
-        for (int t = 0; t < XB; ++t) o[t] = pr[t];
-      }
-    });
   }
   if (doCFL) {
     m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
