@@ -58,7 +58,7 @@ struct lh_handle {
   void *cap;  // captured physical planes of the immersed levels, in the transform precision
   IbRec *d_ibrec;   // forced points, sorted by (plane of du, row)
   int *d_iboff;     // [3 nib G2 + 1] record ranges per (plane, row)
-  double2 *duib;
+  void *duib;  // du of the immersed levels [ibslot][3][col], complex in the transform precision
   // plane views of the nonlinear launches: wall-band planes, then core planes
   // (multiblock); one view when single-resolution
   Geo gv[2];
@@ -527,7 +527,7 @@ extern "C" int lh_create(const lh_config *cfg, lh_handle **out) {
     h->d_lev2cap_u = (int *)upload_vec(lev2cap_u, ce); h->d_lev2cap_v = (int *)upload_vec(lev2cap_v, ce);
     if (ce != cudaSuccess) { int rc = fail(h, LH_ECUDA, cudaGetErrorString(ce)); lh_destroy(h); return rc; }
     ZA(h->cap, h->vsz / 2 * (size_t)h->ncap * 3 * pp);
-    ZA(h->duib, cz * (size_t)h->nib * 3 * nc);
+    ZA(h->duib, vs * (size_t)h->nib * 3 * nc);
   }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1145,17 +1145,17 @@ static int triad_nonlinear(lh_handle *h, int kRK) {
 // plane transforms through scratch buffers in precision T (leaves: FP64; immersed
 // boundaries: the form's transform precision)
 template <typename T, int N>
-static int launch_spec_zinv(lh_handle *h, const double2 *spec, void *Ascr, int npl, const void *twz) {
+static int launch_spec_zinv(lh_handle *h, const void *spec, void *Ascr, int npl, const void *twz) {
   typedef typename C2<T>::t V;
   if constexpr (sizeof(T) == 4) {  // the two-stage register form (immersed boundaries, mixed form)
     using P = zp2<N>;
     dim3 g1((h->g.N1h + P::KB - 1) / P::KB, npl);
-    KL("k_spec_zinv", k_spec_zinv2<N><<<g1, P::NT, P::SMEM, h->st>>>(spec, (float2 *)Ascr, h->g, (const float2 *)twz));
+    KL("k_spec_zinv", k_spec_zinv2<N><<<g1, P::NT, P::SMEM, h->st>>>((const float2 *)spec, (float2 *)Ascr, h->g, (const float2 *)twz));
     return LH_OK;
   }
   constexpr int KB = kb_zinv<V>(N);
   dim3 g1((h->g.N1h + KB - 1) / KB, npl);
-  KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>(spec, (V *)Ascr, h->g, (const V *)twz));
+  KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const double2 *)spec, (V *)Ascr, h->g, (const V *)twz));
   return LH_OK;
 }
 template <typename T, int N>
@@ -1175,17 +1175,17 @@ static int launch_xfwd_phys(lh_handle *h, const double *phys, void *Bscr, int np
   return LH_OK;
 }
 template <typename T, int N>
-static int launch_zfwd_spec(lh_handle *h, const void *Bscr, double2 *spec, int npl, const void *twz) {
+static int launch_zfwd_spec(lh_handle *h, const void *Bscr, void *spec, int npl, const void *twz) {
   typedef typename C2<T>::t V;
   if constexpr (sizeof(T) == 4) {  // the two-stage register form (immersed boundaries, mixed form)
     using P = zp2<N>;
     dim3 g2((h->g.N1h + P::KB - 1) / P::KB, npl);
-    KL("k_zfwd_spec", k_zfwd_spec2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)Bscr, spec, h->g, (const float2 *)twz));
+    KL("k_zfwd_spec", k_zfwd_spec2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)Bscr, (float2 *)spec, h->g, (const float2 *)twz));
     return LH_OK;
   }
   constexpr int KB = kb_zinv<V>(N);
   dim3 g2((h->g.N1h + KB - 1) / KB, npl);
-  KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, spec, h->g, (const V *)twz));
+  KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, (double2 *)spec, h->g, (const V *)twz));
   return LH_OK;
 }
 
@@ -1262,12 +1262,12 @@ static int substep_launches_t(lh_handle *h, int kRK) {
       KL("k_ib_du", k_ib_du<T><<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (V *)h->Nu1, (V *)h->Nu2, (V *)h->Nu3,
                                                          (const V *)h->N1xz, (const V *)h->N2xz, (const V *)h->N3xz,
                                                          (const V *)h->uvf, (const V *)h->vvc, (const V *)h->wvf, h->p,
-                                                         h->duib, h->d_iblev, h->nib, g, h->sc, kRK));
+                                                         (double2 *)h->duib, h->d_iblev, h->nib, g, h->sc, kRK));
     } else {
       KL("k_ib_du", k_ib_du_mx<<<gd, NTHR_H, 0, h->st>>>(h->u1, h->u2, h->u3, (float2 *)h->Nu1, (float2 *)h->Nu2,
                                                          (float2 *)h->Nu3, (const float2 *)h->N1xz, (const float2 *)h->N2xz,
                                                          (const float2 *)h->N3xz, (const float2 *)h->uvf,
-                                                         (const float2 *)h->vvc, (const float2 *)h->wvf, h->p, h->duib,
+                                                         (const float2 *)h->vvc, (const float2 *)h->wvf, h->p, (float2 *)h->duib,
                                                          h->d_iblev, h->nib, g, h->sc, kRK));
     }
     rc = LH_EINVAL;
@@ -1285,7 +1285,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     KL("k_helm00", k_helm00_pcr<<<6, 512, sm00, h->st>>>(
                        (double *)h->u1, (double *)h->u3, (double *)h->u2, (const float *)h->N1xz, (const float *)h->N3xz,
                        (const float *)h->N2xz, (const float *)h->uvf, (const float *)h->wvf, (const float *)h->vvc,
-                       (const double *)h->p, h->duib, h->ib ? h->d_ibslot_u : nullptr, h->ib ? h->d_ibslot_v : nullptr,
+                       (const double *)h->p, (const float2 *)h->duib, h->ib ? h->d_ibslot_u : nullptr, h->ib ? h->d_ibslot_v : nullptr,
                        g, h->sc, kRK, h->a3s));
   }
   // The u/w and v solves are independent: v runs on the side stream while u/w and the
@@ -1300,7 +1300,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
   if (!fork) prof_begin(h, "k_helm_v");
   if (h->prec == LH_PREC_FP64) {
     k_helm_v<T><<<nbv, h->tb_v, 0, sv>>>(h->u2, (double2 *)h->Nu2, (const V *)h->N2xz, (const V *)h->vvc, h->p,
-                                         h->a3v, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, h->duib);
+                                         h->a3v, g, h->sc, kRK, h->ib ? h->d_ibslot_v : nullptr, (const double2 *)h->duib);
   } else {
     const int nb2v = (2 * g.nvc + h->tb_v - 1) / h->tb_v;
     const size_t sm = staged_smem(g.nv, h->pf_v, h->tb_v);
@@ -1311,10 +1311,10 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     const double *PP = (const double *)h->p;
     float2 *YS = (float2 *)h->ysv;
     switch (h->pf_v) {
-      case 0: k_helm_v_mx2<<<nb2v, h->tb_v, 0, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
-      case 2: k_helm_v_mx3<2><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
-      case 8: k_helm_v_mx3<8><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
-      default: k_helm_v_mx3<4><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, h->duib); break;
+      case 0: k_helm_v_mx2<<<nb2v, h->tb_v, 0, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, (const float2 *)h->duib); break;
+      case 2: k_helm_v_mx3<2><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, (const float2 *)h->duib); break;
+      case 8: k_helm_v_mx3<8><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, (const float2 *)h->duib); break;
+      default: k_helm_v_mx3<4><<<nb2v, h->tb_v, sm, sv>>>(V, NV, XV, VV, PP, YS, g, h->sc, kRK, ibv, (const float2 *)h->duib); break;
     }
   }
   if ((rc = count_launch(h))) return rc;
@@ -1323,7 +1323,7 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     KL("k_helm_uw", k_helm_uw<T><<<nbu, h->tb_uw, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
                                                            (const V *)h->N1xz, (const V *)h->N3xz, (const V *)h->uvf,
                                                            (const V *)h->wvf, h->p, h->a3s, g, h->sc, kRK,
-                                                           h->ib ? h->d_ibslot_u : nullptr, h->duib));
+                                                           h->ib ? h->d_ibslot_u : nullptr, (const double2 *)h->duib));
   } else {
     const int nb2u = (2 * g.nvc + h->tb_uw - 1) / h->tb_uw;
     const size_t sm = staged_smem(g.nu, h->pf_uw, h->tb_uw);
@@ -1335,10 +1335,10 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     const int *ibu = h->ib ? h->d_ibslot_u : nullptr;
     float2 *YS = (float2 *)h->ysf;
     switch (h->pf_uw) {
-      case 0: KL("k_helm_uw", k_helm_u_mx2<<<gr, h->tb_uw, 0, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
-      case 2: KL("k_helm_uw", k_helm_u_mx3<2><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
-      case 8: KL("k_helm_uw", k_helm_u_mx3<8><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
-      default: KL("k_helm_uw", k_helm_u_mx3<4><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, h->duib)); break;
+      case 0: KL("k_helm_uw", k_helm_u_mx2<<<gr, h->tb_uw, 0, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, (const float2 *)h->duib)); break;
+      case 2: KL("k_helm_uw", k_helm_u_mx3<2><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, (const float2 *)h->duib)); break;
+      case 8: KL("k_helm_uw", k_helm_u_mx3<8><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, (const float2 *)h->duib)); break;
+      default: KL("k_helm_uw", k_helm_u_mx3<4><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, (const float2 *)h->duib)); break;
     }
   }
   if ((rc = meanflow(h, kRK))) return rc;

@@ -798,7 +798,7 @@ __global__ void __launch_bounds__(512) k_helm00_pcr(double *__restrict__ u1, dou
                                                     const float *__restrict__ N3xz, const float *__restrict__ N2xz,
                                                     const float *__restrict__ uvf, const float *__restrict__ wvf,
                                                     const float *__restrict__ vvc, const double *__restrict__ p,
-                                                    const double2 *__restrict__ duib, const int *__restrict__ ibslot_u,
+                                                    const float2 *__restrict__ duib, const int *__restrict__ ibslot_u,
                                                     const int *__restrict__ ibslot_v, Geo g,
                                                     const DevScalars *__restrict__ sc, int kRK,
                                                     double *__restrict__ nuo_all) {
@@ -845,8 +845,8 @@ __global__ void __launch_bounds__(512) k_helm00_pcr(double *__restrict__ u1, dou
         du = ((C1 * L + C2 * nuo[q]) + rest) + G * nq;
         nuo[q] = nq;
       } else {
-        const double2 di = duib[((size_t)ibs * 3 + fw2f(fw)) * g.ncol];
-        du = part ? di.y : di.x;
+        const float2 di = duib[((size_t)ibs * 3 + fw2f(fw)) * g.ncol];
+        du = f2d_alu(part ? di.y : di.x);
       }
       a = -beta * d0q; b = 1.0 - beta * d1q; c = -beta * d2q;
       d = u0 + dt * du;
@@ -907,7 +907,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
                                                      const float *__restrict__ uvf, const float *__restrict__ wvf,
                                                      const double2 *__restrict__ p, float2 *__restrict__ ys2, Geo g,
                                                      const DevScalars *__restrict__ sc, int kRK,
-                                                     const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
+                                                     const int *__restrict__ ibslot_u, const float2 *__restrict__ duib) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int vc = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
@@ -991,8 +991,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
         Nu[e] = n;
         du += G * n;
       } else {
-        const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
-        du = d2f_alu(part ? di.y : di.x);
+        const float2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+        du = part ? di.y : di.x;
       }
       const float rr = dtf * du + beta * L;
       const float a1 = -beta * a;
@@ -1029,8 +1029,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx2(double *__restrict__ u1, do
       Nu[e] = n;
       du += G * n;
     } else {
-      const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
-      du = d2f_alu(part ? di.y : di.x);
+      const float2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+      du = part ? di.y : di.x;
     }
     const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
@@ -1062,7 +1062,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
                                                      const float *__restrict__ N2xz, const float *__restrict__ vvc,
                                                      const double *__restrict__ p, float2 *__restrict__ ys, Geo g,
                                                      const DevScalars *__restrict__ sc, int kRK,
-                                                     const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
+                                                     const int *__restrict__ ibslot_v, const float2 *__restrict__ duib) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int vc = tid >> 1, part = tid & 1;
   const int nc = g.ncol;
@@ -1132,8 +1132,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx2(double *__restrict__ u2, fl
         Nu2[e] = n;
         du += G * n;
       } else {
-        const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
-        du = d2f_alu(part ? di.y : di.x);
+        const float2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
+        du = part ? di.y : di.x;
       }
       const float rr = dtf * du + beta * L;
       const float a1 = -beta * a;
@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx3(double *__restrict__ u1, do
                                                      const float *__restrict__ uvf, const float *__restrict__ wvf,
                                                      const double2 *__restrict__ p, float2 *__restrict__ ys2, Geo g,
                                                      const DevScalars *__restrict__ sc, int kRK,
-                                                     const int *__restrict__ ibslot_u, const double2 *__restrict__ duib) {
+                                                     const int *__restrict__ ibslot_u, const float2 *__restrict__ duib) {
   constexpr int NS = D + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nu = g.nu, nt = blockDim.x;
@@ -1289,8 +1289,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_u_mx3(double *__restrict__ u1, do
       Nu[e] = n;
       du += G * n;
     } else {
-      const double2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
-      du = d2f_alu(part ? di.y : di.x);
+      const float2 di = duib[((size_t)ibs * 3 + (fw ? 2 : 0)) * nc + c];
+      du = part ? di.y : di.x;
     }
     const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
@@ -1324,7 +1324,7 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx3(double *__restrict__ u2, fl
                                                      const float *__restrict__ N2xz, const float *__restrict__ vvc,
                                                      const double *__restrict__ p, float2 *__restrict__ ys, Geo g,
                                                      const DevScalars *__restrict__ sc, int kRK,
-                                                     const int *__restrict__ ibslot_v, const double2 *__restrict__ duib) {
+                                                     const int *__restrict__ ibslot_v, const float2 *__restrict__ duib) {
   constexpr int NS = D + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nv = g.nv, nt = blockDim.x;
@@ -1406,8 +1406,8 @@ __global__ void __launch_bounds__(NTHR) k_helm_v_mx3(double *__restrict__ u2, fl
       Nu2[e] = n;
       du += G * n;
     } else {
-      const double2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
-      du = d2f_alu(part ? di.y : di.x);
+      const float2 di = duib[((size_t)ibs * 3 + 1) * nc + c];
+      du = part ? di.y : di.x;
     }
     const float rr = dtf * du + beta * L;
     const float a1 = -beta * a;
@@ -2383,7 +2383,8 @@ __global__ void __launch_bounds__(NTHR) k_zfwd_spec(const typename C2<T>::t *__r
 // ============================================================================
 // Immersed boundaries (FOU3D.f90:806-998): assemble du at the listed levels,
 // then (after the inverse transform) the forcing at the solid points.
-// duib layout: [ibslot][field 0..2][col]; ib levels of u (fields 0, 2) and v (1).
+// duib layout: [ibslot][field 0..2][col], complex128 (FP64 form) or complex64 (mixed form, whose
+// values are FP32); ib levels of u (fields 0, 2) and v (1).
 // ============================================================================
 template <typename TN>
 __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
@@ -2457,14 +2458,14 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
 }
 
 // Mixed form of k_ib_du: the same right-hand side in FP32 (FP64 neighbour
-// differences for the Laplacian, integer-pipe conversions), N stored in FP32.
+// differences for the Laplacian, integer-pipe conversions), N and du stored in FP32.
 __global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                    const double2 *__restrict__ u3, float2 *__restrict__ Nu1o,
                                                    float2 *__restrict__ Nu2o, float2 *__restrict__ Nu3o,
                                                    const float2 *__restrict__ N1xz, const float2 *__restrict__ N2xz,
                                                    const float2 *__restrict__ N3xz, const float2 *__restrict__ uvf,
                                                    const float2 *__restrict__ vvc, const float2 *__restrict__ wvf,
-                                                   const double2 *__restrict__ p, double2 *__restrict__ duib,
+                                                   const double2 *__restrict__ p, float2 *__restrict__ duib,
                                                    const int *__restrict__ iblev, int nib, Geo g,
                                                    const DevScalars *__restrict__ sc, int kRK) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2507,7 +2508,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u
       n.x = x.x + (fq.x - fm.x) * th * dd; n.y = x.y + (fq.y - fm.y) * th * dd;
       No[o] = n;
       du.x += G * n.x; du.y += G * n.y;
-      duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = make_double2(f2d_alu(du.x), f2d_alu(du.y));
+      duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = du;
     }
   }
   if (qv > 0) {
@@ -2530,7 +2531,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u
     n.x = x.x + (vp1.x - vq.x) * th * dd; n.y = x.y + (vp1.y - vq.y) * th * dd;
     Nu2o[o] = n;
     du.x += G * n.x; du.y += G * n.y;
-    duib[((size_t)s * 3 + 1) * nc + c] = make_double2(f2d_alu(du.x), f2d_alu(du.y));
+    duib[((size_t)s * 3 + 1) * nc + c] = du;
   }
 }
 

@@ -351,18 +351,15 @@ __global__ void __launch_bounds__(zp2<N>::NT, zp2<N>::MINB) k_zinv2(const double
   zinv2_body<N>(gather, A + (size_t)(slot * 3 + f) * N * g.N1h, g.N1h, kx0, tw);
 }
 
-// The inverse z transforms of spectral planes [pl][N2][N1h] complex128 (the immersed-boundary
-// du planes) into A [pl][l][kx] in FP32, as k_spec_zinv<float, N>.
+// The inverse z transforms of spectral planes [pl][N2][N1h] complex64 (the immersed-boundary
+// du planes of the mixed form) into A [pl][l][kx] in FP32, as k_spec_zinv<float, N>.
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_spec_zinv2(const double2 *__restrict__ spec, float2 *__restrict__ A,
+__global__ void __launch_bounds__(zp2<N>::NT) k_spec_zinv2(const float2 *__restrict__ spec, float2 *__restrict__ A,
                                                             Geo g, const float2 *__restrict__ tw) {
   const int pl = blockIdx.y, kx0 = blockIdx.x * zp2<N>::KB;
-  const double2 *S = spec + (size_t)pl * g.ncol;
+  const float2 *S = spec + (size_t)pl * g.ncol;
   const int N1h = g.N1h;
-  auto gather = [&](int r, int kx) {
-    const double2 a = S[(size_t)r * N1h + kx];
-    return make_float2(d2f_alu(a.x), d2f_alu(a.y));
-  };
+  auto gather = [&](int r, int kx) { return S[(size_t)r * N1h + kx]; };
   zinv2_body<N>(gather, A + (size_t)pl * N * N1h, N1h, kx0, tw);
 }
 
@@ -492,10 +489,10 @@ __global__ void __launch_bounds__(zf2<N>::NTH, zf2<N>::MINB) k_zfwd2(const float
 
 // ============================================================================
 // The forward z transforms of physical-x planes B [pl][l][kx] (FP32) into spectral planes
-// [pl][N2][N1h] complex128, x 1/N, the retained kz rows only (as k_zfwd_spec<float, N>).
+// [pl][N2][N1h] complex64, x 1/N, the retained kz rows only (as k_zfwd_spec<float, N>).
 // ============================================================================
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restrict__ Bp, double2 *__restrict__ spec,
+__global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restrict__ Bp, float2 *__restrict__ spec,
                                                             Geo g, const float2 *__restrict__ tw) {
   using P = zp2<N>;
   // the inverse pass's plan read backwards: stage 1 ZA threads per line (ZB-point DFTs of rows
@@ -537,7 +534,7 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restr
     regfft::dft_reg<ZA, false>(v);
     if (kx < N1h) {
       const float s = 1.f / (float)N;
-      double2 *dst = spec + (size_t)pl * g.ncol + kx;
+      float2 *dst = spec + (size_t)pl * g.ncol + kx;
       regfft::static_for<0, ZA>([&](auto t_) {
         constexpr int t = decltype(t_)::value;
         constexpr int mlo = ZB * t, mhi = ZB * t + ZB - 1;
@@ -545,7 +542,7 @@ __global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restr
         int r = -1;
         if (mlo < H && m < H) r = m;
         else if (mhi >= N - H && m >= N - H) r = m - N + 2 * H;
-        if (r >= 0) dst[(size_t)r * N1h] = make_double2(f2d_alu(v[t].x * s), f2d_alu(v[t].y * s));
+        if (r >= 0) dst[(size_t)r * N1h] = make_float2(v[t].x * s, v[t].y * s);
       });
     }
   }
