@@ -10,8 +10,10 @@
 //   inverse stage 1: XB threads per line, each an XA-point DFT of elements jj + XB t, read
 //                    straight from A with the Hermitian completion (the gather) -> shared E1
 //   inverse stage 2 + products + forward stage 1 (fused, registers): XA threads per row pair,
-//                    thread jj holds physical points jj + XA t (t < 8) of u, v and w, forms the
-//                    products there and transforms them with the forward 8-point DFT -> E2
+//                    thread jj holds physical points jj + XA t (t < 8) of at most two of u, v,
+//                    w at a time, forms the products there and transforms them with the forward
+//                    8-point DFT, written over the E1 elements it has read (a fourth line for a
+//                    u level's fourth product)
 //   forward stage 2: XB threads per product line, each an XA-point DFT; the thread holds
 //                    outputs jj + XB t, the conjugate-symmetric partner N - k of every output k
 //                    is in lane (XB - jj) mod XB of the same 8-lane group, fetched by shuffle,
@@ -40,12 +42,12 @@ template <int N> struct xp2 {
   // threads: enough for every stage (fused: XA PB; the first and last stages: 3 and 4 lines x
   // PB pairs x XB), in whole warps (the shuffles of the fused and last stages)
   static constexpr int NT = ((XA * PB > 4 * PB * XB ? XA * PB : 4 * PB * XB) + 31) / 32 * 32;
-  // padded shared-memory lines: E1 (stage-1 output e = jj XA + t at e + e / XA), E2
-  // (forward stage-1 output e = jj 8 + t at e + e / 8); line strides = 8 (mod 16) float2 so
-  // that the lanes of two lines fall on different banks
+  // padded shared-memory lines E1 (stage-1 output e = jj XA + t at e + e / XA; the fused stage's
+  // outputs in place); line strides = 8 (mod 16) float2 so that the lanes of two lines fall on
+  // different banks
   static constexpr int pad16(int v) { return v + ((8 - v % 16) + 16) % 16; }
-  static constexpr int LS1 = pad16(N + N / XA), LS2 = pad16(N + N / XB);
-  static constexpr int SMEM = (3 * LS1 > 4 * LS2 ? 3 * LS1 : 4 * LS2) * PB * 8;
+  static constexpr int LS1 = pad16(N + N / XA);
+  static constexpr int SMEM = 4 * LS1 * PB * 8;  // 3 field lines + 1 product line per pair
 #ifdef LH_XPASS2_MINB
   static constexpr int MINB = LH_XPASS2_MINB;
 #else
@@ -58,7 +60,7 @@ __global__ void __launch_bounds__(xp2<N>::NT, xp2<N>::MINB) k_xpass2(const float
                                                         const float2 *__restrict__ tw, int doCFL, DevScalars *sc,
                                                         const int *__restrict__ capslot, float *__restrict__ cap) {
   using P = xp2<N>;
-  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1, LS2 = P::LS2;
+  constexpr int XA = P::XA, XB = P::XB, PB = P::PB, LS1 = P::LS1;
   constexpr int NK = N / 3 + 1;  // retained x-modes 0..N1/2 (N1 = 2 (Ngal1 / 3), checked at create)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *E = reinterpret_cast<float2 *>(smem_raw);
@@ -106,104 +108,96 @@ __global__ void __launch_bounds__(xp2<N>::NT, xp2<N>::MINB) k_xpass2(const float
   __syncthreads();
 
   // ---- fused: inverse stage 2 (8-point DFTs), products, CFL maxima, forward stage 1 ----
+  // thread (pb, jj) reads element jj of the 8 stage-1 regions of each field line (positions
+  // jj + (XA + 1) t) and writes each product's 8 outputs back there, over a field line it has
+  // finished reading (the positions only it reads; a u level's fourth product into line 3),
+  // holding at most two fields: u level: v -> vv; u, w -> uu, uw, ww; v level: v; u -> uv; w -> wv
   const int pb = tid / XA, jj = tid - pb * XA;
   const bool act = pb < PB;  // the threads that round the block up to whole warps only take part in the shuffles
-  float2 ph[3][XB];
-  if (!act) {
-#pragma unroll
-    for (int f = 0; f < 3; ++f)
-#pragma unroll
-      for (int t = 0; t < XB; ++t) ph[f][t] = make_float2(0.f, 0.f);
-  } else {
-    float2 w[XB];  // exp(+2 pi i jj t / N): the inverse twiddles of stage 2
-    w[0] = make_float2(1.f, 0.f);
-    regfft::static_for<1, XB>([&](auto t_) {
-      constexpr int t = decltype(t_)::value;
-      const float2 x = __ldg(tw + jj * t);
-      w[t] = make_float2(x.x, -x.y);
-    });
-#pragma unroll
-    for (int f = 0; f < 3; ++f) {
-      const float2 *e1 = E + (f * PB + pb) * LS1 + jj;
-      regfft::static_for<0, XB>([&](auto t_) {
-        constexpr int t = decltype(t_)::value;
-        const float2 x = e1[t * (XA + 1)];
-        ph[f][t] = t == 0 ? x : make_float2(x.x * w[t].x - x.y * w[t].y, x.x * w[t].y + x.y * w[t].x);
-      });
-      regfft::dft_reg<XB, true>(ph[f]);
-    }
-  }
   const bool valid = act && pb < npairs;
-  if (capslot && valid) {
-    const int cs = capslot[slot];
-    if (cs >= 0) {
-      const int l = l0 + 2 * pb;
+  const int cs = (capslot && valid) ? capslot[slot] : -1;
+  float m1 = 0.f, m2 = 0.f, m3 = 0.f;
+  if (act) {
+    // inverse stage 2 of field f: twiddles exp(+2 pi i jj t / N), 8-point DFT -> points jj + XA t
+    auto field = [&](int f, float2 *ph) {
+      const float2 *e1 = E + (f * PB + pb) * LS1 + jj;
 #pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + jj;
-        regfft::static_for<0, XB>([&](auto t_) {
-          constexpr int t = decltype(t_)::value;
-          cp[t * XA] = ph[f][t].x;
-          cp[N + t * XA] = ph[f][t].y;
-        });
+      for (int t = 0; t < XB; ++t) {
+        const float2 x = e1[t * (XA + 1)];
+        if (t == 0) {
+          ph[0] = x;
+        } else {
+          const float2 w = __ldg(tw + jj * t);
+          ph[t] = make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);  // x * conj(w)
+        }
       }
+      regfft::dft_reg<XB, true>(ph);
+      if (cs >= 0) {
+        const int l = l0 + 2 * pb;
+        float *cp = cap + ((size_t)cs * 3 + f) * (size_t)G2 * N + (size_t)l * N + jj;
+#pragma unroll
+        for (int t = 0; t < XB; ++t) {
+          cp[t * XA] = ph[t].x;
+          cp[N + t * XA] = ph[t].y;
+        }
+      }
+    };
+    // product of two fields (row a in .x, row b in .y), forward 8-point DFT, into line L
+    auto product = [&](const float2 *x0, const float2 *x1, int L) {
+      float2 pr[XB];
+#pragma unroll
+      for (int t = 0; t < XB; ++t) pr[t] = make_float2(x0[t].x * x1[t].x, x0[t].y * x1[t].y);
+      regfft::dft_reg<XB, false>(pr);
+      float2 *e = E + (L * PB + pb) * LS1 + jj;
+#pragma unroll
+      for (int t = 0; t < XB; ++t) e[t * (XA + 1)] = pr[t];
+    };
+    auto amax = [](const float2 *x) {
+      float m = 0.f;
+#pragma unroll
+      for (int t = 0; t < XB; ++t) m = nmax(m, nmax(fabsf(x[t].x), fabsf(x[t].y)));
+      return m;
+    };
+    float2 pa[XB], pc[XB];
+    if (isU) {
+      field(1, pa);
+      product(pa, pa, 1);
+      field(0, pa);
+      field(2, pc);
+      if (valid) { m1 = amax(pa); m3 = amax(pc); }
+      product(pa, pa, 0);
+      product(pa, pc, 3);
+      product(pc, pc, 2);
+    } else {
+      field(1, pc);
+      if (valid) m2 = amax(pc) * g.thvf[q];
+      field(0, pa);
+      product(pa, pc, 0);
+      field(2, pa);
+      product(pa, pc, 2);
     }
   }
   if (doCFL) {
-    float m1 = 0.f, m2 = 0.f, m3 = 0.f;
-    if (valid) {
-      if (isU) {
-#pragma unroll
-        for (int t = 0; t < XB; ++t) {
-          m1 = nmax(m1, nmax(fabsf(ph[0][t].x), fabsf(ph[0][t].y)));
-          m3 = nmax(m3, nmax(fabsf(ph[2][t].x), fabsf(ph[2][t].y)));
-        }
-      } else {
-        const float thv = g.thvf[q];
-#pragma unroll
-        for (int t = 0; t < XB; ++t) m2 = nmax(m2, nmax(fabsf(ph[1][t].x), fabsf(ph[1][t].y)) * thv);
-      }
-    }
     m1 = warp_max(m1); m2 = warp_max(m2); m3 = warp_max(m3);
     if ((tid & 31) == 0) {
       if (isU) { atomic_max_pos(&sc->u1m, f2d_alu(m1)); atomic_max_pos(&sc->u3m, f2d_alu(m3)); }
       else atomic_max_pos(&sc->u2m, f2d_alu(m2));
     }
   }
-  __syncthreads();  // E1 is read: E2 reuses the shared memory
-  const int nprod = isU ? 4 : 2;
-  if (act) {
-    // u level: uu, uw, vv, ww; v level: uv, wv (per row of the pair); field indices are
-    // compile-time so that ph stays in registers
-    regfft::static_for<0, 4>([&](auto p_) {
-      constexpr int p = decltype(p_)::value;
-      constexpr int ua = p == 2 ? 1 : (p == 3 ? 2 : 0), ub = p == 0 ? 0 : (p == 1 ? 2 : (p == 2 ? 1 : 2));
-      constexpr int va = p == 0 ? 0 : 2, vb = 1;
-      if (p < 2 || isU) {
-        float2 pr[XB];
-#pragma unroll
-        for (int t = 0; t < XB; ++t) {
-          const float2 x0 = isU ? ph[ua][t] : ph[va][t], x1 = isU ? ph[ub][t] : ph[vb][t];
-          pr[t] = make_float2(x0.x * x1.x, x0.y * x1.y);
-        }
-        regfft::dft_reg<XB, false>(pr);
-        float2 *e2 = E + (p * PB + pb) * LS2 + jj * (XB + 1);
-#pragma unroll
-        for (int t = 0; t < XB; ++t) e2[t] = pr[t];
-      }
-    });
-  }
   __syncthreads();
+  const int nprod = isU ? 4 : 2;
 
   // ---- forward stage 2: line (p, pb), thread jj < 8: twiddles, XA-point DFT of jj + 8 t ----
   if (tid < nprod * PB * XB) {
     const int line = tid / XB, jj2 = tid - line * XB;
     const int p = line / PB, pb2 = line - p * PB;
+    const int L = isU ? (p == 0 ? 0 : p == 1 ? 3 : p == 2 ? 1 : 2) : (p == 0 ? 0 : 2);
     float2 v[XA];
-    const float2 *e2 = E + line * LS2 + jj2;
+    // element t (the fused thread t's output jj2) at position t + (XA + 1) jj2 of line L
+    const float2 *e2 = E + (L * PB + pb2) * LS1 + jj2 * (XA + 1);
     regfft::static_for<0, XA>([&](auto t_) {
       constexpr int t = decltype(t_)::value;
-      const float2 x = e2[t * (XB + 1)];
+      const float2 x = e2[t];
       if constexpr (t == 0) {
         v[0] = x;
       } else {
