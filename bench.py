@@ -503,6 +503,15 @@ def kernel_roofline(s, kern, form, tl, peak, peak_kind, workload):
     if dname == "k_xpass_nl":  # the same without the captured physical planes of the immersed levels
         ab = 3 * algorithmic_bytes(s, dname, form, ib=False) / (dms * 1e-3) / 1e9
         out["frac_A_B_only"] = ab / peak
+    if dname == "k_press":
+        out["limiter"] = "FP64 pipe: the FP64 state updates and sweeps (ncu: FP64 pipe ~83 % busy, DRAM ~46 %)"
+    # the other large kernels against the same HBM roofline (live CUDA-event times)
+    others = {}
+    for name, (nl, ms) in sorted(kern.items(), key=lambda kv: -kv[1][1])[:6]:
+        ab = 3 * algorithmic_bytes(s, name, form, triad_terms(s, tl) if tl is not None else 0)
+        if name != dname and math.isfinite(ab) and ms > 0:
+            others[name] = {"frac": ab / (ms * 1e-3) / 1e9 / peak, "share": ms / step_total}
+    out["others"] = others
     return out
 
 
