@@ -30,6 +30,9 @@
 // DFTs need more), capped (5 / 6 / 3). At 384 (the fastest of a sweep at 256²×301 with posts):
 // x pass 5 blocks of 96 threads, inverse z pass 6 of 192, forward z pass 3 of 384.
 // LH_*_MINB override them for sweeps.
+#ifndef LH_SPECZ_MINB  // the z transforms of the immersed levels' du planes (sweep knob; 1: unconstrained)
+#define LH_SPECZ_MINB(N) 1
+#endif
 __host__ __device__ constexpr int lh_minb(int threads, int regs, int cap) {
   const int b = 65536 / (regs * threads);
   return b < 1 ? 1 : (b > cap ? cap : b);
@@ -246,7 +249,11 @@ template <int N> struct zp2 {
   static constexpr int ZA = N == 24 ? 4 : N == 48 ? 6 : N == 72 ? 8 : N == 96 ? 8 : N == 144 ? 12 : N == 192 ? 12
                           : N == 288 ? 16 : N == 384 ? 16 : N == 576 ? 24 : N == 768 ? 24 : 32;
   static constexpr int ZB = N / ZA;
+#ifdef LH_ZP2_KB
+  static constexpr int KB = LH_ZP2_KB;
+#else
   static constexpr int KB = 8;
+#endif
   static constexpr int NT = ((ZA > ZB ? ZA : ZB) * KB + 31) / 32 * 32;
   static constexpr int SMEM = (N + ZB) * KB * 8;  // float2, one pad element per ZA-block
 #ifdef LH_ZINV2_MINB
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(zp2<N>::NT, zp2<N>::MINB) k_zinv2(const double
 // The inverse z transforms of spectral planes [pl][N2][N1h] complex64 (the immersed-boundary
 // du planes of the mixed form) into A [pl][l][kx] in FP32, as k_spec_zinv<float, N>.
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_spec_zinv2(const float2 *__restrict__ spec, float2 *__restrict__ A,
+__global__ void __launch_bounds__(zp2<N>::NT, LH_SPECZ_MINB(N)) k_spec_zinv2(const float2 *__restrict__ spec, float2 *__restrict__ A,
                                                             Geo g, const float2 *__restrict__ tw) {
   const int pl = blockIdx.y, kx0 = blockIdx.x * zp2<N>::KB;
   const float2 *S = spec + (size_t)pl * g.ncol;
@@ -486,7 +493,7 @@ __global__ void __launch_bounds__(zf2<N>::NTH, zf2<N>::MINB) k_zfwd2(const float
 // [pl][N2][N1h] complex64, x 1/N, the retained kz rows only (as k_zfwd_spec<float, N>).
 // ============================================================================
 template <int N>
-__global__ void __launch_bounds__(zp2<N>::NT) k_zfwd_spec2(const float2 *__restrict__ Bp, float2 *__restrict__ spec,
+__global__ void __launch_bounds__(zp2<N>::NT, LH_SPECZ_MINB(N)) k_zfwd_spec2(const float2 *__restrict__ Bp, float2 *__restrict__ spec,
                                                             Geo g, const float2 *__restrict__ tw) {
   using P = zp2<N>;
   // the inverse pass's plan read backwards: stage 1 ZA threads per line (ZB-point DFTs of rows
