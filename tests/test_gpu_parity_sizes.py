@@ -11,7 +11,8 @@ transform kernels run at their largest compiled lengths:
 * the leaf transforms (four_to_phys / phys_to_four) at every compiled length, 24 ... 1152,
   within 1e-13 of the oracle's;
 * one mixed-form step of textured channels whose x transforms have the lengths 192, 288 and
-  384 (the two-stage register x pass), against the oracle.
+  384 (the two-stage register x pass) and 576, 768, 1152 (the three-stage one), against the
+  oracle.
 The oracle runs on all host cores."""
 import os
 
@@ -189,7 +190,7 @@ def test_leaf_transforms_every_length(cuda_ok, G):
     o.close()
 
 
-@pytest.mark.parametrize("G", (192, 288, 384))
+@pytest.mark.parametrize("G", (192, 288, 384, 576, 768, 1152))
 def test_mixed_step_at_x_lengths(cuda_ok, G):
     """x length G (z length 96), posts on a 16-point period: one RK3 step of the mixed form
     within TOL_MIXED_VEL (velocities) and PRESS_MIXED (pressure) of the oracle"""
