@@ -29,6 +29,13 @@
 #include "lh_internal.cuh"
 
 #define NTHR 256
+// blocks per SM the compiler leaves registers for in the immersed-boundary kernels (sweep knobs)
+#ifndef LH_IBDU_MINB
+#define LH_IBDU_MINB 1
+#endif
+#ifndef LH_IBX_MINB
+#define LH_IBX_MINB 1
+#endif
 
 __device__ __forceinline__ void atomic_max_pos(unsigned long long *addr, double v) {
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
@@ -2459,7 +2466,7 @@ __global__ void __launch_bounds__(NTHR) k_ib_du(const double2 *__restrict__ u1, 
 
 // Mixed form of k_ib_du: the same right-hand side in FP32 (FP64 neighbour
 // differences for the Laplacian, integer-pipe conversions), N and du stored in FP32.
-__global__ void __launch_bounds__(NTHR) k_ib_du_mx(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
+__global__ void __launch_bounds__(NTHR, LH_IBDU_MINB) k_ib_du_mx(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                    const double2 *__restrict__ u3, float2 *__restrict__ Nu1o,
                                                    float2 *__restrict__ Nu2o, float2 *__restrict__ Nu3o,
                                                    const float2 *__restrict__ N1xz, const float2 *__restrict__ N2xz,
@@ -2551,7 +2558,7 @@ struct IbRec {
   double A;
 };
 template <typename T, int N>
-__global__ void __launch_bounds__(NTHR) k_ib_xforce(const typename C2<T>::t *__restrict__ A, typename C2<T>::t *__restrict__ B,
+__global__ void __launch_bounds__(NTHR, LH_IBX_MINB) k_ib_xforce(const typename C2<T>::t *__restrict__ A, typename C2<T>::t *__restrict__ B,
                                                     Geo g, const typename C2<T>::t *__restrict__ twx,
                                                     const IbRec *__restrict__ rec, const int *__restrict__ rec_off,
                                                     const T *__restrict__ cap, const DevScalars *__restrict__ sc) {
