@@ -192,16 +192,18 @@ template <typename T, int N>
 static cudaError_t set_attrs_sized(int lim) {
   cudaError_t e = cudaSuccess;
   const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv_nl<T, N>, A, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass_nl<T, N>, A, lim);
   // k_xstats also holds a small static reduction array
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xstats<T, N>, A, lim - 1024);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_nl<T, N>, A, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<T, N>, A, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<T, N>, A, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xfwd_phys<T, N>, A, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_ib_xforce<T, N>, A, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec<T, N>, A, lim);
+  if constexpr (sizeof(T) == 8) {  // the Stockham passes (FP64 form and the FP64 leaf transforms)
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv_nl<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xpass_nl<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_nl<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_spec_zinv<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xinv_phys<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_xfwd_phys<T, N>, A, lim);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd_spec<T, N>, A, lim);
+  }
   if constexpr (sizeof(T) == 4) {  // the two-stage mixed-form passes
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zinv2<N>, A, lim);
     if (e == cudaSuccess) e = cudaFuncSetAttribute((const void *)k_zfwd2<N>, A, lim);
@@ -1046,12 +1048,12 @@ static int launch_zinv(lh_handle *h, const Geo &g, int nslots, const void *twz) 
     dim3 grid((g.N1h + P::KB - 1) / P::KB, nslots, 3);
     KL("k_zinv_nl", k_zinv2<N><<<grid, P::NT, P::SMEM, h->st>>>(h->u1, h->u2, h->u3, (float2 *)h->A, g,
                                                                 (const float2 *)twz));
-    return LH_OK;
+  } else {  // FP64: Stockham
+    constexpr int KB = kb_zinv<V>(N);
+    dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
+    KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, LH_ZINV_THREADS, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
+                        h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)twz));
   }
-  constexpr int KB = kb_zinv<V>(N);
-  dim3 grid((g.N1h + KB - 1) / KB, nslots, 3);
-  KL("k_zinv_nl", k_zinv_nl<T, N><<<grid, LH_ZINV_THREADS, 2 * (size_t)KB * N * sizeof(V), h->st>>>(
-                      h->u1, h->u2, h->u3, (V *)h->A, g, (const V *)twz));
   return LH_OK;
 }
 template <typename T, int N>
@@ -1062,18 +1064,18 @@ static int launch_xpass(lh_handle *h, const Geo &g, int nslots, int doCFL, const
     dim3 grid((g.G2 / 2 + P::PB - 1) / P::PB, nslots);
     KL("k_xpass_nl", k_xpass2<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
                                                                   (const float2 *)twx, doCFL, h->sc, capslot, (float *)h->cap));
-    return LH_OK;
   } else if constexpr (sizeof(T) == 4 && (N == 576 || N == 768 || N == 1152)) {  // three-stage register form
     using P = xp3<N>;
     dim3 grid(g.G2 / 2, nslots);
     KL("k_xpass_nl", k_xpass3<N><<<grid, P::NT, P::SMEM, h->st>>>((const float2 *)h->A, (float2 *)h->B, g,
                                                                   (const float2 *)twx, doCFL, h->sc, capslot, (float *)h->cap));
-    return LH_OK;
+  } else {  // FP64: Stockham
+    static_assert(sizeof(T) == 8, "the mixed x pass has a register form for every compiled length");
+    constexpr int PB = pb_xpass<V>(N);
+    dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
+    KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, LH_XPASS_THREADS, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
+                         (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, (T *)h->cap));
   }
-  constexpr int PB = pb_xpass<V>(N);
-  dim3 grid((g.G2 / 2 + PB - 1) / PB, nslots);
-  KL("k_xpass_nl", k_xpass_nl<T, N><<<grid, LH_XPASS_THREADS, 8 * (size_t)PB * N * sizeof(V), h->st>>>(
-                       (const V *)h->A, (V *)h->B, g, (const V *)twx, doCFL, h->sc, capslot, (T *)h->cap));
   return LH_OK;
 }
 template <typename T, int N>
@@ -1085,13 +1087,13 @@ static int launch_zfwd(lh_handle *h, const Geo &g, int nslots, const void *twz) 
     KL("k_zfwd_nl", k_zfwd2<N><<<grid, P::NTH, P::SMEM, h->st>>>(
                         (const float2 *)h->B, g, (const float2 *)twz, (float2 *)h->N1xz, (float2 *)h->N2xz,
                         (float2 *)h->N3xz, (float2 *)h->uvf, (float2 *)h->vvc, (float2 *)h->wvf));
-    return LH_OK;
+  } else {  // FP64: Stockham
+    constexpr int KB = kb_zfwd<V>(N);
+    dim3 grid((g.N1h + KB - 1) / KB, nslots);
+    KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, LH_ZFWD_THREADS, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
+                        (const V *)h->B, g, (const V *)twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
+                        (V *)h->vvc, (V *)h->wvf));
   }
-  constexpr int KB = kb_zfwd<V>(N);
-  dim3 grid((g.N1h + KB - 1) / KB, nslots);
-  KL("k_zfwd_nl", k_zfwd_nl<T, N><<<grid, LH_ZFWD_THREADS, 8 * (size_t)KB * N * sizeof(V), h->st>>>(
-                      (const V *)h->B, g, (const V *)twz, (V *)h->N1xz, (V *)h->N2xz, (V *)h->N3xz, (V *)h->uvf,
-                      (V *)h->vvc, (V *)h->wvf));
   return LH_OK;
 }
 
@@ -1151,11 +1153,11 @@ static int launch_spec_zinv(lh_handle *h, const void *spec, void *Ascr, int npl,
     using P = zp2<N>;
     dim3 g1((h->g.N1h + P::KB - 1) / P::KB, npl);
     KL("k_spec_zinv", k_spec_zinv2<N><<<g1, P::NT, P::SMEM, h->st>>>((const float2 *)spec, (float2 *)Ascr, h->g, (const float2 *)twz));
-    return LH_OK;
+  } else {  // FP64: Stockham
+    constexpr int KB = kb_zinv<V>(N);
+    dim3 g1((h->g.N1h + KB - 1) / KB, npl);
+    KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const double2 *)spec, (V *)Ascr, h->g, (const V *)twz));
   }
-  constexpr int KB = kb_zinv<V>(N);
-  dim3 g1((h->g.N1h + KB - 1) / KB, npl);
-  KL("k_spec_zinv", k_spec_zinv<T, N><<<g1, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const double2 *)spec, (V *)Ascr, h->g, (const V *)twz));
   return LH_OK;
 }
 template <typename T, int N>
@@ -1181,11 +1183,11 @@ static int launch_zfwd_spec(lh_handle *h, const void *Bscr, void *spec, int npl,
     using P = zp2<N>;
     dim3 g2((h->g.N1h + P::KB - 1) / P::KB, npl);
     KL("k_zfwd_spec", k_zfwd_spec2<N><<<g2, P::NT, P::SMEM, h->st>>>((const float2 *)Bscr, (float2 *)spec, h->g, (const float2 *)twz));
-    return LH_OK;
+  } else {  // FP64: Stockham
+    constexpr int KB = kb_zinv<V>(N);
+    dim3 g2((h->g.N1h + KB - 1) / KB, npl);
+    KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, (double2 *)spec, h->g, (const V *)twz));
   }
-  constexpr int KB = kb_zinv<V>(N);
-  dim3 g2((h->g.N1h + KB - 1) / KB, npl);
-  KL("k_zfwd_spec", k_zfwd_spec<T, N><<<g2, NTHR_H, 2 * (size_t)KB * N * sizeof(V), h->st>>>((const V *)Bscr, (double2 *)spec, h->g, (const V *)twz));
   return LH_OK;
 }
 
