@@ -56,6 +56,15 @@ __host__ __device__ __forceinline__ int grow(const Geo &g, int r) { return r < g
 __device__ __forceinline__ int slot_level(const Geo &g, int slot, bool isU) {
   return g.slotq ? g.slotq[slot] : (isU ? slot + 1 : slot - g.nuI + 1);
 }
+// The slot of launch row y in the inverse z passes: u and v slots interleaved (u slot i, then
+// v slot i), so the levels a staggered interpolation reads (v faces q - 1, q for u level q;
+// u levels q, q + 1 for v level q) are also read by the neighbouring rows and come from L2
+// the second time; a bijection of [0, nuI + nvI).
+__device__ __forceinline__ int zinv_slot(const Geo &g, int y) {
+  const int m = g.nuI < g.nvI ? g.nuI : g.nvI;
+  if (y < 2 * m) return (y & 1) ? g.nuI + (y >> 1) : (y >> 1);
+  return g.nuI > g.nvI ? y - m : g.nuI + (y - m);
+}
 // column and band of a virtual column
 __device__ __forceinline__ void vcol_of(const Geo &g, int vc, int &c, int &b) {
   if (g.vcol) { const int2 e = g.vcol[vc]; c = e.x; b = e.y; }

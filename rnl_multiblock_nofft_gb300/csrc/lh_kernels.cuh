@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(LH_ZINV_THREADS) k_zinv_nl(const double2 *__re
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *b0 = reinterpret_cast<V *>(smem_raw);
   V *b1 = b0 + KB * N;
-  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * KB;
+  const int slot = zinv_slot(g, blockIdx.y), f = blockIdx.z, kx0 = blockIdx.x * KB;
   const bool isU = slot < g.nuI;
   const int q = slot_level(g, slot, isU);
   const int nc = g.ncolF;

@@ -324,7 +324,7 @@ template <int N>
 __global__ void __launch_bounds__(zp2<N>::NT, zp2<N>::MINB) k_zinv2(const double2 *__restrict__ u1, const double2 *__restrict__ u2,
                                                        const double2 *__restrict__ u3, float2 *__restrict__ A, Geo g,
                                                        const float2 *__restrict__ tw) {
-  const int slot = blockIdx.y, f = blockIdx.z, kx0 = blockIdx.x * zp2<N>::KB;
+  const int slot = zinv_slot(g, blockIdx.y), f = blockIdx.z, kx0 = blockIdx.x * zp2<N>::KB;
   const bool isU = slot < g.nuI;
   const int q = slot_level(g, slot, isU);
   const size_t nc = g.ncolF;
