@@ -2487,56 +2487,67 @@ __global__ void __launch_bounds__(NTHR, LH_IBDU_MINB) k_ib_du_mx(const double2 *
   const float G = (float)(-g.gRK[kRK - 1]);
   const float dd = (float)g.dd;
   const int qu = iblev[2 * s], qv = iblev[2 * s + 1];
+  // every input of the thread is loaded before the first store, so that the latencies of the
+  // u-level and v-level loads overlap (the kernel is bound by them, not by bandwidth)
+  const size_t ou = (size_t)qu * nc + c, ov = (size_t)qv * nc + c;
+  double2 um[2], u0[2], up[2], pj, vm, v0, vp, pp, pm;
+  float2 no[2], xq[2], fq[2], fm[2], nov, xv, vp1, vq;
+  double mpgx = 0.0;
+  if (qu > 0) {
+    pj = p[(size_t)(qu - 1) * nc + c];
+    if (c == 0) mpgx = sc->mpgx;
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const double2 *U = f ? u3 : u1;
+      const float2 *F = f ? wvf : uvf;
+      um[f] = U[ou - nc]; u0[f] = U[ou]; up[f] = U[ou + nc];
+      no[f] = (f ? Nu3o : Nu1o)[ou];
+      xq[f] = (f ? N3xz : N1xz)[ou];
+      fq[f] = F[ou]; fm[f] = F[ou - nc];
+    }
+  }
+  if (qv > 0) {
+    vm = u2[ov - nc]; v0 = u2[ov]; vp = u2[ov + nc];
+    pp = p[(size_t)qv * nc + c]; pm = p[(size_t)(qv - 1) * nc + c];
+    nov = Nu2o[ov]; xv = N2xz[ov]; vp1 = vvc[ov + nc]; vq = vvc[ov];
+  }
   if (qu > 0) {
     const int nu = g.nu;
-    const size_t o = (size_t)qu * nc + c;
     const float a = g.d2uf[qu], cc = g.d2uf[2 * nu + qu], sdg = g.sdgu[qu] + k2f;
-    const double2 pj = p[(size_t)(qu - 1) * nc + c];
     const float pjx = d2f_alu(pj.x), pjy = d2f_alu(pj.y);
     const float C3x = (float)(-dR * g.k1x[kx]), C3z = (float)(-dR * g.k1z[r]);
     const float th = g.thuf[qu];
+#pragma unroll
     for (int f = 0; f < 2; ++f) {
-      const double2 *U = f ? u3 : u1;
-      float2 *No = f ? Nu3o : Nu1o;
-      const float2 *X = f ? N3xz : N1xz;
-      const float2 *F = f ? wvf : uvf;
       const float C3 = f ? C3z : C3x;
-      const double2 um = U[o - nc], u0 = U[o], up = U[o + nc];
       float2 L;
-      L.x = a * d2f_alu(um.x - u0.x) + cc * d2f_alu(up.x - u0.x) + sdg * d2f_alu(u0.x);
-      L.y = a * d2f_alu(um.y - u0.y) + cc * d2f_alu(up.y - u0.y) + sdg * d2f_alu(u0.y);
-      const float2 no = No[o];
+      L.x = a * d2f_alu(um[f].x - u0[f].x) + cc * d2f_alu(up[f].x - u0[f].x) + sdg * d2f_alu(u0[f].x);
+      L.y = a * d2f_alu(um[f].y - u0[f].y) + cc * d2f_alu(up[f].y - u0[f].y) + sdg * d2f_alu(u0[f].y);
       float2 du;
-      du.x = (C1 * L.x + C2 * no.x) + (-C3 * pjy);
-      du.y = (C1 * L.y + C2 * no.y) + (C3 * pjx);
-      if (f == 0 && c == 0) du.x += (float)(-dR * sc->mpgx);
-      const float2 x = X[o], fq = F[o], fm = F[o - nc];
+      du.x = (C1 * L.x + C2 * no[f].x) + (-C3 * pjy);
+      du.y = (C1 * L.y + C2 * no[f].y) + (C3 * pjx);
+      if (f == 0 && c == 0) du.x += (float)(-dR * mpgx);
       float2 n;
-      n.x = x.x + (fq.x - fm.x) * th * dd; n.y = x.y + (fq.y - fm.y) * th * dd;
-      No[o] = n;
+      n.x = xq[f].x + (fq[f].x - fm[f].x) * th * dd; n.y = xq[f].y + (fq[f].y - fm[f].y) * th * dd;
+      (f ? Nu3o : Nu1o)[ou] = n;
       du.x += G * n.x; du.y += G * n.y;
       duib[((size_t)s * 3 + (f ? 2 : 0)) * nc + c] = du;
     }
   }
   if (qv > 0) {
     const int nv = g.nv;
-    const size_t o = (size_t)qv * nc + c;
     const float a = g.d2vf[qv], cc = g.d2vf[2 * nv + qv], sdg = g.sdgv[qv] + k2f;
-    const double2 vm = u2[o - nc], v0 = u2[o], vp = u2[o + nc];
     float2 L;
     L.x = a * d2f_alu(vm.x - v0.x) + cc * d2f_alu(vp.x - v0.x) + sdg * d2f_alu(v0.x);
     L.y = a * d2f_alu(vm.y - v0.y) + cc * d2f_alu(vp.y - v0.y) + sdg * d2f_alu(v0.y);
     const float C3 = -dRf * dd * g.thvf[qv];
-    const double2 pp = p[(size_t)qv * nc + c], pm = p[(size_t)(qv - 1) * nc + c];
-    const float2 no = Nu2o[o];
     float2 du;
-    du.x = (C1 * L.x + C2 * no.x) + C3 * (d2f_alu(pp.x) - d2f_alu(pm.x));
-    du.y = (C1 * L.y + C2 * no.y) + C3 * (d2f_alu(pp.y) - d2f_alu(pm.y));
+    du.x = (C1 * L.x + C2 * nov.x) + C3 * (d2f_alu(pp.x) - d2f_alu(pm.x));
+    du.y = (C1 * L.y + C2 * nov.y) + C3 * (d2f_alu(pp.y) - d2f_alu(pm.y));
     const float th = g.thvf[qv];
-    const float2 x = N2xz[o], vp1 = vvc[o + nc], vq = vvc[o];
     float2 n;
-    n.x = x.x + (vp1.x - vq.x) * th * dd; n.y = x.y + (vp1.y - vq.y) * th * dd;
-    Nu2o[o] = n;
+    n.x = xv.x + (vp1.x - vq.x) * th * dd; n.y = xv.y + (vp1.y - vq.y) * th * dd;
+    Nu2o[ov] = n;
     du.x += G * n.x; du.y += G * n.y;
     duib[((size_t)s * 3 + 1) * nc + c] = du;
   }
