@@ -2608,14 +2608,20 @@ __global__ void __launch_bounds__(NTHR, LH_IBX_MINB) k_ib_xforce(const typename 
   V *oth = (res == b0) ? b1 : b0;
   {
     const double Kibdt = g.Kib / sc->dt;
+    const float Kibdtf = d2f_alu(Kibdt);
     const int r0 = rec_off[(size_t)pl * G2 + l0], r1 = rec_off[(size_t)pl * G2 + l0 + 2 * npairs];
     for (int e = r0 + threadIdx.x; e < r1; e += blockDim.x) {
       const IbRec R = rec[e];
-      const double val = Kibdt * (R.A * to_d(cap[R.ref]) - to_d(cap[R.src]));
+      T val;
+      if constexpr (sizeof(T) == 4) {  // FP32 values: one rounding of A u_ref - u (fused), one of the scaling
+        val = Kibdtf * fmaf(d2f_alu(R.A), cap[R.ref], -cap[R.src]);
+      } else {
+        val = Kibdt * (R.A * cap[R.ref] - cap[R.src]);
+      }
       const int rr = R.k - l0;
       V *z = res + (rr >> 1) * G1 + R.i;
-      if (rr & 1) z->y = to_t<T>(val);
-      else z->x = to_t<T>(val);
+      if (rr & 1) z->y = val;
+      else z->x = val;
     }
   }
   __syncthreads();
