@@ -212,7 +212,10 @@ def column_levels(s, grid: int) -> int:
 def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0, ib: bool = True) -> float:
     """Compulsory HBM bytes of one substep's launches of a kernel: every input and
     output element once. Spectral fields are complex128; the transform intermediates
-    are complex128 in the FP64 form and complex64 in the mixed form. The triad kernel
+    and the forward z pass's outputs are complex128 in the FP64 form and complex64 in
+    the mixed form. The inverse z pass reads each field on its own planes (u and w on
+    the u planes, v on the v planes); the staggered interpolation's neighbour planes are
+    the same elements again (a plane at each band edge aside) and count once. The triad kernel
     reads one 4-byte term per complex multiply-add (`nterms` per substep), the three
     velocities of every interior plane and writes five (u planes) / three (v planes)
     products in the transform precision."""
@@ -223,21 +226,24 @@ def algorithmic_bytes(s, kernel: str, form: str, nterms: int = 0, ib: bool = Tru
         A = (nuI + nvI) * 3 * G2 * N1h * vs
         B = (4 * nuI + 2 * nvI) * N1h * G2 * vs
         if kernel == "k_zinv_nl":
-            tot += (nuI + nvI) * 3 * ncv * z + A
+            tot += (2 * nuI + nvI) * ncv * z + A
         elif kernel == "k_xpass_nl":
             tot += A + B
         elif kernel == "k_zfwd_nl":
-            tot += B + (nuI + nvI) * 3 * ncv * z
+            tot += B + (nuI + nvI) * 3 * ncv * vs
     if kernel == "k_xpass_nl" and ib and s.dny > 0 and s.p.ib_enable and s.p.geometry_type == 2:
         # physical planes of the immersed-boundary levels (and the two tip levels) captured
         # for the forcing: 3 fields, in the transform precision
         tot += (4 * s.dny + 2) * 3 * s.G1 * s.G2 * (8 if form == "fp64" else 4)
     if kernel in ("k_zinv_nl", "k_xpass_nl", "k_zfwd_nl"):
         return tot
+    # the solves: the FP64 state read and written (u and w / v) and p read, the nonlinear
+    # term N read and written, the z pass's output and the y-flux read, in the transform
+    # precision (FP64 form: 13 / 7 complex128 per column level)
     if kernel == "k_helm_uw":
-        return column_levels(s, 2) * z * 13
+        return column_levels(s, 2) * (4 * z + z + 2 * 4 * vs)
     if kernel == "k_helm_v":
-        return column_levels(s, 1) * z * 7
+        return column_levels(s, 1) * (2 * z + z + 4 * vs)
     if kernel == "k_press":
         return column_levels(s, 2) * z * 8
     if kernel == "k_triad":
