@@ -1282,17 +1282,12 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     LH_DISPATCH(g.G2, rc = launch_zfwd_spec<T, N>(h, h->B, h->duib, 3 * h->nib, h->twz));
     if (rc) return rc;
   }
-  if (h->prec == LH_PREC_MIXED) {  // mode (0,0) in FP64, before the solves of the other columns
-    const size_t sm00 = 8 * sizeof(double) * (size_t)(std::max(g.nu, g.nv) + 1);
-    KL("k_helm00", k_helm00_pcr<<<6, 512, sm00, h->st>>>(
-                       (double *)h->u1, (double *)h->u3, (double *)h->u2, (const float *)h->N1xz, (const float *)h->N3xz,
-                       (const float *)h->N2xz, (const float *)h->uvf, (const float *)h->wvf, (const float *)h->vvc,
-                       (const double *)h->p, (const float2 *)h->duib, h->ib ? h->d_ibslot_u : nullptr, h->ib ? h->d_ibslot_v : nullptr,
-                       g, h->sc, kRK, h->a3s));
-  }
   // The u/w and v solves are independent: v runs on the side stream while u/w and the
   // mean-flow correction (which follows u) run on the main stream; each solve has its
-  // own scratch. (Sequential on the main stream while per-kernel times are profiled.)
+  // own scratch. In the mixed form mode (0,0) is solved in FP64 by its own kernel on the
+  // side stream after v (the other solves skip column 0), overlapping the longer u/w solve;
+  // the mean-flow correction, which reads u(0,0), follows the join. (Sequential on the main
+  // stream while per-kernel times are profiled.)
   const bool fork = !h->prof;
   cudaStream_t sv = fork ? h->st2 : h->st;
   if (fork) {
@@ -1320,6 +1315,15 @@ static int substep_launches_t(lh_handle *h, int kRK) {
     }
   }
   if ((rc = count_launch(h))) return rc;
+  const bool mixed00 = h->prec == LH_PREC_MIXED;
+  if (mixed00) {
+    const size_t sm00 = 8 * sizeof(double) * (size_t)(std::max(g.nu, g.nv) + 1);
+    KL("k_helm00", k_helm00_pcr<<<6, 512, sm00, sv>>>(
+                       (double *)h->u1, (double *)h->u3, (double *)h->u2, (const float *)h->N1xz, (const float *)h->N3xz,
+                       (const float *)h->N2xz, (const float *)h->uvf, (const float *)h->wvf, (const float *)h->vvc,
+                       (const double *)h->p, (const float2 *)h->duib, h->ib ? h->d_ibslot_u : nullptr, h->ib ? h->d_ibslot_v : nullptr,
+                       g, h->sc, kRK, h->a3s));
+  }
   if (fork) CK(cudaEventRecord(h->ev_join, h->st2));
   if (h->prec == LH_PREC_FP64) {
     KL("k_helm_uw", k_helm_uw<T><<<nbu, h->tb_uw, 0, h->st>>>(h->u1, h->u3, (double2 *)h->Nu1, (double2 *)h->Nu3,
@@ -1343,8 +1347,8 @@ static int substep_launches_t(lh_handle *h, int kRK) {
       default: KL("k_helm_uw", k_helm_u_mx3<4><<<gr, h->tb_uw, sm, h->st>>>(U1, U3, N1, N3, X1, X3, F1, F3, h->p, YS, g, h->sc, kRK, ibu, (const float2 *)h->duib)); break;
     }
   }
-  if ((rc = meanflow(h, kRK))) return rc;
   if (fork) CK(cudaStreamWaitEvent(h->st, h->ev_join, 0));
+  if ((rc = meanflow(h, kRK))) return rc;
   const int need_div = (kRK == 3) ? 1 : 0;
   if (need_div) KL("k_reset_err", k_reset_err<<<1, 32, 0, h->st>>>(h->sc));
   const int nbp2 = (2 * g.nvc + h->tb_p - 1) / h->tb_p;
