@@ -60,7 +60,7 @@ __device__ __forceinline__ int slot_level(const Geo &g, int slot, bool isU) {
 // v slot i), so the levels a staggered interpolation reads (v faces q - 1, q for u level q;
 // u levels q, q + 1 for v level q) are also read by the neighbouring rows and come from L2
 // the second time; a bijection of [0, nuI + nvI).
-__device__ __forceinline__ int zinv_slot(const Geo &g, int y) {
+__host__ __device__ __forceinline__ int zinv_slot(const Geo &g, int y) {
   const int m = g.nuI < g.nvI ? g.nuI : g.nvI;
   if (y < 2 * m) return (y & 1) ? g.nuI + (y >> 1) : (y >> 1);
   return g.nuI > g.nvI ? y - m : g.nuI + (y - m);

@@ -49,3 +49,18 @@ def test_register_dfts_against_direct_dft(tmp_path):
     for n, e in rows.items():
         assert max(e[:2]) < 1e-15, (n, e)   # FP64 forward / inverse
         assert max(e[2:]) < 5e-7, (n, e)    # FP32
+
+
+def test_inverse_z_pass_slot_order(tmp_path):
+    """The inverse z passes' launch rows (zinv_slot, tests/slot_order_check.cu): a bijection
+    onto the slots for every split of u and v slots, each row following the row that read a
+    level it reads again."""
+    cc = nvcc()
+    if cc is None:
+        pytest.skip("nvcc not found")
+    exe = str(tmp_path / "slot_order_check")
+    subprocess.run([cc, "-O2", "-std=c++17", "-x", "cu", os.path.join(HERE, "slot_order_check.cu"), "-o", exe],
+                   check=True, capture_output=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.strip() == "ok %d" % (161 * 161), out.stdout
+
